@@ -1,0 +1,71 @@
+/*
+ * Internal interfaces shared by the CUDA translation units of the gravity
+ * library (not part of the public C-ABI in include/).
+ */
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "cuda_typedef.h"
+#include "changa_gb300.h"
+
+namespace chg {
+
+enum Form : int { kF32 = 0, kF64 = 1, kMix = 2 };
+
+/* Arguments of one interaction-list launch. */
+struct ListArgs {
+  const void* src;      // kF32: CudaMultipoleMoments* or CompactPartData*
+                        // kF64: double* (12 or 5 per row); kMix: packed float4
+  long long n_src;
+  const void* tgt;      // kF32: CompactPartData*; kF64: double*; kMix: packed float4
+  long long n_tgt;
+  void* vars;           // kF32: VariablePartData*; kF64/kMix: double* (5 per row)
+  const int2* list;     // ILCell {index, offsetID}
+  long long n_entries;  // entries in list (markers are clamped to it)
+  const int* markers;   // n_buckets + 1
+  const int* starts;
+  const int* sizes;
+  int n_buckets;
+  float fperiod_f;
+  double fperiod_d;
+  unsigned int* queue;  // work counter, zero at launch
+};
+
+/* Packed FP32-mixed layouts (built by pack kernels from FP64 inputs):
+ *   cell   : 4 float4 per node  {hi.xyz, M} {lo.xyz, soft} {xx,xy,xz,yy}
+ *            {yz, zz, tr, 0}
+ *   particle: 2 float4 per particle {hi.xyz, mass} {lo.xyz, soft}
+ * hi = (float)x, lo = (float)(x - hi), both exact in FP64. */
+constexpr int kCellPackF4 = 4;
+constexpr int kPartPackF4 = 2;
+
+/* launchers (grav_lists.cu) */
+cudaError_t launch_list(int form, bool cell, const ListArgs& a, cudaStream_t s);
+cudaError_t launch_pack_cells(const double* moments, long long n, float4* out, cudaStream_t s);
+cudaError_t launch_pack_parts(const double* parts, long long n, float4* out, cudaStream_t s);
+cudaError_t launch_zero_vars_f32(VariablePartData* v, long long n, cudaStream_t s);
+
+/* Ewald (ewald.cu) */
+struct EwaldArgsF32;  // defined in ewald.cu
+cudaError_t launch_ewald_f32(const CompactPartData* parts, VariablePartData* vars,
+                             const int* markers, int largephase, int first, int last,
+                             const EwaldReadOnlyData& ro, const EwtData* ewt,
+                             cudaStream_t s);
+cudaError_t launch_ewald_fp(int form, const double* parts, long long n_parts, const int* idx,
+                            long long n_idx, const ChangaEwaldParams& p, double* vars,
+                            cudaStream_t s);
+
+/* runtime helpers (hostcuda.cu) */
+int sm_count();
+void count_launch(unsigned n = 1);
+int record_error(int code, const char* what, const char* file, int line);
+
+}  // namespace chg
+
+#define CHG_CUDA(call)                                                            \
+  do {                                                                            \
+    cudaError_t e_ = (call);                                                      \
+    if (e_ != cudaSuccess) return ::chg::record_error((int)e_, #call, __FILE__, __LINE__); \
+  } while (0)

@@ -1,0 +1,489 @@
+/*
+ * Interaction-list force kernels: cell (quadrupole) lists and particle lists.
+ *
+ * Reference behaviour (HostCUDA.cu:1008-1205 nodeGravityComputation,
+ * HostCUDA.cu:1565-1751 particleGravityComputation; CPU gravity.h:267-303,
+ * 398-475): for every bucket b of a request, every target particle in
+ * [starts[b], starts[b]+sizes[b]) interacts with every list entry in
+ * [markers[b], markers[b+1]); results accumulate (+=, max for dtGrav).
+ *
+ * GB300 design (not the reference's 8x16 thread tile):
+ *   - a persistent grid, one warp per bucket at a time, buckets taken from
+ *     a device work queue (one atomicAdd per bucket) so uneven list lengths
+ *     balance themselves;
+ *   - the warp's 32 lanes are split into G = 32/nt groups of nt target
+ *     lanes (nt = targets in the current chunk of <= 32), so small buckets
+ *     still fill the warp; group g takes list entries g, g+G, g+2G, ...;
+ *   - list entries are staged 32 at a time: each lane loads one ILCell
+ *     (coalesced) and gathers its source record (the moment array is small
+ *     enough to stay resident in the 126 MB L2), adds the replica offset
+ *     and writes a ready-to-use record to the warp's shared-memory slice;
+ *     every target lane then reads records by broadcast, so the hot loop is
+ *     FP32 FMA plus one MUFU rsqrt per interaction;
+ *   - targets live in registers; the group partial sums are reduced through
+ *     shared memory once per bucket, not per list tile.
+ * Three arithmetic forms share the code:
+ *   kF32  the drop-in form on the FP32 ABI structs (no accidental FP64);
+ *   kF64  plain FP64 on FP64 arrays;
+ *   kMix  FP32 arithmetic on bucket-relative coordinates: positions are
+ *         packed as float hi + float lo parts, the bucket-centre subtraction
+ *         (hi - c_hi) + (lo - c_lo) keeps the result accurate to FP32
+ *         rounding of the *relative* vector, and per-tile FP32 partial sums
+ *         are folded into Kahan-compensated per-particle totals.
+ */
+#include <type_traits>
+
+#include "chg_internal.h"
+
+namespace chg {
+namespace {
+
+constexpr int kWarps = 8;
+constexpr int kThreads = kWarps * 32;
+constexpr unsigned kFull = 0xffffffffu;
+
+__device__ __forceinline__ float rsqrt_t(float x) { return rsqrtf(x); }
+__device__ __forceinline__ double rsqrt_t(double x) { return rsqrt(x); }
+__device__ __forceinline__ float two_over(float t) { return __fdividef(2.0f, t); }
+__device__ __forceinline__ double two_over(double t) { return 2.0 / t; }
+__device__ __forceinline__ float max_t(float a, float b) { return fmaxf(a, b); }
+__device__ __forceinline__ double max_t(double a, double b) { return fmax(a, b); }
+
+/* SPLINEQ inside the softening radius (gravity.h:27-59): both branches. */
+template <typename T>
+__device__ __forceinline__ void splineq_near(T dir, T rsq, T twoh, T& a, T& b, T& c, T& d) {
+  const T dih = two_over(twoh);
+  const T u = dih * (rsq * dir);
+  const T dih2 = dih * dih, dih3 = dih2 * dih, dih5 = dih3 * dih2;
+  const T u2 = u * u;
+  if (u < T(1)) {
+    a = dih * (T(7.0 / 5.0) - T(2.0 / 3.0) * u2 + T(3.0 / 10.0) * u2 * u2 -
+               T(1.0 / 10.0) * u2 * u2 * u);
+    b = dih3 * (T(4.0 / 3.0) - T(6.0 / 5.0) * u2 + T(0.5) * u2 * u);
+    c = dih5 * (T(12.0 / 5.0) - T(1.5) * u);
+    d = T(1.5) * dih5 * dih * dir;
+  } else {
+    const T dir2 = dir * dir, dir3 = dir2 * dir;
+    a = T(-1.0 / 15.0) * dir +
+        dih * (T(8.0 / 5.0) - T(4.0 / 3.0) * u2 + u2 * u - T(3.0 / 10.0) * u2 * u2 +
+               T(1.0 / 30.0) * u2 * u2 * u);
+    b = T(-1.0 / 15.0) * dir3 +
+        dih3 * (T(8.0 / 3.0) - T(3) * u + T(6.0 / 5.0) * u2 - T(1.0 / 6.0) * u2 * u);
+    c = T(-1.0 / 5.0) * dir3 * dir2 + T(3) * dih2 * dih2 * dir + dih5 * (T(-12.0 / 5.0) + T(0.5) * u);
+    d = -dir3 * dir3 * dir + T(3) * dih2 * dih2 * dir3 - T(0.5) * dih5 * dih * dir;
+  }
+}
+
+/* SPLINE inside the softening radius (gravity.h:152-176). */
+template <typename T>
+__device__ __forceinline__ void spline_near(T r, T dir, T twoh, T& a, T& b) {
+  const T dih = two_over(twoh);
+  const T u = r * dih;
+  const T u2 = u * u, dih3 = dih * dih * dih;
+  if (u < T(1)) {
+    a = dih * (T(7.0 / 5.0) - T(2.0 / 3.0) * u2 + T(3.0 / 10.0) * u2 * u2 -
+               T(1.0 / 10.0) * u2 * u2 * u);
+    b = dih3 * (T(4.0 / 3.0) - T(6.0 / 5.0) * u2 + T(0.5) * u2 * u);
+  } else {
+    a = T(-1.0 / 15.0) * dir +
+        dih * (T(8.0 / 5.0) - T(4.0 / 3.0) * u2 + u2 * u - T(3.0 / 10.0) * u2 * u2 +
+               T(1.0 / 30.0) * u2 * u2 * u);
+    b = T(-1.0 / 15.0) * dir * dir * dir +
+        dih3 * (T(8.0 / 3.0) - T(3) * u + T(6.0 / 5.0) * u2 - T(1.0 / 6.0) * u2 * u);
+  }
+}
+
+template <typename T>
+struct Acc {
+  T ax, ay, az, pot, idt2;
+};
+
+/* One cell on one target (gravity.h:436-472 / HostCUDA.cu:1091-1164).
+ * rec: {sx, sy, sz, M, soft, tr, xx, xy, xz, yy, yz, zz}; r = target - s. */
+template <typename T>
+__device__ __forceinline__ void pc_interact(const T* rec, T tx, T ty, T tz, T tsoft, T tmass,
+                                            Acc<T>& acc) {
+  const T rx = tx - rec[0], ry = ty - rec[1], rz = tz - rec[2];
+  const T M = rec[3];
+  const T rsq = rx * rx + ry * ry + rz * rz;
+  if (rsq != T(0)) {
+    const T dir = rsqrt_t(rsq);
+    const T twoh = rec[4] + tsoft;
+    T a, b, c, d;
+    if (rsq < twoh * twoh) {
+      splineq_near(dir, rsq, twoh, a, b, c, d);
+    } else {
+      const T dir2 = dir * dir;
+      a = dir;
+      b = dir2 * dir;
+      c = T(3) * b * dir2;
+      d = T(5) * c * dir2;
+    }
+    const T xx = rec[6], xy = rec[7], xz = rec[8], yy = rec[9], yz = rec[10], zz = rec[11];
+    const T qirx = xx * rx + xy * ry + xz * rz;
+    const T qiry = xy * rx + yy * ry + yz * rz;
+    const T qirz = xz * rx + yz * ry + zz * rz;
+    const T qir = T(0.5) * (qirx * rx + qiry * ry + qirz * rz);
+    const T tr = rec[5];
+    const T qir3 = b * M + d * qir - c * tr;
+    acc.pot -= M * a + c * qir - b * tr;
+    acc.ax -= qir3 * rx - c * qirx;
+    acc.ay -= qir3 * ry - c * qiry;
+    acc.az -= qir3 * rz - c * qirz;
+    acc.idt2 = max_t(acc.idt2, (tmass + M) * b);
+  }
+}
+
+/* One source particle on one target (gravity.h:276-301 /
+ * HostCUDA.cu:1654-1711).  rec: {sx, sy, sz, m, soft}; r = s - target. */
+template <typename T>
+__device__ __forceinline__ void pp_interact(const T* rec, T tx, T ty, T tz, T tsoft, T tmass,
+                                            Acc<T>& acc) {
+  const T rx = rec[0] - tx, ry = rec[1] - ty, rz = rec[2] - tz;
+  const T m = rec[3];
+  const T rsq = rx * rx + ry * ry + rz * rz;
+  if (rsq != T(0)) {
+    const T twoh = rec[4] + tsoft;
+    const T dir = rsqrt_t(rsq);
+    const T r1 = rsq * dir;
+    T a, b;
+    if (r1 < twoh) {
+      spline_near(r1, dir, twoh, a, b);
+    } else {
+      a = dir;
+      b = dir * dir * dir;
+    }
+    const T bm = b * m;
+    acc.pot -= m * a;
+    acc.ax += rx * bm;
+    acc.ay += ry * bm;
+    acc.az += rz * bm;
+    acc.idt2 = max_t(acc.idt2, (tmass + m) * b);
+  }
+}
+
+__device__ __forceinline__ void kahan_add(float& sum, float& comp, float x) {
+  const float y = x - comp;
+  const float t = sum + y;
+  comp = (t - sum) - y;
+  sum = t;
+}
+
+template <int FORM>
+struct FormT {
+  using T = float;  // arithmetic
+  using A = float;  // reduction / output
+};
+template <>
+struct FormT<kF64> {
+  using T = double;
+  using A = double;
+};
+template <>
+struct FormT<kMix> {
+  using T = float;
+  using A = double;
+};
+
+/* Builds the staged record of list entry e in dst. */
+template <int FORM, bool CELL>
+__device__ __forceinline__ void stage_entry(const ListArgs& a, int e, float3 chi, float3 clo,
+                                            typename FormT<FORM>::T* dst) {
+  const int2 ent = __ldg(a.list + e);
+  long long idx = ent.x;
+  if ((unsigned long long)idx >= (unsigned long long)a.n_src) idx = 0;  // memory safety
+  const int code = (ent.y >> 22) & 0x1ff;
+  const int ox = (code & 7) - 3, oy = ((code >> 3) & 7) - 3, oz = ((code >> 6) & 7) - 3;
+  if constexpr (FORM == kF32) {
+    const float fp = a.fperiod_f;
+    if constexpr (CELL) {
+      const float4* m = reinterpret_cast<const float4*>(
+          static_cast<const CudaMultipoleMoments*>(a.src) + idx);
+      const float4 m0 = __ldg(m), m1 = __ldg(m + 1), m2 = __ldg(m + 2);
+      // m0 {radius, soft, M, cm.x}  m1 {cm.y, cm.z, xx, xy}  m2 {xz, yy, yz, zz}
+      float4* d4 = reinterpret_cast<float4*>(dst);
+      d4[0] = make_float4((float)ox * fp + m0.w, (float)oy * fp + m1.x, (float)oz * fp + m1.y, m0.z);
+      d4[1] = make_float4(m0.y, 0.5f * (m1.z + m2.y + m2.w), m1.z, m1.w);
+      d4[2] = m2;
+    } else {
+      const CompactPartData* p = static_cast<const CompactPartData*>(a.src) + idx;
+      const float m = __ldg(&p->mass), s = __ldg(&p->soft);
+      const float px = __ldg(&p->position.x), py = __ldg(&p->position.y), pz = __ldg(&p->position.z);
+      float4* d4 = reinterpret_cast<float4*>(dst);
+      d4[0] = make_float4((float)ox * fp + px, (float)oy * fp + py, (float)oz * fp + pz, m);
+      d4[1] = make_float4(s, 0.f, 0.f, 0.f);
+    }
+  } else if constexpr (FORM == kF64) {
+    const double fp = a.fperiod_d;
+    if constexpr (CELL) {
+      const double* m = static_cast<const double*>(a.src) + 12 * idx;
+      dst[0] = (double)ox * fp + __ldg(m + 3);
+      dst[1] = (double)oy * fp + __ldg(m + 4);
+      dst[2] = (double)oz * fp + __ldg(m + 5);
+      dst[3] = __ldg(m + 2);
+      dst[4] = __ldg(m + 1);
+      const double xx = __ldg(m + 6), xy = __ldg(m + 7), xz = __ldg(m + 8);
+      const double yy = __ldg(m + 9), yz = __ldg(m + 10), zz = __ldg(m + 11);
+      dst[5] = 0.5 * (xx + yy + zz);
+      dst[6] = xx;
+      dst[7] = xy;
+      dst[8] = xz;
+      dst[9] = yy;
+      dst[10] = yz;
+      dst[11] = zz;
+    } else {
+      const double* p = static_cast<const double*>(a.src) + 5 * idx;
+      dst[0] = (double)ox * fp + __ldg(p + 2);
+      dst[1] = (double)oy * fp + __ldg(p + 3);
+      dst[2] = (double)oz * fp + __ldg(p + 4);
+      dst[3] = __ldg(p + 0);
+      dst[4] = __ldg(p + 1);
+    }
+  } else {  // kMix
+    const float fp = a.fperiod_f;
+    float4* d4 = reinterpret_cast<float4*>(dst);
+    if constexpr (CELL) {
+      const float4* m = static_cast<const float4*>(a.src) + kCellPackF4 * idx;
+      const float4 h = __ldg(m), l = __ldg(m + 1), q0 = __ldg(m + 2), q1 = __ldg(m + 3);
+      const float sx = ((h.x - chi.x) + (float)ox * fp) + (l.x - clo.x);
+      const float sy = ((h.y - chi.y) + (float)oy * fp) + (l.y - clo.y);
+      const float sz = ((h.z - chi.z) + (float)oz * fp) + (l.z - clo.z);
+      d4[0] = make_float4(sx, sy, sz, h.w);
+      d4[1] = make_float4(l.w, q1.z, q0.x, q0.y);
+      d4[2] = make_float4(q0.z, q0.w, q1.x, q1.y);
+    } else {
+      const float4* p = static_cast<const float4*>(a.src) + kPartPackF4 * idx;
+      const float4 h = __ldg(p), l = __ldg(p + 1);
+      const float sx = ((h.x - chi.x) + (float)ox * fp) + (l.x - clo.x);
+      const float sy = ((h.y - chi.y) + (float)oy * fp) + (l.y - clo.y);
+      const float sz = ((h.z - chi.z) + (float)oz * fp) + (l.z - clo.z);
+      d4[0] = make_float4(sx, sy, sz, h.w);
+      d4[1] = make_float4(l.w, 0.f, 0.f, 0.f);
+    }
+  }
+}
+
+template <int FORM, bool CELL>
+__global__ void __launch_bounds__(kThreads, 2) list_kernel(const ListArgs a) {
+  using T = typename FormT<FORM>::T;
+  using A = typename FormT<FORM>::A;
+  constexpr int RW = CELL ? 12 : 8;  // record width in T, multiple of 4
+  __shared__ __align__(16) T stage[kWarps][32 * RW];
+  __shared__ A red[kWarps][5][32];
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  T* st = stage[warp];
+
+  for (;;) {
+    int b = 0;
+    if (lane == 0) b = (int)atomicAdd(a.queue, 1u);
+    b = __shfl_sync(kFull, b, 0);
+    if (b >= a.n_buckets) break;
+    const int e_begin = max(__ldg(a.markers + b), 0);
+    const int e_end = (int)min((long long)__ldg(a.markers + b + 1), a.n_entries);  // memory safety
+    const long long tbase = __ldg(a.starts + b);
+    const int n = __ldg(a.sizes + b);
+    if (n <= 0 || tbase < 0 || tbase + n > a.n_tgt) continue;  // memory safety
+
+    float3 chi = make_float3(0.f, 0.f, 0.f), clo = chi;
+    if constexpr (FORM == kMix) {
+      const float4* tp = static_cast<const float4*>(a.tgt) + kPartPackF4 * tbase;
+      const float4 h = __ldg(tp), l = __ldg(tp + 1);
+      chi = make_float3(h.x, h.y, h.z);
+      clo = make_float3(l.x, l.y, l.z);
+    }
+
+    for (int t0 = 0; t0 < n; t0 += 32) {
+      const int nt = min(32, n - t0);
+      const int G = 32 / nt;
+      const int g = lane / nt;
+      const int t = lane - g * nt;
+      const bool active = g < G;
+      const long long ti = tbase + t0 + t;
+
+      T tx, ty, tz, tsoft, tmass;
+      if constexpr (FORM == kF32) {
+        const CompactPartData* p = static_cast<const CompactPartData*>(a.tgt) + ti;
+        tmass = __ldg(&p->mass);
+        tsoft = __ldg(&p->soft);
+        tx = __ldg(&p->position.x);
+        ty = __ldg(&p->position.y);
+        tz = __ldg(&p->position.z);
+      } else if constexpr (FORM == kF64) {
+        const double* p = static_cast<const double*>(a.tgt) + 5 * ti;
+        tmass = __ldg(p);
+        tsoft = __ldg(p + 1);
+        tx = __ldg(p + 2);
+        ty = __ldg(p + 3);
+        tz = __ldg(p + 4);
+      } else {
+        const float4* p = static_cast<const float4*>(a.tgt) + kPartPackF4 * ti;
+        const float4 h = __ldg(p), l = __ldg(p + 1);
+        tx = (h.x - chi.x) + (l.x - clo.x);
+        ty = (h.y - chi.y) + (l.y - clo.y);
+        tz = (h.z - chi.z) + (l.z - clo.z);
+        tmass = h.w;
+        tsoft = l.w;
+      }
+
+      /* running totals: plain for kF32/kF64, Kahan pairs for kMix */
+      T sx = 0, sy = 0, sz = 0, sp = 0, idt2 = 0;
+      float cx = 0.f, cy = 0.f, cz = 0.f, cp = 0.f;
+
+      for (int e0 = e_begin; e0 < e_end; e0 += 32) {
+        const int ne = min(32, e_end - e0);
+        if (lane < ne) stage_entry<FORM, CELL>(a, e0 + lane, chi, clo, st + lane * RW);
+        __syncwarp();
+        if (active) {
+          Acc<T> acc{T(0), T(0), T(0), T(0), idt2};
+#pragma unroll 4
+          for (int k = g; k < ne; k += G) {
+            if constexpr (CELL) pc_interact<T>(st + k * RW, tx, ty, tz, tsoft, tmass, acc);
+            else pp_interact<T>(st + k * RW, tx, ty, tz, tsoft, tmass, acc);
+          }
+          idt2 = acc.idt2;
+          if constexpr (FORM == kMix) {
+            kahan_add(sx, cx, acc.ax);
+            kahan_add(sy, cy, acc.ay);
+            kahan_add(sz, cz, acc.az);
+            kahan_add(sp, cp, acc.pot);
+          } else {
+            sx += acc.ax;
+            sy += acc.ay;
+            sz += acc.az;
+            sp += acc.pot;
+          }
+        }
+        __syncwarp();
+      }
+
+      if (active) {
+        if constexpr (FORM == kMix) {
+          red[warp][0][lane] = (double)sx - (double)cx;
+          red[warp][1][lane] = (double)sy - (double)cy;
+          red[warp][2][lane] = (double)sz - (double)cz;
+          red[warp][3][lane] = (double)sp - (double)cp;
+        } else {
+          red[warp][0][lane] = sx;
+          red[warp][1][lane] = sy;
+          red[warp][2][lane] = sz;
+          red[warp][3][lane] = sp;
+        }
+        red[warp][4][lane] = (A)idt2;
+      }
+      __syncwarp();
+      if (lane < nt) {
+        A rx = 0, ry = 0, rz = 0, rp = 0, ri = 0;
+        for (int gg = 0; gg < G; ++gg) {
+          const int l = gg * nt + lane;
+          rx += red[warp][0][l];
+          ry += red[warp][1][l];
+          rz += red[warp][2][l];
+          rp += red[warp][3][l];
+          ri = max_t(ri, red[warp][4][l]);
+        }
+        const long long to = tbase + t0 + lane;
+        if constexpr (FORM == kF32) {
+          VariablePartData* v = static_cast<VariablePartData*>(a.vars) + to;
+          v->a.x += rx;
+          v->a.y += ry;
+          v->a.z += rz;
+          v->potential += rp;
+          v->dtGrav = fmaxf(ri, v->dtGrav);
+        } else {
+          double* v = static_cast<double*>(a.vars) + 5 * to;
+          v[0] += rx;
+          v[1] += ry;
+          v[2] += rz;
+          v[3] += rp;
+          v[4] = fmax(ri, v[4]);
+        }
+      }
+      __syncwarp();
+    }
+  }
+}
+
+__global__ void pack_cells_kernel(const double* __restrict__ m, long long n, float4* __restrict__ out) {
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
+       i += (long long)gridDim.x * blockDim.x) {
+    const double* r = m + 12 * i;
+    const double x = r[3], y = r[4], z = r[5];
+    const float hx = (float)x, hy = (float)y, hz = (float)z;
+    out[4 * i + 0] = make_float4(hx, hy, hz, (float)r[2]);
+    out[4 * i + 1] = make_float4((float)(x - (double)hx), (float)(y - (double)hy),
+                                 (float)(z - (double)hz), (float)r[1]);
+    out[4 * i + 2] = make_float4((float)r[6], (float)r[7], (float)r[8], (float)r[9]);
+    out[4 * i + 3] = make_float4((float)r[10], (float)r[11], (float)(0.5 * (r[6] + r[9] + r[11])), 0.f);
+  }
+}
+
+__global__ void pack_parts_kernel(const double* __restrict__ p, long long n, float4* __restrict__ out) {
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
+       i += (long long)gridDim.x * blockDim.x) {
+    const double* r = p + 5 * i;
+    const double x = r[2], y = r[3], z = r[4];
+    const float hx = (float)x, hy = (float)y, hz = (float)z;
+    out[2 * i + 0] = make_float4(hx, hy, hz, (float)r[0]);
+    out[2 * i + 1] = make_float4((float)(x - (double)hx), (float)(y - (double)hy),
+                                 (float)(z - (double)hz), (float)r[1]);
+  }
+}
+
+template <int FORM, bool CELL>
+int blocks_per_sm() {
+  static int cached = 0;
+  if (!cached) {
+    int nb = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, list_kernel<FORM, CELL>, kThreads, 0) !=
+            cudaSuccess ||
+        nb < 1)
+      nb = 1;
+    cached = nb;
+  }
+  return cached;
+}
+
+template <int FORM, bool CELL>
+cudaError_t launch_t(const ListArgs& a, cudaStream_t s) {
+  if (a.n_buckets <= 0) return cudaSuccess;
+  long long want = ((long long)a.n_buckets + kWarps - 1) / kWarps;
+  long long cap = (long long)sm_count() * blocks_per_sm<FORM, CELL>();
+  int grid = (int)(want < cap ? want : cap);
+  list_kernel<FORM, CELL><<<grid, kThreads, 0, s>>>(a);
+  count_launch();
+  return cudaGetLastError();
+}
+
+}  // namespace
+
+cudaError_t launch_list(int form, bool cell, const ListArgs& a, cudaStream_t s) {
+  switch (form) {
+    case kF32: return cell ? launch_t<kF32, true>(a, s) : launch_t<kF32, false>(a, s);
+    case kF64: return cell ? launch_t<kF64, true>(a, s) : launch_t<kF64, false>(a, s);
+    case kMix: return cell ? launch_t<kMix, true>(a, s) : launch_t<kMix, false>(a, s);
+  }
+  return cudaErrorInvalidValue;
+}
+
+static int grid_for(long long n, int threads) {
+  long long g = (n + threads - 1) / threads;
+  long long cap = (long long)sm_count() * 8;
+  if (g > cap) g = cap;
+  return g < 1 ? 1 : (int)g;
+}
+
+cudaError_t launch_pack_cells(const double* moments, long long n, float4* out, cudaStream_t s) {
+  if (n <= 0) return cudaSuccess;
+  pack_cells_kernel<<<grid_for(n, 256), 256, 0, s>>>(moments, n, out);
+  count_launch();
+  return cudaGetLastError();
+}
+
+cudaError_t launch_pack_parts(const double* parts, long long n, float4* out, cudaStream_t s) {
+  if (n <= 0) return cudaSuccess;
+  pack_parts_kernel<<<grid_for(n, 256), 256, 0, s>>>(parts, n, out);
+  count_launch();
+  return cudaGetLastError();
+}
+
+}  // namespace chg

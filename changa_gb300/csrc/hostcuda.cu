@@ -1,0 +1,803 @@
+/*
+ * C-ABI entry layer of the gravity library.
+ *
+ * Implements the drop-in boundary declared in include/HostCUDA.h and
+ * include/EwaldCUDA.h (reference: HostCUDA.cu:66-630, 1887-1956) and the
+ * extension forms in include/changa_gb300.h.
+ *
+ * Per request the reference does cudaMalloc + four H2D copies + kernel +
+ * cudaFree (HostCUDA.cu:578-613), and cudaFree synchronises the device.
+ * Here one stream-ordered allocation holds the request's list, markers,
+ * starts, sizes and the kernel's work-queue counter; it is released with
+ * cudaFreeAsync on the same stream, so an entry point never blocks the host
+ * or other streams.  Source-array bounds for the kernels' index guards come
+ * from cuMemGetAddressRange on the device pointer the request names.
+ */
+#include <atomic>
+#include <climits>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <mutex>
+#include <unordered_map>
+
+#include <cuda.h>
+
+#include "chg_internal.h"
+
+namespace chg {
+
+static std::atomic<int> g_error_mode{CHANGA_ERRORS_ABORT};
+static std::atomic<int> g_last_error{0};
+static std::atomic<int> g_validate{0};
+static std::atomic<unsigned long long> g_launches{0};
+static std::atomic<changa_completion_hook> g_hook{nullptr};
+
+int record_error(int code, const char* what, const char* file, int line) {
+  if (code == 0) return 0;
+  int expected = 0;
+  g_last_error.compare_exchange_strong(expected, code);
+  if (g_error_mode.load() == CHANGA_ERRORS_ABORT) {
+    fprintf(stderr, "changa_gb300: fatal error %d (%s) at %s:%d from '%s'\n", code,
+            changa_gb300_error_string(code), file, line, what);
+    abort();
+  }
+  return code;
+}
+
+void count_launch(unsigned n) { g_launches.fetch_add(n); }
+
+int sm_count() {
+  static int cached[64] = {0};
+  int dev = 0;
+  cudaGetDevice(&dev);
+  if (dev < 0 || dev >= 64) dev = 0;
+  if (!cached[dev]) {
+    int n = 0;
+    if (cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || n < 1)
+      n = 1;
+    cached[dev] = n;
+  }
+  return cached[dev];
+}
+
+/* Keeps memory freed with cudaFreeAsync cached in the default pool so
+ * per-request allocations do not return to the OS at every synchronise
+ * (a process-local pool attribute). */
+static void prepare_pool() {
+  static bool done[64] = {false};
+  static std::mutex mu;
+  int dev = 0;
+  cudaGetDevice(&dev);
+  if (dev < 0 || dev >= 64) return;
+  std::lock_guard<std::mutex> lk(mu);
+  if (done[dev]) return;
+  cudaMemPool_t pool;
+  if (cudaDeviceGetDefaultMemPool(&pool, dev) == cudaSuccess) {
+    uint64_t thr = UINT64_MAX;
+    cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &thr);
+  }
+  done[dev] = true;
+}
+
+/* Elements of size elem from p to the end of its allocation; LLONG_MAX
+ * when the range cannot be determined. */
+/* cuMemGetAddressRange, resolved through the runtime so the library loads
+ * (and its symbols can be inspected) on machines without a driver. */
+typedef CUresult (*AddrRangeFn)(CUdeviceptr*, size_t*, CUdeviceptr);
+static AddrRangeFn addr_range_fn() {
+  static std::atomic<int> state{0};
+  static AddrRangeFn fn = nullptr;
+  if (state.load() == 0) {
+    void* f = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuMemGetAddressRange", &f, 12000, cudaEnableDefault, &q) ==
+            cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      fn = (AddrRangeFn)f;
+    else
+      cudaGetLastError();
+    state.store(1);
+  }
+  return fn;
+}
+
+static long long elems_to_end(const void* p, size_t elem) {
+  if (!p) return 0;
+  CUdeviceptr base = 0;
+  size_t size = 0;
+  AddrRangeFn fn = addr_range_fn();
+  if (!fn || fn(&base, &size, (CUdeviceptr)p) != CUDA_SUCCESS) return LLONG_MAX;
+  size_t off = (size_t)((CUdeviceptr)p - base);
+  if (off > size) return 0;
+  return (long long)((size - off) / elem);
+}
+
+static void signal(cudaStream_t s, void* cb) {
+  changa_completion_hook h = g_hook.load();
+  if (h) h(s, cb);
+}
+
+static size_t align256(size_t x) { return (x + 255) & ~(size_t)255; }
+
+/* Device copy of one request (list, markers, starts, sizes, queue). */
+struct ReqDev {
+  char* block = nullptr;
+  int2* list = nullptr;
+  int* markers = nullptr;
+  int* starts = nullptr;
+  int* sizes = nullptr;
+  unsigned int* queue = nullptr;
+  cudaStream_t stream = 0;
+};
+
+static int upload_request(const void* h_list, long long n_entries, const int* h_markers,
+                          const int* h_starts, const int* h_sizes, int n_buckets, cudaStream_t s,
+                          ReqDev& d) {
+  prepare_pool();
+  size_t lb = align256((size_t)(n_entries > 0 ? n_entries : 0) * sizeof(ILCell));
+  size_t mb = align256((size_t)(n_buckets + 1) * sizeof(int));
+  size_t sb = align256((size_t)(n_buckets > 0 ? n_buckets : 0) * sizeof(int));
+  size_t total = lb + mb + 2 * sb + 256;
+  CHG_CUDA(cudaMallocAsync((void**)&d.block, total, s));
+  d.stream = s;
+  d.list = (int2*)d.block;
+  d.markers = (int*)(d.block + lb);
+  d.starts = (int*)(d.block + lb + mb);
+  d.sizes = (int*)(d.block + lb + mb + sb);
+  d.queue = (unsigned int*)(d.block + lb + mb + 2 * sb);
+  if (n_entries > 0)
+    CHG_CUDA(cudaMemcpyAsync(d.list, h_list, (size_t)n_entries * sizeof(ILCell),
+                             cudaMemcpyHostToDevice, s));
+  CHG_CUDA(cudaMemcpyAsync(d.markers, h_markers, (size_t)(n_buckets + 1) * sizeof(int),
+                           cudaMemcpyHostToDevice, s));
+  if (n_buckets > 0) {
+    CHG_CUDA(cudaMemcpyAsync(d.starts, h_starts, (size_t)n_buckets * sizeof(int),
+                             cudaMemcpyHostToDevice, s));
+    CHG_CUDA(cudaMemcpyAsync(d.sizes, h_sizes, (size_t)n_buckets * sizeof(int),
+                             cudaMemcpyHostToDevice, s));
+  }
+  CHG_CUDA(cudaMemsetAsync(d.queue, 0, sizeof(unsigned int), s));
+  return 0;
+}
+
+static int release_request(ReqDev& d) {
+  if (d.block) CHG_CUDA(cudaFreeAsync(d.block, d.stream));
+  d.block = nullptr;
+  return 0;
+}
+
+/* Drop-in request: cell lists when cell, particle lists otherwise. */
+static int run_request(CudaRequest* r, bool cell, const void* sources, long long n_src) {
+  if (!r) return record_error(CHANGA_E_INVALID_ARG, "NULL request", __FILE__, __LINE__);
+  int nb = r->numBucketsPlusOne - 1;
+  if (nb <= 0) {
+    signal(r->stream, r->cb);
+    return 0;
+  }
+  if (!r->list || !r->bucketMarkers || !r->bucketStarts || !r->bucketSizes || !r->d_localParts ||
+      !r->d_localVars || !sources)
+    return record_error(CHANGA_E_INVALID_ARG, "request pointers", __FILE__, __LINE__);
+  /* moments are read as float4 triples: 16-byte alignment is required */
+  if (cell && ((uintptr_t)sources & 15))
+    return record_error(CHANGA_E_INVALID_ARG, "moments not 16-byte aligned", __FILE__, __LINE__);
+  long long n_tgt = elems_to_end(r->d_localParts, sizeof(CompactPartData));
+  long long n_var = elems_to_end(r->d_localVars, sizeof(VariablePartData));
+  if (n_var < n_tgt) n_tgt = n_var;
+  if (g_validate.load()) {
+    int rc = changa_validate_request((const ILCell*)r->list, r->numInteractions, r->bucketMarkers,
+                                     r->bucketStarts, r->bucketSizes, nb, n_src, n_tgt);
+    if (rc) return record_error(rc, "request validation", __FILE__, __LINE__);
+  }
+  ReqDev d;
+  int rc = upload_request(r->list, r->numInteractions, r->bucketMarkers, r->bucketStarts,
+                          r->bucketSizes, nb, r->stream, d);
+  if (rc) return rc;
+  ListArgs a;
+  a.src = sources;
+  a.n_src = n_src;
+  a.tgt = r->d_localParts;
+  a.n_tgt = n_tgt;
+  a.vars = r->d_localVars;
+  a.list = d.list;
+  a.n_entries = r->numInteractions;
+  a.markers = d.markers;
+  a.starts = d.starts;
+  a.sizes = d.sizes;
+  a.n_buckets = nb;
+  a.fperiod_f = r->fperiod;
+  a.fperiod_d = r->fperiod;
+  a.queue = d.queue;
+  CHG_CUDA(launch_list(kF32, cell, a, r->stream));
+  rc = release_request(d);
+  if (rc) return rc;
+  signal(r->stream, r->cb);
+  return 0;
+}
+
+/* Stream recorded by TreePieceDataTransferBasic for its Cleanup. */
+static std::mutex g_basic_mu;
+static std::unordered_map<void*, cudaStream_t> g_basic_streams;
+
+}  // namespace chg
+
+using namespace chg;
+
+/* ------------------------------------------------------------------ */
+/* implementations shared by the C names and the C++-mangled names     */
+/* ------------------------------------------------------------------ */
+
+extern "C" {
+
+void chg_impl_allocatePinnedHostMemory(void** ptr, size_t size) {
+  if (!ptr) return;
+  if (size == 0) {
+    *ptr = nullptr;
+    record_error(CHANGA_E_INVALID_ARG, "allocatePinnedHostMemory(size 0)", __FILE__, __LINE__);
+    return;
+  }
+  cudaError_t e = cudaMallocHost(ptr, size);
+  if (e != cudaSuccess) {
+    *ptr = nullptr;
+    record_error((int)e, "cudaMallocHost", __FILE__, __LINE__);
+  }
+}
+
+void chg_impl_freePinnedHostMemory(void* ptr) {
+  if (!ptr) {
+    record_error(CHANGA_E_INVALID_ARG, "freePinnedHostMemory(NULL)", __FILE__, __LINE__);
+    return;
+  }
+  cudaError_t e = cudaFreeHost(ptr);
+  if (e != cudaSuccess) record_error((int)e, "cudaFreeHost", __FILE__, __LINE__);
+}
+
+static int transfer_local_tree(void* moments, size_t sMoments, void* compactParts,
+                               size_t sCompactParts, void* varParts, size_t sVarParts,
+                               void** d_localMoments, void** d_compactParts, void** d_varParts,
+                               cudaStream_t stream, int numParticles, void* callback) {
+  if (!d_localMoments || !d_compactParts || !d_varParts)
+    return record_error(CHANGA_E_INVALID_ARG, "DataManagerTransferLocalTree", __FILE__, __LINE__);
+  if ((size_t)numParticles * sizeof(VariablePartData) > sVarParts)
+    return record_error(CHANGA_E_INVALID_ARG, "numParticles > sVarParts", __FILE__, __LINE__);
+  CHG_CUDA(cudaMalloc(d_localMoments, sMoments));
+  CHG_CUDA(cudaMalloc(d_compactParts, sCompactParts));
+  CHG_CUDA(cudaMalloc(d_varParts, sVarParts));
+  if (sMoments)
+    CHG_CUDA(cudaMemcpyAsync(*d_localMoments, moments, sMoments, cudaMemcpyHostToDevice, stream));
+  if (sCompactParts)
+    CHG_CUDA(cudaMemcpyAsync(*d_compactParts, compactParts, sCompactParts, cudaMemcpyHostToDevice,
+                             stream));
+  if (sVarParts)
+    CHG_CUDA(cudaMemcpyAsync(*d_varParts, varParts, sVarParts, cudaMemcpyHostToDevice, stream));
+  /* ZeroVars (HostCUDA.cu:2195-2205): all-zero bits are 0.0f */
+  if (numParticles > 0)
+    CHG_CUDA(cudaMemsetAsync(*d_varParts, 0, (size_t)numParticles * sizeof(VariablePartData),
+                             stream));
+  signal(stream, callback);
+  return 0;
+}
+
+void chg_impl_DataManagerTransferLocalTree(void* moments, size_t sMoments, void* compactParts,
+                                           size_t sCompactParts, void* varParts, size_t sVarParts,
+                                           void** d_localMoments, void** d_compactParts,
+                                           void** d_varParts, cudaStream_t stream,
+                                           int numParticles, void* callback) {
+  transfer_local_tree(moments, sMoments, compactParts, sCompactParts, varParts, sVarParts,
+                      d_localMoments, d_compactParts, d_varParts, stream, numParticles, callback);
+}
+
+static int transfer_remote_chunk(void* moments, size_t sMoments, void* compactParts,
+                                 size_t sCompactParts, void** d_remoteMoments,
+                                 void** d_remoteParts, cudaStream_t stream, void* callback) {
+  if (!d_remoteMoments || !d_remoteParts)
+    return record_error(CHANGA_E_INVALID_ARG, "DataManagerTransferRemoteChunk", __FILE__, __LINE__);
+  CHG_CUDA(cudaMalloc(d_remoteMoments, sMoments));
+  CHG_CUDA(cudaMalloc(d_remoteParts, sCompactParts));
+  if (sMoments)
+    CHG_CUDA(cudaMemcpyAsync(*d_remoteMoments, moments, sMoments, cudaMemcpyHostToDevice, stream));
+  if (sCompactParts)
+    CHG_CUDA(cudaMemcpyAsync(*d_remoteParts, compactParts, sCompactParts, cudaMemcpyHostToDevice,
+                             stream));
+  signal(stream, callback);
+  return 0;
+}
+
+void chg_impl_DataManagerTransferRemoteChunk(void* moments, size_t sMoments, void* compactParts,
+                                             size_t sCompactParts, void** d_remoteMoments,
+                                             void** d_remoteParts, cudaStream_t stream,
+                                             void* callback) {
+  transfer_remote_chunk(moments, sMoments, compactParts, sCompactParts, d_remoteMoments,
+                        d_remoteParts, stream, callback);
+}
+
+void chg_impl_TransferParticleVarsBack(VariablePartData* hostBuffer, size_t size,
+                                       void* d_varParts, cudaStream_t stream, void* cb) {
+  if (size) {
+    cudaError_t e = cudaMemcpyAsync(hostBuffer, d_varParts, size, cudaMemcpyDeviceToHost, stream);
+    if (e != cudaSuccess) {
+      record_error((int)e, "TransferParticleVarsBack", __FILE__, __LINE__);
+      return;
+    }
+  }
+  signal(stream, cb);
+}
+
+void chg_impl_TreePieceCellListDataTransferLocal(CudaRequest* d) {
+  if (!d) {
+    record_error(CHANGA_E_INVALID_ARG, "NULL request", __FILE__, __LINE__);
+    return;
+  }
+  run_request(d, true, d->d_localMoments,
+              elems_to_end(d->d_localMoments, sizeof(CudaMultipoleMoments)));
+}
+
+void chg_impl_TreePieceCellListDataTransferRemote(CudaRequest* d) {
+  if (!d) {
+    record_error(CHANGA_E_INVALID_ARG, "NULL request", __FILE__, __LINE__);
+    return;
+  }
+  run_request(d, true, d->d_remoteMoments,
+              elems_to_end(d->d_remoteMoments, sizeof(CudaMultipoleMoments)));
+}
+
+/* Missed nodes/particles travel with the request (HostCUDA.cu:296-341). */
+static void run_resume(CudaRequest* d, bool cell) {
+  if (!d) {
+    record_error(CHANGA_E_INVALID_ARG, "NULL request", __FILE__, __LINE__);
+    return;
+  }
+  const void* host = cell ? d->missedNodes : d->missedParts;
+  if (d->numBucketsPlusOne <= 1) {
+    signal(d->stream, d->cb);
+    return;
+  }
+  if (!host || d->sMissed == 0) {
+    record_error(CHANGA_E_INVALID_ARG, "resume request without missed data", __FILE__, __LINE__);
+    return;
+  }
+  prepare_pool();
+  void* dev = nullptr;
+  cudaError_t e = cudaMallocAsync(&dev, d->sMissed, d->stream);
+  if (e != cudaSuccess) {
+    record_error((int)e, "cudaMallocAsync(missed)", __FILE__, __LINE__);
+    return;
+  }
+  e = cudaMemcpyAsync(dev, host, d->sMissed, cudaMemcpyHostToDevice, d->stream);
+  if (e != cudaSuccess) {
+    record_error((int)e, "cudaMemcpyAsync(missed)", __FILE__, __LINE__);
+    return;
+  }
+  long long n = (long long)(d->sMissed / (cell ? sizeof(CudaMultipoleMoments) : sizeof(CompactPartData)));
+  int rc = run_request(d, cell, dev, n);
+  e = cudaFreeAsync(dev, d->stream);
+  if (!rc && e != cudaSuccess) record_error((int)e, "cudaFreeAsync(missed)", __FILE__, __LINE__);
+}
+
+void chg_impl_TreePieceCellListDataTransferRemoteResume(CudaRequest* d) { run_resume(d, true); }
+
+void chg_impl_TreePiecePartListDataTransferLocal(CudaRequest* d) {
+  if (!d) {
+    record_error(CHANGA_E_INVALID_ARG, "NULL request", __FILE__, __LINE__);
+    return;
+  }
+  run_request(d, false, d->d_localParts, elems_to_end(d->d_localParts, sizeof(CompactPartData)));
+}
+
+void chg_impl_TreePiecePartListDataTransferLocalSmallPhase(CudaRequest* d, CompactPartData* parts,
+                                                           int len) {
+  if (!d) {
+    record_error(CHANGA_E_INVALID_ARG, "NULL request", __FILE__, __LINE__);
+    return;
+  }
+  if (d->numBucketsPlusOne <= 1) {
+    signal(d->stream, d->cb);
+    return;
+  }
+  if (!parts || len <= 0) {
+    record_error(CHANGA_E_INVALID_ARG, "small-phase particles", __FILE__, __LINE__);
+    return;
+  }
+  prepare_pool();
+  size_t bytes = (size_t)len * sizeof(CompactPartData);
+  void* dev = nullptr;
+  cudaError_t e = cudaMallocAsync(&dev, bytes, d->stream);
+  if (e != cudaSuccess) {
+    record_error((int)e, "cudaMallocAsync(small phase)", __FILE__, __LINE__);
+    return;
+  }
+  e = cudaMemcpyAsync(dev, parts, bytes, cudaMemcpyHostToDevice, d->stream);
+  if (e != cudaSuccess) {
+    record_error((int)e, "cudaMemcpyAsync(small phase)", __FILE__, __LINE__);
+    return;
+  }
+  int rc = run_request(d, false, dev, len);
+  e = cudaFreeAsync(dev, d->stream);
+  if (!rc && e != cudaSuccess) record_error((int)e, "cudaFreeAsync(small phase)", __FILE__, __LINE__);
+}
+
+void chg_impl_TreePiecePartListDataTransferRemote(CudaRequest* d) {
+  if (!d) {
+    record_error(CHANGA_E_INVALID_ARG, "NULL request", __FILE__, __LINE__);
+    return;
+  }
+  run_request(d, false, d->d_remoteParts, elems_to_end(d->d_remoteParts, sizeof(CompactPartData)));
+}
+
+void chg_impl_TreePiecePartListDataTransferRemoteResume(CudaRequest* d) { run_resume(d, false); }
+
+void chg_impl_TreePieceDataTransferBasic(CudaRequest* data, CudaDevPtr* ptr) {
+  if (!data || !ptr) {
+    record_error(CHANGA_E_INVALID_ARG, "TreePieceDataTransferBasic", __FILE__, __LINE__);
+    return;
+  }
+  int nb = data->numBucketsPlusOne - 1;
+  ReqDev d;
+  if (upload_request(data->list, data->numInteractions, data->bucketMarkers, data->bucketStarts,
+                     data->bucketSizes, nb < 0 ? 0 : nb, data->stream, d))
+    return;
+  ptr->d_list = d.list;
+  ptr->d_bucketMarkers = d.markers;
+  ptr->d_bucketStarts = d.starts;
+  ptr->d_bucketSizes = d.sizes;
+  std::lock_guard<std::mutex> lk(g_basic_mu);
+  g_basic_streams[d.block] = data->stream;
+}
+
+void chg_impl_TreePieceDataTransferBasicCleanup(CudaDevPtr* ptr) {
+  if (!ptr || !ptr->d_list) return;
+  cudaStream_t s = 0;
+  {
+    std::lock_guard<std::mutex> lk(g_basic_mu);
+    auto it = g_basic_streams.find(ptr->d_list);
+    if (it == g_basic_streams.end()) {
+      record_error(CHANGA_E_INVALID_ARG, "Cleanup of unknown block", __FILE__, __LINE__);
+      return;
+    }
+    s = it->second;
+    g_basic_streams.erase(it);
+  }
+  cudaError_t e = cudaFreeAsync(ptr->d_list, s);
+  if (e != cudaSuccess) record_error((int)e, "cudaFreeAsync(basic)", __FILE__, __LINE__);
+  ptr->d_list = nullptr;
+  ptr->d_bucketMarkers = ptr->d_bucketStarts = ptr->d_bucketSizes = nullptr;
+}
+
+void chg_impl_EwaldHostMemorySetup(EwaldData* h, int size, int nEwhLoop, int largephase) {
+  if (!h) return;
+  if (largephase) chg_impl_allocatePinnedHostMemory((void**)&h->EwaldMarkers, (size_t)size * sizeof(int));
+  else h->EwaldMarkers = nullptr;
+  chg_impl_allocatePinnedHostMemory((void**)&h->ewt, (size_t)nEwhLoop * sizeof(EwtData));
+  chg_impl_allocatePinnedHostMemory((void**)&h->cachedData, sizeof(EwaldReadOnlyData));
+}
+
+void chg_impl_EwaldHostMemoryFree(EwaldData* h, int largephase) {
+  if (!h) return;
+  if (largephase) chg_impl_freePinnedHostMemory(h->EwaldMarkers);
+  chg_impl_freePinnedHostMemory(h->ewt);
+  chg_impl_freePinnedHostMemory(h->cachedData);
+}
+
+void chg_impl_EwaldHost(CompactPartData* d_localParts, VariablePartData* d_localVars,
+                        EwaldData* h, cudaStream_t stream, void* cb, int myIndex, int largephase) {
+  (void)myIndex;
+  if (!h || !h->cachedData || (h->cachedData->nEwhLoop > 0 && !h->ewt)) {
+    record_error(CHANGA_E_INVALID_ARG, "EwaldHost", __FILE__, __LINE__);
+    return;
+  }
+  const EwaldReadOnlyData& ro = *h->cachedData;
+  if (ro.nEwhLoop > NEWH) {
+    record_error(CHANGA_E_TOO_LARGE, "EwaldHost: nEwhLoop > NEWH", __FILE__, __LINE__);
+    return;
+  }
+  int n = ro.n;
+  int* d_markers = nullptr;
+  if (largephase && n > 0) {
+    prepare_pool();
+    cudaError_t e = cudaMallocAsync((void**)&d_markers, (size_t)n * sizeof(int), stream);
+    if (e == cudaSuccess)
+      e = cudaMemcpyAsync(d_markers, h->EwaldMarkers, (size_t)n * sizeof(int),
+                          cudaMemcpyHostToDevice, stream);
+    if (e != cudaSuccess) {
+      record_error((int)e, "EwaldHost markers", __FILE__, __LINE__);
+      return;
+    }
+  }
+  int first = largephase ? 0 : h->EwaldRange[0];
+  int last = largephase ? n - 1 : h->EwaldRange[1];
+  cudaError_t e = launch_ewald_f32(d_localParts, d_localVars, d_markers, largephase, first, last,
+                                   ro, h->ewt, stream);
+  if (e != cudaSuccess) {
+    record_error((int)e, "EwaldKernel launch", __FILE__, __LINE__);
+    return;
+  }
+  if (d_markers) {
+    e = cudaFreeAsync(d_markers, stream);
+    if (e != cudaSuccess) {
+      record_error((int)e, "cudaFreeAsync(markers)", __FILE__, __LINE__);
+      return;
+    }
+  }
+  signal(stream, cb);
+}
+
+/* ---- public C names (include/HostCUDA.h, include/EwaldCUDA.h) ---- */
+
+void allocatePinnedHostMemory(void** p, size_t s) { chg_impl_allocatePinnedHostMemory(p, s); }
+void freePinnedHostMemory(void* p) { chg_impl_freePinnedHostMemory(p); }
+void DataManagerTransferLocalTree(void* a, size_t b, void* c, size_t d, void* e, size_t f, void** g,
+                                  void** h, void** i, cudaStream_t s, int n, void* cb) {
+  chg_impl_DataManagerTransferLocalTree(a, b, c, d, e, f, g, h, i, s, n, cb);
+}
+void DataManagerTransferRemoteChunk(void* a, size_t b, void* c, size_t d, void** e, void** f,
+                                    cudaStream_t s, void* cb) {
+  chg_impl_DataManagerTransferRemoteChunk(a, b, c, d, e, f, s, cb);
+}
+void TransferParticleVarsBack(VariablePartData* h, size_t n, void* d, cudaStream_t s, void* cb) {
+  chg_impl_TransferParticleVarsBack(h, n, d, s, cb);
+}
+void TreePieceCellListDataTransferLocal(CudaRequest* d) { chg_impl_TreePieceCellListDataTransferLocal(d); }
+void TreePieceCellListDataTransferRemote(CudaRequest* d) { chg_impl_TreePieceCellListDataTransferRemote(d); }
+void TreePieceCellListDataTransferRemoteResume(CudaRequest* d) {
+  chg_impl_TreePieceCellListDataTransferRemoteResume(d);
+}
+void TreePiecePartListDataTransferLocal(CudaRequest* d) { chg_impl_TreePiecePartListDataTransferLocal(d); }
+void TreePiecePartListDataTransferLocalSmallPhase(CudaRequest* d, CompactPartData* p, int n) {
+  chg_impl_TreePiecePartListDataTransferLocalSmallPhase(d, p, n);
+}
+void TreePiecePartListDataTransferRemote(CudaRequest* d) { chg_impl_TreePiecePartListDataTransferRemote(d); }
+void TreePiecePartListDataTransferRemoteResume(CudaRequest* d) {
+  chg_impl_TreePiecePartListDataTransferRemoteResume(d);
+}
+void TreePieceDataTransferBasic(CudaRequest* d, CudaDevPtr* p) { chg_impl_TreePieceDataTransferBasic(d, p); }
+void TreePieceDataTransferBasicCleanup(CudaDevPtr* p) { chg_impl_TreePieceDataTransferBasicCleanup(p); }
+void EwaldHostMemorySetup(EwaldData* h, int s, int n, int l) { chg_impl_EwaldHostMemorySetup(h, s, n, l); }
+void EwaldHostMemoryFree(EwaldData* h, int l) { chg_impl_EwaldHostMemoryFree(h, l); }
+void EwaldHost(CompactPartData* p, VariablePartData* v, EwaldData* h, cudaStream_t s, void* cb, int i,
+               int l) {
+  chg_impl_EwaldHost(p, v, h, s, cb, i, l);
+}
+
+/* ---- extension API (include/changa_gb300.h) ---- */
+
+void changa_gb300_set_error_mode(int mode) { g_error_mode.store(mode); }
+int changa_gb300_last_error(void) { return g_last_error.exchange(0); }
+const char* changa_gb300_error_string(int code) {
+  switch (code) {
+    case 0: return "no error";
+    case CHANGA_E_INVALID_ARG: return "invalid argument";
+    case CHANGA_E_INVALID_LIST: return "interaction list index or marker out of range";
+    case CHANGA_E_TOO_LARGE: return "size beyond a fixed limit";
+  }
+  return cudaGetErrorString((cudaError_t)code);
+}
+void changa_gb300_set_completion_hook(changa_completion_hook hook) { g_hook.store(hook); }
+void changa_gb300_set_validate(int on) { g_validate.store(on); }
+int changa_gb300_version(void) { return 100; }
+unsigned long long changa_gb300_kernel_launches(void) { return g_launches.load(); }
+
+int changa_validate_request(const ILCell* list, long long n_entries, const int* markers,
+                            const int* starts, const int* sizes, int n_buckets,
+                            long long n_sources, long long n_targets) {
+  if (n_buckets < 0 || n_entries < 0) return CHANGA_E_INVALID_ARG;
+  if (n_buckets == 0) return 0;
+  if (!markers || !starts || !sizes || (n_entries > 0 && !list)) return CHANGA_E_INVALID_ARG;
+  if (markers[0] < 0 || (long long)markers[n_buckets] > n_entries) return CHANGA_E_INVALID_LIST;
+  for (int b = 0; b < n_buckets; ++b) {
+    if (markers[b + 1] < markers[b]) return CHANGA_E_INVALID_LIST;
+    if (sizes[b] < 0 || starts[b] < 0) return CHANGA_E_INVALID_LIST;
+    if ((long long)starts[b] + sizes[b] > n_targets) return CHANGA_E_INVALID_LIST;
+  }
+  for (long long e = markers[0]; e < markers[n_buckets]; ++e) {
+    int idx = list[e].index;
+    if (idx < 0 || (long long)idx >= n_sources) return CHANGA_E_INVALID_LIST;
+    int code = list[e].offsetID >> 22;
+    if (code < 0 || code > 0x1ff) return CHANGA_E_INVALID_LIST;
+  }
+  return 0;
+}
+
+static int check_req(const ChangaListRequest* r) {
+  if (!r) return CHANGA_E_INVALID_ARG;
+  if (r->n_buckets < 0 || r->n_entries < 0) return CHANGA_E_INVALID_ARG;
+  if (r->n_buckets > 0 && (!r->markers || !r->starts || !r->sizes)) return CHANGA_E_INVALID_ARG;
+  if (r->n_entries > 0 && !r->list) return CHANGA_E_INVALID_ARG;
+  return 0;
+}
+
+/* One list evaluation over device-resident inputs (FP64 or mixed form). */
+static int run_fp(int form, bool cell, const void* src, long long n_src, const void* tgt,
+                  long long n_tgt, const ChangaListRequest* req, double fperiod, double* vars,
+                  cudaStream_t s, unsigned int* queue) {
+  ListArgs a;
+  a.src = src;
+  a.n_src = n_src;
+  a.tgt = tgt;
+  a.n_tgt = n_tgt;
+  a.vars = vars;
+  a.list = (const int2*)req->list;
+  a.n_entries = req->n_entries;
+  a.markers = req->markers;
+  a.starts = req->starts;
+  a.sizes = req->sizes;
+  a.n_buckets = req->n_buckets;
+  a.fperiod_f = (float)fperiod;
+  a.fperiod_d = fperiod;
+  a.queue = queue;
+  CHG_CUDA(cudaMemsetAsync(queue, 0, sizeof(unsigned int), s));
+  CHG_CUDA(launch_list(form, cell, a, s));
+  return 0;
+}
+
+static int forces_entry(int form, bool cell, const double* src, long long n_src,
+                        const double* tgt, long long n_tgt, const ChangaListRequest* req,
+                        double fperiod, double* vars, cudaStream_t s) {
+  int rc = check_req(req);
+  if (rc || !src || !tgt || !vars || n_src < 0 || n_tgt < 0)
+    return record_error(rc ? rc : CHANGA_E_INVALID_ARG, "forces: arguments", __FILE__, __LINE__);
+  if (req->n_buckets == 0) return 0;
+  prepare_pool();
+  size_t src_b = 0, tgt_b = 0;
+  if (form == kMix) {
+    src_b = align256((size_t)n_src * (cell ? kCellPackF4 : kPartPackF4) * sizeof(float4));
+    tgt_b = align256((size_t)n_tgt * kPartPackF4 * sizeof(float4));
+  }
+  char* block = nullptr;
+  CHG_CUDA(cudaMallocAsync((void**)&block, src_b + tgt_b + 256, s));
+  unsigned int* queue = (unsigned int*)(block + src_b + tgt_b);
+  const void* ksrc = src;
+  const void* ktgt = tgt;
+  if (form == kMix) {
+    float4* ps = (float4*)block;
+    float4* pt = (float4*)(block + src_b);
+    if (cell) CHG_CUDA(launch_pack_cells(src, n_src, ps, s));
+    else CHG_CUDA(launch_pack_parts(src, n_src, ps, s));
+    CHG_CUDA(launch_pack_parts(tgt, n_tgt, pt, s));
+    ksrc = ps;
+    ktgt = pt;
+  }
+  rc = run_fp(form, cell, ksrc, n_src, ktgt, n_tgt, req, fperiod, vars, s, queue);
+  if (rc) return rc;
+  CHG_CUDA(cudaFreeAsync(block, s));
+  return 0;
+}
+
+int changa_cell_forces_fp64(const double* moments, long long n_moments, const double* targets,
+                            long long n_targets, const ChangaListRequest* req, double fperiod,
+                            double* vars, cudaStream_t stream) {
+  return forces_entry(kF64, true, moments, n_moments, targets, n_targets, req, fperiod, vars, stream);
+}
+int changa_part_forces_fp64(const double* sources, long long n_sources, const double* targets,
+                            long long n_targets, const ChangaListRequest* req, double fperiod,
+                            double* vars, cudaStream_t stream) {
+  return forces_entry(kF64, false, sources, n_sources, targets, n_targets, req, fperiod, vars, stream);
+}
+int changa_cell_forces_mixed(const double* moments, long long n_moments, const double* targets,
+                             long long n_targets, const ChangaListRequest* req, double fperiod,
+                             double* vars, cudaStream_t stream) {
+  return forces_entry(kMix, true, moments, n_moments, targets, n_targets, req, fperiod, vars, stream);
+}
+int changa_part_forces_mixed(const double* sources, long long n_sources, const double* targets,
+                             long long n_targets, const ChangaListRequest* req, double fperiod,
+                             double* vars, cudaStream_t stream) {
+  return forces_entry(kMix, false, sources, n_sources, targets, n_targets, req, fperiod, vars, stream);
+}
+
+int changa_gravity_step(int form, const double* moments, long long n_moments, const double* parts,
+                        long long n_parts, const ChangaListRequest* cells,
+                        const ChangaListRequest* plist, double fperiod,
+                        const ChangaEwaldParams* ewald, double* vars, cudaStream_t s) {
+  if (form != CHANGA_FORM_FP64 && form != CHANGA_FORM_MIXED)
+    return record_error(CHANGA_E_INVALID_ARG, "gravity_step: form", __FILE__, __LINE__);
+  if (!moments || !parts || !vars || n_moments < 0 || n_parts < 0)
+    return record_error(CHANGA_E_INVALID_ARG, "gravity_step: arrays", __FILE__, __LINE__);
+  if ((cells && check_req(cells)) || (plist && check_req(plist)))
+    return record_error(CHANGA_E_INVALID_ARG, "gravity_step: requests", __FILE__, __LINE__);
+  const int f = form == CHANGA_FORM_FP64 ? kF64 : kMix;
+  prepare_pool();
+  size_t cb = 0, pb = 0;
+  if (f == kMix) {
+    cb = align256((size_t)n_moments * kCellPackF4 * sizeof(float4));
+    pb = align256((size_t)n_parts * kPartPackF4 * sizeof(float4));
+  }
+  char* block = nullptr;
+  CHG_CUDA(cudaMallocAsync((void**)&block, cb + pb + 512, s));
+  unsigned int* q = (unsigned int*)(block + cb + pb);
+  const void* ksrc = moments;
+  const void* kpart = parts;
+  if (f == kMix) {
+    CHG_CUDA(launch_pack_cells(moments, n_moments, (float4*)block, s));
+    CHG_CUDA(launch_pack_parts(parts, n_parts, (float4*)(block + cb), s));
+    ksrc = block;
+    kpart = block + cb;
+  }
+  int rc = 0;
+  if (cells && cells->n_buckets > 0)
+    rc = run_fp(f, true, ksrc, n_moments, kpart, n_parts, cells, fperiod, vars, s, q);
+  if (!rc && plist && plist->n_buckets > 0)
+    rc = run_fp(f, false, kpart, n_parts, kpart, n_parts, plist, fperiod, vars, s, q + 64);
+  if (!rc && ewald) {
+    cudaError_t e = launch_ewald_fp(f, parts, n_parts, nullptr, n_parts, *ewald, vars, s);
+    if (e != cudaSuccess) rc = record_error((int)e, "gravity_step: ewald", __FILE__, __LINE__);
+  }
+  cudaError_t e = cudaFreeAsync(block, s);
+  if (!rc && e != cudaSuccess) rc = record_error((int)e, "gravity_step: free", __FILE__, __LINE__);
+  return rc;
+}
+
+int changa_gravity_step_host(int form, const double* moments, long long n_moments,
+                             const double* parts, long long n_parts, const ChangaListRequest* cells,
+                             const ChangaListRequest* plist, double fperiod,
+                             const ChangaEwaldParams* ewald, double* vars, cudaStream_t s) {
+  if (!moments || !parts || !vars || n_moments < 0 || n_parts < 0)
+    return record_error(CHANGA_E_INVALID_ARG, "gravity_step_host: arrays", __FILE__, __LINE__);
+  if ((cells && check_req(cells)) || (plist && check_req(plist)))
+    return record_error(CHANGA_E_INVALID_ARG, "gravity_step_host: requests", __FILE__, __LINE__);
+  prepare_pool();
+  const ChangaListRequest* reqs[2] = {cells, plist};
+  size_t off[2][4], sz[2][4];
+  const size_t mb = align256((size_t)n_moments * 12 * sizeof(double));
+  const size_t pb = align256((size_t)n_parts * 5 * sizeof(double));
+  size_t total = mb + pb + pb;  // moments, parts, vars, then the requests
+  for (int k = 0; k < 2; ++k) {
+    const ChangaListRequest* r = reqs[k];
+    long long ne = r ? r->n_entries : 0;
+    int nb = r ? r->n_buckets : 0;
+    sz[k][0] = (size_t)ne * sizeof(ILCell);
+    sz[k][1] = (size_t)(nb + 1) * sizeof(int);
+    sz[k][2] = (size_t)nb * sizeof(int);
+    sz[k][3] = (size_t)nb * sizeof(int);
+    for (int j = 0; j < 4; ++j) {
+      off[k][j] = total;
+      total += align256(sz[k][j]);
+    }
+  }
+  char* block = nullptr;
+  CHG_CUDA(cudaMallocAsync((void**)&block, total, s));
+  double* d_mom = (double*)block;
+  double* d_parts = (double*)(block + mb);
+  double* d_vars = (double*)(block + mb + pb);
+  CHG_CUDA(cudaMemcpyAsync(d_mom, moments, (size_t)n_moments * 12 * sizeof(double),
+                           cudaMemcpyHostToDevice, s));
+  CHG_CUDA(cudaMemcpyAsync(d_parts, parts, (size_t)n_parts * 5 * sizeof(double),
+                           cudaMemcpyHostToDevice, s));
+  CHG_CUDA(cudaMemcpyAsync(d_vars, vars, (size_t)n_parts * 5 * sizeof(double),
+                           cudaMemcpyHostToDevice, s));
+  ChangaListRequest dreq[2];
+  for (int k = 0; k < 2; ++k) {
+    const ChangaListRequest* r = reqs[k];
+    dreq[k].list = (const ILCell*)(block + off[k][0]);
+    dreq[k].markers = (const int*)(block + off[k][1]);
+    dreq[k].starts = (const int*)(block + off[k][2]);
+    dreq[k].sizes = (const int*)(block + off[k][3]);
+    dreq[k].n_buckets = r ? r->n_buckets : 0;
+    dreq[k].n_entries = r ? r->n_entries : 0;
+    if (!r || r->n_buckets == 0) continue;
+    const void* src[4] = {r->list, r->markers, r->starts, r->sizes};
+    for (int j = 0; j < 4; ++j)
+      if (sz[k][j]) CHG_CUDA(cudaMemcpyAsync(block + off[k][j], src[j], sz[k][j], cudaMemcpyHostToDevice, s));
+  }
+  int rc = changa_gravity_step(form, d_mom, n_moments, d_parts, n_parts, cells ? &dreq[0] : nullptr,
+                               plist ? &dreq[1] : nullptr, fperiod, ewald, d_vars, s);
+  if (rc) return rc;
+  CHG_CUDA(cudaMemcpyAsync(vars, d_vars, (size_t)n_parts * 5 * sizeof(double),
+                           cudaMemcpyDeviceToHost, s));
+  CHG_CUDA(cudaFreeAsync(block, s));
+  CHG_CUDA(cudaStreamSynchronize(s));
+  return 0;
+}
+
+int changa_ewald_forces(int form, const double* parts, long long n_parts, const int* idx,
+                        long long n_idx, const ChangaEwaldParams* p, double* vars,
+                        cudaStream_t stream) {
+  if (!p || !parts || !vars || n_idx < 0 || (form != CHANGA_FORM_FP64 && form != CHANGA_FORM_MIXED))
+    return record_error(CHANGA_E_INVALID_ARG, "ewald_forces: arguments", __FILE__, __LINE__);
+  if (p->nEwhLoop > CHANGA_MAX_EWH)
+    return record_error(CHANGA_E_TOO_LARGE, "ewald_forces: nEwhLoop", __FILE__, __LINE__);
+  cudaError_t e = launch_ewald_fp(form == CHANGA_FORM_FP64 ? kF64 : kMix, parts, n_parts, idx,
+                                  n_idx, *p, vars, stream);
+  if (e != cudaSuccess) return record_error((int)e, "ewald_forces: launch", __FILE__, __LINE__);
+  return 0;
+}
+
+}  // extern "C"

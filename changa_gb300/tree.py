@@ -1,0 +1,176 @@
+"""Host side of the gravity path: tree, walk and the boundary arrays.
+
+``build_lists`` runs the native tree build and dual walk
+(changa_gb300/host/tree.cpp) and returns every array the GPU entry points
+consume, in the reference's layouts:
+
+* ``parts``     N x 5 FP64  {mass, soft, x, y, z} in bucket (key) order
+* ``moments``   M x 12 FP64 {radius, soft, totalMass, cm, xx..zz}, BFS order
+* ``cells``     the cell-list request: list (L x 2 int32 ILCell), markers,
+                starts, sizes, bucket ids (only buckets with a non-empty list)
+* ``plist``     the particle-list request, flattened to one ILCell per source
+                particle
+* ``perm``      GPU order -> caller order
+
+``interactions`` follows the reference's counter (Compute.cpp:1643-1651):
+sum over buckets of n_b (|cell list| + |particle list|).
+"""
+from __future__ import annotations
+
+import ctypes as C
+from dataclasses import dataclass, field
+
+import numpy as np
+
+from ._native import host_lib
+
+
+def _ptr(a):
+    return a.ctypes.data_as(C.c_void_p) if a is not None else None
+
+
+@dataclass
+class ListRequest:
+    list: np.ndarray      # (L, 2) int32
+    markers: np.ndarray   # (nb + 1,) int32
+    starts: np.ndarray    # (nb,) int32
+    sizes: np.ndarray     # (nb,) int32
+    bucket_ids: np.ndarray
+
+    @property
+    def n_buckets(self):
+        return int(len(self.starts))
+
+    @property
+    def n_entries(self):
+        return int(self.list.shape[0])
+
+    def interactions(self):
+        lens = np.diff(self.markers.astype(np.int64))
+        return int((lens * self.sizes.astype(np.int64)).sum())
+
+
+@dataclass
+class TreeLists:
+    n: int
+    parts: np.ndarray
+    moments: np.ndarray
+    root: np.ndarray
+    perm: np.ndarray
+    bucket_starts: np.ndarray
+    bucket_sizes: np.ndarray
+    bucket_bbox: np.ndarray
+    cells: ListRequest
+    plist: ListRequest
+    period: float
+    n_replicas: int
+    theta: float
+    n_bucket: int
+    meta: dict = field(default_factory=dict)
+
+    @property
+    def interactions(self):
+        return self.cells.interactions() + self.plist.interactions()
+
+    def abi_moments(self):
+        """CudaMultipoleMoments array (M x 12 float32)."""
+        return np.ascontiguousarray(self.moments, dtype=np.float32)
+
+    def abi_parts(self):
+        """CompactPartData array (N x 5 float32)."""
+        return np.ascontiguousarray(self.parts, dtype=np.float32)
+
+
+def _serialize(lib, h, kind, nb_total, lens):
+    n_entries = int(lens.sum())
+    filled = int((lens > 0).sum())
+    lst = np.empty((n_entries, 2), dtype=np.int32)
+    markers = np.empty(filled + 1, dtype=np.int32)
+    starts = np.empty(filled, dtype=np.int32)
+    sizes = np.empty(filled, dtype=np.int32)
+    ids = np.empty(filled, dtype=np.int32)
+    got = lib.chg_tree_serialize(h, kind, 0, nb_total, _ptr(lst), _ptr(markers), _ptr(starts),
+                                 _ptr(sizes), _ptr(ids), 0, 0)
+    assert got == filled
+    return ListRequest(lst, markers, starts, sizes, ids)
+
+
+def build_lists(pos, mass, soft, n_bucket=16, theta=0.7, period=0.0, n_replicas=0,
+                nthreads=0) -> TreeLists:
+    """Tree + walk + serialisation for one system (FP64 inputs)."""
+    lib = host_lib()
+    pos = np.ascontiguousarray(pos, dtype=np.float64)
+    mass = np.ascontiguousarray(mass, dtype=np.float64)
+    soft = np.ascontiguousarray(soft, dtype=np.float64)
+    n = pos.shape[0]
+    if n >= 2 ** 31 - 1:
+        raise ValueError("at most 2^31-2 particles per system")
+    if period and n_replicas == 0:
+        n_replicas = 1
+    h = lib.chg_tree_build(_ptr(pos), _ptr(mass), _ptr(soft), n, int(n_bucket), float(theta),
+                           float(period), int(n_replicas))
+    if not h:
+        raise ValueError("tree build rejected its arguments")
+    try:
+        perm = np.empty(n, dtype=np.int64)
+        lib.chg_tree_get_order(h, _ptr(perm))
+        nm = lib.chg_tree_num_moments(h)
+        moments = np.empty((nm, 12), dtype=np.float64)
+        lib.chg_tree_get_moments(h, _ptr(moments))
+        root = np.empty(12, dtype=np.float64)
+        lib.chg_tree_get_root(h, _ptr(root))
+        nb = lib.chg_tree_num_buckets(h)
+        bstarts = np.empty(nb, dtype=np.int32)
+        bsizes = np.empty(nb, dtype=np.int32)
+        bbox = np.empty((nb, 6), dtype=np.float64)
+        lib.chg_tree_get_buckets(h, _ptr(bstarts), _ptr(bsizes), _ptr(bbox), None)
+        lib.chg_tree_walk(h, int(nthreads))
+        nc = np.empty(nb, dtype=np.int64)
+        npl = np.empty(nb, dtype=np.int64)
+        lib.chg_tree_list_lengths(h, _ptr(nc), _ptr(npl))
+        cells = _serialize(lib, h, 0, nb, nc)
+        plist = _serialize(lib, h, 1, nb, npl)
+    finally:
+        lib.chg_tree_free(h)
+    parts = np.empty((n, 5), dtype=np.float64)
+    parts[:, 0] = mass[perm]
+    parts[:, 1] = soft[perm]
+    parts[:, 2:5] = pos[perm]
+    return TreeLists(n=n, parts=parts, moments=moments, root=root, perm=perm,
+                     bucket_starts=bstarts, bucket_sizes=bsizes, bucket_bbox=bbox,
+                     cells=cells, plist=plist, period=float(period), n_replicas=int(n_replicas),
+                     theta=float(theta), n_bucket=int(n_bucket))
+
+
+def concat_systems(systems):
+    """Concatenates independent systems into one set of arrays and one pair
+    of requests (indices and starts shifted), for one batched evaluation.
+    Returns (parts, moments, cells, plist, offsets)."""
+    parts = np.concatenate([s.parts for s in systems], axis=0)
+    moments = np.concatenate([s.moments for s in systems], axis=0)
+    p_off = np.cumsum([0] + [s.n for s in systems])
+    m_off = np.cumsum([0] + [s.moments.shape[0] for s in systems])
+
+    def cat(reqs, idx_off):
+        lists, markers, starts, sizes, ids = [], [np.zeros(1, np.int64)], [], [], []
+        base = 0
+        for k, r in enumerate(reqs):
+            l = r.list.copy()
+            l[:, 0] += idx_off[k]
+            lists.append(l)
+            markers.append(r.markers[1:].astype(np.int64) + base)
+            base += r.n_entries
+            starts.append(r.starts.astype(np.int64) + p_off[k])
+            sizes.append(r.sizes)
+            ids.append(r.bucket_ids)
+        mk = np.concatenate(markers)
+        if mk[-1] >= 2 ** 31:
+            raise ValueError("batched list exceeds int32 markers")
+        return ListRequest(np.concatenate(lists, axis=0).astype(np.int32), mk.astype(np.int32),
+                           np.concatenate(starts).astype(np.int32),
+                           np.concatenate(sizes).astype(np.int32),
+                           np.concatenate(ids).astype(np.int32))
+
+    cells = cat([s.cells for s in systems], m_off)
+    plist = cat([s.plist for s in systems], p_off)
+    return parts, moments, cells, plist, p_off

@@ -1,0 +1,150 @@
+/*
+ * Extension entry points of the GB300 gravity library.
+ *
+ * HostCUDA.h / EwaldCUDA.h carry the reference's FP32 boundary unchanged.
+ * The forms below have no counterpart there; they take FP64 inputs that
+ * live on the device and add:
+ *   - the plain FP64 form (all arithmetic FP64),
+ *   - the FP32-mixed form (positions split into a float high part and a
+ *     float low part, the bucket-centre subtraction done in that split
+ *     arithmetic, interactions in FP32, per-particle sums with Kahan
+ *     compensation, FP64 results),
+ *   - host helpers (Ewald h-table, request validation, error and completion
+ *     plumbing).
+ * All calls are asynchronous on the given stream and return 0 or a
+ * CHANGA_E_* / cudaError_t code.
+ *
+ * Array layouts (row-major FP64):
+ *   moments : 12 per node  {radius, soft, totalMass, cm.x, cm.y, cm.z,
+ *             xx, xy, xz, yy, yz, zz}        (CudaMultipoleMoments order)
+ *   parts   : 5 per particle {mass, soft, x, y, z} (CompactPartData order)
+ *   vars    : 5 per particle {a.x, a.y, a.z, potential, dtGrav}; results
+ *             accumulate (+=, max for dtGrav) like the reference kernels.
+ */
+#ifndef CHANGA_GB300_H_
+#define CHANGA_GB300_H_
+
+#include "HostCUDA.h"
+#include "EwaldCUDA.h"
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- errors, completion, validation ---- */
+
+#define CHANGA_E_INVALID_ARG 1001   /* bad pointer / size / count */
+#define CHANGA_E_INVALID_LIST 1002  /* list index or marker out of range */
+#define CHANGA_E_TOO_LARGE 1003     /* size beyond a fixed limit */
+
+#define CHANGA_ERRORS_ABORT 0   /* print and abort() (reference behaviour) */
+#define CHANGA_ERRORS_RECORD 1  /* record; read with changa_gb300_last_error */
+
+void changa_gb300_set_error_mode(int mode);
+/* Returns and clears the first error recorded since the last call (0: none). */
+int changa_gb300_last_error(void);
+const char *changa_gb300_error_string(int code);
+
+/* Called by every drop-in entry point after its work is enqueued; the
+ * stand-in for Charm++'s hapiAddCallback(stream, cb).  NULL (the default)
+ * ignores cb. */
+typedef void (*changa_completion_hook)(cudaStream_t stream, void *cb);
+void changa_gb300_set_completion_hook(changa_completion_hook hook);
+
+/* When on, the drop-in entry points check every list index, marker and
+ * bucket range of a request on the host before any copy and reject a bad
+ * request with CHANGA_E_INVALID_LIST (nothing is launched). */
+void changa_gb300_set_validate(int on);
+
+/* Host check of one request against its source and target array sizes. */
+int changa_validate_request(const ILCell *list, long long n_entries, const int *markers,
+                            const int *starts, const int *sizes, int n_buckets,
+                            long long n_sources, long long n_targets);
+
+int changa_gb300_version(void);
+
+/* Number of kernels this library has launched since load (all forms). */
+unsigned long long changa_gb300_kernel_launches(void);
+
+/* ---- device-resident list requests for the extension forms ---- */
+
+typedef struct ChangaListRequest {
+  const ILCell *list;   /* device: entries, ILCell {index, offsetID} */
+  const int *markers;   /* device: n_buckets + 1 CSR offsets into list */
+  const int *starts;    /* device: first target of each bucket */
+  const int *sizes;     /* device: targets in each bucket */
+  int n_buckets;
+  long long n_entries;
+} ChangaListRequest;
+
+/* Plain FP64 form: cell lists (nodeBucketForce) / particle lists
+ * (partBucketForce) over FP64 arrays. */
+int changa_cell_forces_fp64(const double *moments, long long n_moments,
+                            const double *targets, long long n_targets,
+                            const ChangaListRequest *req, double fperiod, double *vars,
+                            cudaStream_t stream);
+int changa_part_forces_fp64(const double *sources, long long n_sources,
+                            const double *targets, long long n_targets,
+                            const ChangaListRequest *req, double fperiod, double *vars,
+                            cudaStream_t stream);
+
+/* FP32-mixed form of the same two evaluations. */
+int changa_cell_forces_mixed(const double *moments, long long n_moments,
+                             const double *targets, long long n_targets,
+                             const ChangaListRequest *req, double fperiod, double *vars,
+                             cudaStream_t stream);
+int changa_part_forces_mixed(const double *sources, long long n_sources,
+                             const double *targets, long long n_targets,
+                             const ChangaListRequest *req, double fperiod, double *vars,
+                             cudaStream_t stream);
+
+/* One whole force evaluation: cell lists + particle lists (+ Ewald when
+ * ewald != NULL) for particles that are both sources and targets.
+ * form: CHANGA_FORM_FP64 or CHANGA_FORM_MIXED. */
+#define CHANGA_FORM_FP32 0
+#define CHANGA_FORM_FP64 1
+#define CHANGA_FORM_MIXED 2
+
+typedef struct ChangaEwaldParams {
+  double root[12];   /* root moments, moments layout */
+  double L;          /* period */
+  int nReps;         /* replicas the walk covered (the erf hole) */
+  double fEwCut;     /* real-space cut in periods */
+  int nEwhLoop;      /* rows in ewt, at most CHANGA_MAX_EWH */
+  const double *ewt; /* HOST: nEwhLoop x 5 {hx, hy, hz, hCfac, hSfac} */
+} ChangaEwaldParams;
+
+#define CHANGA_MAX_EWH 256
+
+int changa_gravity_step(int form, const double *moments, long long n_moments,
+                        const double *parts, long long n_parts,
+                        const ChangaListRequest *cells, const ChangaListRequest *plist,
+                        double fperiod, const ChangaEwaldParams *ewald,
+                        double *vars, cudaStream_t stream);
+
+/* The same evaluation from HOST arrays: the requests' pointers, moments,
+ * parts and the ewt table are host memory (pinned memory copies fastest).
+ * Uploads everything on `stream`, runs changa_gravity_step, ACCUMULATES the
+ * results into vars (host, n_parts x 5) and returns after the stream has
+ * finished, so vars is ready on return. */
+int changa_gravity_step_host(int form, const double *moments, long long n_moments,
+                             const double *parts, long long n_parts,
+                             const ChangaListRequest *cells, const ChangaListRequest *plist,
+                             double fperiod, const ChangaEwaldParams *ewald,
+                             double *vars, cudaStream_t stream);
+
+/* Ewald correction for parts[idx[k]] into vars[idx[k]] (idx == NULL: the
+ * first n_idx particles).  form: FP64 or MIXED. */
+int changa_ewald_forces(int form, const double *parts, long long n_parts, const int *idx,
+                        long long n_idx, const ChangaEwaldParams *p, double *vars,
+                        cudaStream_t stream);
+
+/* Host restatement of TreePiece::EwaldInit (Ewald.cpp:285-383): fills up to
+ * max_h rows of ewt; returns nEwhLoop, or -1 if max_h is too small. */
+int changa_ewald_table(const double *root, double L, double dEwhCut, double *ewt, int max_h);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* CHANGA_GB300_H_ */

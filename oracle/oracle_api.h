@@ -1,0 +1,67 @@
+/*
+ * CPU oracle API for the gravity hot path.
+ *
+ * TEST INFRASTRUCTURE ONLY.  Two libraries implement this header:
+ *   - oracle/_ref/libchanga_ref.so : ChaNGa's own gravity.h (SPLINEQ,
+ *     SPLINE, nodeBucketForce, partBucketForce) and Ewald.cpp (EwaldInit,
+ *     BucketEwald) compiled unchanged against oracle/shim (ref_driver.cpp).
+ *     Built only where the reference sources are present.
+ *   - oracle/_build/libchanga_port.so : grav_oracle.c, this project's plain
+ *     C restatement of the same functions, pinned against the former and
+ *     against tests/golden.  It is the oracle wherever the reference sources
+ *     are absent, and the timed CPU baseline.
+ * Only tests/, __graft_entry__.smoke() and bench.py's CPU-baseline leg load
+ * either library; the product never does.
+ *
+ * Layouts (all FP64 mirrors of the boundary structs in include/cuda_typedef.h):
+ *   moments  : 12 doubles per node  {radius, soft, totalMass, cm.x, cm.y,
+ *              cm.z, xx, xy, xz, yy, yz, zz}   (CudaMultipoleMoments order)
+ *   parts    : 5 doubles per particle {mass, soft, x, y, z} (CompactPartData)
+ *   vars     : 5 doubles per particle {a.x, a.y, a.z, potential, dtGrav}
+ *              (VariablePartData); results ACCUMULATE (+= and max) as the
+ *              reference does (gravity.h:293-298, 460-472, Ewald.cpp:275-279).
+ *   list     : int32 pairs {index, offsetID} (ILCell); the periodic replica
+ *              is bits 22-30 of offsetID (TreePiece.cpp:3631-3652).
+ *   markers  : CSR offsets into list per bucket, starts/sizes: target range
+ *              of each bucket in the particle array.
+ */
+#ifndef CHANGA_ORACLE_API_H
+#define CHANGA_ORACLE_API_H
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* Cell (quadrupole multipole) interaction lists: nodeBucketForce per entry.
+ * bucket_ids (may be NULL) restricts the work to those buckets. */
+int oracle_cell_list_forces(const double* moments, long n_moments,
+                            const double* parts, long n_parts,
+                            const int* list, const int* markers,
+                            const int* starts, const int* sizes, int n_buckets,
+                            const int* bucket_ids, int n_ids,
+                            double fperiod, double* vars, int nthreads);
+
+/* Particle interaction lists (flattened to one entry per source particle):
+ * partBucketForce per entry. */
+int oracle_part_list_forces(const double* sources, long n_sources,
+                            const double* targets, long n_targets,
+                            const int* list, const int* markers,
+                            const int* starts, const int* sizes, int n_buckets,
+                            const int* bucket_ids, int n_ids,
+                            double fperiod, double* vars, int nthreads);
+
+/* Ewald h-loop table (EwaldInit): writes up to max_h rows of 5 doubles
+ * {hx, hy, hz, hCfac, hSfac}; returns nEwhLoop or -1 if max_h too small. */
+int oracle_ewald_table(const double* root_moments, double L, double dEwhCut,
+                       double* ewt, int max_h);
+
+/* Ewald correction (BucketEwald) for parts[idx[k]] into vars[k]
+ * (idx may be NULL: k indexes parts directly, n_idx = count). */
+int oracle_ewald_forces(const double* parts, long n_parts, const int* idx, long n_idx,
+                        const double* root_moments, double L, int nReps,
+                        double fEwCut, double dEwhCut, double* vars, int nthreads);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,30 @@
+import os
+import sys
+
+import pytest
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+if ROOT not in sys.path:
+    sys.path.insert(0, ROOT)
+
+
+def pytest_configure(config):
+    config.addinivalue_line("markers", "gpu: needs a CUDA GPU (GB300); run with -m gpu")
+
+
+@pytest.fixture(scope="session")
+def built():
+    """Builds the native libraries and the oracle once per session."""
+    from changa_gb300 import build
+    build.build_all()
+    build.build_oracle()
+    return True
+
+
+@pytest.fixture(scope="session")
+def cuda_ok(built):
+    import torch
+    if not torch.cuda.is_available():
+        pytest.fail("GPU test run without a CUDA device")
+    torch.cuda.init()
+    return True

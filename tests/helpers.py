@@ -1,0 +1,30 @@
+"""Shared helpers of the test suite (fixtures, error metrics)."""
+import os
+
+import numpy as np
+
+GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
+FIXTURES = ["plummer_1k", "plummer_ragged_2k", "lattice_8", "plummer_32k_sample"]
+
+
+def load_golden(name):
+    z = np.load(os.path.join(GOLDEN, name + ".npz"))
+    return {k: z[k] for k in z.files}
+
+
+def lists_from_golden(g):
+    from changa_gb300 import tree
+    return tree.build_lists(g["pos"].astype(np.float64), g["mass"], g["soft"],
+                            n_bucket=int(g["n_bucket"]), theta=float(g["theta"]),
+                            period=float(g["period"]))
+
+
+def force_rel_err(a, ref):
+    """Per-particle |a - ref| / |ref| over the acceleration rows."""
+    num = np.linalg.norm(a[:, :3] - ref[:, :3], axis=1)
+    den = np.linalg.norm(ref[:, :3], axis=1)
+    return num / np.maximum(den, 1e-300)
+
+
+def pot_rel_err(a, ref):
+    return np.abs(a[:, 3] - ref[:, 3]) / np.maximum(np.abs(ref[:, 3]), 1e-300)

@@ -1,0 +1,185 @@
+"""GPU parity: every form of the list kernels and the Ewald kernels against
+the CPU oracle on the same lists (and against the committed fixtures that
+ChaNGa's own CPU code produced)."""
+import ctypes as C
+
+import numpy as np
+import pytest
+
+import oracle
+from changa_gb300 import _native as N
+from changa_gb300 import gravity, ics, tree
+from helpers import FIXTURES, force_rel_err, load_golden, lists_from_golden, pot_rel_err
+
+pytestmark = pytest.mark.gpu
+
+# Tolerances (per particle, |da|/|a| and |dpot|/|pot|):
+FP64_TOL = 1e-6        # the plain FP64 form (stated bar: 1e-6 relative)
+F32_MEDIAN_TOL = 2e-6  # FP32 drop-in vs FP64 oracle on the same FP32 inputs
+F32_P99_TOL = 1e-4
+MIX_MEDIAN_TOL = 2e-6  # FP32-mixed vs the FP64 form
+MIX_P99_TOL = 1e-4
+
+
+def oracle_vars(L, period=0.0, ewald=None, f32_inputs=False):
+    mom, parts = L.moments, L.parts
+    if f32_inputs:
+        mom = mom.astype(np.float32).astype(np.float64)
+        parts = parts.astype(np.float32).astype(np.float64)
+    v = oracle.cell_forces(mom, parts, L.cells, fperiod=period)
+    v = oracle.part_forces(parts, parts, L.plist, fperiod=period, vars=v)
+    if ewald is not None:
+        root = L.root if not f32_inputs else L.root.astype(np.float32).astype(np.float64)
+        v = oracle.ewald_forces(parts, root, ewald.L, ewald.n_reps, ewald.fEwCut, ewald.dEwhCut,
+                                vars=v)
+    return v
+
+
+@pytest.fixture(scope="module")
+def plummer(cuda_ok):
+    p = ics.plummer(32768, ics.rng_for(0), soft=0.01)
+    L = tree.build_lists(p["pos"], p["mass"], p["soft"], n_bucket=16, theta=0.7)
+    return L, oracle_vars(L), oracle_vars(L, f32_inputs=True)
+
+
+@pytest.fixture(scope="module")
+def lattice(cuda_ok):
+    p = ics.lattice_grf(24, ics.rng_for(1))
+    L = tree.build_lists(p["pos"], p["mass"], p["soft"], n_bucket=16, theta=0.7, period=1.0)
+    ew = gravity.EwaldConfig(1.0, 1, 2.6, 2.8)
+    return L, ew, oracle_vars(L, 1.0, ew)
+
+
+def test_fp64_form_matches_oracle(plummer):
+    L, ref, _ = plummer
+    before = N.cuda_lib().changa_gb300_kernel_launches()
+    v = gravity.DeviceSystem(L).step("fp64").cpu().numpy()
+    assert N.cuda_lib().changa_gb300_kernel_launches() > before
+    assert force_rel_err(v, ref).max() < FP64_TOL
+    assert pot_rel_err(v, ref).max() < FP64_TOL
+    np.testing.assert_allclose(v[:, 4], ref[:, 4], rtol=FP64_TOL)
+
+
+def test_fp32_dropin_matches_oracle(plummer):
+    L, _, ref32 = plummer
+    inp = gravity.DropInInputs(L)
+    try:
+        v = gravity.dropin_step(inp).astype(np.float64)
+    finally:
+        inp.free()
+    e = force_rel_err(v, ref32)
+    assert np.median(e) < F32_MEDIAN_TOL
+    assert np.percentile(e, 99) < F32_P99_TOL
+    assert np.median(pot_rel_err(v, ref32)) < F32_MEDIAN_TOL
+    np.testing.assert_allclose(v[:, 4], ref32[:, 4], rtol=1e-4)
+
+
+def test_mixed_form_matches_fp64(plummer):
+    L, ref, _ = plummer
+    v = gravity.DeviceSystem(L).step("mixed").cpu().numpy()
+    e = force_rel_err(v, ref)
+    assert np.median(e) < MIX_MEDIAN_TOL
+    assert np.percentile(e, 99) < MIX_P99_TOL
+    assert np.median(pot_rel_err(v, ref)) < MIX_MEDIAN_TOL
+
+
+def test_host_entry_matches_device_entry(plummer):
+    L, ref, _ = plummer
+    v = gravity.gravity_step_host(L, "fp64")
+    assert force_rel_err(v, ref).max() < FP64_TOL
+
+
+@pytest.mark.parametrize("name", FIXTURES)
+def test_fp64_form_matches_golden(cuda_ok, name):
+    g = load_golden(name)
+    L = lists_from_golden(g)
+    per = float(g["period"])
+    ew = None
+    if "ewald_vars" in g:
+        cut, hcut = g["ewald_cfg"]
+        ew = gravity.EwaldConfig(per, 1, float(cut), float(hcut))
+    v = gravity.DeviceSystem(L, ewald=ew).step("fp64").cpu().numpy()[g["rows"]]
+    ref = g["tree_vars"] + (g["ewald_vars"] if ew else 0.0)
+    if ew:
+        ref[:, 4] = g["tree_vars"][:, 4]
+    assert force_rel_err(v, ref).max() < FP64_TOL
+    assert pot_rel_err(v, ref).max() < FP64_TOL
+
+
+def test_ewald_forms(lattice):
+    L, ew, ref = lattice
+    v64 = gravity.DeviceSystem(L, ewald=ew).step("fp64").cpu().numpy()
+    assert force_rel_err(v64, ref).max() < FP64_TOL
+    assert pot_rel_err(v64, ref).max() < FP64_TOL
+    vmx = gravity.DeviceSystem(L, ewald=ew).step("mixed").cpu().numpy()
+    e = force_rel_err(vmx, ref)
+    assert np.median(e) < 1e-5 and np.percentile(e, 99) < 1e-3
+
+
+def test_ewald_dropin(lattice):
+    L, ew, _ = lattice
+    ref32 = oracle_vars(L, 1.0, ew, f32_inputs=True)
+    inp = gravity.DropInInputs(L, ewald=ew)
+    try:
+        v = gravity.dropin_step(inp).astype(np.float64)
+    finally:
+        inp.free()
+    e = force_rel_err(v, ref32)
+    assert np.median(e) < 1e-4
+    assert np.percentile(e, 99) < 1e-2
+
+
+def test_ragged_and_tiny_buckets(cuda_ok):
+    """Buckets above 32 targets (chunked), buckets of 1, and a 1-particle
+    system."""
+    p = ics.plummer(3000, ics.rng_for(5), soft=0.05)
+    for nb in (1, 5, 33, 64, 100):
+        L = tree.build_lists(p["pos"], p["mass"], p["soft"], n_bucket=nb, theta=0.6)
+        ref = oracle_vars(L)
+        v = gravity.DeviceSystem(L).step("fp64").cpu().numpy()
+        assert force_rel_err(v, ref).max() < FP64_TOL, nb
+        vm = gravity.DeviceSystem(L).step("mixed").cpu().numpy()
+        assert np.median(force_rel_err(vm, ref)) < MIX_MEDIAN_TOL, nb
+    one = tree.build_lists(np.zeros((1, 3)), np.ones(1), np.full(1, 0.1))
+    v = gravity.DeviceSystem(one).step("mixed").cpu().numpy()
+    assert np.all(v == 0)
+
+
+def test_empty_request_and_validation(cuda_ok):
+    """numBucketsPlusOne == 1 enqueues nothing; with validation on, a
+    request with an out-of-range index is rejected on the host before any
+    copy or launch and reported through the error code."""
+    lib = N.cuda_lib()
+    p = ics.plummer(512, ics.rng_for(6))
+    L = tree.build_lists(p["pos"], p["mass"], p["soft"], n_bucket=16)
+    inp = gravity.DropInInputs(L)
+    rt = gravity._cudart()
+    d_m, d_p, d_v = C.c_void_p(), C.c_void_p(), C.c_void_p()
+    lib.DataManagerTransferLocalTree(inp.moments.ptr, inp.moments.nbytes, inp.parts.ptr,
+                                     inp.parts.nbytes, inp.vars.ptr, inp.vars.nbytes,
+                                     C.byref(d_m), C.byref(d_p), C.byref(d_v), None, L.n, None)
+    try:
+        lib.changa_gb300_set_error_mode(N.CHANGA_ERRORS_RECORD)
+        lib.changa_gb300_set_validate(1)
+        lst, mk, st, sz, req = inp.reqs[0]
+        r = N.CudaRequest()
+        r.d_localMoments, r.d_localParts, r.d_localVars = d_m, d_p, d_v
+        r.list, r.bucketMarkers, r.bucketStarts, r.bucketSizes = lst.ptr, mk.ptr, st.ptr, sz.ptr
+        r.numInteractions = req.n_entries
+        r.numBucketsPlusOne = 1
+        before = lib.changa_gb300_kernel_launches()
+        lib.TreePieceCellListDataTransferLocal(C.byref(r))
+        assert lib.changa_gb300_kernel_launches() == before
+        assert lib.changa_gb300_last_error() == 0
+        lst.array[0, 0] = L.moments.shape[0] + 7  # out of range
+        r.numBucketsPlusOne = req.n_buckets + 1
+        lib.TreePieceCellListDataTransferLocal(C.byref(r))
+        assert lib.changa_gb300_kernel_launches() == before
+        assert lib.changa_gb300_last_error() == 1002
+    finally:
+        lib.changa_gb300_set_validate(0)
+        lib.changa_gb300_set_error_mode(N.CHANGA_ERRORS_ABORT)
+        rt.cudaStreamSynchronize(None)
+        for q in (d_m, d_p, d_v):
+            rt.cudaFree(q)
+        inp.free()

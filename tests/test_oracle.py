@@ -1,0 +1,104 @@
+"""The CPU oracle: the restated port against ChaNGa's own CPU force code and
+against the committed golden fixtures (which that code produced)."""
+import numpy as np
+import pytest
+
+import oracle
+from changa_gb300 import ics, tree
+from helpers import FIXTURES, load_golden, lists_from_golden
+import sys, os
+sys.path.insert(0, os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden"))
+from make_golden import list_digest  # noqa: E402
+
+
+@pytest.fixture(scope="module", autouse=True)
+def _build(built):
+    return built
+
+
+@pytest.mark.parametrize("name", FIXTURES)
+def test_port_matches_golden(name):
+    g = load_golden(name)
+    L = lists_from_golden(g)
+    assert list_digest(L) == str(g["digest"]), "host tree/walk changed the lists"
+    per = float(g["period"])
+    v = oracle.cell_forces(L.moments, L.parts, L.cells, fperiod=per, kind="port")
+    v = oracle.part_forces(L.parts, L.parts, L.plist, fperiod=per, vars=v, kind="port")
+    rows = g["rows"]
+    # the golden came from gravity.h itself; the port is the same arithmetic
+    np.testing.assert_allclose(v[rows], g["tree_vars"], rtol=1e-13, atol=1e-300)
+    if "ewald_vars" in g:
+        cut, hcut = g["ewald_cfg"]
+        ew = oracle.ewald_forces(L.parts, L.root, per, 1, cut, hcut, idx=rows, kind="port")
+        np.testing.assert_allclose(ew, g["ewald_vars"], rtol=1e-12, atol=1e-15)
+        tb = oracle.ewald_table(L.root, per, hcut, kind="port")
+        np.testing.assert_allclose(tb, g["ewt"], rtol=1e-14, atol=1e-300)
+
+
+@pytest.mark.skipif(not oracle.available("ref"), reason="reference sources not built here")
+@pytest.mark.parametrize("period,bucket,theta", [(0.0, 16, 0.7), (0.0, 8, 0.4), (1.0, 16, 0.7)])
+def test_port_bitexact_vs_reference(period, bucket, theta):
+    rng = ics.rng_for(7)
+    if period:
+        p = ics.lattice_grf(12, rng)
+    else:
+        p = ics.plummer(3000, rng, soft=0.03)
+    L = tree.build_lists(p["pos"], p["mass"], p["soft"], n_bucket=bucket, theta=theta, period=period)
+    out = {}
+    for kind in ("port", "ref"):
+        v = oracle.cell_forces(L.moments, L.parts, L.cells, fperiod=period, kind=kind)
+        v = oracle.part_forces(L.parts, L.parts, L.plist, fperiod=period, vars=v, kind=kind)
+        if period:
+            v = oracle.ewald_forces(L.parts, L.root, period, 1, 2.6, 2.8, vars=v, kind=kind)
+        out[kind] = v
+    assert np.array_equal(out["port"], out["ref"])
+
+
+def test_two_body_known_answer():
+    """Unit masses at distance 1, far outside softening: a = +-1, pot = -1
+    (partBucketForce, gravity.h:267-303)."""
+    parts = np.array([[1.0, 1e-3, 0.0, 0.0, 0.0], [1.0, 1e-3, 1.0, 0.0, 0.0]])
+    code = (3 | 3 << 3 | 3 << 6) << 22  # replica (0, 0, 0)
+    req = tree.ListRequest(np.array([[1, code], [0, code]], np.int32), np.array([0, 1, 2], np.int32),
+                           np.array([0, 1], np.int32), np.array([1, 1], np.int32),
+                           np.array([0, 1], np.int32))
+    v = oracle.part_forces(parts, parts, req)
+    np.testing.assert_allclose(v[0, :4], [1.0, 0.0, 0.0, -1.0], rtol=1e-15)
+    np.testing.assert_allclose(v[1, :4], [-1.0, 0.0, 0.0, -1.0], rtol=1e-15)
+    np.testing.assert_allclose(v[:, 4], [2.0, 2.0], rtol=1e-15)
+
+
+def test_spline_branches_continuous():
+    """The softened pair force is continuous across u = 1 and r = twoh."""
+    twoh = 0.1
+    r = np.array([0.05 * (1 - 1e-9), 0.05 * (1 + 1e-9), 0.1 * (1 - 1e-9), 0.1 * (1 + 1e-9)])
+    a, b = oracle.spline_ab(r * r, np.full(4, twoh))
+    assert abs(a[0] - a[1]) < 1e-6 * a[0] and abs(b[0] - b[1]) < 1e-6 * b[0]
+    assert abs(a[2] - a[3]) < 1e-6 * a[2] and abs(b[2] - b[3]) < 1e-6 * b[2]
+
+
+def test_tree_force_accuracy_vs_direct_sum():
+    """theta = 0.7 quadrupole tree forces are within the expected ~1e-3 of an
+    FP64 direct sum (median), on the oracle."""
+    rng = ics.rng_for(8)
+    p = ics.plummer(8192, rng, soft=0.01)
+    L = tree.build_lists(p["pos"], p["mass"], p["soft"], n_bucket=16, theta=0.7)
+    v = oracle.cell_forces(L.moments, L.parts, L.cells)
+    v = oracle.part_forces(L.parts, L.parts, L.plist, vars=v)
+    idx = rng.choice(L.n, 200, replace=False)
+    acc, pot = oracle.direct_sum(L.parts, idx)
+    err = np.linalg.norm(v[idx, :3] - acc, axis=1) / np.linalg.norm(acc, axis=1)
+    assert np.median(err) < 3e-3
+    assert np.percentile(err, 99) < 3e-2
+    assert np.median(np.abs(v[idx, 3] - pot) / np.abs(pot)) < 1e-3
+
+
+def test_ewald_single_particle_no_self_force():
+    """A single particle in a periodic box feels no net force from its own
+    replicas (tree replicas + Ewald correction cancel by symmetry)."""
+    p = dict(pos=np.array([[0.3, 0.6, 0.45]]), mass=np.array([1.0]), soft=np.array([1e-3]))
+    L = tree.build_lists(p["pos"], p["mass"], p["soft"], n_bucket=16, theta=0.7, period=1.0)
+    v = oracle.cell_forces(L.moments, L.parts, L.cells, fperiod=1.0)
+    v = oracle.part_forces(L.parts, L.parts, L.plist, fperiod=1.0, vars=v)
+    v = oracle.ewald_forces(L.parts, L.root, 1.0, 1, 2.6, 2.8, vars=v)
+    assert np.abs(v[0, :3]).max() < 1e-6
