@@ -1,0 +1,473 @@
+#!/usr/bin/env python
+"""Gravity-force benchmark: interactions/s of the FP32-mixed form.
+
+One "step" is one complete force evaluation of the workload: the cell
+(quadrupole) interaction lists, the particle interaction lists and the
+periodic Ewald correction, over lists that are already resident in HBM
+(the host tree walk that builds them runs once, outside the timed region,
+as it does on ChaNGa's CPU).  Interactions follow ChaNGa's own counter
+(Compute.cpp:1643-1651): per bucket, targets x (cell-list + particle-list
+entries).
+
+Default workload: nfw8m (N = 2^23 NFW halos + background, periodic, Ewald,
+bucket 32, theta 0.7).  Other lines of the JSON:
+  e2e          the same metric through changa_gravity_step_host with host
+               (pinned) buffers, host<->device copies inside the timed region;
+  roofline     the dominant kernel (FP32-mixed cell-list kernel) against the
+               FP32 FMA peak of the GPU;
+  cpu_baseline the CPU oracle (ChaNGa's own gravity.h/Ewald.cpp when it was
+               built here, else its C restatement) on a bounded sample.
+--impl reference times that CPU implementation alone on the same workload.
+
+Launch: python bench.py [--gpus N --steps K --warmup W]; for N > 1 under
+torch.distributed.run, one rank per GPU; every rank evaluates its own copy
+of the workload (weak scaling) and value = all ranks' interactions / max time.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+FLOP_PC = 67  # FLOP per quadrupole cell interaction (counted convention)
+FLOP_PP = 23  # FLOP per particle-particle interaction
+METRIC = "gravity interactions/s (FP32-mixed form, N=8M NFW + Ewald)"
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--workload", default="nfw8m")
+    ap.add_argument("--fp64-steps", type=int, default=2)
+    ap.add_argument("--e2e-steps", type=int, default=3)
+    ap.add_argument("--cpu-sample", type=float, default=1.5e9,
+                    help="interactions in the bounded CPU sample")
+    ap.add_argument("--no-cpu", action="store_true")
+    return ap.parse_args()
+
+
+class ClockSampler:
+    """nvidia-smi clocks/throttle sampling during the timed region."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index):
+        self.index = index
+        self.proc = None
+        self.out = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.index), "--query-gpu=" + self.Q,
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except OSError:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.out.append(line.strip())
+
+    def stop(self):
+        if self.proc is None:
+            return None
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        self.t.join(timeout=5)
+        mhz, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in self.out:
+            f = [x.strip() for x in line.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                mhz.append(float(f[1]))
+                mx = float(f[2])
+            except ValueError:
+                continue
+            for name, v in zip(names, f[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(name)
+        if not mhz:
+            return None
+        mhz.sort()
+        return {"sm_mhz": mhz[len(mhz) // 2], "sm_max_mhz": mx, "reasons": sorted(reasons),
+                "samples": len(mhz)}
+
+
+def dist_setup(args):
+    import torch
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if world > 1:
+        import torch.distributed as dist
+        torch.cuda.set_device(local)
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+    elif torch.cuda.is_available():
+        torch.cuda.set_device(0)
+    return world, rank, local
+
+
+def barrier(world):
+    if world > 1:
+        import torch.distributed as dist
+        dist.barrier()
+
+
+def max_over_ranks(world, x):
+    if world == 1:
+        return x
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([x], dtype=torch.float64, device="cuda")
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def sum_over_ranks(world, x):
+    if world == 1:
+        return x
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([x], dtype=torch.float64, device="cuda")
+    dist.all_reduce(t, op=dist.ReduceOp.SUM)
+    return float(t.item())
+
+
+def cpu_sample(lists, target, seed=12345):
+    """A random subset of buckets whose interactions add up to ~target:
+    returns (bucket ids of the cell request, of the particle request, count)."""
+    import numpy as np
+    rng = np.random.default_rng(seed)
+    nb = len(lists.bucket_starts)
+    order = rng.permutation(nb)
+    cl, pl = lists.cells, lists.plist
+    c_of = {int(b): i for i, b in enumerate(cl.bucket_ids)}
+    p_of = {int(b): i for i, b in enumerate(pl.bucket_ids)}
+    c_len = np.diff(cl.markers.astype(np.int64)) * cl.sizes
+    p_len = np.diff(pl.markers.astype(np.int64)) * pl.sizes
+    cid, pid, tot = [], [], 0
+    for b in order:
+        b = int(b)
+        if b in c_of:
+            cid.append(c_of[b])
+            tot += int(c_len[c_of[b]])
+        if b in p_of:
+            pid.append(p_of[b])
+            tot += int(p_len[p_of[b]])
+        if tot >= target:
+            break
+    return np.array(cid, np.int32), np.array(pid, np.int32), tot
+
+
+def run_cpu(lists, ewald, target, kind_pref="auto", reps=1):
+    """Times the CPU oracle on a bounded sample; returns dict."""
+    import numpy as np
+
+    import oracle
+    kind = "ref" if (kind_pref == "auto" and oracle.available("ref")) else "port"
+    oracle.load(kind)
+    cid, pid, tot = cpu_sample(lists, target)
+    cores = os.cpu_count() or 1
+    # Ewald targets: the particles of the sampled buckets
+    rows = []
+    for i in pid:
+        s, n = int(lists.plist.starts[i]), int(lists.plist.sizes[i])
+        rows.extend(range(s, s + n))
+    rows = np.array(sorted(set(rows)), np.int32)
+    times = []
+    for _ in range(reps):
+        v = np.zeros((lists.n, 5))
+        t0 = time.perf_counter()
+        oracle.cell_forces(lists.moments, lists.parts, lists.cells, fperiod=lists.period, vars=v,
+                           bucket_ids=cid, kind=kind, nthreads=cores)
+        oracle.part_forces(lists.parts, lists.parts, lists.plist, fperiod=lists.period, vars=v,
+                           bucket_ids=pid, kind=kind, nthreads=cores)
+        if ewald is not None and len(rows):
+            oracle.ewald_forces(lists.parts, lists.root, ewald.L, ewald.n_reps, ewald.fEwCut,
+                                ewald.dEwhCut, idx=rows, kind=kind, nthreads=cores)
+        times.append(time.perf_counter() - t0)
+    dt = min(times)
+    return {"value": tot / dt, "unit": "interactions/s", "cores": cores,
+            "kind": "reference" if kind == "ref" else "port",
+            "sample": "%d random buckets of the workload (%.3g interactions, cell+particle lists"
+                      "%s), FP64, OpenMP over buckets, best of %d" %
+                      (len(set(cid.tolist()) | set(pid.tolist())), tot,
+                       " + Ewald on their %d particles" % len(rows) if ewald else "", reps),
+            "seconds": dt}
+
+
+def fp32_peak_tflops():
+    """FP32 FMA peak: SMs x 128 lanes x 2 FLOP x max SM clock."""
+    import torch
+    sms = torch.cuda.get_device_properties(0).multi_processor_count
+    mhz, src = None, None
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        with open(p) as f:
+            mp = json.load(f)
+        mhz = mp.get("sm_max_mhz")
+        src = "%d SMs x 128 FP32 lanes x 2 x sm_max_mhz %.0f (MEASURED_PEAKS.json)" % (sms, mhz)
+    if mhz is None:
+        mhz = 2070.0
+        src = "%d SMs x 128 FP32 lanes x 2 x 2070 MHz (nominal max clock)" % sms
+    return sms * 128 * 2 * mhz * 1e6 / 1e12, src
+
+
+def traffic_from_profiles():
+    p = os.path.join(ROOT, "profiles", "traffic.json")
+    if os.path.exists(p):
+        with open(p) as f:
+            return json.load(f)
+    return {}
+
+
+def main_reference(args):
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return 0
+    from changa_gb300 import build as b
+    from changa_gb300.workloads import WORKLOADS
+    b.build_host()
+    b.build_oracle()
+    wl = WORKLOADS[args.workload]
+    lists = wl.lists()
+    ew = wl.ewald_config()
+    for _ in range(args.warmup):
+        run_cpu(lists, ew, args.cpu_sample / 4)
+    vals = []
+    t_all = time.perf_counter()
+    for _ in range(args.steps):
+        r = run_cpu(lists, ew, args.cpu_sample)
+        vals.append(r)
+    wall = time.perf_counter() - t_all
+    value = sum(r["value"] for r in vals) / len(vals)
+    ms = 1e3 * sum(r["seconds"] for r in vals) / len(vals)
+    cb = dict(vals[0])
+    cb["value"] = value
+    out = {"metric": METRIC, "value": value, "unit": "interactions/s", "impl": "reference",
+           "n_gpus": world, "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms,
+           "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+           "data": "synthetic (seeded %s)" % wl.name,
+           "config": dict(wl.describe(), sample_interactions=vals[0]["sample"], wall_s=wall),
+           "cpu_baseline": cb,
+           "e2e": {"value": value, "unit": "interactions/s", "h2d_bytes_per_step": 0,
+                   "d2h_bytes_per_step": 0}}
+    print(json.dumps(out), flush=True)
+    return 0
+
+
+def main_ours(args):
+    import numpy as np
+    import torch
+
+    import __graft_entry__
+    __graft_entry__.build()
+    from changa_gb300 import _native as N
+    from changa_gb300 import gravity
+    from changa_gb300.workloads import WORKLOADS
+
+    world, rank, local = dist_setup(args)
+    lib = N.cuda_lib()
+    wl = WORKLOADS[args.workload]
+    t0 = time.perf_counter()
+    lists = wl.lists()
+    t_walk = time.perf_counter() - t0
+    ew = wl.ewald_config()
+    I = lists.interactions
+    I_c, I_p = lists.cells.interactions(), lists.plist.interactions()
+    ds = gravity.DeviceSystem(lists, device="cuda", ewald=ew)
+    stream = torch.cuda.current_stream()
+    flush = torch.empty(256 * 2 ** 20 // 4, dtype=torch.float32, device="cuda")  # > L2
+
+    for _ in range(args.warmup):
+        ds.step("mixed")
+    torch.cuda.synchronize()
+    barrier(world)
+    torch.cuda.synchronize()
+    clocks = ClockSampler(local)
+    clocks.start()
+    lib.changa_gb300_set_timing(1)
+    for k in N.KERNEL_IDS:
+        N.kernel_time(k)
+    launches0 = lib.changa_gb300_kernel_launches()
+    evs = []
+    t_wall = time.perf_counter()
+    for _ in range(args.steps):
+        flush.fill_(1.0)
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        ds.step("mixed")
+        e1.record(stream)
+        evs.append((e0, e1))
+    torch.cuda.synchronize()
+    t_wall = time.perf_counter() - t_wall
+    barrier(world)
+    torch.cuda.synchronize()
+    launches = lib.changa_gb300_kernel_launches() - launches0
+    ktimes = {k: N.kernel_time(k) for k in N.KERNEL_IDS}
+    lib.changa_gb300_set_timing(0)
+    clk = clocks.stop()
+    ms_steps = [a.elapsed_time(b) for a, b in evs]
+    ms = sum(ms_steps) / len(ms_steps)
+    ms_max = max_over_ranks(world, ms)
+    value = sum_over_ranks(world, float(I)) / (ms_max / 1e3)
+    v_mixed = ds.vars.cpu().numpy().copy()
+
+    # FP64 form on the same lists (the precision yardstick and the 3x target)
+    fp64 = None
+    if args.fp64_steps > 0:
+        ds.step("fp64")
+        torch.cuda.synchronize()
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(args.fp64_steps):
+            ds.step("fp64")
+        e1.record(stream)
+        torch.cuda.synchronize()
+        ms64 = e0.elapsed_time(e1) / args.fp64_steps
+        v64 = ds.vars.cpu().numpy()
+        rng = np.random.default_rng(7)
+        samp = rng.choice(lists.n, min(16384, lists.n), replace=False)
+        num = np.linalg.norm(v_mixed[samp, :3] - v64[samp, :3], axis=1)
+        den = np.linalg.norm(v64[samp, :3], axis=1)
+        err = num / den
+        fp64 = {"ms_per_step": ms64, "interactions_per_s": I / (ms64 / 1e3),
+                "mixed_over_fp64": (I / (ms / 1e3)) / (I / (ms64 / 1e3)),
+                "median_rel_force_err_vs_fp64": float(np.median(err)),
+                "p99_rel_force_err_vs_fp64": float(np.percentile(err, 99)),
+                "sampled_particles": int(len(samp))}
+        for k in N.KERNEL_IDS:
+            N.kernel_time(k)
+
+    # end to end through the public C-ABI with pinned host buffers
+    e2e = None
+    if args.e2e_steps > 0:
+        import ctypes as C
+        pin = {k: gravity.PinnedArray(a) for k, a in (
+            ("moments", lists.moments), ("parts", lists.parts),
+            ("cl", lists.cells.list), ("cm", lists.cells.markers), ("cs", lists.cells.starts),
+            ("cz", lists.cells.sizes), ("pl", lists.plist.list), ("pm", lists.plist.markers),
+            ("ps", lists.plist.starts), ("pz", lists.plist.sizes))}
+        out = gravity.PinnedArray(np.zeros((lists.n, 5)))
+
+        def req(l, m, s, z, r):
+            q = N.ChangaListRequest()
+            q.list, q.markers, q.starts, q.sizes = pin[l].ptr, pin[m].ptr, pin[s].ptr, pin[z].ptr
+            q.n_buckets, q.n_entries = r.n_buckets, r.n_entries
+            return q
+        cq = req("cl", "cm", "cs", "cz", lists.cells)
+        pq = req("pl", "pm", "ps", "pz", lists.plist)
+        ep = ew.params(lists.root) if ew else None
+        sh = stream.cuda_stream
+
+        def one():
+            out.array[...] = 0.0
+            rc = lib.changa_gravity_step_host(N.CHANGA_FORM_MIXED, pin["moments"].ptr,
+                                              lists.moments.shape[0], pin["parts"].ptr, lists.n,
+                                              C.byref(cq), C.byref(pq), float(lists.period),
+                                              C.byref(ep) if ep else None, out.ptr, sh)
+            N.check(rc, "changa_gravity_step_host")
+        one()
+        tt = []
+        for _ in range(args.e2e_steps):
+            t1 = time.perf_counter()
+            one()
+            tt.append(time.perf_counter() - t1)
+        t_e2e = max_over_ranks(world, sum(tt) / len(tt))
+        h2d = (lists.moments.nbytes + 2 * lists.parts.nbytes + lists.cells.list.nbytes +
+               lists.cells.markers.nbytes + lists.cells.starts.nbytes + lists.cells.sizes.nbytes +
+               lists.plist.list.nbytes + lists.plist.markers.nbytes + lists.plist.starts.nbytes +
+               lists.plist.sizes.nbytes)
+        e2e = {"value": sum_over_ranks(world, float(I)) / t_e2e, "unit": "interactions/s",
+               "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(lists.parts.nbytes),
+               "ms_per_step": 1e3 * t_e2e,
+               "api": "changa_gravity_step_host (include/changa_gb300.h), pinned host buffers"}
+        for a in list(pin.values()) + [out]:
+            a.free()
+
+    # roofline of the dominant kernel (FP32-mixed cell lists) and the P-P kernel
+    peak, peak_src = fp32_peak_tflops()
+    tr = traffic_from_profiles()
+    roof = None
+    ms_pc, n_pc = ktimes["list_mixed_cell"]
+    ms_pp, n_pp = ktimes["list_mixed_part"]
+    if n_pc:
+        t_pc = ms_pc / n_pc / 1e3
+        ach = I_c * FLOP_PC / t_pc / 1e12
+        roof = {"bound": "fp32", "kernel": "list_kernel<kMix, cell> (FP32-mixed cell lists)",
+                "achieved": ach, "peak": peak, "unit": "TFLOP/s", "frac": ach / peak,
+                "peak_source": peak_src,
+                "algorithmic_flop_per_launch": I_c * FLOP_PC,
+                "flop_per_interaction": FLOP_PC, "interactions_per_launch": I_c,
+                "avg_launch_ms": 1e3 * t_pc,
+                "traffic": tr.get("list_mixed_cell_bytes_per_launch"),
+                "traffic_note": tr.get("note")}
+    roof_pp = None
+    if n_pp:
+        t_pp = ms_pp / n_pp / 1e3
+        ach = I_p * FLOP_PP / t_pp / 1e12
+        roof_pp = {"bound": "fp32", "kernel": "list_kernel<kMix, part> (FP32-mixed particle lists)",
+                   "achieved": ach, "peak": peak, "unit": "TFLOP/s", "frac": ach / peak,
+                   "algorithmic_flop_per_launch": I_p * FLOP_PP, "avg_launch_ms": 1e3 * t_pp,
+                   "traffic": tr.get("list_mixed_part_bytes_per_launch")}
+    kshare = {k: {"ms_per_step": v[0] / max(1, args.steps), "launches": v[1]}
+              for k, v in ktimes.items() if v[1]}
+
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu:
+        cpu = run_cpu(lists, ew, args.cpu_sample)
+
+    if rank == 0:
+        out = {"metric": METRIC, "value": value, "unit": "interactions/s", "n_gpus": world,
+               "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_max,
+               "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+               "data": "synthetic (seeded %s; no dataset)" % wl.name,
+               "config": dict(wl.describe(), form="FP32-mixed", interactions=I,
+                              cell_interactions=I_c, particle_interactions=I_p,
+                              list_bytes=int(lists.cells.list.nbytes + lists.plist.list.nbytes),
+                              l2="inputs larger than L2 (%.2f GB of lists) and a 256 MB flush "
+                                 "write between timed steps" %
+                                 ((lists.cells.list.nbytes + lists.plist.list.nbytes) / 1e9),
+                              host_walk_s=t_walk, fp64_form=fp64, kernels=kshare,
+                              parallelism="replicas x%d" % world),
+               "roofline": roof, "roofline_pp": roof_pp, "cpu_baseline": cpu, "e2e": e2e,
+               "gpu_launches": int(launches), "clocks": clk}
+        print(json.dumps(out), flush=True)
+    if world > 1:
+        import torch.distributed as dist
+        dist.destroy_process_group()
+    return 0
+
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        return main_reference(args)
+    return main_ours(args)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -101,6 +101,19 @@ CHANGA_FORM_FP64 = 1
 CHANGA_FORM_MIXED = 2
 CHANGA_MAX_EWH = 256
 
+# kernel ids of changa_gb300_kernel_time
+KERNEL_IDS = {"list_f32_cell": 0, "list_f32_part": 1, "list_f64_cell": 2, "list_f64_part": 3,
+              "list_mixed_cell": 4, "list_mixed_part": 5, "ewald_f32": 6, "ewald_f64": 7,
+              "ewald_mixed": 8, "pack": 9}
+
+
+def kernel_time(name):
+    """(total ms, launches) of one kernel since its last read (timing on)."""
+    ms, n = C.c_double(), C.c_longlong()
+    check(cuda_lib().changa_gb300_kernel_time(KERNEL_IDS[name], C.byref(ms), C.byref(n)),
+          "kernel_time")
+    return ms.value, n.value
+
 # Every C-ABI function of include/HostCUDA.h, include/EwaldCUDA.h and
 # include/changa_gb300.h with (restype, argtypes).
 _VP, _SZ, _I, _LL, _D = C.c_void_p, C.c_size_t, C.c_int, C.c_longlong, C.c_double
@@ -133,6 +146,8 @@ CUDA_SIGNATURES = {
     "changa_validate_request": (_I, [_VP, _LL, _VP, _VP, _VP, _I, _LL, _LL]),
     "changa_gb300_version": (_I, []),
     "changa_gb300_kernel_launches": (C.c_ulonglong, []),
+    "changa_gb300_set_timing": (None, [_I]),
+    "changa_gb300_kernel_time": (_I, [_I, C.POINTER(C.c_double), C.POINTER(C.c_longlong)]),
     "changa_cell_forces_fp64": (_I, [_VP, _LL, _VP, _LL, C.POINTER(ChangaListRequest), _D, _VP, _VP]),
     "changa_part_forces_fp64": (_I, [_VP, _LL, _VP, _LL, C.POINTER(ChangaListRequest), _D, _VP, _VP]),
     "changa_cell_forces_mixed": (_I, [_VP, _LL, _VP, _LL, C.POINTER(ChangaListRequest), _D, _VP, _VP]),

@@ -62,6 +62,23 @@ int sm_count();
 void count_launch(unsigned n = 1);
 int record_error(int code, const char* what, const char* file, int line);
 
+/* Kernel ids for the optional per-kernel event timing
+ * (changa_gb300_set_timing / changa_gb300_kernel_time). */
+enum KernelId : int {
+  kKidListF32Cell = 0, kKidListF32Part, kKidListF64Cell, kKidListF64Part, kKidListMixCell,
+  kKidListMixPart, kKidEwaldF32, kKidEwaldF64, kKidEwaldMix, kKidPack, kKidCount
+};
+inline int list_kernel_id(int form, bool cell) { return 2 * form + (cell ? 0 : 1); }
+
+/* Records CUDA events around one launch on stream s when timing is on. */
+struct TimingScope {
+  TimingScope(int kid, cudaStream_t s);
+  ~TimingScope();
+  int kid;
+  cudaStream_t s;
+  void* start;
+};
+
 }  // namespace chg
 
 #define CHG_CUDA(call)                                                            \

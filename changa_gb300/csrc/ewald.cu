@@ -12,14 +12,20 @@
  * Root data travel as a __grid_constant__ kernel parameter (the reference
  * writes __constant__ symbols per call, a race between concurrent streams).
  * Forms:
- *   ewald_f32_kernel  the drop-in form on the FP32 ABI (reference constants,
- *                     including its single-precision fInner2 = 1.1e-2 L^2);
- *   kF64              all FP64 with the CPU constants (fInner2 = 1.2e-3 L^2);
- *   kMix              FP32 everywhere except the terms with r^2 < 0.05 L^2
- *                     (only the central replica can get there), which are
- *                     evaluated in FP64 where the hole's -erf and the 1/r^k
- *                     terms cancel.  d = x - cm is formed in FP64 and
- *                     rounded once, so it is accurate to FP32 rounding of d.
+ *   ewald_f32_kernel  the drop-in form on the FP32 ABI: the reference's
+ *                     algorithm and constants, including its single-precision
+ *                     fInner2 = 1.1e-2 L^2;
+ *   ewald_f64_kernel  all FP64 with the CPU constants (fInner2 = 1.2e-3 L^2);
+ *   ewald_mix_kernel  FP32-mixed: d = x - cm in FP64 rounded once; each warp
+ *                     first culls the replica lattice against the bounding box
+ *                     of its 32 particles (so threads loop over ~90 candidate
+ *                     replicas, not 343); hole terms with alpha^2 r^2 < 1 use
+ *                     the convergent power series of the g_n (no cancellation
+ *                     between -erf(ar)/r and the 1/r^k terms); other terms use
+ *                     a rational erfc with fractional error < 1.2e-7 (Press et
+ *                     al., Numerical Recipes, "erfcc", a Chebyshev fit) and
+ *                     the hardware exp2; the k-space phase is reduced to one
+ *                     turn from the integer h before the hardware sin/cos.
  */
 #include "chg_internal.h"
 
@@ -119,7 +125,6 @@ __global__ void __launch_bounds__(128) ewald_f32_kernel(const CompactPartData* _
   v.a.z += az;
   v.potential += fPot;
 }
-
 struct EwaldFpArgs {
   double mom[12];
   double L, fEwCut2, alpha, alpha2, k1, ka;
@@ -170,14 +175,12 @@ __device__ __forceinline__ void ewald_term_f64(const EwaldFpArgs& P, double x, d
   az += g2 * Q2mirz - z * Qta;
 }
 
-constexpr double kMixInner = 0.05;  // FP64 below r^2 < 0.05 L^2 in the mixed form
 
-template <int FORM>
-__global__ void __launch_bounds__(128) ewald_fp_kernel(const double* __restrict__ parts,
-                                                       long long n_parts,
-                                                       const int* __restrict__ idx, long long n_idx,
-                                                       double* __restrict__ vars,
-                                                       const __grid_constant__ EwaldFpArgs P) {
+__global__ void __launch_bounds__(128) ewald_f64_kernel(const double* __restrict__ parts,
+                                                        long long n_parts,
+                                                        const int* __restrict__ idx,
+                                                        long long n_idx, double* __restrict__ vars,
+                                                        const __grid_constant__ EwaldFpArgs P) {
   const long long k = blockIdx.x * (long long)blockDim.x + threadIdx.x;
   if (k >= n_idx) return;
   const long long j = idx ? (long long)idx[k] : k;
@@ -186,104 +189,227 @@ __global__ void __launch_bounds__(128) ewald_fp_kernel(const double* __restrict_
   const double dxd = p[2] - P.mom[3], dyd = p[3] - P.mom[4], dzd = p[4] - P.mom[5];
   const int nE = P.nEwReps, nR = P.nReps;
   double fPot = P.mom[2] * P.k1, ax = 0, ay = 0, az = 0;
-  if constexpr (FORM == kF64) {
-    const double fInner2 = 1.2e-3 * P.L * P.L;
-    for (int ix = -nE; ix <= nE; ++ix) {
-      const bool hx = (ix >= -nR && ix <= nR);
-      const double x = dxd + ix * P.L;
-      for (int iy = -nE; iy <= nE; ++iy) {
-        const bool hxy = hx && (iy >= -nR && iy <= nR);
-        const double y = dyd + iy * P.L;
-        for (int iz = -nE; iz <= nE; ++iz) {
-          const bool hole = hxy && (iz >= -nR && iz <= nR);
-          const double z = dzd + iz * P.L;
-          const double r2 = x * x + y * y + z * z;
-          if (r2 > P.fEwCut2 && !hole) continue;
-          ewald_term_f64(P, x, y, z, hole, fInner2, fPot, ax, ay, az);
-        }
+  const double fInner2 = 1.2e-3 * P.L * P.L;
+  for (int ix = -nE; ix <= nE; ++ix) {
+    const bool hx = (ix >= -nR && ix <= nR);
+    const double x = dxd + ix * P.L;
+    for (int iy = -nE; iy <= nE; ++iy) {
+      const bool hxy = hx && (iy >= -nR && iy <= nR);
+      const double y = dyd + iy * P.L;
+      for (int iz = -nE; iz <= nE; ++iz) {
+        const bool hole = hxy && (iz >= -nR && iz <= nR);
+        const double z = dzd + iz * P.L;
+        const double r2 = x * x + y * y + z * z;
+        if (r2 > P.fEwCut2 && !hole) continue;
+        ewald_term_f64(P, x, y, z, hole, fInner2, fPot, ax, ay, az);
       }
     }
-    for (int i = 0; i < P.nEwhLoop; ++i) {
-      const double* e = P.ewt[i];
-      const double hdotx = e[0] * dxd + e[1] * dyd + e[2] * dzd;
-      double s, c;
-      sincos(hdotx, &s, &c);
-      fPot += e[3] * c + e[4] * s;
-      const double t = e[3] * s - e[4] * c;
-      ax += e[0] * t;
-      ay += e[1] * t;
-      az += e[2] * t;
-    }
-  } else {
-    const float L = (float)P.L, alpha = (float)P.alpha, alpha2 = (float)P.alpha2;
-    const float ka = (float)P.ka, cut2 = (float)P.fEwCut2;
-    const float inner2 = (float)(kMixInner * P.L * P.L);
-    const float M = (float)P.mom[2];
-    const float mxx = (float)P.mom[6], mxy = (float)P.mom[7], mxz = (float)P.mom[8];
-    const float myy = (float)P.mom[9], myz = (float)P.mom[10], mzz = (float)P.mom[11];
-    const float Q2 = 0.5f * (mxx + myy + mzz);
-    const float dx = (float)dxd, dy = (float)dyd, dz = (float)dzd;
-    float fx = 0.f, fy = 0.f, fz = 0.f, fp = 0.f;
-    for (int ix = -nE; ix <= nE; ++ix) {
-      const bool hx = (ix >= -nR && ix <= nR);
-      const float x = dx + ix * L;
-      for (int iy = -nE; iy <= nE; ++iy) {
-        const bool hxy = hx && (iy >= -nR && iy <= nR);
-        const float y = dy + iy * L;
-        for (int iz = -nE; iz <= nE; ++iz) {
-          const bool hole = hxy && (iz >= -nR && iz <= nR);
-          const float z = dz + iz * L;
-          const float r2 = x * x + y * y + z * z;
-          if (r2 > cut2 && !hole) continue;
-          if (r2 < inner2) {
-            ewald_term_f64(P, dxd + ix * P.L, dyd + iy * P.L, dzd + iz * P.L, hole,
-                           1.2e-3 * P.L * P.L, fPot, ax, ay, az);
-            continue;
-          }
-          const float dir = rsqrtf(r2);
-          const float dir2 = dir * dir;
-          const float a = expf(-r2 * alpha2) * (ka * dir2);
-          const float ar = alpha * (r2 * dir);
-          float g0 = hole ? -erff(ar) : erfcf(ar);
-          g0 *= dir;
-          const float g1 = g0 * dir2 + a;
-          const float g2 = 3.f * g1 * dir2 + (2.f * alpha2) * a;
-          const float g3 = 5.f * g2 * dir2 + (4.f * alpha2 * alpha2) * a;
-          const float Q2mirx = mxx * x + mxy * y + mxz * z;
-          const float Q2miry = mxy * x + myy * y + myz * z;
-          const float Q2mirz = mxz * x + myz * y + mzz * z;
-          const float Q2mir = 0.5f * (Q2mirx * x + Q2miry * y + Q2mirz * z);
-          const float Qta = g1 * M - g2 * Q2 + g3 * Q2mir;
-          fp -= g0 * M - g1 * Q2 + g2 * Q2mir;
-          fx += g2 * Q2mirx - x * Qta;
-          fy += g2 * Q2miry - y * Qta;
-          fz += g2 * Q2mirz - z * Qta;
-        }
-      }
-    }
-    for (int i = 0; i < P.nEwhLoop; ++i) {
-      const double* e = P.ewt[i];
-      const float hx = (float)e[0], hy = (float)e[1], hz = (float)e[2];
-      const float hc = (float)e[3], hs = (float)e[4];
-      const float hdotx = hx * dx + hy * dy + hz * dz;
-      float s, c;
-      sincosf(hdotx, &s, &c);
-      fp += hc * c + hs * s;
-      const float t = hc * s - hs * c;
-      fx += hx * t;
-      fy += hy * t;
-      fz += hz * t;
-    }
-    fPot += fp;
-    ax += fx;
-    ay += fy;
-    az += fz;
+  }
+  for (int i = 0; i < P.nEwhLoop; ++i) {
+    const double* e = P.ewt[i];
+    const double hdotx = e[0] * dxd + e[1] * dyd + e[2] * dzd;
+    double s, c;
+    sincos(hdotx, &s, &c);
+    fPot += e[3] * c + e[4] * s;
+    const double t = e[3] * s - e[4] * c;
+    ax += e[0] * t;
+    ay += e[1] * t;
+    az += e[2] * t;
   }
   double* v = vars + 5 * j;
   v[0] += ax;
   v[1] += ay;
   v[2] += az;
   v[3] += fPot;
+}
+
+/* ---- FP32-mixed form ---- */
+
+constexpr int kMixMaxReps = 4;                       // nEwReps limit of the mixed kernel
+constexpr int kMixMaxRepl = (2 * kMixMaxReps + 1) * (2 * kMixMaxReps + 1) * (2 * kMixMaxReps + 1);
+constexpr int kMixWarps = 4;
+
+struct EwaldMixArgs {
+  double cm[3];
+  float M, xx, xy, xz, yy, yz, zz, Q2;
+  float L, alpha2, ka, cut2, k1M, twopi_over_L;
+  int nReps, nEwReps, nEwhLoop;
+  float4 h[CHANGA_MAX_EWH];  // integer h as floats, hCfac
+  float hs[CHANGA_MAX_EWH];  // hSfac
+};
+
+/* Series of the hole terms, g_n = -(2 alpha^2)^n ka S_n(s), s = alpha^2 r^2,
+ * S_n(s) = sum_j (-1)^j s^j / (j! (2j + 2n + 1)): the Taylor series of
+ * -erf(alpha r)/r and of its derivatives g_{n+1} = -(1/r) dg_n/dr.  For
+ * s < 1, twelve terms reach FP32 rounding and every term is smaller than
+ * the previous one, so nothing cancels. */
+__host__ __device__ constexpr double hole_coef(int n, int j) {
+  double f = 1.0;
+  for (int q = 2; q <= j; ++q) f *= q;
+  return ((j & 1) ? -1.0 : 1.0) / (f * (2 * j + 2 * n + 1));
+}
+
+template <int NN>
+__device__ __forceinline__ float hole_series(float s) {
+  constexpr float c0 = (float)hole_coef(NN, 0), c1 = (float)hole_coef(NN, 1);
+  constexpr float c2 = (float)hole_coef(NN, 2), c3 = (float)hole_coef(NN, 3);
+  constexpr float c4 = (float)hole_coef(NN, 4), c5 = (float)hole_coef(NN, 5);
+  constexpr float c6 = (float)hole_coef(NN, 6), c7 = (float)hole_coef(NN, 7);
+  constexpr float c8 = (float)hole_coef(NN, 8), c9 = (float)hole_coef(NN, 9);
+  constexpr float c10 = (float)hole_coef(NN, 10), c11 = (float)hole_coef(NN, 11);
+  float a = c11;
+  a = fmaf(a, s, c10);
+  a = fmaf(a, s, c9);
+  a = fmaf(a, s, c8);
+  a = fmaf(a, s, c7);
+  a = fmaf(a, s, c6);
+  a = fmaf(a, s, c5);
+  a = fmaf(a, s, c4);
+  a = fmaf(a, s, c3);
+  a = fmaf(a, s, c2);
+  a = fmaf(a, s, c1);
+  return fmaf(a, s, c0);
+}
+
+/* erfc(x) for x >= 0 with fractional error below 1.2e-7: the rational
+ * Chebyshev fit of Press, Teukolsky, Vetterling & Flannery, Numerical
+ * Recipes (2nd ed., section 6.2, "erfcc"); e = exp(-x^2 - 1.26551223 + ...)
+ * evaluated with the hardware exp2. */
+__device__ __forceinline__ float erfc_nr(float x, float x2) {
+  const float t = __fdividef(1.0f, fmaf(0.5f, x, 1.0f));
+  float p = 0.17087277f;
+  p = fmaf(p, t, -0.82215223f);
+  p = fmaf(p, t, 1.48851587f);
+  p = fmaf(p, t, -1.13520398f);
+  p = fmaf(p, t, 0.27886807f);
+  p = fmaf(p, t, -0.18628806f);
+  p = fmaf(p, t, 0.09678418f);
+  p = fmaf(p, t, 0.37409196f);
+  p = fmaf(p, t, 1.00002368f);
+  p = fmaf(p, t, -1.26551223f);
+  return t * __expf(p - x2);
+}
+
+__global__ void __launch_bounds__(kMixWarps * 32) ewald_mix_kernel(
+    const double* __restrict__ parts, long long n_parts, const int* __restrict__ idx,
+    long long n_idx, double* __restrict__ vars, const __grid_constant__ EwaldMixArgs P) {
+  __shared__ short repl[kMixWarps][kMixMaxRepl];
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const long long k = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  long long j = -1;
+  if (k < n_idx) {
+    j = idx ? (long long)idx[k] : k;
+    if (j < 0 || j >= n_parts) j = -1;
+  }
+  const bool live = j >= 0;
+  float dx = 0.f, dy = 0.f, dz = 0.f;
+  if (live) {
+    const double* p = parts + 5 * j;
+    dx = (float)(p[2] - P.cm[0]);
+    dy = (float)(p[3] - P.cm[1]);
+    dz = (float)(p[4] - P.cm[2]);
+  }
+  /* bounding box of the warp's offsets */
+  float lo[3] = {live ? dx : 1e30f, live ? dy : 1e30f, live ? dz : 1e30f};
+  float hi[3] = {live ? dx : -1e30f, live ? dy : -1e30f, live ? dz : -1e30f};
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+#pragma unroll
+    for (int c = 0; c < 3; ++c) {
+      lo[c] = fminf(lo[c], __shfl_xor_sync(0xffffffffu, lo[c], o));
+      hi[c] = fmaxf(hi[c], __shfl_xor_sync(0xffffffffu, hi[c], o));
+    }
+  }
+  const int nE = P.nEwReps, nR = P.nReps, side = 2 * nE + 1, nrep = side * side * side;
+  const float L = P.L;
+  /* candidate replicas: inside the hole, or within the cut of some point of
+   * the warp's box */
+  int count = 0;
+  for (int base = 0; base < nrep; base += 32) {
+    const int r = base + lane;
+    bool keep = false;
+    if (r < nrep) {
+      const int ix = r / (side * side) - nE, iy = (r / side) % side - nE, iz = r % side - nE;
+      const bool hole = ix >= -nR && ix <= nR && iy >= -nR && iy <= nR && iz >= -nR && iz <= nR;
+      float d2 = 0.f;
+      const int ii[3] = {ix, iy, iz};
+#pragma unroll
+      for (int c = 0; c < 3; ++c) {
+        const float a = lo[c] + ii[c] * L, b = hi[c] + ii[c] * L;
+        const float m = a > 0.f ? a : (b < 0.f ? -b : 0.f);
+        d2 = fmaf(m, m, d2);
+      }
+      keep = hole || d2 <= P.cut2 * 1.0001f;
+    }
+    const unsigned bal = __ballot_sync(0xffffffffu, keep);
+    if (keep) repl[warp][count + __popc(bal & ((1u << lane) - 1u))] = (short)r;
+    count += __popc(bal);
+  }
+  __syncwarp();
+  if (!live) return;
+
+  const float a2 = P.alpha2, twoa2 = 2.f * a2, foura4 = twoa2 * twoa2, ka = P.ka;
+  const float M = P.M, Q2 = P.Q2;
+  float fp = P.k1M, fx = 0.f, fy = 0.f, fz = 0.f;
+  for (int q = 0; q < count; ++q) {
+    const int r = repl[warp][q];
+    const int ix = r / (side * side) - nE, iy = (r / side) % side - nE, iz = r % side - nE;
+    const bool hole = ix >= -nR && ix <= nR && iy >= -nR && iy <= nR && iz >= -nR && iz <= nR;
+    const float x = dx + ix * L, y = dy + iy * L, z = dz + iz * L;
+    const float r2 = x * x + y * y + z * z;
+    if (r2 > P.cut2 && !hole) continue;
+    const float s = a2 * r2;
+    float g0, g1, g2, g3;
+    if (hole && s < 1.0f) {
+      g0 = -ka * hole_series<0>(s);
+      g1 = -twoa2 * ka * hole_series<1>(s);
+      g2 = -foura4 * ka * hole_series<2>(s);
+      g3 = -foura4 * twoa2 * ka * hole_series<3>(s);
+    } else {
+      const float dir = rsqrtf(r2);
+      const float dir2 = dir * dir;
+      const float ar = sqrtf(s);
+      const float e = __expf(-s);
+      const float a = ka * dir2 * e;
+      const float ec = erfc_nr(ar, s);
+      g0 = (hole ? ec - 1.0f : ec) * dir;
+      g1 = fmaf(g0, dir2, a);
+      g2 = fmaf(3.f * g1, dir2, twoa2 * a);
+      g3 = fmaf(5.f * g2, dir2, foura4 * a);
+    }
+    const float Q2mirx = P.xx * x + P.xy * y + P.xz * z;
+    const float Q2miry = P.xy * x + P.yy * y + P.yz * z;
+    const float Q2mirz = P.xz * x + P.yz * y + P.zz * z;
+    const float Q2mir = 0.5f * (Q2mirx * x + Q2miry * y + Q2mirz * z);
+    const float Qta = g1 * M - g2 * Q2 + g3 * Q2mir;
+    fp -= g0 * M - g1 * Q2 + g2 * Q2mir;
+    fx += g2 * Q2mirx - x * Qta;
+    fy += g2 * Q2miry - y * Qta;
+    fz += g2 * Q2mirz - z * Qta;
+  }
+  /* k-space: phase = 2 pi (h . d) / L, reduced to one turn */
+  const float invL = 1.0f / L;
+  const float ux = dx * invL, uy = dy * invL, uz = dz * invL;
+  float kx = 0.f, ky = 0.f, kz = 0.f;
+  for (int i = 0; i < P.nEwhLoop; ++i) {
+    const float4 h = P.h[i];
+    float f = fmaf(h.x, ux, fmaf(h.y, uy, h.z * uz));
+    f -= rintf(f);
+    float sn, cs;
+    __sincosf(6.28318530717958647692f * f, &sn, &cs);
+    const float hs = P.hs[i];
+    fp += h.w * cs + hs * sn;
+    const float t = h.w * sn - hs * cs;
+    kx = fmaf(h.x, t, kx);
+    ky = fmaf(h.y, t, ky);
+    kz = fmaf(h.z, t, kz);
+  }
+  const float tl = P.twopi_over_L;
+  double* v = vars + 5 * j;
+  v[0] += (double)fx + (double)(tl * kx);
+  v[1] += (double)fy + (double)(tl * ky);
+  v[2] += (double)fz + (double)(tl * kz);
+  v[3] += (double)fp;
 }
 
 }  // namespace
@@ -300,6 +426,7 @@ cudaError_t launch_ewald_f32(const CompactPartData* parts, VariablePartData* var
   for (int i = 0; i < nh; ++i) P.ewt[i] = ewt[i];
   for (int i = nh; i < NEWH; ++i) P.ewt[i] = EwtData{0, 0, 0, 0, 0};
   int blocks = (n + 127) / 128;
+  TimingScope ts(kKidEwaldF32, s);
   ewald_f32_kernel<<<blocks, 128, 0, s>>>(parts, vars, markers, largephase, first, last, P);
   count_launch();
   return cudaGetLastError();
@@ -309,28 +436,63 @@ cudaError_t launch_ewald_fp(int form, const double* parts, long long n_parts, co
                             long long n_idx, const ChangaEwaldParams& p, double* vars,
                             cudaStream_t s) {
   if (n_idx <= 0) return cudaSuccess;
-  if (p.nEwhLoop < 0 || p.nEwhLoop > CHANGA_MAX_EWH || (p.nEwhLoop > 0 && !p.ewt))
+  if (p.nEwhLoop < 0 || p.nEwhLoop > CHANGA_MAX_EWH || (p.nEwhLoop > 0 && !p.ewt) || !(p.L > 0))
     return cudaErrorInvalidValue;
-  EwaldFpArgs P;
-  for (int i = 0; i < 12; ++i) P.mom[i] = p.root[i];
   const double L = p.L;
-  P.L = L;
-  P.fEwCut2 = p.fEwCut * p.fEwCut * L * L;
-  P.alpha = 2.0 / L;
-  P.alpha2 = P.alpha * P.alpha;
-  P.k1 = M_PI / (P.alpha2 * L * L * L);
-  P.ka = 2.0 * P.alpha / sqrt(M_PI);
+  const double alpha = 2.0 / L, alpha2 = alpha * alpha;
+  const int nE0 = (int)ceil(p.fEwCut);
+  const int nE = nE0 > p.nReps ? nE0 : p.nReps;
+  if (form == kF64) {
+    EwaldFpArgs P;
+    for (int i = 0; i < 12; ++i) P.mom[i] = p.root[i];
+    P.L = L;
+    P.fEwCut2 = p.fEwCut * p.fEwCut * L * L;
+    P.alpha = alpha;
+    P.alpha2 = alpha2;
+    P.k1 = M_PI / (alpha2 * L * L * L);
+    P.ka = 2.0 * alpha / sqrt(M_PI);
+    P.nReps = p.nReps;
+    P.nEwReps = nE;
+    P.nEwhLoop = p.nEwhLoop;
+    for (int i = 0; i < p.nEwhLoop; ++i)
+      for (int k = 0; k < 5; ++k) P.ewt[i][k] = p.ewt[5 * i + k];
+    int blocks = (int)((n_idx + 127) / 128);
+    TimingScope ts(kKidEwaldF64, s);
+    ewald_f64_kernel<<<blocks, 128, 0, s>>>(parts, n_parts, idx, n_idx, vars, P);
+    count_launch();
+    return cudaGetLastError();
+  }
+  if (nE > kMixMaxReps) return cudaErrorInvalidValue;
+  EwaldMixArgs P;
+  for (int c = 0; c < 3; ++c) P.cm[c] = p.root[3 + c];
+  P.M = (float)p.root[2];
+  P.xx = (float)p.root[6];
+  P.xy = (float)p.root[7];
+  P.xz = (float)p.root[8];
+  P.yy = (float)p.root[9];
+  P.yz = (float)p.root[10];
+  P.zz = (float)p.root[11];
+  P.Q2 = (float)(0.5 * (p.root[6] + p.root[9] + p.root[11]));
+  P.L = (float)L;
+  P.alpha2 = (float)alpha2;
+  P.ka = (float)(2.0 * alpha / sqrt(M_PI));
+  P.cut2 = (float)(p.fEwCut * p.fEwCut * L * L);
+  P.k1M = (float)(p.root[2] * M_PI / (alpha2 * L * L * L));
+  P.twopi_over_L = (float)(2.0 * M_PI / L);
   P.nReps = p.nReps;
-  int nE = (int)ceil(p.fEwCut);
-  P.nEwReps = nE > p.nReps ? nE : p.nReps;
+  P.nEwReps = nE;
   P.nEwhLoop = p.nEwhLoop;
-  for (int i = 0; i < p.nEwhLoop; ++i)
-    for (int k = 0; k < 5; ++k) P.ewt[i][k] = p.ewt[5 * i + k];
-  int blocks = (int)((n_idx + 127) / 128);
-  if (form == kF64)
-    ewald_fp_kernel<kF64><<<blocks, 128, 0, s>>>(parts, n_parts, idx, n_idx, vars, P);
-  else
-    ewald_fp_kernel<kMix><<<blocks, 128, 0, s>>>(parts, n_parts, idx, n_idx, vars, P);
+  for (int i = 0; i < p.nEwhLoop; ++i) {
+    const double* e = p.ewt + 5 * i;
+    const double f = L / (2.0 * M_PI);
+    P.h[i] = make_float4((float)rint(e[0] * f), (float)rint(e[1] * f), (float)rint(e[2] * f),
+                         (float)e[3]);
+    P.hs[i] = (float)e[4];
+  }
+  int threads = kMixWarps * 32;
+  int blocks = (int)((n_idx + threads - 1) / threads);
+  TimingScope ts(kKidEwaldMix, s);
+  ewald_mix_kernel<<<blocks, threads, 0, s>>>(parts, n_parts, idx, n_idx, vars, P);
   count_launch();
   return cudaGetLastError();
 }

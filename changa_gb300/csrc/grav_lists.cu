@@ -42,11 +42,9 @@ constexpr int kWarps = 8;
 constexpr int kThreads = kWarps * 32;
 constexpr unsigned kFull = 0xffffffffu;
 
-__device__ __forceinline__ float rsqrt_t(float x) { return rsqrtf(x); }
 __device__ __forceinline__ double rsqrt_t(double x) { return rsqrt(x); }
 __device__ __forceinline__ float two_over(float t) { return __fdividef(2.0f, t); }
 __device__ __forceinline__ double two_over(double t) { return 2.0 / t; }
-__device__ __forceinline__ float max_t(float a, float b) { return fmaxf(a, b); }
 __device__ __forceinline__ double max_t(double a, double b) { return fmax(a, b); }
 
 /* SPLINEQ inside the softening radius (gravity.h:27-59): both branches. */
@@ -403,6 +401,301 @@ __global__ void __launch_bounds__(kThreads, 2) list_kernel(const ListArgs a) {
   }
 }
 
+/* ------------------------------------------------------------------ */
+/* Source-parallel kernel for the FP32 arithmetic forms (kF32, kMix).  */
+/*                                                                    */
+/* Lanes own list entries instead of targets: each lane holds one     */
+/* source record in registers and the bucket's targets are broadcast  */
+/* from shared memory in chunks of kTC.  A tile of 32 sources x kTC   */
+/* targets leaves every lane with kTC x 4 partial sums, which a       */
+/* butterfly reduce-scatter (31 shuffles) turns into one warp total   */
+/* per lane: lane l ends with target l/4, quantity l%4.  Every lane   */
+/* works whatever the bucket size (buckets average ~0.7 of nBucket),  */
+/* and one broadcast LDS.128 per interaction feeds ~40 FP32 ops.      */
+/* ------------------------------------------------------------------ */
+
+constexpr int kTC = 8;   // targets per reduction chunk
+constexpr int kTB = 32;  // targets staged per block; larger buckets loop
+
+/* v[k] summed over the warp; lane l returns the total of index l. */
+__device__ __forceinline__ float reduce_scatter32(float (&v)[32], int lane) {
+#pragma unroll
+  for (int s = 0; s < 5; ++s) {
+    const int o = 16 >> s, h = 16 >> s;
+    const bool up = (lane & o) != 0;
+#pragma unroll
+    for (int i = 0; i < h; ++i) {
+      const float send = up ? v[i] : v[i + h];
+      const float keep = up ? v[i + h] : v[i];
+      v[i] = keep + __shfl_xor_sync(kFull, send, o);
+    }
+  }
+  return v[0];
+}
+
+/* max over the warp of v[k], k < 8; lane l returns the max of index l/4. */
+__device__ __forceinline__ float max_scatter8(float (&v)[8], int lane) {
+#pragma unroll
+  for (int s = 0; s < 3; ++s) {
+    const int o = 16 >> s, h = 4 >> s;
+    const bool up = (lane & o) != 0;
+#pragma unroll
+    for (int i = 0; i < h; ++i) {
+      const float send = up ? v[i] : v[i + h];
+      const float keep = up ? v[i + h] : v[i];
+      v[i] = fmaxf(keep, __shfl_xor_sync(kFull, send, o));
+    }
+  }
+  v[0] = fmaxf(v[0], __shfl_xor_sync(kFull, v[0], 2));
+  v[0] = fmaxf(v[0], __shfl_xor_sync(kFull, v[0], 1));
+  return v[0];
+}
+
+/* Source record held by one lane (FP32). */
+struct SrcRec {
+  float x, y, z, m, soft;
+  float tr, xx, xy, xz, yy, yz, zz;  // cells only
+};
+
+template <int FORM, bool CELL>
+__device__ __forceinline__ SrcRec load_source(const ListArgs& a, int e, float3 chi, float3 clo) {
+  const int2 ent = __ldg(a.list + e);
+  long long idx = ent.x;
+  if ((unsigned long long)idx >= (unsigned long long)a.n_src) idx = 0;  // memory safety
+  const int code = (ent.y >> 22) & 0x1ff;
+  const float fp = a.fperiod_f;
+  const float ox = (float)((code & 7) - 3) * fp, oy = (float)(((code >> 3) & 7) - 3) * fp,
+              oz = (float)(((code >> 6) & 7) - 3) * fp;
+  SrcRec r;
+  if constexpr (FORM == kF32) {
+    if constexpr (CELL) {
+      const float4* m = reinterpret_cast<const float4*>(
+          static_cast<const CudaMultipoleMoments*>(a.src) + idx);
+      const float4 m0 = __ldg(m), m1 = __ldg(m + 1), m2 = __ldg(m + 2);
+      // m0 {radius, soft, M, cm.x}  m1 {cm.y, cm.z, xx, xy}  m2 {xz, yy, yz, zz}
+      r.x = ox + m0.w;
+      r.y = oy + m1.x;
+      r.z = oz + m1.y;
+      r.m = m0.z;
+      r.soft = m0.y;
+      r.xx = m1.z;
+      r.xy = m1.w;
+      r.xz = m2.x;
+      r.yy = m2.y;
+      r.yz = m2.z;
+      r.zz = m2.w;
+      r.tr = 0.5f * (r.xx + r.yy + r.zz);
+    } else {
+      const CompactPartData* p = static_cast<const CompactPartData*>(a.src) + idx;
+      r.m = __ldg(&p->mass);
+      r.soft = __ldg(&p->soft);
+      r.x = ox + __ldg(&p->position.x);
+      r.y = oy + __ldg(&p->position.y);
+      r.z = oz + __ldg(&p->position.z);
+    }
+  } else {  // kMix: (hi - c_hi + offset) + (lo - c_lo)
+    if constexpr (CELL) {
+      const float4* m = static_cast<const float4*>(a.src) + kCellPackF4 * idx;
+      const float4 h = __ldg(m), l = __ldg(m + 1), q0 = __ldg(m + 2), q1 = __ldg(m + 3);
+      r.x = ((h.x - chi.x) + ox) + (l.x - clo.x);
+      r.y = ((h.y - chi.y) + oy) + (l.y - clo.y);
+      r.z = ((h.z - chi.z) + oz) + (l.z - clo.z);
+      r.m = h.w;
+      r.soft = l.w;
+      r.xx = q0.x;
+      r.xy = q0.y;
+      r.xz = q0.z;
+      r.yy = q0.w;
+      r.yz = q1.x;
+      r.zz = q1.y;
+      r.tr = q1.z;
+    } else {
+      const float4* p = static_cast<const float4*>(a.src) + kPartPackF4 * idx;
+      const float4 h = __ldg(p), l = __ldg(p + 1);
+      r.x = ((h.x - chi.x) + ox) + (l.x - clo.x);
+      r.y = ((h.y - chi.y) + oy) + (l.y - clo.y);
+      r.z = ((h.z - chi.z) + oz) + (l.z - clo.z);
+      r.m = h.w;
+      r.soft = l.w;
+    }
+  }
+  return r;
+}
+
+/* The near-field spline branches of the FP32 forms, out of line: they are
+ * rare, and inlining them at every unrolled call site would multiply the
+ * hot loop's code size past the instruction cache. */
+__device__ __noinline__ float4 splineq_near_f(float dir, float rsq, float twoh) {
+  float4 k;
+  splineq_near(dir, rsq, twoh, k.x, k.y, k.z, k.w);
+  return k;
+}
+__device__ __noinline__ float2 spline_near_f(float r, float dir, float twoh) {
+  float2 k;
+  spline_near(r, dir, twoh, k.x, k.y);
+  return k;
+}
+
+constexpr int kGroup = 16;  // source chunks per reduction (16 terms per lane)
+
+template <int FORM, bool CELL>
+__global__ void __launch_bounds__(kThreads, 2) list_kernel_src(const ListArgs a) {
+  static_assert(FORM != kF64, "FP32 arithmetic forms only");
+  __shared__ __align__(16) float4 tpos[kWarps][kTB];  // target x, y, z, mass
+  __shared__ float tsoft[kWarps][kTB];
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+
+  for (;;) {
+    int b = 0;
+    if (lane == 0) b = (int)atomicAdd(a.queue, 1u);
+    b = __shfl_sync(kFull, b, 0);
+    if (b >= a.n_buckets) break;
+    const int e_begin = max(__ldg(a.markers + b), 0);
+    const int e_end = (int)min((long long)__ldg(a.markers + b + 1), a.n_entries);  // memory safety
+    const long long tbase = __ldg(a.starts + b);
+    const int n = __ldg(a.sizes + b);
+    if (n <= 0 || tbase < 0 || tbase + n > a.n_tgt) continue;  // memory safety
+
+    float3 chi = make_float3(0.f, 0.f, 0.f), clo = chi;
+    if constexpr (FORM == kMix) {
+      const float4* tp = static_cast<const float4*>(a.tgt) + kPartPackF4 * tbase;
+      const float4 h = __ldg(tp), l = __ldg(tp + 1);
+      chi = make_float3(h.x, h.y, h.z);
+      clo = make_float3(l.x, l.y, l.z);
+    }
+
+    for (int tb0 = 0; tb0 < n; tb0 += kTB) {
+      const int nt = min(kTB, n - tb0);
+      __syncwarp();
+      if (lane < nt) {
+        const long long ti = tbase + tb0 + lane;
+        if constexpr (FORM == kF32) {
+          const CompactPartData* p = static_cast<const CompactPartData*>(a.tgt) + ti;
+          tpos[warp][lane] = make_float4(__ldg(&p->position.x), __ldg(&p->position.y),
+                                         __ldg(&p->position.z), __ldg(&p->mass));
+          tsoft[warp][lane] = __ldg(&p->soft);
+        } else {
+          const float4* p = static_cast<const float4*>(a.tgt) + kPartPackF4 * ti;
+          const float4 h = __ldg(p), l = __ldg(p + 1);
+          tpos[warp][lane] = make_float4((h.x - chi.x) + (l.x - clo.x),
+                                         (h.y - chi.y) + (l.y - clo.y),
+                                         (h.z - chi.z) + (l.z - clo.z), h.w);
+          tsoft[warp][lane] = l.w;
+        }
+      }
+      __syncwarp();
+      const int nch = (nt + kTC - 1) / kTC;
+      for (int c = 0; c < nch; ++c) {
+        const int t0 = c * kTC;
+        const int ntc = min(kTC, nt - t0);
+        /* largest target softening of the chunk: pairs beyond
+         * (source soft + this)^2 cannot be inside the spline */
+        float smax = 0.f;
+        for (int tt = 0; tt < ntc; ++tt) smax = fmaxf(smax, tsoft[warp][t0 + tt]);
+        float tot = 0.f, comp = 0.f, idt = 0.f;
+        for (int g0 = e_begin; g0 < e_end; g0 += 32 * kGroup) {
+          const int g1 = min(e_end, g0 + 32 * kGroup);
+          float v[32], id[8];
+#pragma unroll
+          for (int k = 0; k < 32; ++k) v[k] = 0.f;
+#pragma unroll
+          for (int k = 0; k < 8; ++k) id[k] = 0.f;
+          for (int e = g0 + lane; e < g1; e += 32) {
+            const SrcRec s = load_source<FORM, CELL>(a, e, chi, clo);
+            const float tw = s.soft + smax;
+            const float near2 = tw * tw;
+#pragma unroll
+            for (int tt = 0; tt < kTC; ++tt) {
+              if (tt < ntc) {
+                const float4 tp = tpos[warp][t0 + tt];
+                if constexpr (CELL) {
+                  /* gravity.h:436-472: r = target - cell */
+                  const float rx = tp.x - s.x, ry = tp.y - s.y, rz = tp.z - s.z;
+                  const float rsq = rx * rx + ry * ry + rz * rz;
+                  const float dir = rsqrtf(rsq);
+                  const float dir2 = dir * dir;
+                  float av = dir, bv = dir2 * dir;
+                  float cv = 3.f * bv * dir2, dv = 5.f * cv * dir2;
+                  if (rsq <= near2) {
+                    const float twoh = s.soft + tsoft[warp][t0 + tt];
+                    if (rsq == 0.f) {
+                      av = bv = cv = dv = 0.f;
+                    } else if (rsq < twoh * twoh) {
+                      const float4 k = splineq_near_f(dir, rsq, twoh);
+                      av = k.x;
+                      bv = k.y;
+                      cv = k.z;
+                      dv = k.w;
+                    }
+                  }
+                  const float qirx = s.xx * rx + s.xy * ry + s.xz * rz;
+                  const float qiry = s.xy * rx + s.yy * ry + s.yz * rz;
+                  const float qirz = s.xz * rx + s.yz * ry + s.zz * rz;
+                  const float qir = 0.5f * (qirx * rx + qiry * ry + qirz * rz);
+                  const float bM = bv * s.m;
+                  const float qir3 = bM + dv * qir - cv * s.tr;
+                  v[4 * tt + 3] -= s.m * av + cv * qir - bv * s.tr;
+                  v[4 * tt + 0] -= qir3 * rx - cv * qirx;
+                  v[4 * tt + 1] -= qir3 * ry - cv * qiry;
+                  v[4 * tt + 2] -= qir3 * rz - cv * qirz;
+                  id[tt] = fmaxf(id[tt], fmaf(tp.w, bv, bM));
+                } else {
+                  /* gravity.h:276-301: r = source - target */
+                  const float rx = s.x - tp.x, ry = s.y - tp.y, rz = s.z - tp.z;
+                  const float rsq = rx * rx + ry * ry + rz * rz;
+                  const float dir = rsqrtf(rsq);
+                  float av = dir, bv = dir * dir * dir;
+                  if (rsq <= near2) {
+                    const float twoh = s.soft + tsoft[warp][t0 + tt];
+                    if (rsq == 0.f) {
+                      av = bv = 0.f;
+                    } else {
+                      const float r1 = rsq * dir;
+                      if (r1 < twoh) {
+                        const float2 k = spline_near_f(r1, dir, twoh);
+                        av = k.x;
+                        bv = k.y;
+                      }
+                    }
+                  }
+                  const float bm = bv * s.m;
+                  v[4 * tt + 3] -= s.m * av;
+                  v[4 * tt + 0] += rx * bm;
+                  v[4 * tt + 1] += ry * bm;
+                  v[4 * tt + 2] += rz * bm;
+                  id[tt] = fmaxf(id[tt], fmaf(tp.w, bv, bm));
+                }
+              }
+            }
+          }
+          /* 32 sources' partials -> lane l holds target t0 + l/4, quantity
+           * l%4; groups of kGroup chunks are combined with Kahan
+           * compensation (the mixed form) */
+          const float r = reduce_scatter32(v, lane);
+          const float mx = max_scatter8(id, lane);
+          if constexpr (FORM == kMix) kahan_add(tot, comp, r);
+          else tot += r;
+          idt = fmaxf(idt, mx);
+        }
+        const int t = lane >> 2;
+        if (t < ntc) {
+          const int q = lane & 3;
+          const long long to = tbase + tb0 + t0 + t;
+          if constexpr (FORM == kF32) {
+            float* vo = reinterpret_cast<float*>(static_cast<VariablePartData*>(a.vars) + to);
+            vo[q] += tot;
+            if (q == 0) vo[4] = fmaxf(idt, vo[4]);
+          } else {
+            double* vo = static_cast<double*>(a.vars) + 5 * to;
+            vo[q] += (double)tot - (double)comp;
+            if (q == 0) vo[4] = fmax((double)idt, vo[4]);
+          }
+        }
+      }
+    }
+  }
+}
+
 __global__ void pack_cells_kernel(const double* __restrict__ m, long long n, float4* __restrict__ out) {
   for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
        i += (long long)gridDim.x * blockDim.x) {
@@ -429,12 +722,20 @@ __global__ void pack_parts_kernel(const double* __restrict__ p, long long n, flo
   }
 }
 
+/* The FP64 form keeps the target-parallel kernel (its cost is the FP64
+ * pipe, not lane occupancy); the FP32 forms use the source-parallel one. */
+template <int FORM, bool CELL>
+constexpr auto kernel_for() {
+  if constexpr (FORM == kF64) return list_kernel<FORM, CELL>;
+  else return list_kernel_src<FORM, CELL>;
+}
+
 template <int FORM, bool CELL>
 int blocks_per_sm() {
   static int cached = 0;
   if (!cached) {
     int nb = 0;
-    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, list_kernel<FORM, CELL>, kThreads, 0) !=
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, kernel_for<FORM, CELL>(), kThreads, 0) !=
             cudaSuccess ||
         nb < 1)
       nb = 1;
@@ -449,7 +750,8 @@ cudaError_t launch_t(const ListArgs& a, cudaStream_t s) {
   long long want = ((long long)a.n_buckets + kWarps - 1) / kWarps;
   long long cap = (long long)sm_count() * blocks_per_sm<FORM, CELL>();
   int grid = (int)(want < cap ? want : cap);
-  list_kernel<FORM, CELL><<<grid, kThreads, 0, s>>>(a);
+  TimingScope ts(list_kernel_id(FORM, CELL), s);
+  kernel_for<FORM, CELL>()<<<grid, kThreads, 0, s>>>(a);
   count_launch();
   return cudaGetLastError();
 }
@@ -474,6 +776,7 @@ static int grid_for(long long n, int threads) {
 
 cudaError_t launch_pack_cells(const double* moments, long long n, float4* out, cudaStream_t s) {
   if (n <= 0) return cudaSuccess;
+  TimingScope ts(kKidPack, s);
   pack_cells_kernel<<<grid_for(n, 256), 256, 0, s>>>(moments, n, out);
   count_launch();
   return cudaGetLastError();
@@ -481,6 +784,7 @@ cudaError_t launch_pack_cells(const double* moments, long long n, float4* out, c
 
 cudaError_t launch_pack_parts(const double* parts, long long n, float4* out, cudaStream_t s) {
   if (n <= 0) return cudaSuccess;
+  TimingScope ts(kKidPack, s);
   pack_parts_kernel<<<grid_for(n, 256), 256, 0, s>>>(parts, n, out);
   count_launch();
   return cudaGetLastError();

@@ -20,6 +20,7 @@
 #include <cstring>
 #include <mutex>
 #include <unordered_map>
+#include <vector>
 
 #include <cuda.h>
 
@@ -46,6 +47,35 @@ int record_error(int code, const char* what, const char* file, int line) {
 }
 
 void count_launch(unsigned n) { g_launches.fetch_add(n); }
+
+/* ---- optional per-kernel event timing ---- */
+
+static std::atomic<int> g_timing{0};
+static std::mutex g_timing_mu;
+struct EventPair {
+  cudaEvent_t start, stop;
+};
+static std::vector<EventPair> g_timing_events[kKidCount];
+
+TimingScope::TimingScope(int k, cudaStream_t st) : kid(k), s(st), start(nullptr) {
+  if (!g_timing.load() || k < 0 || k >= kKidCount) return;
+  cudaEvent_t e;
+  if (cudaEventCreate(&e) != cudaSuccess) return;
+  cudaEventRecord(e, s);
+  start = e;
+}
+
+TimingScope::~TimingScope() {
+  if (!start) return;
+  cudaEvent_t e;
+  if (cudaEventCreate(&e) != cudaSuccess) {
+    cudaEventDestroy((cudaEvent_t)start);
+    return;
+  }
+  cudaEventRecord(e, s);
+  std::lock_guard<std::mutex> lk(g_timing_mu);
+  g_timing_events[kid].push_back(EventPair{(cudaEvent_t)start, e});
+}
 
 int sm_count() {
   static int cached[64] = {0};
@@ -575,6 +605,28 @@ void changa_gb300_set_completion_hook(changa_completion_hook hook) { g_hook.stor
 void changa_gb300_set_validate(int on) { g_validate.store(on); }
 int changa_gb300_version(void) { return 100; }
 unsigned long long changa_gb300_kernel_launches(void) { return g_launches.load(); }
+
+void changa_gb300_set_timing(int on) { g_timing.store(on); }
+
+int changa_gb300_kernel_time(int kernel, double* total_ms, long long* launches) {
+  if (kernel < 0 || kernel >= kKidCount || !total_ms || !launches) return CHANGA_E_INVALID_ARG;
+  std::vector<EventPair> ev;
+  {
+    std::lock_guard<std::mutex> lk(g_timing_mu);
+    ev.swap(g_timing_events[kernel]);
+  }
+  double sum = 0.0;
+  for (const EventPair& p : ev) {
+    float ms = 0.f;
+    cudaEventSynchronize(p.stop);
+    if (cudaEventElapsedTime(&ms, p.start, p.stop) == cudaSuccess) sum += ms;
+    cudaEventDestroy(p.start);
+    cudaEventDestroy(p.stop);
+  }
+  *total_ms = sum;
+  *launches = (long long)ev.size();
+  return 0;
+}
 
 int changa_validate_request(const ILCell* list, long long n_entries, const int* markers,
                             const int* starts, const int* sizes, int n_buckets,

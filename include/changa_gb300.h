@@ -66,6 +66,15 @@ int changa_gb300_version(void);
 /* Number of kernels this library has launched since load (all forms). */
 unsigned long long changa_gb300_kernel_launches(void);
 
+/* Optional per-kernel timing: while on, every launch is bracketed by CUDA
+ * events on its own stream.  changa_gb300_kernel_time() waits for and sums
+ * the recorded launches of one kernel since its last read, then forgets
+ * them.  Kernel ids: 0/1 drop-in FP32 cell/particle lists, 2/3 FP64,
+ * 4/5 FP32-mixed, 6/7/8 Ewald FP32/FP64/mixed, 9 mixed-form packing. */
+#define CHANGA_KERNEL_COUNT 10
+void changa_gb300_set_timing(int on);
+int changa_gb300_kernel_time(int kernel, double *total_ms, long long *launches);
+
 /* ---- device-resident list requests for the extension forms ---- */
 
 typedef struct ChangaListRequest {

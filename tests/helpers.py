@@ -28,3 +28,16 @@ def force_rel_err(a, ref):
 
 def pot_rel_err(a, ref):
     return np.abs(a[:, 3] - ref[:, 3]) / np.maximum(np.abs(ref[:, 3]), 1e-300)
+
+
+def force_rms_err(a, ref):
+    """Per-particle |a - ref| / rms|ref|: the metric for periodic sets, where
+    net forces on a near-uniform lattice are a small residual of O(1)
+    replica terms and per-particle relative errors lose meaning."""
+    num = np.linalg.norm(a[:, :3] - ref[:, :3], axis=1)
+    return num / np.sqrt((ref[:, :3] ** 2).sum(axis=1).mean())
+
+
+def pot_rms_err(a, ref):
+    """|dpot| / rms(pot); the periodic potential's zero point is arbitrary."""
+    return np.abs(a[:, 3] - ref[:, 3]) / np.sqrt((ref[:, 3] ** 2).mean())
