@@ -152,6 +152,8 @@ CUDA_SIGNATURES = {
     "changa_part_forces_fp64": (_I, [_VP, _LL, _VP, _LL, C.POINTER(ChangaListRequest), _D, _VP, _VP]),
     "changa_cell_forces_mixed": (_I, [_VP, _LL, _VP, _LL, C.POINTER(ChangaListRequest), _D, _VP, _VP]),
     "changa_part_forces_mixed": (_I, [_VP, _LL, _VP, _LL, C.POINTER(ChangaListRequest), _D, _VP, _VP]),
+    "changa_cell_forces_mixed_noalloc": (_I, [_VP, _LL, _VP, _LL, C.POINTER(ChangaListRequest), _D,
+                                              _VP, _VP]),
     "changa_gravity_step": (_I, [_I, _VP, _LL, _VP, _LL, C.POINTER(ChangaListRequest),
                                  C.POINTER(ChangaListRequest), _D, C.POINTER(ChangaEwaldParams),
                                  _VP, _VP]),

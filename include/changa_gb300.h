@@ -107,6 +107,24 @@ int changa_part_forces_mixed(const double *sources, long long n_sources,
                              const ChangaListRequest *req, double fperiod, double *vars,
                              cudaStream_t stream);
 
+/* changa_cell_forces_mixed without any device allocation.  No counterpart
+ * in the reference.  For callers that must not let a library allocate (a
+ * host code whose device memory is all handed to its own pool allocator, or
+ * one that enqueues from a thread that must never wait for the device, as
+ * cudaMalloc/cudaFree can synchronise it).  The scratch (packed moments,
+ * packed targets, work-queue counter) lives in one fixed 16 MiB + 256 B
+ * array inside the library, held on every GPU that loads it until exit;
+ * 64 B x n_moments + 32 B x n_targets must fit in 16 MiB (each rounded up to
+ * 256 B), else CHANGA_E_TOO_LARGE and nothing is enqueued.  The first call
+ * on a device looks up the array's device address: make it before any
+ * stream capture.  Calls share the array: two calls that overlap on the GPU
+ * race; order them on one stream.  Inputs and outputs as for
+ * changa_cell_forces_mixed (device pointers). */
+int changa_cell_forces_mixed_noalloc(const double *moments, long long n_moments,
+                                     const double *targets, long long n_targets,
+                                     const ChangaListRequest *req, double fperiod,
+                                     double *vars, cudaStream_t stream);
+
 /* One whole force evaluation: cell lists + particle lists (+ Ewald when
  * ewald != NULL) for particles that are both sources and targets.
  * form: CHANGA_FORM_FP64 or CHANGA_FORM_MIXED. */
