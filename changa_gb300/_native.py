@@ -147,6 +147,9 @@ CUDA_SIGNATURES = {
     "changa_gb300_version": (_I, []),
     "changa_gb300_kernel_launches": (C.c_ulonglong, []),
     "changa_gb300_set_timing": (None, [_I]),
+    "changa_gb300_list_variant_count": (_I, []),
+    "changa_gb300_set_list_variant": (_I, [_I, _I]),
+    "changa_gb300_get_list_variant": (_I, [_I]),
     "changa_gb300_kernel_time": (_I, [_I, C.POINTER(C.c_double), C.POINTER(C.c_longlong)]),
     "changa_cell_forces_fp64": (_I, [_VP, _LL, _VP, _LL, C.POINTER(ChangaListRequest), _D, _VP, _VP]),
     "changa_part_forces_fp64": (_I, [_VP, _LL, _VP, _LL, C.POINTER(ChangaListRequest), _D, _VP, _VP]),
@@ -160,6 +163,13 @@ CUDA_SIGNATURES = {
     "changa_gravity_step_host": (_I, [_I, _VP, _LL, _VP, _LL, C.POINTER(ChangaListRequest),
                                       C.POINTER(ChangaListRequest), _D,
                                       C.POINTER(ChangaEwaldParams), _VP, _VP]),
+    "changa_gravity_graph_create": (_VP, [_I, _VP, _LL, _VP, _LL, C.POINTER(ChangaListRequest),
+                                         C.POINTER(ChangaListRequest), _D,
+                                         C.POINTER(ChangaEwaldParams), _VP, _I]),
+    "changa_gravity_graph_launch": (_I, [_VP, _VP]),
+    "changa_gravity_vjp_mixed": (_I, [_VP, _LL, _VP, _LL, C.POINTER(ChangaListRequest),
+                                      C.POINTER(ChangaListRequest), _D, _VP, _VP, _VP, _VP, _VP]),
+    "changa_gravity_graph_destroy": (None, [_VP]),
     "changa_ewald_forces": (_I, [_I, _VP, _LL, _VP, _LL, C.POINTER(ChangaEwaldParams), _VP, _VP]),
     "changa_ewald_table": (_I, [_VP, _D, _D, _VP, _I]),
 }
@@ -179,6 +189,7 @@ HOST_SIGNATURES = {
     "chg_tree_serialize": (C.c_long, [_VP, _I, C.c_long, C.c_long, _VP, _VP, _VP, _VP, _VP,
                                       C.c_long, C.c_long]),
     "chg_tree_drop_lists": (None, [_VP]),
+    "chg_tree_get_structure": (None, [_VP, _VP, _VP]),
 }
 
 

@@ -32,6 +32,7 @@
  *         are folded into Kahan-compensated per-particle totals.
  */
 #include <type_traits>
+#include <utility>
 
 #include "chg_internal.h"
 
@@ -457,21 +458,65 @@ struct SrcRec {
   float tr, xx, xy, xz, yy, yz, zz;  // cells only
 };
 
+/* ---- asynchronous gathers (cp.async, sm_80+) ---- */
+
+__device__ __forceinline__ void cp_async16(void* smem, const void* gmem) {
+  const unsigned s = (unsigned)__cvta_generic_to_shared(smem);
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 16;\n" ::"r"(s), "l"(gmem) : "memory");
+}
+__device__ __forceinline__ void cp_async4(void* smem, const void* gmem) {
+  const unsigned s = (unsigned)__cvta_generic_to_shared(smem);
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 4;\n" ::"r"(s), "l"(gmem) : "memory");
+}
+__device__ __forceinline__ void cp_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
+template <int N>
+__device__ __forceinline__ void cp_wait() {
+  asm volatile("cp.async.wait_group %0;\n" ::"n"(N) : "memory");
+}
+
+/* Words of one source record: 16-byte words (kMix cells 4, kF32 cells 3,
+ * kMix particles 2) or, for the 20-byte kF32 particles, 5 single words.
+ * Stored per lane as structure of arrays, so reads are conflict-free. */
 template <int FORM, bool CELL>
-__device__ __forceinline__ SrcRec load_source(const ListArgs& a, int e, float3 chi, float3 clo) {
-  const int2 ent = __ldg(a.list + e);
-  long long idx = ent.x;
-  if ((unsigned long long)idx >= (unsigned long long)a.n_src) idx = 0;  // memory safety
-  const int code = (ent.y >> 22) & 0x1ff;
+struct RawWords {
+  static constexpr int kWords = FORM == kMix ? (CELL ? 4 : 2) : (CELL ? 3 : 5);
+  static constexpr bool kWide = !(FORM == kF32 && !CELL);
+};
+
+/* Issues the asynchronous copy of source record idx into this lane's slot. */
+template <int FORM, bool CELL>
+__device__ __forceinline__ void fetch_source(const ListArgs& a, long long idx, float4* buf4,
+                                             float* buf1, int lane) {
+  using R = RawWords<FORM, CELL>;
+  if constexpr (R::kWide) {
+    const float4* src;
+    if constexpr (FORM == kF32)
+      src = reinterpret_cast<const float4*>(static_cast<const CudaMultipoleMoments*>(a.src) + idx);
+    else
+      src = static_cast<const float4*>(a.src) + (CELL ? kCellPackF4 : kPartPackF4) * idx;
+#pragma unroll
+    for (int w = 0; w < R::kWords; ++w) cp_async16(buf4 + w * 32 + lane, src + w);
+  } else {
+    const float* src =
+        reinterpret_cast<const float*>(static_cast<const CompactPartData*>(a.src) + idx);
+#pragma unroll
+    for (int w = 0; w < R::kWords; ++w) cp_async4(buf1 + w * 32 + lane, src + w);
+  }
+}
+
+/* Builds the lane's record from its landed words, the replica code and the
+ * bucket centre (kMix: (hi - c_hi + offset) + (lo - c_lo)). */
+template <int FORM, bool CELL>
+__device__ __forceinline__ SrcRec finish_source(const ListArgs& a, const float4* buf4,
+                                                const float* buf1, int lane, int code, float3 chi,
+                                                float3 clo) {
   const float fp = a.fperiod_f;
   const float ox = (float)((code & 7) - 3) * fp, oy = (float)(((code >> 3) & 7) - 3) * fp,
               oz = (float)(((code >> 6) & 7) - 3) * fp;
   SrcRec r;
   if constexpr (FORM == kF32) {
     if constexpr (CELL) {
-      const float4* m = reinterpret_cast<const float4*>(
-          static_cast<const CudaMultipoleMoments*>(a.src) + idx);
-      const float4 m0 = __ldg(m), m1 = __ldg(m + 1), m2 = __ldg(m + 2);
+      const float4 m0 = buf4[lane], m1 = buf4[32 + lane], m2 = buf4[64 + lane];
       // m0 {radius, soft, M, cm.x}  m1 {cm.y, cm.z, xx, xy}  m2 {xz, yy, yz, zz}
       r.x = ox + m0.w;
       r.y = oy + m1.x;
@@ -486,22 +531,21 @@ __device__ __forceinline__ SrcRec load_source(const ListArgs& a, int e, float3 c
       r.zz = m2.w;
       r.tr = 0.5f * (r.xx + r.yy + r.zz);
     } else {
-      const CompactPartData* p = static_cast<const CompactPartData*>(a.src) + idx;
-      r.m = __ldg(&p->mass);
-      r.soft = __ldg(&p->soft);
-      r.x = ox + __ldg(&p->position.x);
-      r.y = oy + __ldg(&p->position.y);
-      r.z = oz + __ldg(&p->position.z);
+      r.m = buf1[lane];
+      r.soft = buf1[32 + lane];
+      r.x = ox + buf1[64 + lane];
+      r.y = oy + buf1[96 + lane];
+      r.z = oz + buf1[128 + lane];
     }
-  } else {  // kMix: (hi - c_hi + offset) + (lo - c_lo)
+  } else {
+    const float4 h = buf4[lane], l = buf4[32 + lane];
+    r.x = ((h.x - chi.x) + ox) + (l.x - clo.x);
+    r.y = ((h.y - chi.y) + oy) + (l.y - clo.y);
+    r.z = ((h.z - chi.z) + oz) + (l.z - clo.z);
+    r.m = h.w;
+    r.soft = l.w;
     if constexpr (CELL) {
-      const float4* m = static_cast<const float4*>(a.src) + kCellPackF4 * idx;
-      const float4 h = __ldg(m), l = __ldg(m + 1), q0 = __ldg(m + 2), q1 = __ldg(m + 3);
-      r.x = ((h.x - chi.x) + ox) + (l.x - clo.x);
-      r.y = ((h.y - chi.y) + oy) + (l.y - clo.y);
-      r.z = ((h.z - chi.z) + oz) + (l.z - clo.z);
-      r.m = h.w;
-      r.soft = l.w;
+      const float4 q0 = buf4[64 + lane], q1 = buf4[96 + lane];
       r.xx = q0.x;
       r.xy = q0.y;
       r.xz = q0.z;
@@ -509,14 +553,6 @@ __device__ __forceinline__ SrcRec load_source(const ListArgs& a, int e, float3 c
       r.yz = q1.x;
       r.zz = q1.y;
       r.tr = q1.z;
-    } else {
-      const float4* p = static_cast<const float4*>(a.src) + kPartPackF4 * idx;
-      const float4 h = __ldg(p), l = __ldg(p + 1);
-      r.x = ((h.x - chi.x) + ox) + (l.x - clo.x);
-      r.y = ((h.y - chi.y) + oy) + (l.y - clo.y);
-      r.z = ((h.z - chi.z) + oz) + (l.z - clo.z);
-      r.m = h.w;
-      r.soft = l.w;
     }
   }
   return r;
@@ -536,13 +572,31 @@ __device__ __noinline__ float2 spline_near_f(float r, float dir, float twoh) {
   return k;
 }
 
-constexpr int kGroup = 16;  // source chunks per reduction (16 terms per lane)
+/* Variants of the source-parallel kernel, chosen at run time (by the
+ * autotuner or changa_gb300_set_list_variant): MINB resident blocks per SM
+ * (the register cap) x GROUP source chunks per reduction (the list tile). */
+struct Variant {
+  int minb, group;
+};
+constexpr Variant kVariants[] = {{2, 16}, {3, 16}, {4, 16}, {3, 32}, {2, 32}};
+constexpr int kNumVariants = sizeof(kVariants) / sizeof(kVariants[0]);
 
-template <int FORM, bool CELL>
-__global__ void __launch_bounds__(kThreads, 2) list_kernel_src(const ListArgs a) {
+/* Source-parallel list kernel of the FP32 forms.  Per warp and bucket: the
+ * targets (kTB at a time) sit in shared memory; for each chunk of kTC
+ * targets the list streams 32 entries at a time, one per lane.  The record
+ * of chunk k+1 travels to shared memory by cp.async while chunk k computes,
+ * and its ILCell was loaded one chunk earlier still, so neither the list
+ * stream from HBM nor the gather from L2 waits on the critical path. */
+template <int FORM, bool CELL, int MINB, int GROUP>
+__global__ void __launch_bounds__(kThreads, MINB) list_kernel_src(const ListArgs a) {
   static_assert(FORM != kF64, "FP32 arithmetic forms only");
+  using R = RawWords<FORM, CELL>;
+  constexpr int kW = R::kWords;
+  constexpr int kGroup = GROUP;
   __shared__ __align__(16) float4 tpos[kWarps][kTB];  // target x, y, z, mass
   __shared__ float tsoft[kWarps][kTB];
+  __shared__ __align__(16) float4 rbuf4[kWarps][2][R::kWide ? kW * 32 : 1];
+  __shared__ float rbuf1[kWarps][2][R::kWide ? 1 : kW * 32];
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
 
   for (;;) {
@@ -595,75 +649,105 @@ __global__ void __launch_bounds__(kThreads, 2) list_kernel_src(const ListArgs a)
         float tot = 0.f, comp = 0.f, idt = 0.f;
         for (int g0 = e_begin; g0 < e_end; g0 += 32 * kGroup) {
           const int g1 = min(e_end, g0 + 32 * kGroup);
+          const int nk = (g1 - g0 + 31) >> 5;  // chunks in this group (uniform)
           float v[32], id[8];
 #pragma unroll
           for (int k = 0; k < 32; ++k) v[k] = 0.f;
 #pragma unroll
           for (int k = 0; k < 8; ++k) id[k] = 0.f;
-          for (int e = g0 + lane; e < g1; e += 32) {
-            const SrcRec s = load_source<FORM, CELL>(a, e, chi, clo);
-            const float tw = s.soft + smax;
-            const float near2 = tw * tw;
+          /* prologue: chunk 0's record in flight, chunk 1's ILCell loaded */
+          int e = g0 + lane;
+          int2 ent = e < g1 ? __ldg(a.list + e) : make_int2(0, 0);
+          {
+            long long idx = ent.x;
+            if ((unsigned long long)idx >= (unsigned long long)a.n_src) idx = 0;  // memory safety
+            if (e < g1) fetch_source<FORM, CELL>(a, idx, rbuf4[warp][0], rbuf1[warp][0], lane);
+            cp_commit();
+          }
+          int2 ent_next = e + 32 < g1 ? __ldg(a.list + e + 32) : make_int2(0, 0);
+          for (int k = 0; k < nk; ++k, e += 32) {
+            const int buf = k & 1;
+            const bool valid = e < g1;
+            const int code = (ent.y >> 22) & 0x1ff;
+            /* start chunk k+1's gather, then wait for chunk k's */
+            if (k + 1 < nk) {
+              long long idx = ent_next.x;
+              if ((unsigned long long)idx >= (unsigned long long)a.n_src) idx = 0;
+              if (e + 32 < g1)
+                fetch_source<FORM, CELL>(a, idx, rbuf4[warp][buf ^ 1], rbuf1[warp][buf ^ 1], lane);
+              cp_commit();
+              ent = ent_next;
+              ent_next = e + 64 < g1 ? __ldg(a.list + e + 64) : make_int2(0, 0);
+              cp_wait<1>();
+            } else {
+              cp_wait<0>();
+            }
+            if (valid) {
+              const SrcRec s = finish_source<FORM, CELL>(a, rbuf4[warp][buf], rbuf1[warp][buf],
+                                                         lane, code, chi, clo);
+              const float tw = s.soft + smax;
+              const float near2 = tw * tw;
 #pragma unroll
-            for (int tt = 0; tt < kTC; ++tt) {
-              if (tt < ntc) {
-                const float4 tp = tpos[warp][t0 + tt];
-                if constexpr (CELL) {
-                  /* gravity.h:436-472: r = target - cell */
-                  const float rx = tp.x - s.x, ry = tp.y - s.y, rz = tp.z - s.z;
-                  const float rsq = rx * rx + ry * ry + rz * rz;
-                  const float dir = rsqrtf(rsq);
-                  const float dir2 = dir * dir;
-                  float av = dir, bv = dir2 * dir;
-                  float cv = 3.f * bv * dir2, dv = 5.f * cv * dir2;
-                  if (rsq <= near2) {
-                    const float twoh = s.soft + tsoft[warp][t0 + tt];
-                    if (rsq == 0.f) {
-                      av = bv = cv = dv = 0.f;
-                    } else if (rsq < twoh * twoh) {
-                      const float4 k = splineq_near_f(dir, rsq, twoh);
-                      av = k.x;
-                      bv = k.y;
-                      cv = k.z;
-                      dv = k.w;
-                    }
-                  }
-                  const float qirx = s.xx * rx + s.xy * ry + s.xz * rz;
-                  const float qiry = s.xy * rx + s.yy * ry + s.yz * rz;
-                  const float qirz = s.xz * rx + s.yz * ry + s.zz * rz;
-                  const float qir = 0.5f * (qirx * rx + qiry * ry + qirz * rz);
-                  const float bM = bv * s.m;
-                  const float qir3 = bM + dv * qir - cv * s.tr;
-                  v[4 * tt + 3] -= s.m * av + cv * qir - bv * s.tr;
-                  v[4 * tt + 0] -= qir3 * rx - cv * qirx;
-                  v[4 * tt + 1] -= qir3 * ry - cv * qiry;
-                  v[4 * tt + 2] -= qir3 * rz - cv * qirz;
-                  id[tt] = fmaxf(id[tt], fmaf(tp.w, bv, bM));
-                } else {
-                  /* gravity.h:276-301: r = source - target */
-                  const float rx = s.x - tp.x, ry = s.y - tp.y, rz = s.z - tp.z;
-                  const float rsq = rx * rx + ry * ry + rz * rz;
-                  const float dir = rsqrtf(rsq);
-                  float av = dir, bv = dir * dir * dir;
-                  if (rsq <= near2) {
-                    const float twoh = s.soft + tsoft[warp][t0 + tt];
-                    if (rsq == 0.f) {
-                      av = bv = 0.f;
-                    } else {
-                      const float r1 = rsq * dir;
-                      if (r1 < twoh) {
-                        const float2 k = spline_near_f(r1, dir, twoh);
-                        av = k.x;
-                        bv = k.y;
+              for (int tt = 0; tt < kTC; ++tt) {
+                if (tt < ntc) {
+                  const float4 tp = tpos[warp][t0 + tt];
+                  if constexpr (CELL) {
+                    /* gravity.h:436-472: r = target - cell */
+                    const float rx = tp.x - s.x, ry = tp.y - s.y, rz = tp.z - s.z;
+                    const float rsq = fmaf(rx, rx, fmaf(ry, ry, rz * rz));
+                    const float dir = rsqrtf(rsq);
+                    const float dir2 = dir * dir;
+                    float av = dir, bv = dir2 * dir;
+                    float cv = bv * (3.f * dir2), dv = cv * (5.f * dir2);
+                    if (rsq <= near2) {
+                      const float twoh = s.soft + tsoft[warp][t0 + tt];
+                      if (rsq == 0.f) {
+                        av = bv = cv = dv = 0.f;
+                      } else if (rsq < twoh * twoh) {
+                        const float4 kk = splineq_near_f(dir, rsq, twoh);
+                        av = kk.x;
+                        bv = kk.y;
+                        cv = kk.z;
+                        dv = kk.w;
                       }
                     }
+                    const float qirx = fmaf(s.xx, rx, fmaf(s.xy, ry, s.xz * rz));
+                    const float qiry = fmaf(s.xy, rx, fmaf(s.yy, ry, s.yz * rz));
+                    const float qirz = fmaf(s.xz, rx, fmaf(s.yz, ry, s.zz * rz));
+                    const float qir = 0.5f * fmaf(qirx, rx, fmaf(qiry, ry, qirz * rz));
+                    const float bM = bv * s.m;
+                    const float qir3 = fmaf(dv, qir, fmaf(-cv, s.tr, bM));
+                    v[4 * tt + 3] -= fmaf(s.m, av, fmaf(cv, qir, -bv * s.tr));
+                    v[4 * tt + 0] = fmaf(cv, qirx, fmaf(-qir3, rx, v[4 * tt + 0]));
+                    v[4 * tt + 1] = fmaf(cv, qiry, fmaf(-qir3, ry, v[4 * tt + 1]));
+                    v[4 * tt + 2] = fmaf(cv, qirz, fmaf(-qir3, rz, v[4 * tt + 2]));
+                    id[tt] = fmaxf(id[tt], fmaf(tp.w, bv, bM));
+                  } else {
+                    /* gravity.h:276-301: r = source - target */
+                    const float rx = s.x - tp.x, ry = s.y - tp.y, rz = s.z - tp.z;
+                    const float rsq = fmaf(rx, rx, fmaf(ry, ry, rz * rz));
+                    const float dir = rsqrtf(rsq);
+                    float av = dir, bv = dir * dir * dir;
+                    if (rsq <= near2) {
+                      const float twoh = s.soft + tsoft[warp][t0 + tt];
+                      if (rsq == 0.f) {
+                        av = bv = 0.f;
+                      } else {
+                        const float r1 = rsq * dir;
+                        if (r1 < twoh) {
+                          const float2 kk = spline_near_f(r1, dir, twoh);
+                          av = kk.x;
+                          bv = kk.y;
+                        }
+                      }
+                    }
+                    const float bm = bv * s.m;
+                    v[4 * tt + 3] = fmaf(-s.m, av, v[4 * tt + 3]);
+                    v[4 * tt + 0] = fmaf(rx, bm, v[4 * tt + 0]);
+                    v[4 * tt + 1] = fmaf(ry, bm, v[4 * tt + 1]);
+                    v[4 * tt + 2] = fmaf(rz, bm, v[4 * tt + 2]);
+                    id[tt] = fmaxf(id[tt], fmaf(tp.w, bv, bm));
                   }
-                  const float bm = bv * s.m;
-                  v[4 * tt + 3] -= s.m * av;
-                  v[4 * tt + 0] += rx * bm;
-                  v[4 * tt + 1] += ry * bm;
-                  v[4 * tt + 2] += rz * bm;
-                  id[tt] = fmaxf(id[tt], fmaf(tp.w, bv, bm));
                 }
               }
             }
@@ -724,39 +808,75 @@ __global__ void pack_parts_kernel(const double* __restrict__ p, long long n, flo
 
 /* The FP64 form keeps the target-parallel kernel (its cost is the FP64
  * pipe, not lane occupancy); the FP32 forms use the source-parallel one. */
-template <int FORM, bool CELL>
-constexpr auto kernel_for() {
-  if constexpr (FORM == kF64) return list_kernel<FORM, CELL>;
-  else return list_kernel_src<FORM, CELL>;
-}
-
-template <int FORM, bool CELL>
-int blocks_per_sm() {
-  static int cached = 0;
-  if (!cached) {
+template <typename K>
+int blocks_per_sm(K kernel, int* cache) {
+  if (!*cache) {
     int nb = 0;
-    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, kernel_for<FORM, CELL>(), kThreads, 0) !=
-            cudaSuccess ||
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, kernel, kThreads, 0) != cudaSuccess ||
         nb < 1)
       nb = 1;
-    cached = nb;
+    *cache = nb;
   }
-  return cached;
+  return *cache;
 }
 
-template <int FORM, bool CELL>
-cudaError_t launch_t(const ListArgs& a, cudaStream_t s) {
+template <typename K>
+cudaError_t launch_kernel(K kernel, int* occ_cache, int kid, const ListArgs& a, cudaStream_t s) {
   if (a.n_buckets <= 0) return cudaSuccess;
   long long want = ((long long)a.n_buckets + kWarps - 1) / kWarps;
-  long long cap = (long long)sm_count() * blocks_per_sm<FORM, CELL>();
+  long long cap = (long long)sm_count() * blocks_per_sm(kernel, occ_cache);
   int grid = (int)(want < cap ? want : cap);
-  TimingScope ts(list_kernel_id(FORM, CELL), s);
-  kernel_for<FORM, CELL>()<<<grid, kThreads, 0, s>>>(a);
+  TimingScope ts(kid, s);
+  kernel<<<grid, kThreads, 0, s>>>(a);
   count_launch();
   return cudaGetLastError();
 }
 
+/* current variant per list kernel id (FP32 forms) */
+int g_variant[6] = {1, 1, 0, 0, 1, 1};
+
+template <int FORM, bool CELL, int V>
+cudaError_t launch_variant(const ListArgs& a, cudaStream_t s) {
+  static int occ = 0;
+  constexpr Variant var = kVariants[V];
+  return launch_kernel(list_kernel_src<FORM, CELL, var.minb, var.group>, &occ,
+                       list_kernel_id(FORM, CELL), a, s);
+}
+
+template <int FORM, bool CELL, int... V>
+cudaError_t launch_src(int v, const ListArgs& a, cudaStream_t s, std::integer_sequence<int, V...>) {
+  cudaError_t e = cudaErrorInvalidValue;
+  ((v == V ? (e = launch_variant<FORM, CELL, V>(a, s), 0) : 0), ...);
+  return e;
+}
+
+template <int FORM, bool CELL>
+cudaError_t launch_t(const ListArgs& a, cudaStream_t s) {
+  if constexpr (FORM == kF64) {
+    static int occ = 0;
+    return launch_kernel(list_kernel<FORM, CELL>, &occ, list_kernel_id(FORM, CELL), a, s);
+  } else {
+    return launch_src<FORM, CELL>(g_variant[list_kernel_id(FORM, CELL)], a, s,
+                                  std::make_integer_sequence<int, kNumVariants>{});
+  }
+}
+
 }  // namespace
+
+int list_variant_count() { return kNumVariants; }
+
+int set_list_variant(int kernel, int variant) {
+  if (kernel < 0 || kernel >= 6 || kernel == kKidListF64Cell || kernel == kKidListF64Part)
+    return -1;
+  if (variant < 0 || variant >= kNumVariants) return -1;
+  g_variant[kernel] = variant;
+  return 0;
+}
+
+int get_list_variant(int kernel) {
+  if (kernel < 0 || kernel >= 6) return -1;
+  return g_variant[kernel];
+}
 
 cudaError_t launch_list(int form, bool cell, const ListArgs& a, cudaStream_t s) {
   switch (form) {

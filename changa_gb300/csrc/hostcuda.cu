@@ -608,6 +608,12 @@ unsigned long long changa_gb300_kernel_launches(void) { return g_launches.load()
 
 void changa_gb300_set_timing(int on) { g_timing.store(on); }
 
+int changa_gb300_list_variant_count(void) { return list_variant_count(); }
+int changa_gb300_set_list_variant(int kernel, int variant) {
+  return set_list_variant(kernel, variant) ? CHANGA_E_INVALID_ARG : 0;
+}
+int changa_gb300_get_list_variant(int kernel) { return get_list_variant(kernel); }
+
 int changa_gb300_kernel_time(int kernel, double* total_ms, long long* launches) {
   if (kernel < 0 || kernel >= kKidCount || !total_ms || !launches) return CHANGA_E_INVALID_ARG;
   std::vector<EventPair> ev;
@@ -853,3 +859,80 @@ int changa_ewald_forces(int form, const double* parts, long long n_parts, const 
 }
 
 }  // extern "C"
+
+/* ---- CUDA-graph replay of one evaluation (the batching form) ---- */
+
+struct ChangaGravityGraph {
+  cudaGraph_t graph;
+  cudaGraphExec_t exec;
+  unsigned kernels;  // kernel nodes in the graph
+};
+
+extern "C" ChangaGravityGraph* changa_gravity_graph_create(
+    int form, const double* moments, long long n_moments, const double* parts, long long n_parts,
+    const ChangaListRequest* cells, const ChangaListRequest* plist, double fperiod,
+    const ChangaEwaldParams* ewald, double* vars, int zero_vars) {
+  prepare_pool();
+  cudaStream_t s;
+  if (cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking) != cudaSuccess) {
+    record_error(CHANGA_E_INVALID_ARG, "graph: stream", __FILE__, __LINE__);
+    return nullptr;
+  }
+  /* warm the occupancy/SM-count caches outside the capture */
+  sm_count();
+  cudaError_t e = cudaStreamBeginCapture(s, cudaStreamCaptureModeRelaxed);
+  if (e != cudaSuccess) {
+    cudaStreamDestroy(s);
+    record_error((int)e, "graph: begin capture", __FILE__, __LINE__);
+    return nullptr;
+  }
+  int rc = 0;
+  if (zero_vars && vars && n_parts > 0) {
+    e = cudaMemsetAsync(vars, 0, (size_t)n_parts * 5 * sizeof(double), s);
+    if (e != cudaSuccess) rc = (int)e;
+  }
+  if (!rc)
+    rc = changa_gravity_step(form, moments, n_moments, parts, n_parts, cells, plist, fperiod,
+                             ewald, vars, s);
+  cudaGraph_t graph = nullptr;
+  e = cudaStreamEndCapture(s, &graph);
+  cudaStreamDestroy(s);
+  if (rc || e != cudaSuccess || !graph) {
+    if (graph) cudaGraphDestroy(graph);
+    record_error(rc ? rc : (int)e, "graph: capture", __FILE__, __LINE__);
+    return nullptr;
+  }
+  cudaGraphExec_t exec = nullptr;
+  e = cudaGraphInstantiate(&exec, graph, 0);
+  if (e != cudaSuccess) {
+    cudaGraphDestroy(graph);
+    record_error((int)e, "graph: instantiate", __FILE__, __LINE__);
+    return nullptr;
+  }
+  size_t nn = 0;
+  unsigned nk = 0;
+  if (cudaGraphGetNodes(graph, nullptr, &nn) == cudaSuccess && nn) {
+    std::vector<cudaGraphNode_t> nodes(nn);
+    if (cudaGraphGetNodes(graph, nodes.data(), &nn) == cudaSuccess)
+      for (size_t i = 0; i < nn; ++i) {
+        cudaGraphNodeType t;
+        if (cudaGraphNodeGetType(nodes[i], &t) == cudaSuccess && t == cudaGraphNodeTypeKernel) ++nk;
+      }
+  }
+  ChangaGravityGraph* g = new ChangaGravityGraph{graph, exec, nk};
+  return g;
+}
+
+extern "C" int changa_gravity_graph_launch(ChangaGravityGraph* g, cudaStream_t stream) {
+  if (!g) return record_error(CHANGA_E_INVALID_ARG, "graph: NULL", __FILE__, __LINE__);
+  CHG_CUDA(cudaGraphLaunch(g->exec, stream));
+  count_launch(g->kernels);
+  return 0;
+}
+
+extern "C" void changa_gravity_graph_destroy(ChangaGravityGraph* g) {
+  if (!g) return;
+  cudaGraphExecDestroy(g->exec);
+  cudaGraphDestroy(g->graph);
+  delete g;
+}

@@ -274,3 +274,30 @@ class DeviceSystem:
             C.byref(ep) if ep else None, self.vars.data_ptr(), s)
         N.check(rc, "changa_gravity_step")
         return self.vars
+
+
+class GravityGraph:
+    """One evaluation of a DeviceSystem captured into a CUDA graph
+    (changa_gravity_graph_create) and replayed with one launch."""
+
+    def __init__(self, ds: DeviceSystem, form="mixed"):
+        self.ds = ds
+        ep = ds.ewald_params
+        self.handle = N.cuda_lib().changa_gravity_graph_create(
+            FORMS[form], ds.moments.data_ptr(), ds.moments.shape[0], ds.parts.data_ptr(), ds.n,
+            C.byref(ds.reqs[0]["c"]), C.byref(ds.reqs[1]["c"]), float(ds.lists.period),
+            C.byref(ep) if ep else None, ds.vars.data_ptr(), 1)
+        if not self.handle:
+            N.check(N.cuda_lib().changa_gb300_last_error() or N.CHANGA_ERRORS_RECORD,
+                    "changa_gravity_graph_create")
+
+    def launch(self, stream=None):
+        torch = self.ds.torch
+        s = stream if stream is not None else torch.cuda.current_stream().cuda_stream
+        N.check(N.cuda_lib().changa_gravity_graph_launch(self.handle, s), "graph launch")
+        return self.ds.vars
+
+    def close(self):
+        if self.handle:
+            N.cuda_lib().changa_gravity_graph_destroy(self.handle)
+            self.handle = None

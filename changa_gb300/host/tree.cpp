@@ -573,6 +573,30 @@ void chg_tree_get_buckets(void* h, int* starts, int* sizes, double* bbox, int* m
   }
 }
 
+/* Tree structure in moment (BFS) indices, for gradients through the moment
+ * construction: parent[i] = moment index of node i's parent (-1 at the
+ * root); leaf[k] = moment index of the bucket holding GPU particle k. */
+void chg_tree_get_structure(void* h, int* parent, int* leaf) {
+  Tree* t = (Tree*)h;
+  if (parent) {
+    for (size_t i = 0; i < t->bfs_nodes.size(); ++i) parent[i] = -1;
+    for (size_t i = 0; i < t->bfs_nodes.size(); ++i) {
+      const Node& nd = t->nodes[t->bfs_nodes[i]];
+      if (nd.type != T_INTERNAL) continue;
+      for (int c = 0; c < 2; ++c) {
+        const Node& ch = t->nodes[nd.child[c]];
+        if (ch.bfs >= 0) parent[ch.bfs] = (int)i;
+      }
+    }
+  }
+  if (leaf) {
+    for (size_t b = 0; b < t->bucket_nodes.size(); ++b) {
+      const Node& nd = t->nodes[t->bucket_nodes[b]];
+      for (int k = nd.first; k < nd.first + nd.count; ++k) leaf[k] = nd.bfs;
+    }
+  }
+}
+
 /* Runs the walk; returns 0 on success. */
 int chg_tree_walk(void* h, int nthreads) {
   Tree* t = (Tree*)h;

@@ -124,6 +124,9 @@ def build_lists(pos, mass, soft, n_bucket=16, theta=0.7, period=0.0, n_replicas=
         bsizes = np.empty(nb, dtype=np.int32)
         bbox = np.empty((nb, 6), dtype=np.float64)
         lib.chg_tree_get_buckets(h, _ptr(bstarts), _ptr(bsizes), _ptr(bbox), None)
+        parent = np.empty(nm, dtype=np.int32)
+        leaf = np.empty(n, dtype=np.int32)
+        lib.chg_tree_get_structure(h, _ptr(parent), _ptr(leaf))
         lib.chg_tree_walk(h, int(nthreads))
         nc = np.empty(nb, dtype=np.int64)
         npl = np.empty(nb, dtype=np.int64)
@@ -139,13 +142,14 @@ def build_lists(pos, mass, soft, n_bucket=16, theta=0.7, period=0.0, n_replicas=
     return TreeLists(n=n, parts=parts, moments=moments, root=root, perm=perm,
                      bucket_starts=bstarts, bucket_sizes=bsizes, bucket_bbox=bbox,
                      cells=cells, plist=plist, period=float(period), n_replicas=int(n_replicas),
-                     theta=float(theta), n_bucket=int(n_bucket))
+                     theta=float(theta), n_bucket=int(n_bucket),
+                     meta={"parent": parent, "leaf": leaf})
 
 
 def concat_systems(systems):
-    """Concatenates independent systems into one set of arrays and one pair
-    of requests (indices and starts shifted), for one batched evaluation.
-    Returns (parts, moments, cells, plist, offsets)."""
+    """Concatenates independent systems into one TreeLists with one pair of
+    requests (list indices and bucket starts shifted), for one batched
+    evaluation.  meta["offsets"] holds each system's first particle."""
     parts = np.concatenate([s.parts for s in systems], axis=0)
     moments = np.concatenate([s.moments for s in systems], axis=0)
     p_off = np.cumsum([0] + [s.n for s in systems])
@@ -173,4 +177,13 @@ def concat_systems(systems):
 
     cells = cat([s.cells for s in systems], m_off)
     plist = cat([s.plist for s in systems], p_off)
-    return parts, moments, cells, plist, p_off
+    n = int(p_off[-1])
+    return TreeLists(n=n, parts=parts, moments=moments, root=None,
+                     perm=np.concatenate([s.perm + p_off[k] for k, s in enumerate(systems)]),
+                     bucket_starts=np.concatenate([s.bucket_starts + p_off[k]
+                                                   for k, s in enumerate(systems)]),
+                     bucket_sizes=np.concatenate([s.bucket_sizes for s in systems]),
+                     bucket_bbox=np.concatenate([s.bucket_bbox for s in systems]),
+                     cells=cells, plist=plist, period=0.0, n_replicas=0,
+                     theta=systems[0].theta, n_bucket=systems[0].n_bucket,
+                     meta={"offsets": p_off, "moment_offsets": m_off})

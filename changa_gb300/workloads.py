@@ -59,7 +59,43 @@ class Workload:
                     moments="quadrupole", seed=ics.SEED_BASE + self.index)
 
 
+@dataclass
+class ClusterBatch:
+    """Many independent isolated Plummer clusters evaluated as one batch:
+    N per cluster log-uniform in [nmin, nmax], mass 1, scale radius uniform
+    in [0.5, 2], softening 0.01 x scale radius."""
+    name: str
+    index: int
+    n_clusters: int
+    nmin: int
+    nmax: int
+    n_bucket: int = 16
+    theta: float = 0.6
+    period: float = 0.0
+    ewald: tuple | None = None
+
+    def systems(self, nthreads=0):
+        rng = ics.rng_for(self.index)
+        out = []
+        for p in ics.plummer_clusters(self.n_clusters, rng, self.nmin, self.nmax):
+            out.append(tree.build_lists(p["pos"], p["mass"], p["soft"], n_bucket=self.n_bucket,
+                                        theta=self.theta, nthreads=nthreads))
+        return out
+
+    def lists(self, nthreads=0):
+        return tree.concat_systems(self.systems(nthreads))
+
+    def ewald_config(self):
+        return None
+
+    def describe(self):
+        return dict(workload=self.name, clusters=self.n_clusters, n_range=[self.nmin, self.nmax],
+                    bucket=self.n_bucket, theta=self.theta, periodic=False, ewald=False,
+                    moments="quadrupole", seed=ics.SEED_BASE + self.index)
+
+
 WORKLOADS = {
+    "clusters512": ClusterBatch("clusters512", 3, 512, 1024, 65536),
     "plummer32k": Workload("plummer32k", 0, 32768, 16, 0.7, 0.0, None, soft=0.01),
     "lattice1m": Workload("lattice1m", 1, 128 ** 3, 16, 0.7, 1.0, (2.6, 2.8)),
     "nfw8m": Workload("nfw8m", 2, 2 ** 23, 32, 0.7, 1.0, (2.6, 2.8), soft=2e-4),

@@ -75,6 +75,13 @@ unsigned long long changa_gb300_kernel_launches(void);
 void changa_gb300_set_timing(int on);
 int changa_gb300_kernel_time(int kernel, double *total_ms, long long *launches);
 
+/* Shape variants of the FP32-form list kernels (kernel ids 0, 1, 4, 5):
+ * resident blocks per SM x list entries per reduction tile.  The autotuner
+ * (changa_gb300/autotune.py) times them on a workload and selects one. */
+int changa_gb300_list_variant_count(void);
+int changa_gb300_set_list_variant(int kernel, int variant);
+int changa_gb300_get_list_variant(int kernel);
+
 /* ---- device-resident list requests for the extension forms ---- */
 
 typedef struct ChangaListRequest {
@@ -159,6 +166,37 @@ int changa_gravity_step_host(int form, const double *moments, long long n_moment
                              const ChangaListRequest *cells, const ChangaListRequest *plist,
                              double fperiod, const ChangaEwaldParams *ewald,
                              double *vars, cudaStream_t stream);
+
+/* changa_gravity_step captured once into a CUDA graph and replayed: the
+ * batching form.  The requests may span many independent systems
+ * concatenated (indices and starts shifted); the persistent list kernels'
+ * device work queue balances their uneven buckets inside one replay.  The
+ * graph keeps the device pointers it was created with: update the arrays in
+ * place between launches.  The ChangaEwaldParams and requests are read at
+ * creation only.  Returns NULL on error (see changa_gb300_last_error). */
+typedef struct ChangaGravityGraph ChangaGravityGraph;
+ChangaGravityGraph *changa_gravity_graph_create(int form, const double *moments,
+                                                long long n_moments, const double *parts,
+                                                long long n_parts,
+                                                const ChangaListRequest *cells,
+                                                const ChangaListRequest *plist, double fperiod,
+                                                const ChangaEwaldParams *ewald, double *vars,
+                                                int zero_vars);
+int changa_gravity_graph_launch(ChangaGravityGraph *g, cudaStream_t stream);
+void changa_gravity_graph_destroy(ChangaGravityGraph *g);
+
+/* Adjoint of the cell + particle list accelerations (FP32-mixed; no
+ * reference counterpart): given lam = dL/da (n_parts x 3), ACCUMULATES
+ * dL/dx and dL/dm into grad (n_parts x 4 {dx, dy, dz, dm}) through the same
+ * lists, the tidal tensor of every interaction and the moment construction
+ * (tree topology held fixed).  parent: BFS parent of every moment (-1 at
+ * the root); leaf: moment index of each particle's bucket.  Isolated
+ * systems (the Ewald term has no adjoint here). */
+int changa_gravity_vjp_mixed(const double *moments, long long n_moments, const double *parts,
+                             long long n_parts, const ChangaListRequest *cells,
+                             const ChangaListRequest *plist, double fperiod, const int *parent,
+                             const int *leaf, const double *lam, double *grad,
+                             cudaStream_t stream);
 
 /* Ewald correction for parts[idx[k]] into vars[idx[k]] (idx == NULL: the
  * first n_idx particles).  form: FP64 or MIXED. */
