@@ -16,7 +16,10 @@ bucket 32, theta 0.7).  Other lines of the JSON:
   roofline     the dominant kernel (FP32-mixed cell-list kernel) against the
                FP32 FMA peak of the GPU;
   cpu_baseline the CPU oracle (ChaNGa's own gravity.h/Ewald.cpp when it was
-               built here, else its C restatement) on a bounded sample.
+               built here, else its C restatement) on a bounded sample;
+  adjoint      plummer64k: one adjoint (VJP) evaluation against one forward
+               evaluation on the same tree, and the 16-step leapfrog forward /
+               checkpointed reverse pass (--no-adjoint skips it).
 --impl reference times that CPU implementation alone on the same workload.
 
 Launch: python bench.py [--gpus N --steps K --warmup W]; for N > 1 under
@@ -56,9 +59,12 @@ def parse():
     ap.add_argument("--workload", default="nfw8m")
     ap.add_argument("--fp64-steps", type=int, default=2)
     ap.add_argument("--e2e-steps", type=int, default=3)
-    ap.add_argument("--cpu-sample", type=float, default=1.5e9,
+    ap.add_argument("--cpu-sample", type=float, default=1.5e10,
                     help="interactions in the bounded CPU sample")
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-adjoint", dest="adjoint", action="store_false",
+                    help="skip the adjoint / forward cost measurement (plummer64k)")
+    ap.add_argument("--no-adjoint-leapfrog", dest="adjoint_leapfrog", action="store_false")
     return ap.parse_args()
 
 
@@ -283,6 +289,74 @@ def main_reference(args):
     return 0
 
 
+def measure_adjoint(leapfrog=True, reps=20):
+    """The differentiation workload (plummer64k): one FP32-mixed force
+    evaluation vs one adjoint (VJP) evaluation on the same tree, by kernel
+    time and by CUDA events around the whole call; optionally the 16-step
+    KDK leapfrog forward and its checkpointed reverse pass (wall clock,
+    host tree builds included)."""
+    import numpy as np
+    import torch
+    from changa_gb300 import _native as N
+    from changa_gb300 import autotune
+    from changa_gb300.adjoint import Leapfrog, TreeStep, loss_weights
+    from changa_gb300.workloads import WORKLOADS
+    wl = WORKLOADS["plummer64k"]
+    p = wl.particles()
+    t = lambda a: torch.from_numpy(np.ascontiguousarray(a, dtype=np.float64)).cuda()
+    x, v, m, s = t(p["pos"]), t(p["vel"]), t(p["mass"]), t(p["soft"])
+    ts = TreeStep(x, m, s, theta=wl.theta, n_bucket=wl.n_bucket)
+    autotune.tune(ts.ds, "mixed")
+    lam = loss_weights(wl.n, 99)
+    for _ in range(3):
+        ts.accel("mixed")
+        ts.vjp(lam)
+    torch.cuda.synchronize()
+    lib = N.cuda_lib()
+    lib.changa_gb300_set_timing(1)
+    for k in N.KERNEL_IDS:
+        N.kernel_time(k)
+    for _ in range(reps):
+        ts.ds.step("mixed")
+    torch.cuda.synchronize()
+    fw = {k: N.kernel_time(k)[0] / reps for k in ("list_mixed_cell", "list_mixed_part", "pack")}
+    for _ in range(reps):
+        ts.vjp(lam)
+    torch.cuda.synchronize()
+    bw = {k: N.kernel_time(k)[0] / reps for k in ("vjp_cell", "vjp_part", "pack", "moments")}
+    lib.changa_gb300_set_timing(0)
+    ev = []
+    for fn in (lambda: ts.ds.step("mixed"), lambda: ts.vjp(lam)):
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        for _ in range(reps):
+            fn()
+        e1.record()
+        torch.cuda.synchronize()
+        ev.append(e0.elapsed_time(e1) / reps)
+    out = {"workload": wl.name, "n": wl.n, "interactions": ts.interactions,
+           "forward_kernel_ms": fw, "vjp_kernel_ms": bw,
+           "forward_ms": sum(fw.values()), "vjp_ms": sum(bw.values()),
+           "vjp_over_forward": sum(bw.values()) / sum(fw.values()),
+           "event_forward_ms": ev[0], "event_vjp_ms": ev[1],
+           "event_vjp_over_forward": ev[1] / ev[0]}
+    if leapfrog:
+        lf = Leapfrog(m, s, 0.005, 16, theta=wl.theta, n_bucket=wl.n_bucket, checkpoint_every=4)
+        w = loss_weights(wl.n, 13)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        lf.forward(x, v)
+        torch.cuda.synchronize()
+        t1 = time.perf_counter()
+        lf.backward(w, torch.zeros_like(w))
+        torch.cuda.synchronize()
+        t2 = time.perf_counter()
+        out["leapfrog"] = {"steps": 16, "dt": 0.005, "checkpoint_every": 4,
+                           "forward_wall_s": t1 - t0, "reverse_wall_s": t2 - t1,
+                           "tree_builds": lf.tree_builds, "force_evals": lf.force_evals}
+    return out
+
+
 def main_ours(args):
     import numpy as np
     import torch
@@ -475,6 +549,10 @@ def main_ours(args):
     kshare = {k: {"ms_per_step": v[0] / max(1, args.steps), "launches": v[1]}
               for k, v in ktimes.items() if v[1]}
 
+    adj = None
+    if rank == 0 and args.adjoint:
+        adj = measure_adjoint(args.adjoint_leapfrog)
+
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu:
         cpu = run_cpu(lists, ew, args.cpu_sample)
@@ -495,7 +573,7 @@ def main_ours(args):
                               autotune=tuning,
                               parallelism="replicas x%d" % world),
                "roofline": roof, "roofline_pp": roof_pp, "cpu_baseline": cpu, "e2e": e2e,
-               "gpu_launches": int(launches), "clocks": clk}
+               "gpu_launches": int(launches), "clocks": clk, "adjoint": adj}
         print(json.dumps(out), flush=True)
     if world > 1:
         import torch.distributed as dist

@@ -104,7 +104,8 @@ CHANGA_MAX_EWH = 256
 # kernel ids of changa_gb300_kernel_time
 KERNEL_IDS = {"list_f32_cell": 0, "list_f32_part": 1, "list_f64_cell": 2, "list_f64_part": 3,
               "list_mixed_cell": 4, "list_mixed_part": 5, "ewald_f32": 6, "ewald_f64": 7,
-              "ewald_mixed": 8, "pack": 9}
+              "ewald_mixed": 8, "pack": 9, "vjp_cell": 10, "vjp_part": 11,
+              "moments": 12}
 
 
 def kernel_time(name):
@@ -170,6 +171,7 @@ CUDA_SIGNATURES = {
     "changa_gravity_vjp_mixed": (_I, [_VP, _LL, _VP, _LL, C.POINTER(ChangaListRequest),
                                       C.POINTER(ChangaListRequest), _D, _VP, _VP, _VP, _VP, _VP]),
     "changa_gravity_graph_destroy": (None, [_VP]),
+    "changa_tree_moments": (_I, [_VP, _LL, _VP, _VP, _LL, _VP, _VP]),
     "changa_ewald_forces": (_I, [_I, _VP, _LL, _VP, _LL, C.POINTER(ChangaEwaldParams), _VP, _VP]),
     "changa_ewald_table": (_I, [_VP, _D, _D, _VP, _I]),
 }
@@ -190,6 +192,7 @@ HOST_SIGNATURES = {
                                       C.c_long, C.c_long]),
     "chg_tree_drop_lists": (None, [_VP]),
     "chg_tree_get_structure": (None, [_VP, _VP, _VP]),
+    "chg_tree_get_ranges": (None, [_VP, _VP, _VP]),
 }
 
 

@@ -25,7 +25,8 @@ CUDA_HOME = os.environ.get("CUDA_HOME", "/usr/local/cuda")
 NVCC = os.path.join(CUDA_HOME, "bin", "nvcc")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
-CU_SOURCES = ["grav_lists.cu", "ewald.cu", "hostcuda.cu", "noalloc.cu", "adjoint.cu"]
+CU_SOURCES = ["grav_lists.cu", "ewald.cu", "hostcuda.cu", "noalloc.cu", "adjoint.cu",
+              "moments.cu"]
 CXX_SOURCES = ["cxx_abi.cpp", "ewald_table.cpp"]
 
 CUDA_LIB = os.path.join(BUILD, "libchanga_gb300.so")

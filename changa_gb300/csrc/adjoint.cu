@@ -26,13 +26,25 @@
  *       dL/dx_k += (m_k / M_c) gX + m_k G d,   G = [[2gxx gxy gxz] ...],
  *       dL/dm_k += gM + gX.d / M_c + d^T Gh d,  Gh = G / 2.
  *
- * Kernel design mirrors the forward source-parallel kernel: lanes own list
- * entries, targets (position, mass, lambda) are broadcast from shared memory
- * in chunks of 8, target gradients are reduced with the butterfly
- * reduce-scatter, and each lane adds its source's gradient (summed over the
- * chunk's targets) with one set of FP64 atomics.  Cell softening is treated
- * as a constant (its mass derivative only matters inside the spline, where
- * cells are almost never evaluated).
+ * Kernel design.  One warp per bucket from a device work queue; the
+ * bucket's targets (position relative to the bucket centre, softening,
+ * lambda) sit in shared memory.  Targets go in tiles of 16 split between
+ * the two half-warps (ceil/floor), and both halves walk the same 16 list
+ * entries per step, so a lane pair (l, l + 16) sees every target of the
+ * tile against one source: one shuffle completes the source's gradient,
+ * which is then added once per entry.  The next step's list entry and
+ * source record are loaded into registers while the current step computes.
+ * Per-lane target partials accumulate over the whole list and are reduced
+ * once per tile with a 16-lane butterfly reduce-scatter.
+ * Source gradients go out as vector FP32 reductions (red.global.add.v4.f32:
+ * 3 per cell entry, 1 per particle entry) into kReplicas copies of the
+ * accumulators (chosen by warp), which bounds the terms per FP32 sum; a
+ * finishing kernel adds the copies in FP64.  The moment chain then runs on
+ * per-node coefficients: for particle k under node c,
+ *   dL/dx_k += m_k (A_c + G_c x_k),
+ *   dL/dm_k += c0_c + A_c . x_k + x_k^T G_c x_k / 2,
+ * with A_c = gX/M - G_c X, c0_c = gM - gX.X/M + X^T G_c X / 2, so the sums
+ * over a particle's ancestors become prefix sums down the tree (FP64).
  */
 #include "chg_internal.h"
 
@@ -42,15 +54,18 @@ namespace {
 constexpr int kWarps = 4;
 constexpr int kThreads = kWarps * 32;
 constexpr unsigned kFull = 0xffffffffu;
-constexpr int kTC = 8;
-constexpr int kTB = 32;
+constexpr int kTB = 32;      // targets staged per shared-memory tile
+constexpr int kReplicas = 4; // copies of the FP32 source-gradient accumulators
+constexpr int kCellAcc = 12; // floats per cell accumulator {gX, gM} {gQ xx xy xz yy} {yz zz - -}
+constexpr int kPartAcc = 4;  // floats per particle accumulator {gX, gm}
+constexpr int kCoef = 10;    // FP64 per node coefficient set {A(3), G(6), c0}
 
 /* a, b, c, d, e of the quadrupole spline kernel inside the softening
  * length (gravity.h:27-59 for a..d; e = -(1/r) dd/dr derived from them:
  * u < 1: e = 3/2 dih^6 / r^3; 1 <= u < 2: e = -7/r^9 + 9 dih^4 / r^5 -
  * dih^6 / (2 r^3); both meet 105/r^9 at u = 2). */
 struct Spl5 {
-  float a, b, c, d, e;
+  float b, c, d, e;
 };
 
 __device__ __noinline__ Spl5 spline5_near(float dir, float rsq, float twoh) {
@@ -62,16 +77,12 @@ __device__ __noinline__ Spl5 spline5_near(float dir, float rsq, float twoh) {
   const float dir2 = dir * dir, dir3 = dir2 * dir;
   Spl5 k;
   if (u < 1.0f) {
-    k.a = dih * (7.0f / 5.0f - 2.0f / 3.0f * u2 + 3.0f / 10.0f * u2 * u2 - 1.0f / 10.0f * u2 * u2 * u);
     k.b = dih3 * (4.0f / 3.0f - 6.0f / 5.0f * u2 + 0.5f * u2 * u);
     k.c = dih5 * (12.0f / 5.0f - 1.5f * u);
     k.d = 1.5f * dih6 * dir;
     k.e = 1.5f * dih6 * dir3;
   } else {
     const float dir5 = dir3 * dir2, dir7 = dir5 * dir2, dir9 = dir7 * dir2;
-    k.a = -1.0f / 15.0f * dir +
-          dih * (8.0f / 5.0f - 4.0f / 3.0f * u2 + u2 * u - 3.0f / 10.0f * u2 * u2 +
-                 1.0f / 30.0f * u2 * u2 * u);
     k.b = -1.0f / 15.0f * dir3 +
           dih3 * (8.0f / 3.0f - 3.0f * u + 6.0f / 5.0f * u2 - 1.0f / 6.0f * u2 * u);
     k.c = -1.0f / 5.0f * dir5 + 3.0f * dih4 * dir + dih5 * (-12.0f / 5.0f + 0.5f * u);
@@ -81,10 +92,13 @@ __device__ __noinline__ Spl5 spline5_near(float dir, float rsq, float twoh) {
   return k;
 }
 
-__device__ __forceinline__ float reduce_scatter32(float (&v)[32], int lane) {
+/* Butterfly reduce-scatter of 32 values over the 16 lanes of a half-warp
+ * (offsets 8, 4, 2, 1): lane l ends with the totals of values
+ * 2 (l & 15) and 2 (l & 15) + 1 in v[0], v[1]. */
+__device__ __forceinline__ void reduce_scatter16(float (&v)[32], int lane) {
 #pragma unroll
-  for (int s = 0; s < 5; ++s) {
-    const int o = 16 >> s, h = 16 >> s;
+  for (int s = 0; s < 4; ++s) {
+    const int o = 8 >> s, h = 16 >> s;
     const bool up = (lane & o) != 0;
 #pragma unroll
     for (int i = 0; i < h; ++i) {
@@ -93,7 +107,16 @@ __device__ __forceinline__ float reduce_scatter32(float (&v)[32], int lane) {
       v[i] = keep + __shfl_xor_sync(kFull, send, o);
     }
   }
-  return v[0];
+}
+
+__device__ __forceinline__ void red_add4(float* p, float a, float b, float c, float d) {
+  asm volatile("red.global.add.v4.f32 [%0], {%1, %2, %3, %4};" ::"l"(p), "f"(a), "f"(b), "f"(c),
+               "f"(d)
+               : "memory");
+}
+
+__device__ __forceinline__ void red_add2(float* p, float a, float b) {
+  asm volatile("red.global.add.v2.f32 [%0], {%1, %2};" ::"l"(p), "f"(a), "f"(b) : "memory");
 }
 
 struct VjpArgs {
@@ -109,17 +132,49 @@ struct VjpArgs {
   const int* sizes;
   int n_buckets;
   float fperiod;
-  double* grad_tgt;  // n_tgt x 4 {dx, dy, dz, dm}
-  double* grad_src;  // particles: n_src x 4; cells: n_src x 10 {X(3), M, xx xy xz yy yz zz}
+  double* grad_tgt;  // n_tgt x 4 {dx, dy, dz, dm}; each row written by its bucket's warp only
+  float* acc;        // kReplicas x n_src x (kCellAcc | kPartAcc)
   unsigned int* queue;
 };
 
+/* One list entry as a lane holds it. */
 template <bool CELL>
-__global__ void __launch_bounds__(kThreads, 2) vjp_kernel(const VjpArgs a) {
+struct Src {
+  float4 h, l, q0, q1;
+  int code;
+  bool valid;
+  long long idx;
+};
+
+template <bool CELL>
+__device__ __forceinline__ void load_src(const VjpArgs& a, int e, int e_end, Src<CELL>& s) {
+  s.valid = e < e_end;
+  s.idx = 0;
+  s.code = 0;
+  if (s.valid) {
+    const int2 ent = __ldg(a.list + e);
+    s.idx = ent.x;
+    if ((unsigned long long)s.idx >= (unsigned long long)a.n_src) s.idx = 0;
+    s.code = (ent.y >> 22) & 0x1ff;
+  }
+  const float4* sp = a.src + (CELL ? 4 : 2) * s.idx;
+  s.h = __ldg(sp);
+  s.l = __ldg(sp + 1);
+  if constexpr (CELL) {
+    s.q0 = __ldg(sp + 2);
+    s.q1 = __ldg(sp + 3);
+  }
+}
+
+template <bool CELL>
+__global__ void __launch_bounds__(kThreads, 4) vjp_kernel(const VjpArgs a) {
   __shared__ __align__(16) float4 tpos[kWarps][kTB];
   __shared__ __align__(16) float4 tlam[kWarps][kTB];
   __shared__ float tsoft[kWarps][kTB];
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int half = lane >> 4, hl = lane & 15;
+  constexpr int kStride = CELL ? kCellAcc : kPartAcc;
+  float* acc = a.acc + (size_t)((blockIdx.x * kWarps + warp) % kReplicas) * a.n_src * kStride;
 
   for (;;) {
     int b = 0;
@@ -146,55 +201,46 @@ __global__ void __launch_bounds__(kThreads, 2) vjp_kernel(const VjpArgs a) {
         tlam[warp][lane] = __ldg(a.lam + ti);
       }
       __syncwarp();
-      const int nch = (nt + kTC - 1) / kTC;
-      for (int c = 0; c < nch; ++c) {
-        const int t0 = c * kTC;
-        const int ntc = min(kTC, nt - t0);
-        float tot = 0.f;
-        for (int e0 = e_begin; e0 < e_end; e0 += 32) {
-          const int e = e0 + lane;
-          const bool valid = e < e_end;
-          float v[32];
+      for (int t16 = 0; t16 < nt; t16 += 16) {
+        const int ntile = min(16, nt - t16);
+        const int nh0 = (ntile + 1) >> 1;
+        const int my0 = t16 + (half ? nh0 : 0);
+        const int myn = half ? ntile - nh0 : nh0;
+        float v[32];
 #pragma unroll
-          for (int k = 0; k < 32; ++k) v[k] = 0.f;
-          /* this lane's source */
-          long long idx = 0;
-          int code = 0;
-          if (valid) {
-            const int2 ent = __ldg(a.list + e);
-            idx = ent.x;
-            if ((unsigned long long)idx >= (unsigned long long)a.n_src) idx = 0;
-            code = (ent.y >> 22) & 0x1ff;
-          }
-          const float ox = (float)((code & 7) - 3) * a.fperiod,
-                      oy = (float)(((code >> 3) & 7) - 3) * a.fperiod,
-                      oz = (float)(((code >> 6) & 7) - 3) * a.fperiod;
-          const float4* sp = a.src + (CELL ? 4 : 2) * idx;
-          const float4 h = __ldg(sp), l = __ldg(sp + 1);
-          const float sx = ((h.x - chi.x) + ox) + (l.x - clo.x);
-          const float sy = ((h.y - chi.y) + oy) + (l.y - clo.y);
-          const float sz = ((h.z - chi.z) + oz) + (l.z - clo.z);
-          const float sm = h.w, ss = l.w;
+        for (int k = 0; k < 32; ++k) v[k] = 0.f;
+        Src<CELL> cur;
+        load_src<CELL>(a, e_begin + hl, e_end, cur);
+        for (int e0 = e_begin; e0 < e_end; e0 += 16) {
+          Src<CELL> nxt;
+          load_src<CELL>(a, e0 + 16 + hl, e_end, nxt);
+          const float ox = (float)((cur.code & 7) - 3) * a.fperiod,
+                      oy = (float)(((cur.code >> 3) & 7) - 3) * a.fperiod,
+                      oz = (float)(((cur.code >> 6) & 7) - 3) * a.fperiod;
+          const float sx = ((cur.h.x - chi.x) + ox) + (cur.l.x - clo.x);
+          const float sy = ((cur.h.y - chi.y) + oy) + (cur.l.y - clo.y);
+          const float sz = ((cur.h.z - chi.z) + oz) + (cur.l.z - clo.z);
+          const float sm = cur.h.w, ss = cur.l.w;
           float xx = 0.f, xy = 0.f, xz = 0.f, yy = 0.f, yz = 0.f, zz = 0.f, tr = 0.f;
           if constexpr (CELL) {
-            const float4 q0 = __ldg(sp + 2), q1 = __ldg(sp + 3);
-            xx = q0.x;
-            xy = q0.y;
-            xz = q0.z;
-            yy = q0.w;
-            yz = q1.x;
-            zz = q1.y;
-            tr = q1.z;
+            xx = cur.q0.x;
+            xy = cur.q0.y;
+            xz = cur.q0.z;
+            yy = cur.q0.w;
+            yz = cur.q1.x;
+            zz = cur.q1.y;
+            tr = cur.q1.z;
           }
-          /* source gradient accumulated over this chunk's targets */
+          /* this source's gradient over this half's targets */
           float g0 = 0.f, g1 = 0.f, g2 = 0.f, g3 = 0.f;
           float q_xx = 0.f, q_xy = 0.f, q_xz = 0.f, q_yy = 0.f, q_yz = 0.f, q_zz = 0.f;
-          if (valid) {
+          if (cur.valid) {
 #pragma unroll
-            for (int tt = 0; tt < kTC; ++tt) {
-              if (tt < ntc) {
-                const float4 tp = tpos[warp][t0 + tt];
-                const float4 la = tlam[warp][t0 + tt];
+            for (int tt = 0; tt < 8; ++tt) {
+              if (tt < myn) {
+                const float4 tp = tpos[warp][my0 + tt];
+                const float4 la = tlam[warp][my0 + tt];
+                const float twoh = ss + tsoft[warp][my0 + tt];
                 if constexpr (CELL) {
                   const float rx = tp.x - sx, ry = tp.y - sy, rz = tp.z - sz;
                   const float rsq = fmaf(rx, rx, fmaf(ry, ry, rz * rz));
@@ -203,7 +249,6 @@ __global__ void __launch_bounds__(kThreads, 2) vjp_kernel(const VjpArgs a) {
                     const float dir2 = dir * dir;
                     float bv = dir2 * dir, cv = bv * (3.f * dir2), dv = cv * (5.f * dir2),
                           ev = dv * (7.f * dir2);
-                    const float twoh = ss + tsoft[warp][t0 + tt];
                     if (rsq < twoh * twoh) {
                       const Spl5 k = spline5_near(dir, rsq, twoh);
                       bv = k.b;
@@ -237,12 +282,13 @@ __global__ void __launch_bounds__(kThreads, 2) vjp_kernel(const VjpArgs a) {
                      * twice in the forward formula) */
                     const float hr = -0.5f * dv * rl;
                     const float ht = 0.5f * cv * rl;
-                    q_xx += hr * rx * rx + ht + cv * la.x * rx;
-                    q_yy += hr * ry * ry + ht + cv * la.y * ry;
-                    q_zz += hr * rz * rz + ht + cv * la.z * rz;
-                    q_xy += 2.f * hr * rx * ry + cv * (la.x * ry + la.y * rx);
-                    q_xz += 2.f * hr * rx * rz + cv * (la.x * rz + la.z * rx);
-                    q_yz += 2.f * hr * ry * rz + cv * (la.y * rz + la.z * ry);
+                    const float hrx = hr * rx, hry = hr * ry;
+                    q_xx += fmaf(hrx, rx, fmaf(cv * la.x, rx, ht));
+                    q_yy += fmaf(hry, ry, fmaf(cv * la.y, ry, ht));
+                    q_zz += fmaf(hr * rz, rz, fmaf(cv * la.z, rz, ht));
+                    q_xy += fmaf(2.f * hrx, ry, cv * fmaf(la.x, ry, la.y * rx));
+                    q_xz += fmaf(2.f * hrx, rz, cv * fmaf(la.x, rz, la.z * rx));
+                    q_yz += fmaf(2.f * hry, rz, cv * fmaf(la.y, rz, la.z * ry));
                   }
                 } else {
                   const float rx = sx - tp.x, ry = sy - tp.y, rz = sz - tp.z;
@@ -251,16 +297,16 @@ __global__ void __launch_bounds__(kThreads, 2) vjp_kernel(const VjpArgs a) {
                     const float dir = rsqrtf(rsq);
                     const float dir2 = dir * dir;
                     float bv = dir2 * dir, cv = bv * (3.f * dir2);
-                    const float twoh = ss + tsoft[warp][t0 + tt];
                     if (rsq < twoh * twoh) {
                       const Spl5 k = spline5_near(dir, rsq, twoh);
                       bv = k.b;
                       cv = k.c;
                     }
                     const float rl = fmaf(rx, la.x, fmaf(ry, la.y, rz * la.z));
-                    const float gx = sm * (bv * la.x - cv * rl * rx);
-                    const float gy = sm * (bv * la.y - cv * rl * ry);
-                    const float gz = sm * (bv * la.z - cv * rl * rz);
+                    const float crl = cv * rl;
+                    const float gx = sm * fmaf(bv, la.x, -crl * rx);
+                    const float gy = sm * fmaf(bv, la.y, -crl * ry);
+                    const float gz = sm * fmaf(bv, la.z, -crl * rz);
                     v[4 * tt + 0] -= gx;
                     v[4 * tt + 1] -= gy;
                     v[4 * tt + 2] -= gz;
@@ -272,24 +318,37 @@ __global__ void __launch_bounds__(kThreads, 2) vjp_kernel(const VjpArgs a) {
                 }
               }
             }
-            double* gs = a.grad_src + (CELL ? 10 : 4) * idx;
-            atomicAdd(gs + 0, (double)g0);
-            atomicAdd(gs + 1, (double)g1);
-            atomicAdd(gs + 2, (double)g2);
-            atomicAdd(gs + 3, (double)g3);
+          }
+          /* lanes l and l + 16 hold the same entry */
+          g0 += __shfl_xor_sync(kFull, g0, 16);
+          g1 += __shfl_xor_sync(kFull, g1, 16);
+          g2 += __shfl_xor_sync(kFull, g2, 16);
+          g3 += __shfl_xor_sync(kFull, g3, 16);
+          if constexpr (CELL) {
+            q_xx += __shfl_xor_sync(kFull, q_xx, 16);
+            q_xy += __shfl_xor_sync(kFull, q_xy, 16);
+            q_xz += __shfl_xor_sync(kFull, q_xz, 16);
+            q_yy += __shfl_xor_sync(kFull, q_yy, 16);
+            q_yz += __shfl_xor_sync(kFull, q_yz, 16);
+            q_zz += __shfl_xor_sync(kFull, q_zz, 16);
+          }
+          if (cur.valid && half == 0) {
+            float* gs = acc + kStride * cur.idx;
+            red_add4(gs, g0, g1, g2, g3);
             if constexpr (CELL) {
-              atomicAdd(gs + 4, (double)q_xx);
-              atomicAdd(gs + 5, (double)q_xy);
-              atomicAdd(gs + 6, (double)q_xz);
-              atomicAdd(gs + 7, (double)q_yy);
-              atomicAdd(gs + 8, (double)q_yz);
-              atomicAdd(gs + 9, (double)q_zz);
+              red_add4(gs + 4, q_xx, q_xy, q_xz, q_yy);
+              red_add2(gs + 8, q_yz, q_zz);
             }
           }
-          tot += reduce_scatter32(v, lane);
+          cur = nxt;
         }
-        const int t = lane >> 2, q = lane & 3;
-        if (t < ntc && q < 3) a.grad_tgt[4 * (tbase + tb0 + t0 + t) + q] += (double)tot;
+        reduce_scatter16(v, lane);
+        const int t = hl >> 1, q = 2 * (hl & 1);
+        if (t < myn) {
+          double* gt = a.grad_tgt + 4 * (tbase + tb0 + my0 + t) + q;
+          gt[0] += (double)v[0];
+          if (q == 0) gt[1] += (double)v[1];
+        }
       }
     }
   }
@@ -302,38 +361,105 @@ __global__ void pack_lambda_kernel(const double* __restrict__ lam, long long n,
     out[i] = make_float4((float)lam[3 * i], (float)lam[3 * i + 1], (float)lam[3 * i + 2], 0.f);
 }
 
-/* Cell gradients to particles: every particle walks its ancestors (FP64). */
-__global__ void moment_grad_kernel(const double* __restrict__ moments,
-                                   const double* __restrict__ gcell, const int* __restrict__ parent,
-                                   const int* __restrict__ leaf, const double* __restrict__ parts,
-                                   long long n, long long n_moments, double* __restrict__ grad) {
-  for (long long k = blockIdx.x * (long long)blockDim.x + threadIdx.x; k < n;
-       k += (long long)gridDim.x * blockDim.x) {
-    const double mk = parts[5 * k], x = parts[5 * k + 2], y = parts[5 * k + 3], z = parts[5 * k + 4];
-    double gx = 0, gy = 0, gz = 0, gm = 0;
-    int node = leaf[k];
+/* Sums the particle accumulator copies into grad (FP64). */
+__global__ void finish_parts_kernel(const float* __restrict__ acc, long long n,
+                                    double* __restrict__ grad) {
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < 4 * n;
+       i += (long long)gridDim.x * blockDim.x) {
+    double s = 0.0;
+#pragma unroll
+    for (int r = 0; r < kReplicas; ++r) s += (double)acc[(size_t)r * 4 * n + i];
+    grad[i] += s;
+  }
+}
+
+/* Per node: the coefficient set {A, G, c0} of the moment chain from the
+ * node's summed gradients {gX, gM, gQ} and its moments (FP64). */
+__device__ void node_coef(const double* __restrict__ moments, const float* __restrict__ acc,
+                          long long n_moments, long long node, double (&c)[kCoef]) {
+  double g[10];
+#pragma unroll
+  for (int k = 0; k < 10; ++k) {
+    double s = 0.0;
+#pragma unroll
+    for (int r = 0; r < kReplicas; ++r)
+      s += (double)acc[((size_t)r * n_moments + node) * kCellAcc + k];
+    g[k] = s;
+  }
+  const double* mo = moments + 12 * node;
+  const double M = mo[2];
+  if (!(M > 0.0)) {
+#pragma unroll
+    for (int k = 0; k < kCoef; ++k) c[k] = 0.0;
+    return;
+  }
+  const double X = mo[3], Y = mo[4], Z = mo[5];
+  const double iM = 1.0 / M;
+  /* G = [[2gxx gxy gxz] [gxy 2gyy gyz] [gxz gyz 2gzz]] */
+  const double Gxx = 2 * g[4], Gxy = g[5], Gxz = g[6], Gyy = 2 * g[7], Gyz = g[8], Gzz = 2 * g[9];
+  const double GX = Gxx * X + Gxy * Y + Gxz * Z;
+  const double GY = Gxy * X + Gyy * Y + Gyz * Z;
+  const double GZ = Gxz * X + Gyz * Y + Gzz * Z;
+  const double ux = g[0] * iM, uy = g[1] * iM, uz = g[2] * iM;
+  c[0] = ux - GX;
+  c[1] = uy - GY;
+  c[2] = uz - GZ;
+  c[3] = Gxx;
+  c[4] = Gxy;
+  c[5] = Gxz;
+  c[6] = Gyy;
+  c[7] = Gyz;
+  c[8] = Gzz;
+  c[9] = g[3] - (ux * X + uy * Y + uz * Z) + 0.5 * (GX * X + GY * Y + GZ * Z);
+}
+
+__global__ void node_coef_kernel(const double* __restrict__ moments, const float* __restrict__ acc,
+                                 long long n_moments, double* __restrict__ coef) {
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n_moments;
+       i += (long long)gridDim.x * blockDim.x) {
+    double c[kCoef];
+    node_coef(moments, acc, n_moments, i, c);
+#pragma unroll
+    for (int k = 0; k < kCoef; ++k) coef[kCoef * i + k] = c[k];
+  }
+}
+
+/* prefix[i] = sum of the coefficient sets of node i and all its ancestors. */
+__global__ void node_prefix_kernel(const double* __restrict__ coef, const int* __restrict__ parent,
+                                   long long n_moments, double* __restrict__ prefix) {
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n_moments;
+       i += (long long)gridDim.x * blockDim.x) {
+    double p[kCoef];
+#pragma unroll
+    for (int k = 0; k < kCoef; ++k) p[k] = 0.0;
+    long long node = i;
     for (int depth = 0; node >= 0 && node < n_moments && depth < 256; ++depth) {
-      const double* gc = gcell + 10 * node;
-      const double* mo = moments + 12 * node;
-      const double M = mo[2];
-      if (M > 0.0) {
-        const double dx = x - mo[3], dy = y - mo[4], dz = z - mo[5];
-        const double gxx = gc[4], gxy = gc[5], gxz = gc[6], gyy = gc[7], gyz = gc[8], gzz = gc[9];
-        /* G d with G = [[2gxx gxy gxz] [gxy 2gyy gyz] [gxz gyz 2gzz]] */
-        const double Gx = 2 * gxx * dx + gxy * dy + gxz * dz;
-        const double Gy = gxy * dx + 2 * gyy * dy + gyz * dz;
-        const double Gz = gxz * dx + gyz * dy + 2 * gzz * dz;
-        gx += mk * (gc[0] / M + Gx);
-        gy += mk * (gc[1] / M + Gy);
-        gz += mk * (gc[2] / M + Gz);
-        gm += gc[3] + (gc[0] * dx + gc[1] * dy + gc[2] * dz) / M + 0.5 * (Gx * dx + Gy * dy + Gz * dz);
-      }
+#pragma unroll
+      for (int k = 0; k < kCoef; ++k) p[k] += coef[kCoef * node + k];
       node = parent[node];
     }
-    grad[4 * k] += gx;
-    grad[4 * k + 1] += gy;
-    grad[4 * k + 2] += gz;
-    grad[4 * k + 3] += gm;
+#pragma unroll
+    for (int k = 0; k < kCoef; ++k) prefix[kCoef * i + k] = p[k];
+  }
+}
+
+/* Moment chain to the particles from their bucket's prefix coefficients. */
+__global__ void moment_grad_kernel(const double* __restrict__ prefix, const int* __restrict__ leaf,
+                                   const double* __restrict__ parts, long long n,
+                                   long long n_moments, double* __restrict__ grad) {
+  for (long long k = blockIdx.x * (long long)blockDim.x + threadIdx.x; k < n;
+       k += (long long)gridDim.x * blockDim.x) {
+    const int node = leaf[k];
+    if (node < 0 || node >= n_moments) continue;
+    const double* c = prefix + kCoef * node;
+    const double mk = parts[5 * k], x = parts[5 * k + 2], y = parts[5 * k + 3], z = parts[5 * k + 4];
+    const double Gx = c[3] * x + c[4] * y + c[5] * z;
+    const double Gy = c[4] * x + c[6] * y + c[7] * z;
+    const double Gz = c[5] * x + c[7] * y + c[8] * z;
+    grad[4 * k] += mk * (c[0] + Gx);
+    grad[4 * k + 1] += mk * (c[1] + Gy);
+    grad[4 * k + 2] += mk * (c[2] + Gz);
+    grad[4 * k + 3] += c[9] + c[0] * x + c[1] * y + c[2] * z + 0.5 * (Gx * x + Gy * y + Gz * z);
   }
 }
 
@@ -365,22 +491,30 @@ extern "C" int changa_gravity_vjp_mixed(const double* moments, long long n_momen
   const size_t cb = al((size_t)n_moments * kCellPackF4 * sizeof(float4));
   const size_t pb = al((size_t)n_parts * kPartPackF4 * sizeof(float4));
   const size_t lb = al((size_t)n_parts * sizeof(float4));
-  const size_t gb = al((size_t)n_moments * 10 * sizeof(double));
+  const size_t fb = al((size_t)n_moments * kCoef * sizeof(double)) * 2;  // coef + prefix
+  const size_t ab = al((size_t)kReplicas * n_moments * kCellAcc * sizeof(float));
+  const size_t qb = al((size_t)kReplicas * n_parts * kPartAcc * sizeof(float));
   char* block = nullptr;
-  CHG_CUDA(cudaMallocAsync((void**)&block, cb + pb + lb + gb + 512, s));
+  CHG_CUDA(cudaMallocAsync((void**)&block, cb + pb + lb + fb + ab + qb + 512, s));
   float4* pc = (float4*)block;
   float4* pp = (float4*)(block + cb);
   float4* pl = (float4*)(block + cb + pb);
-  double* gcell = (double*)(block + cb + pb + lb);
-  unsigned int* q = (unsigned int*)(block + cb + pb + lb + gb);
-  CHG_CUDA(cudaMemsetAsync(gcell, 0, gb + 512, s));
+  double* coef = (double*)(block + cb + pb + lb);
+  double* prefix = coef + (size_t)n_moments * kCoef;
+  float* acc_cell = (float*)(block + cb + pb + lb + fb);
+  float* acc_part = (float*)(block + cb + pb + lb + fb + ab);
+  unsigned int* q = (unsigned int*)(block + cb + pb + lb + fb + ab + qb);
+  CHG_CUDA(cudaMemsetAsync(acc_cell, 0, ab + qb + 512, s));
   CHG_CUDA(launch_pack_cells(moments, n_moments, pc, s));
   CHG_CUDA(launch_pack_parts(parts, n_parts, pp, s));
-  pack_lambda_kernel<<<grid_of(n_parts, 256), 256, 0, s>>>(lam, n_parts, pl);
+  {
+    TimingScope ts(kKidPack, s);
+    pack_lambda_kernel<<<grid_of(n_parts, 256), 256, 0, s>>>(lam, n_parts, pl);
+  }
   count_launch();
   for (int k = 0; k < 2; ++k) {
     const ChangaListRequest* r = reqs[k];
-    if (!r || r->n_buckets == 0) continue;
+    if (!r || r->n_buckets == 0 || n_parts == 0 || (k == 0 ? n_moments : n_parts) == 0) continue;
     VjpArgs va;
     va.src = k == 0 ? pc : pp;
     va.n_src = k == 0 ? n_moments : n_parts;
@@ -395,17 +529,28 @@ extern "C" int changa_gravity_vjp_mixed(const double* moments, long long n_momen
     va.n_buckets = r->n_buckets;
     va.fperiod = (float)fperiod;
     va.grad_tgt = grad;
-    va.grad_src = k == 0 ? gcell : grad;
+    va.acc = k == 0 ? acc_cell : acc_part;
     va.queue = q + 64 * k;
     const int grid = grid_of(((long long)r->n_buckets + kWarps - 1) / kWarps, 1);
-    if (k == 0) vjp_kernel<true><<<grid, kThreads, 0, s>>>(va);
-    else vjp_kernel<false><<<grid, kThreads, 0, s>>>(va);
+    {
+      TimingScope ts(k == 0 ? kKidVjpCell : kKidVjpPart, s);
+      if (k == 0) vjp_kernel<true><<<grid, kThreads, 0, s>>>(va);
+      else vjp_kernel<false><<<grid, kThreads, 0, s>>>(va);
+    }
     count_launch();
     CHG_CUDA(cudaGetLastError());
   }
-  moment_grad_kernel<<<grid_of(n_parts, 256), 256, 0, s>>>(moments, gcell, parent, leaf, parts,
-                                                          n_parts, n_moments, grad);
-  count_launch();
+  {
+    TimingScope ts(kKidMoments, s);
+    finish_parts_kernel<<<grid_of(4 * n_parts, 256), 256, 0, s>>>(acc_part, n_parts, grad);
+    if (n_moments > 0) {
+      node_coef_kernel<<<grid_of(n_moments, 64), 64, 0, s>>>(moments, acc_cell, n_moments, coef);
+      node_prefix_kernel<<<grid_of(n_moments, 64), 64, 0, s>>>(coef, parent, n_moments, prefix);
+      moment_grad_kernel<<<grid_of(n_parts, 256), 256, 0, s>>>(prefix, leaf, parts, n_parts,
+                                                              n_moments, grad);
+    }
+  }
+  count_launch(n_moments > 0 ? 4 : 1);
   CHG_CUDA(cudaGetLastError());
   CHG_CUDA(cudaFreeAsync(block, s));
   return 0;

@@ -69,7 +69,8 @@ int record_error(int code, const char* what, const char* file, int line);
  * (changa_gb300_set_timing / changa_gb300_kernel_time). */
 enum KernelId : int {
   kKidListF32Cell = 0, kKidListF32Part, kKidListF64Cell, kKidListF64Part, kKidListMixCell,
-  kKidListMixPart, kKidEwaldF32, kKidEwaldF64, kKidEwaldMix, kKidPack, kKidCount
+  kKidListMixPart, kKidEwaldF32, kKidEwaldF64, kKidEwaldMix, kKidPack, kKidVjpCell, kKidVjpPart,
+  kKidMoments, kKidCount
 };
 inline int list_kernel_id(int form, bool cell) { return 2 * form + (cell ? 0 : 1); }
 

@@ -597,6 +597,17 @@ void chg_tree_get_structure(void* h, int* parent, int* leaf) {
   }
 }
 
+/* Particle range [first, first + count) of every moment (BFS) index, in GPU
+ * order: what the device moment refresh reduces over. */
+void chg_tree_get_ranges(void* h, int* first, int* count) {
+  Tree* t = (Tree*)h;
+  for (size_t i = 0; i < t->bfs_nodes.size(); ++i) {
+    const Node& nd = t->nodes[t->bfs_nodes[i]];
+    first[i] = nd.first;
+    count[i] = nd.count;
+  }
+}
+
 /* Runs the walk; returns 0 on success. */
 int chg_tree_walk(void* h, int nthreads) {
   Tree* t = (Tree*)h;

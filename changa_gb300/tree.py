@@ -127,6 +127,9 @@ def build_lists(pos, mass, soft, n_bucket=16, theta=0.7, period=0.0, n_replicas=
         parent = np.empty(nm, dtype=np.int32)
         leaf = np.empty(n, dtype=np.int32)
         lib.chg_tree_get_structure(h, _ptr(parent), _ptr(leaf))
+        first = np.empty(nm, dtype=np.int32)
+        count = np.empty(nm, dtype=np.int32)
+        lib.chg_tree_get_ranges(h, _ptr(first), _ptr(count))
         lib.chg_tree_walk(h, int(nthreads))
         nc = np.empty(nb, dtype=np.int64)
         npl = np.empty(nb, dtype=np.int64)
@@ -143,7 +146,7 @@ def build_lists(pos, mass, soft, n_bucket=16, theta=0.7, period=0.0, n_replicas=
                      bucket_starts=bstarts, bucket_sizes=bsizes, bucket_bbox=bbox,
                      cells=cells, plist=plist, period=float(period), n_replicas=int(n_replicas),
                      theta=float(theta), n_bucket=int(n_bucket),
-                     meta={"parent": parent, "leaf": leaf})
+                     meta={"parent": parent, "leaf": leaf, "first": first, "count": count})
 
 
 def concat_systems(systems):

@@ -10,6 +10,9 @@
                   theta 0.7, bucket 32, Ewald on.  The headline workload.
 * ``clusters512`` 512 independent Plummer clusters, N log-uniform in
                   [1024, 65536], theta 0.6, bucket 16 (batched form).
+* ``plummer64k``  Plummer sphere, N = 65536 (with velocities), eps 0.01,
+                  theta 0.7, bucket 16: the differentiated leapfrog
+                  (16 KDK steps, dt 0.005, L = sum w . x(T)).
 Seeds: PCG64(20261203 + index) with the index listed per workload.
 """
 from __future__ import annotations
@@ -100,4 +103,5 @@ WORKLOADS = {
     "lattice1m": Workload("lattice1m", 1, 128 ** 3, 16, 0.7, 1.0, (2.6, 2.8)),
     "nfw8m": Workload("nfw8m", 2, 2 ** 23, 32, 0.7, 1.0, (2.6, 2.8), soft=2e-4),
     "nfw1m": Workload("nfw1m", 2, 2 ** 20, 32, 0.7, 1.0, (2.6, 2.8), soft=2e-4),
+    "plummer64k": Workload("plummer64k", 4, 65536, 16, 0.7, 0.0, None, soft=0.01),
 }

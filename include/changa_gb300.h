@@ -70,8 +70,9 @@ unsigned long long changa_gb300_kernel_launches(void);
  * events on its own stream.  changa_gb300_kernel_time() waits for and sums
  * the recorded launches of one kernel since its last read, then forgets
  * them.  Kernel ids: 0/1 drop-in FP32 cell/particle lists, 2/3 FP64,
- * 4/5 FP32-mixed, 6/7/8 Ewald FP32/FP64/mixed, 9 mixed-form packing. */
-#define CHANGA_KERNEL_COUNT 10
+ * 4/5 FP32-mixed, 6/7/8 Ewald FP32/FP64/mixed, 9 mixed-form packing,
+ * 10/11 adjoint cell/particle lists, 12 moment up-pass and its adjoint. */
+#define CHANGA_KERNEL_COUNT 13
 void changa_gb300_set_timing(int on);
 int changa_gb300_kernel_time(int kernel, double *total_ms, long long *launches);
 
@@ -197,6 +198,16 @@ int changa_gravity_vjp_mixed(const double *moments, long long n_moments, const d
                              const ChangaListRequest *plist, double fperiod, const int *parent,
                              const int *leaf, const double *lam, double *grad,
                              cudaStream_t stream);
+
+/* Moment up-pass on the device over a fixed topology (no reference
+ * counterpart; the reference builds moments on the host,
+ * MultipoleMoments.h:206-352): for every moment i, recomputes soft,
+ * totalMass, cm and xx..zz of moments[i] (FP64, moments layout) from the
+ * particles parts[first[i] .. first[i] + count[i]) (parts layout, GPU
+ * order); the radius is kept.  first/count: device int arrays. */
+int changa_tree_moments(const double *parts, long long n_parts, const int *first,
+                        const int *count, long long n_moments, double *moments,
+                        cudaStream_t stream);
 
 /* Ewald correction for parts[idx[k]] into vars[idx[k]] (idx == NULL: the
  * first n_idx particles).  form: FP64 or MIXED. */
