@@ -65,6 +65,8 @@ def parse():
     ap.add_argument("--no-adjoint", dest="adjoint", action="store_false",
                     help="skip the adjoint / forward cost measurement (plummer64k)")
     ap.add_argument("--no-adjoint-leapfrog", dest="adjoint_leapfrog", action="store_false")
+    ap.add_argument("--variants", default=None,
+                    help="CELL,PART list-kernel shape variants to use instead of the autotuner")
     return ap.parse_args()
 
 
@@ -289,7 +291,7 @@ def main_reference(args):
     return 0
 
 
-def measure_adjoint(leapfrog=True, reps=20):
+def measure_adjoint(leapfrog=True, reps=20, tune=True):
     """The differentiation workload (plummer64k): one FP32-mixed force
     evaluation vs one adjoint (VJP) evaluation on the same tree, by kernel
     time and by CUDA events around the whole call; optionally the 16-step
@@ -306,7 +308,8 @@ def measure_adjoint(leapfrog=True, reps=20):
     t = lambda a: torch.from_numpy(np.ascontiguousarray(a, dtype=np.float64)).cuda()
     x, v, m, s = t(p["pos"]), t(p["vel"]), t(p["mass"]), t(p["soft"])
     ts = TreeStep(x, m, s, theta=wl.theta, n_bucket=wl.n_bucket)
-    autotune.tune(ts.ds, "mixed")
+    if tune:
+        autotune.tune(ts.ds, "mixed")
     lam = loss_weights(wl.n, 99)
     for _ in range(3):
         ts.accel("mixed")
@@ -381,7 +384,14 @@ def main_ours(args):
     flush = torch.empty(256 * 2 ** 20 // 4, dtype=torch.float32, device="cuda")  # > L2
     batched = hasattr(wl, "systems")
     from changa_gb300 import autotune
-    tuning = autotune.tune(ds, "mixed")  # untimed: selects the list-kernel shapes
+    if args.variants:
+        # fixed shapes (profiling runs): no autotuner launches
+        cv, pv = (int(x) for x in args.variants.split(","))
+        tuning = {"list_mixed_cell": {"variant": cv}, "list_mixed_part": {"variant": pv},
+                  "fixed": True}
+        autotune.apply({k: v for k, v in tuning.items() if k != "fixed"})
+    else:
+        tuning = autotune.tune(ds, "mixed")  # untimed: selects the list-kernel shapes
     graph = gravity.GravityGraph(ds, "mixed") if batched else None
 
     def step():
@@ -551,7 +561,7 @@ def main_ours(args):
 
     adj = None
     if rank == 0 and args.adjoint:
-        adj = measure_adjoint(args.adjoint_leapfrog)
+        adj = measure_adjoint(args.adjoint_leapfrog, tune=not args.variants)
 
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu:

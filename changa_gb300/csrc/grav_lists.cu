@@ -577,8 +577,10 @@ __device__ __noinline__ float2 spline_near_f(float r, float dir, float twoh) {
  * (the register cap) x GROUP source chunks per reduction (the list tile). */
 struct Variant {
   int minb, group;
+  bool tp;  // target-parallel kernel (list_kernel_tp); group unused
 };
-constexpr Variant kVariants[] = {{2, 16}, {3, 16}, {4, 16}, {3, 32}, {2, 32}};
+constexpr Variant kVariants[] = {{2, 16, false}, {3, 16, false}, {4, 16, false}, {3, 32, false},
+                                 {2, 32, false}, {2, 0, true},   {3, 0, true},   {4, 0, true}};
 constexpr int kNumVariants = sizeof(kVariants) / sizeof(kVariants[0]);
 
 /* Source-parallel list kernel of the FP32 forms.  Per warp and bucket: the
@@ -780,6 +782,321 @@ __global__ void __launch_bounds__(kThreads, MINB) list_kernel_src(const ListArgs
   }
 }
 
+/* ------------------------------------------------------------------ */
+/* Target-parallel kernel for the FP32 arithmetic forms (kF32, kMix).  */
+/*                                                                    */
+/* Lanes own targets, in G = 32 / nt groups for buckets of nt < 32     */
+/* targets (group g takes the staged entries g, g + G, ...).  The list */
+/* streams in blocks of 32 entries: each lane gathers one entry's raw  */
+/* source record into registers a block ahead, finishes it (replica    */
+/* offset, bucket-relative split coordinates) and stores it to the     */
+/* warp's shared-memory slice, from where every lane reads it by       */
+/* broadcast.  Accumulation is in registers with no cross-lane         */
+/* reduction inside the list; the spline test runs against one         */
+/* near-field radius per block ((max source soft + max target soft)^2)  */
+/* and only pairs inside it take the exact per-pair test.              */
+/* ------------------------------------------------------------------ */
+
+/* Raw words of one list entry as a lane holds them between the gather
+ * and the finishing step. */
+template <int FORM, bool CELL>
+struct RawRec {
+  float4 w0, w1, w2, w3;
+  float f4;
+  int code;
+};
+
+template <int FORM, bool CELL>
+__device__ __forceinline__ void gather_raw(const ListArgs& a, int e, int e_end,
+                                           RawRec<FORM, CELL>& r) {
+  long long idx = 0;
+  r.code = 0x49;  // replica (0, 0, 0)
+  if (e < e_end) {
+    const int2 ent = __ldg(a.list + e);
+    idx = ent.x;
+    if ((unsigned long long)idx >= (unsigned long long)a.n_src) idx = 0;  // memory safety
+    r.code = (ent.y >> 22) & 0x1ff;
+  }
+  if constexpr (FORM == kF32) {
+    if constexpr (CELL) {
+      const float4* m = reinterpret_cast<const float4*>(
+          static_cast<const CudaMultipoleMoments*>(a.src) + idx);
+      r.w0 = __ldg(m);
+      r.w1 = __ldg(m + 1);
+      r.w2 = __ldg(m + 2);
+    } else {
+      const CompactPartData* p = static_cast<const CompactPartData*>(a.src) + idx;
+      r.w0 = make_float4(__ldg(&p->position.x), __ldg(&p->position.y), __ldg(&p->position.z),
+                         __ldg(&p->mass));
+      r.f4 = __ldg(&p->soft);
+    }
+  } else {
+    const float4* p = static_cast<const float4*>(a.src) + (CELL ? kCellPackF4 : kPartPackF4) * idx;
+    r.w0 = __ldg(p);
+    r.w1 = __ldg(p + 1);
+    if constexpr (CELL) {
+      r.w2 = __ldg(p + 2);
+      r.w3 = __ldg(p + 3);
+    }
+  }
+}
+
+/* Finished record words: cells {x, y, z, M} {xx, xy, xz, yy} {yz, zz, tr,
+ * soft}; particles {x, y, z, m} and the softening.  Entries past the list
+ * end become massless records far away (they add exact zeros). */
+template <int FORM, bool CELL>
+__device__ __forceinline__ float finish_raw(const ListArgs& a, const RawRec<FORM, CELL>& r,
+                                            bool valid, float3 chi, float3 clo, float4* dst) {
+  const float fp = a.fperiod_f;
+  const float ox = (float)((r.code & 7) - 3) * fp, oy = (float)(((r.code >> 3) & 7) - 3) * fp,
+              oz = (float)(((r.code >> 6) & 7) - 3) * fp;
+  float4 p0;
+  float soft;
+  if constexpr (FORM == kF32) {
+    if constexpr (CELL) {
+      // w0 {radius, soft, M, cm.x}  w1 {cm.y, cm.z, xx, xy}  w2 {xz, yy, yz, zz}
+      p0 = make_float4(ox + r.w0.w, oy + r.w1.x, oz + r.w1.y, r.w0.z);
+      soft = r.w0.y;
+      dst[1] = make_float4(r.w1.z, r.w1.w, r.w2.x, r.w2.y);
+      dst[2] = make_float4(r.w2.z, r.w2.w, 0.5f * (r.w1.z + r.w2.y + r.w2.w), soft);
+    } else {
+      p0 = make_float4(ox + r.w0.x, oy + r.w0.y, oz + r.w0.z, r.w0.w);
+      soft = r.f4;
+    }
+  } else {
+    p0 = make_float4(((r.w0.x - chi.x) + ox) + (r.w1.x - clo.x),
+                     ((r.w0.y - chi.y) + oy) + (r.w1.y - clo.y),
+                     ((r.w0.z - chi.z) + oz) + (r.w1.z - clo.z), r.w0.w);
+    soft = r.w1.w;
+    if constexpr (CELL) {
+      // w2 {xx, xy, xz, yy}  w3 {yz, zz, tr, 0}
+      dst[1] = r.w2;
+      dst[2] = make_float4(r.w3.x, r.w3.y, r.w3.z, soft);
+    }
+  }
+  if (!valid) {
+    p0 = make_float4(1e30f, 1e30f, 1e30f, 0.f);
+    soft = 0.f;
+    if constexpr (CELL) {
+      dst[1] = make_float4(0.f, 0.f, 0.f, 0.f);
+      dst[2] = make_float4(0.f, 0.f, 0.f, 0.f);
+    }
+  }
+  dst[0] = p0;
+  return soft;
+}
+
+/* Hardware reciprocal square root, flushing subnormal inputs (the
+ * squared separations here are zero or far above the subnormal range):
+ * one MUFU instruction. */
+__device__ __forceinline__ float rsqrt_ftz(float x) {
+  float y;
+  asm("rsqrt.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
+  return y;
+}
+
+__device__ __forceinline__ float warp_max(float v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v = fmaxf(v, __shfl_xor_sync(kFull, v, o));
+  return v;
+}
+
+template <int FORM, bool CELL, int MINB>
+__global__ void __launch_bounds__(kThreads, MINB) list_kernel_tp(const ListArgs a) {
+  static_assert(FORM != kF64, "FP32 arithmetic forms only");
+  constexpr int RW = CELL ? 3 : 1;  // float4 words per staged record
+  __shared__ __align__(16) float4 stage[kWarps][2][32 * RW];
+  __shared__ float ssoft[kWarps][2][32];
+  __shared__ double red[kWarps][5][32];
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+
+  for (;;) {
+    int b = 0;
+    if (lane == 0) b = (int)atomicAdd(a.queue, 1u);
+    b = __shfl_sync(kFull, b, 0);
+    if (b >= a.n_buckets) break;
+    const int e_begin = max(__ldg(a.markers + b), 0);
+    const int e_end = (int)min((long long)__ldg(a.markers + b + 1), a.n_entries);  // memory safety
+    const long long tbase = __ldg(a.starts + b);
+    const int n = __ldg(a.sizes + b);
+    if (n <= 0 || tbase < 0 || tbase + n > a.n_tgt) continue;  // memory safety
+
+    float3 chi = make_float3(0.f, 0.f, 0.f), clo = chi;
+    if constexpr (FORM == kMix) {
+      const float4* tp = static_cast<const float4*>(a.tgt) + kPartPackF4 * tbase;
+      const float4 h = __ldg(tp), l = __ldg(tp + 1);
+      chi = make_float3(h.x, h.y, h.z);
+      clo = make_float3(l.x, l.y, l.z);
+    }
+
+    for (int t0 = 0; t0 < n; t0 += 32) {
+      const int nt = min(32, n - t0);
+      const int G = 32 / nt;
+      const int g = lane / nt;
+      const int t = lane - g * nt;
+      const bool active = g < G;
+      const long long ti = tbase + t0 + t;
+
+      float tx, ty, tz, tsoft, tmass;
+      if constexpr (FORM == kF32) {
+        const CompactPartData* p = static_cast<const CompactPartData*>(a.tgt) + ti;
+        tmass = __ldg(&p->mass);
+        tsoft = __ldg(&p->soft);
+        tx = __ldg(&p->position.x);
+        ty = __ldg(&p->position.y);
+        tz = __ldg(&p->position.z);
+      } else {
+        const float4* p = static_cast<const float4*>(a.tgt) + kPartPackF4 * ti;
+        const float4 h = __ldg(p), l = __ldg(p + 1);
+        tx = (h.x - chi.x) + (l.x - clo.x);
+        ty = (h.y - chi.y) + (l.y - clo.y);
+        tz = (h.z - chi.z) + (l.z - clo.z);
+        tmass = h.w;
+        tsoft = l.w;
+      }
+      const float tsmax = warp_max(active ? tsoft : 0.f);
+
+      /* running totals: plain for kF32, Kahan pairs for kMix */
+      float sx = 0.f, sy = 0.f, sz = 0.f, sp = 0.f, idt2 = 0.f;
+      float cx = 0.f, cy = 0.f, cz = 0.f, cp = 0.f;
+
+      RawRec<FORM, CELL> raw;
+      gather_raw<FORM, CELL>(a, e_begin + lane, e_end, raw);
+      int buf = 0;
+      for (int e0 = e_begin; e0 < e_end; e0 += 32, buf ^= 1) {
+        const int ne = min(32, e_end - e0);
+        float4* st = stage[warp][buf];
+        const float ls = finish_raw<FORM, CELL>(a, raw, lane < ne, chi, clo, st + lane * RW);
+        ssoft[warp][buf][lane] = ls;
+        const float ss = warp_max(ls) + tsmax;
+        const float near2 = ss * ss;
+        __syncwarp();
+        if (e0 + 32 < e_end) gather_raw<FORM, CELL>(a, e0 + 32 + lane, e_end, raw);
+        float ax = 0.f, ay = 0.f, az = 0.f, pot = 0.f;
+        /* one staged entry on this lane's target; entries past the list
+         * end are massless records at 1e30 and add exact zeros, so every
+         * block runs its full 32 slots */
+        auto body = [&](int k) {
+          const float4 s0 = st[k * RW];
+          if constexpr (CELL) {
+            /* gravity.h:436-472: r = target - cell */
+            const float4 q0 = st[k * RW + 1], q1 = st[k * RW + 2];
+            const float rx = tx - s0.x, ry = ty - s0.y, rz = tz - s0.z;
+            const float rsq = fmaf(rx, rx, fmaf(ry, ry, rz * rz));
+            const float dir = rsqrt_ftz(rsq);
+            const float dir2 = dir * dir;
+            float av = dir, bv = dir2 * dir;
+            float cv = bv * (3.f * dir2), dv = cv * (5.f * dir2);
+            if (rsq <= near2) {
+              const float twoh = q1.w + tsoft;
+              if (rsq == 0.f) {
+                av = bv = cv = dv = 0.f;
+              } else if (rsq < twoh * twoh) {
+                const float4 kk = splineq_near_f(dir, rsq, twoh);
+                av = kk.x;
+                bv = kk.y;
+                cv = kk.z;
+                dv = kk.w;
+              }
+            }
+            const float qirx = fmaf(q0.x, rx, fmaf(q0.y, ry, q0.z * rz));
+            const float qiry = fmaf(q0.y, rx, fmaf(q0.w, ry, q1.x * rz));
+            const float qirz = fmaf(q0.z, rx, fmaf(q1.x, ry, q1.y * rz));
+            const float qir = 0.5f * fmaf(qirx, rx, fmaf(qiry, ry, qirz * rz));
+            const float bM = bv * s0.w;
+            const float qir3 = fmaf(dv, qir, fmaf(-cv, q1.z, bM));
+            pot -= fmaf(s0.w, av, fmaf(cv, qir, -bv * q1.z));
+            ax = fmaf(cv, qirx, fmaf(-qir3, rx, ax));
+            ay = fmaf(cv, qiry, fmaf(-qir3, ry, ay));
+            az = fmaf(cv, qirz, fmaf(-qir3, rz, az));
+            idt2 = fmaxf(idt2, fmaf(tmass, bv, bM));
+          } else {
+            /* gravity.h:276-301: r = source - target */
+            const float rx = s0.x - tx, ry = s0.y - ty, rz = s0.z - tz;
+            const float rsq = fmaf(rx, rx, fmaf(ry, ry, rz * rz));
+            const float dir = rsqrt_ftz(rsq);
+            float av = dir, bv = dir * dir * dir;
+            if (rsq <= near2) {
+              const float twoh = ssoft[warp][buf][k] + tsoft;
+              if (rsq == 0.f) {
+                av = bv = 0.f;
+              } else {
+                const float r1 = rsq * dir;
+                if (r1 < twoh) {
+                  const float2 kk = spline_near_f(r1, dir, twoh);
+                  av = kk.x;
+                  bv = kk.y;
+                }
+              }
+            }
+            const float bm = bv * s0.w;
+            pot = fmaf(-s0.w, av, pot);
+            ax = fmaf(rx, bm, ax);
+            ay = fmaf(ry, bm, ay);
+            az = fmaf(rz, bm, az);
+            idt2 = fmaxf(idt2, fmaf(tmass, bv, bm));
+          }
+        };
+        if (G == 1) {
+#pragma unroll 8
+          for (int k = 0; k < 32; ++k) body(k);
+        } else if (active) {
+#pragma unroll 4
+          for (int k = g; k < 32; k += G) body(k);
+        }
+        if constexpr (FORM == kMix) {
+          kahan_add(sx, cx, ax);
+          kahan_add(sy, cy, ay);
+          kahan_add(sz, cz, az);
+          kahan_add(sp, cp, pot);
+        } else {
+          sx += ax;
+          sy += ay;
+          sz += az;
+          sp += pot;
+        }
+      }
+
+      if (active) {
+        red[warp][0][lane] = (double)sx - (double)cx;
+        red[warp][1][lane] = (double)sy - (double)cy;
+        red[warp][2][lane] = (double)sz - (double)cz;
+        red[warp][3][lane] = (double)sp - (double)cp;
+        red[warp][4][lane] = (double)idt2;
+      }
+      __syncwarp();
+      if (lane < nt) {
+        double rx = 0, ry = 0, rz = 0, rp = 0, ri = 0;
+        for (int gg = 0; gg < G; ++gg) {
+          const int l = gg * nt + lane;
+          rx += red[warp][0][l];
+          ry += red[warp][1][l];
+          rz += red[warp][2][l];
+          rp += red[warp][3][l];
+          ri = fmax(ri, red[warp][4][l]);
+        }
+        const long long to = tbase + t0 + lane;
+        if constexpr (FORM == kF32) {
+          VariablePartData* v = static_cast<VariablePartData*>(a.vars) + to;
+          v->a.x += (float)rx;
+          v->a.y += (float)ry;
+          v->a.z += (float)rz;
+          v->potential += (float)rp;
+          v->dtGrav = fmaxf((float)ri, v->dtGrav);
+        } else {
+          double* v = static_cast<double*>(a.vars) + 5 * to;
+          v[0] += rx;
+          v[1] += ry;
+          v[2] += rz;
+          v[3] += rp;
+          v[4] = fmax(ri, v[4]);
+        }
+      }
+      __syncwarp();
+    }
+  }
+}
+
 __global__ void pack_cells_kernel(const double* __restrict__ m, long long n, float4* __restrict__ out) {
   for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
        i += (long long)gridDim.x * blockDim.x) {
@@ -806,8 +1123,9 @@ __global__ void pack_parts_kernel(const double* __restrict__ p, long long n, flo
   }
 }
 
-/* The FP64 form keeps the target-parallel kernel (its cost is the FP64
- * pipe, not lane occupancy); the FP32 forms use the source-parallel one. */
+/* The FP64 form runs list_kernel (its cost is the FP64 pipe); the FP32
+ * forms run one of the variants below, target-parallel by default (the
+ * fastest on every measured workload), source-parallel on request. */
 template <typename K>
 int blocks_per_sm(K kernel, int* cache) {
   if (!*cache) {
@@ -833,14 +1151,18 @@ cudaError_t launch_kernel(K kernel, int* occ_cache, int kid, const ListArgs& a, 
 }
 
 /* current variant per list kernel id (FP32 forms) */
-int g_variant[6] = {1, 1, 0, 0, 1, 1};
+int g_variant[6] = {6, 7, 0, 0, 6, 7};
 
 template <int FORM, bool CELL, int V>
 cudaError_t launch_variant(const ListArgs& a, cudaStream_t s) {
   static int occ = 0;
   constexpr Variant var = kVariants[V];
-  return launch_kernel(list_kernel_src<FORM, CELL, var.minb, var.group>, &occ,
-                       list_kernel_id(FORM, CELL), a, s);
+  if constexpr (var.tp)
+    return launch_kernel(list_kernel_tp<FORM, CELL, var.minb>, &occ, list_kernel_id(FORM, CELL),
+                         a, s);
+  else
+    return launch_kernel(list_kernel_src<FORM, CELL, var.minb, var.group>, &occ,
+                         list_kernel_id(FORM, CELL), a, s);
 }
 
 template <int FORM, bool CELL, int... V>

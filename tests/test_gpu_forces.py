@@ -198,3 +198,41 @@ def test_empty_request_and_validation(cuda_ok):
         for q in (d_m, d_p, d_v):
             rt.cudaFree(q)
         inp.free()
+
+
+def test_every_list_variant(plummer):
+    """Every shape variant of the FP32-form list kernels (source-parallel
+    and target-parallel), on the Plummer lists and on ragged buckets, holds
+    the same tolerances as the default one."""
+    L, ref, ref32 = plummer
+    lib = N.cuda_lib()
+    ids = [N.KERNEL_IDS[k] for k in ("list_f32_cell", "list_f32_part", "list_mixed_cell",
+                                     "list_mixed_part")]
+    saved = [lib.changa_gb300_get_list_variant(k) for k in ids]
+    p = ics.plummer(3000, ics.rng_for(5), soft=0.05)
+    ragged = [tree.build_lists(p["pos"], p["mass"], p["soft"], n_bucket=nb, theta=0.6)
+              for nb in (1, 5, 33, 64)]
+    ragged_ref = [oracle_vars(R) for R in ragged]
+    try:
+        for var in range(lib.changa_gb300_list_variant_count()):
+            for k in ids:
+                assert lib.changa_gb300_set_list_variant(k, var) == 0
+            v = gravity.DeviceSystem(L).step("mixed").cpu().numpy()
+            e = force_rel_err(v, ref)
+            assert np.median(e) < MIX_MEDIAN_TOL and np.percentile(e, 99) < MIX_P99_TOL, var
+            assert np.median(pot_rel_err(v, ref)) < MIX_MEDIAN_TOL, var
+            np.testing.assert_allclose(v[:, 4], ref[:, 4], rtol=1e-4, err_msg=str(var))
+            inp = gravity.DropInInputs(L)
+            try:
+                v32 = gravity.dropin_step(inp).astype(np.float64)
+            finally:
+                inp.free()
+            e = force_rel_err(v32, ref32)
+            assert np.median(e) < F32_MEDIAN_TOL and np.percentile(e, 99) < F32_P99_TOL, var
+            for R, rr in zip(ragged, ragged_ref):
+                vm = gravity.DeviceSystem(R).step("mixed").cpu().numpy()
+                assert np.median(force_rel_err(vm, rr)) < MIX_MEDIAN_TOL, (var, R.n_bucket)
+                assert np.percentile(force_rel_err(vm, rr), 99) < MIX_P99_TOL, (var, R.n_bucket)
+    finally:
+        for k, s in zip(ids, saved):
+            lib.changa_gb300_set_list_variant(k, s)
