@@ -14,7 +14,7 @@ bucket 32, theta 0.7).  Other lines of the JSON:
   e2e          the same metric through changa_gravity_step_host with host
                (pinned) buffers, host<->device copies inside the timed region;
   roofline     the dominant kernel (FP32-mixed cell-list kernel) against the
-               FP32 FMA peak of the GPU;
+               FP32 FMA peak of the GPU (roofline_pp: the particle-list kernel);
   cpu_baseline the CPU oracle (ChaNGa's own gravity.h/Ewald.cpp when it was
                built here, else its C restatement) on a bounded sample;
   adjoint      plummer64k: one adjoint (VJP) evaluation against one forward
@@ -128,43 +128,23 @@ class ClockSampler:
 
 
 def dist_setup(args):
-    import torch
-    world = int(os.environ.get("WORLD_SIZE", "1"))
-    rank = int(os.environ.get("RANK", "0"))
-    local = int(os.environ.get("LOCAL_RANK", "0"))
-    if world > 1:
-        import torch.distributed as dist
-        torch.cuda.set_device(local)
-        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
-    elif torch.cuda.is_available():
-        torch.cuda.set_device(0)
-    return world, rank, local
+    from changa_gb300 import replicas
+    return replicas.setup()
 
 
 def barrier(world):
-    if world > 1:
-        import torch.distributed as dist
-        dist.barrier()
+    from changa_gb300 import replicas
+    replicas.barrier(world)
 
 
 def max_over_ranks(world, x):
-    if world == 1:
-        return x
-    import torch
-    import torch.distributed as dist
-    t = torch.tensor([x], dtype=torch.float64, device="cuda")
-    dist.all_reduce(t, op=dist.ReduceOp.MAX)
-    return float(t.item())
+    from changa_gb300 import replicas
+    return replicas.max_over_ranks(world, x)
 
 
 def sum_over_ranks(world, x):
-    if world == 1:
-        return x
-    import torch
-    import torch.distributed as dist
-    t = torch.tensor([x], dtype=torch.float64, device="cuda")
-    dist.all_reduce(t, op=dist.ReduceOp.SUM)
-    return float(t.item())
+    from changa_gb300 import replicas
+    return replicas.sum_over_ranks(world, x)
 
 
 def cpu_sample(lists, target, seed=12345):
@@ -267,12 +247,13 @@ def main_reference(args):
     wl = WORKLOADS[args.workload]
     lists = wl.lists()
     ew = wl.ewald_config()
+    per_step = args.cpu_sample / 5  # a few seconds of CPU work per step
     for _ in range(args.warmup):
-        run_cpu(lists, ew, args.cpu_sample / 4)
+        run_cpu(lists, ew, per_step / 4)
     vals = []
     t_all = time.perf_counter()
     for _ in range(args.steps):
-        r = run_cpu(lists, ew, args.cpu_sample)
+        r = run_cpu(lists, ew, per_step)
         vals.append(r)
     wall = time.perf_counter() - t_all
     value = sum(r["value"] for r in vals) / len(vals)
@@ -531,31 +512,40 @@ def main_ours(args):
         for a in list(pin.values()) + [out]:
             a.free()
 
-    # roofline of the dominant kernel (FP32-mixed cell lists) and the P-P kernel
+    # roofline of the dominant kernel (FP32-mixed cell lists) and the P-P kernel.
+    # The bound is the FP32 FMA pipe (no tensor-core or HBM bound applies:
+    # DRAM traffic is under 5% of peak); traffic comes from the committed ncu
+    # capture, valid for the nfw8m workload it was scaled to.
     peak, peak_src = fp32_peak_tflops()
-    tr = traffic_from_profiles()
+    tr = traffic_from_profiles() if args.workload == "nfw8m" else {}
+    lib_v = [lib.changa_gb300_get_list_variant(N.KERNEL_IDS[k])
+             for k in ("list_mixed_cell", "list_mixed_part")]
     roof = None
     ms_pc, n_pc = ktimes["list_mixed_cell"]
     ms_pp, n_pp = ktimes["list_mixed_part"]
     if n_pc:
         t_pc = ms_pc / n_pc / 1e3
         ach = I_c * FLOP_PC / t_pc / 1e12
-        roof = {"bound": "fp32", "kernel": "list_kernel<kMix, cell> (FP32-mixed cell lists)",
+        roof = {"bound": "fp32", "kernel": "FP32-mixed cell-list kernel, shape variant %d" % lib_v[0],
                 "achieved": ach, "peak": peak, "unit": "TFLOP/s", "frac": ach / peak,
                 "peak_source": peak_src,
                 "algorithmic_flop_per_launch": I_c * FLOP_PC,
                 "flop_per_interaction": FLOP_PC, "interactions_per_launch": I_c,
                 "avg_launch_ms": 1e3 * t_pc,
                 "traffic": tr.get("list_mixed_cell_bytes_per_launch"),
+                "fma_pipe_active_ncu_pct": tr.get("list_mixed_cell_fma_pipe_pct"),
                 "traffic_note": tr.get("note")}
     roof_pp = None
     if n_pp:
         t_pp = ms_pp / n_pp / 1e3
         ach = I_p * FLOP_PP / t_pp / 1e12
-        roof_pp = {"bound": "fp32", "kernel": "list_kernel<kMix, part> (FP32-mixed particle lists)",
+        roof_pp = {"bound": "fp32",
+                   "kernel": "FP32-mixed particle-list kernel, shape variant %d" % lib_v[1],
                    "achieved": ach, "peak": peak, "unit": "TFLOP/s", "frac": ach / peak,
-                   "algorithmic_flop_per_launch": I_p * FLOP_PP, "avg_launch_ms": 1e3 * t_pp,
-                   "traffic": tr.get("list_mixed_part_bytes_per_launch")}
+                   "algorithmic_flop_per_launch": I_p * FLOP_PP, "flop_per_interaction": FLOP_PP,
+                   "interactions_per_launch": I_p, "avg_launch_ms": 1e3 * t_pp,
+                   "traffic": tr.get("list_mixed_part_bytes_per_launch"),
+                   "fma_pipe_active_ncu_pct": tr.get("list_mixed_part_fma_pipe_pct")}
     kshare = {k: {"ms_per_step": v[0] / max(1, args.steps), "launches": v[1]}
               for k, v in ktimes.items() if v[1]}
 
