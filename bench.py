@@ -65,6 +65,8 @@ def parse():
     ap.add_argument("--no-adjoint", dest="adjoint", action="store_false",
                     help="skip the adjoint / forward cost measurement (plummer64k)")
     ap.add_argument("--no-adjoint-leapfrog", dest="adjoint_leapfrog", action="store_false")
+    ap.add_argument("--no-direct", dest="direct", action="store_false",
+                    help="skip the direct-sum error of the sampled particles")
     ap.add_argument("--variants", default=None,
                     help="CELL,PART list-kernel shape variants to use instead of the autotuner")
     return ap.parse_args()
@@ -455,14 +457,27 @@ def main_ours(args):
         v64 = ds.vars.cpu().numpy()
         rng = np.random.default_rng(7)
         samp = rng.choice(lists.n, min(16384, lists.n), replace=False)
-        num = np.linalg.norm(v_mixed[samp, :3] - v64[samp, :3], axis=1)
-        den = np.linalg.norm(v64[samp, :3], axis=1)
-        err = num / den
+
+        def rel(a, ref):
+            e = np.linalg.norm(a[:, :3] - ref[:, :3], axis=1) / np.linalg.norm(ref[:, :3], axis=1)
+            return float(np.median(e)), float(np.percentile(e, 99))
+        err = rel(v_mixed[samp], v64[samp])
         fp64 = {"ms_per_step": ms64, "interactions_per_s": I / (ms64 / 1e3),
                 "mixed_over_fp64": (I / (ms / 1e3)) / (I / (ms64 / 1e3)),
-                "median_rel_force_err_vs_fp64": float(np.median(err)),
-                "p99_rel_force_err_vs_fp64": float(np.percentile(err, 99)),
+                "median_rel_force_err_vs_fp64": err[0],
+                "p99_rel_force_err_vs_fp64": err[1],
                 "sampled_particles": int(len(samp))}
+        if args.direct:
+            # the same sample against the direct sum (Ewald-summed when periodic)
+            t0 = time.perf_counter()
+            dsum = gravity.direct_forces(ds.parts, samp, period=float(lists.period))
+            em, e64 = rel(v_mixed[samp], dsum), rel(v64[samp], dsum)
+            fp64.update({"median_rel_force_err_mixed_vs_direct": em[0],
+                         "p99_rel_force_err_mixed_vs_direct": em[1],
+                         "median_rel_force_err_fp64_vs_direct": e64[0],
+                         "p99_rel_force_err_fp64_vs_direct": e64[1],
+                         "direct_sum": "changa_direct_forces, FP64-accumulated%s, %.1f s" % (
+                             " Ewald sum" if lists.period else "", time.perf_counter() - t0)})
         for k in N.KERNEL_IDS:
             N.kernel_time(k)
 

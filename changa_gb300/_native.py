@@ -172,6 +172,7 @@ CUDA_SIGNATURES = {
                                       C.POINTER(ChangaListRequest), _D, _VP, _VP, _VP, _VP, _VP]),
     "changa_gravity_graph_destroy": (None, [_VP]),
     "changa_tree_moments": (_I, [_VP, _LL, _VP, _VP, _LL, _VP, _VP]),
+    "changa_direct_forces": (_I, [_VP, _LL, _VP, _LL, _D, _D, _VP, _VP]),
     "changa_ewald_forces": (_I, [_I, _VP, _LL, _VP, _LL, C.POINTER(ChangaEwaldParams), _VP, _VP]),
     "changa_ewald_table": (_I, [_VP, _D, _D, _VP, _I]),
 }

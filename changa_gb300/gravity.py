@@ -301,3 +301,18 @@ class GravityGraph:
         if self.handle:
             N.cuda_lib().changa_gravity_graph_destroy(self.handle)
             self.handle = None
+
+
+def direct_forces(parts, idx, period=0.0, rcut_frac=0.0, stream=None):
+    """The direct-sum yardstick (changa_direct_forces) on the particles idx
+    of `parts` (device FP64 tensor, parts layout): returns a numpy array
+    len(idx) x 4 {ax, ay, az, pot (open boundaries only)}."""
+    import torch
+    i = torch.from_numpy(np.ascontiguousarray(idx, dtype=np.int32)).to(parts.device)
+    out = torch.empty((len(idx), 4), dtype=torch.float64, device=parts.device)
+    s = stream if stream is not None else torch.cuda.current_stream().cuda_stream
+    rc = N.cuda_lib().changa_direct_forces(parts.data_ptr(), parts.shape[0], i.data_ptr(),
+                                           len(idx), float(period), float(rcut_frac),
+                                           out.data_ptr(), s)
+    N.check(rc, "changa_direct_forces")
+    return out.cpu().numpy()

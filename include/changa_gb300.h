@@ -209,6 +209,19 @@ int changa_tree_moments(const double *parts, long long n_parts, const int *first
                         const int *count, long long n_moments, double *moments,
                         cudaStream_t stream);
 
+/* Direct-sum accuracy yardstick (no reference counterpart): the force on
+ * the particles parts[idx[k]] from every particle, without a tree.  L == 0:
+ * open boundaries, SPLINE softening, out[k] = {ax, ay, az, pot}.  L > 0:
+ * periodic cube of side L by Ewald summation (real space within
+ * rcut_frac * L of the minimum image, 0 < rcut_frac <= 0.5, 0 selects 0.5;
+ * k space to exp(-k^2 / 4 alpha^2) = 1e-9), out[k] = {ax, ay, az, 0}.
+ * Pair terms in FP32 on split coordinates with compensated sums, S(k) and
+ * totals in FP64: about 1e-6 of |a|.  parts: device FP64 (parts layout);
+ * idx: device int; out: device FP64 n_idx x 4 (overwritten).  Returns after
+ * the stream has finished. */
+int changa_direct_forces(const double *parts, long long n_parts, const int *idx, long long n_idx,
+                         double L, double rcut_frac, double *out, cudaStream_t stream);
+
 /* Ewald correction for parts[idx[k]] into vars[idx[k]] (idx == NULL: the
  * first n_idx particles).  form: FP64 or MIXED. */
 int changa_ewald_forces(int form, const double *parts, long long n_parts, const int *idx,

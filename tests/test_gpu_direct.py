@@ -1,0 +1,116 @@
+"""The direct-sum yardstick (changa_direct_forces): open boundaries against
+the FP64 CPU direct sum of the oracle, periodic Ewald against a brute-force
+FP64 Ewald sum written here in numpy, independence of the Ewald split, and
+agreement with the FP64 tree + Ewald form to the tree's truncation error."""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+def _direct(parts, idx, L=0.0, rcut=0.0):
+    import torch
+    from changa_gb300 import gravity
+    p = torch.from_numpy(np.ascontiguousarray(parts, dtype=np.float64)).cuda()
+    return gravity.direct_forces(p, idx, period=L, rcut_frac=rcut)
+
+
+def _ewald_numpy(parts, alpha=5.0, nimg=3, nk=14):
+    """Brute-force FP64 Ewald forces in the unit cube (every pair, every
+    image within nimg boxes, every k with |n| <= nk), with the SPLINE
+    softening correction on the minimum-image pair."""
+    import oracle
+    from scipy.special import erfc
+    m, s, x = parts[:, 0], parts[:, 1], parts[:, 2:5]
+    n = len(m)
+    acc = np.zeros((n, 3))
+    rng = np.arange(-nimg, nimg + 1)
+    imgs = np.array(np.meshgrid(rng, rng, rng, indexing="ij")).reshape(3, -1).T
+    for i in range(n):
+        for j in range(n):
+            d = x[j] - x[i] + imgs
+            r = np.sqrt((d * d).sum(1))
+            ok = r > 0
+            d, r = d[ok], r[ok]
+            f = erfc(alpha * r) / r ** 3 + 2 * alpha / np.sqrt(np.pi) * np.exp(-(alpha * r) ** 2) / r ** 2
+            acc[i] += m[j] * (f[:, None] * d).sum(0)
+            if i != j:
+                dm = x[j] - x[i]
+                dm -= np.round(dm)
+                rm = np.sqrt((dm * dm).sum())
+                tw = s[i] + s[j]
+                if rm < tw:
+                    _, b = oracle.spline_ab(np.array([rm * rm]), np.array([tw]))
+                    acc[i] += m[j] * (b[0] - 1.0 / rm ** 3) * dm
+    kr = np.arange(-nk, nk + 1)
+    ks = np.array(np.meshgrid(kr, kr, kr, indexing="ij")).reshape(3, -1).T
+    ks = ks[((ks * ks).sum(1) > 0) & ((ks * ks).sum(1) <= nk * nk)] * 2 * np.pi
+    k2 = (ks * ks).sum(1)
+    g = np.exp(-k2 / (4 * alpha ** 2)) / k2
+    S = (m[None, :] * np.exp(1j * ks @ x.T)).sum(1)
+    for i in range(n):
+        im = np.imag(np.exp(1j * ks @ x[i]) * np.conj(S))
+        acc[i] += -4 * np.pi * ((g * im)[:, None] * ks).sum(0)
+    return acc
+
+
+def test_open_boundaries_match_oracle(cuda_ok):
+    import oracle
+    from changa_gb300 import ics
+    p = ics.plummer(4096, ics.rng_for(0), soft=0.01)
+    parts = np.concatenate([p["mass"][:, None], p["soft"][:, None], p["pos"]], axis=1)
+    idx = np.random.default_rng(1).choice(4096, 512, replace=False).astype(np.int32)
+    got = _direct(parts, idx)
+    acc, pot = oracle.direct_sum(parts, idx)
+    e = np.linalg.norm(got[:, :3] - acc, axis=1) / np.linalg.norm(acc, axis=1)
+    assert e.max() < 1e-5, e.max()
+    assert (np.abs(got[:, 3] - pot) / np.abs(pot)).max() < 1e-5
+
+
+def test_periodic_matches_bruteforce_ewald(cuda_ok):
+    rng = np.random.default_rng(2)
+    n = 12
+    x = rng.uniform(0, 1, (n, 3))
+    x[1] = x[0] + np.array([1.2e-4, -0.5e-4, 0.3e-4])  # one pair inside the softening
+    x[2] = np.array([0.999, 0.5, 0.001])               # straddles the box faces
+    parts = np.concatenate([rng.uniform(0.5, 1.5, (n, 1)) / n, np.full((n, 1), 1e-4), x], axis=1)
+    ref = _ewald_numpy(parts)
+    got = _direct(parts, np.arange(n, dtype=np.int32), L=1.0)
+    scale = np.sqrt((ref ** 2).sum(1).mean())
+    e = np.linalg.norm(got[:, :3] - ref, axis=1) / scale
+    assert e.max() < 2e-6, e
+
+
+def test_periodic_split_independent(cuda_ok):
+    from changa_gb300 import ics, tree
+    p = ics.lattice_grf(24, ics.rng_for(1))
+    L = tree.build_lists(p["pos"], p["mass"], p["soft"], n_bucket=16, theta=0.4, period=1.0)
+    idx = np.random.default_rng(3).choice(L.n, 1024, replace=False).astype(np.int32)
+    a5 = _direct(L.parts, idx, L=1.0, rcut=0.5)
+    a3 = _direct(L.parts, idx, L=1.0, rcut=0.3)
+    rms = np.sqrt((a5[:, :3] ** 2).sum(1).mean())
+    assert (np.linalg.norm(a5[:, :3] - a3[:, :3], axis=1) / rms).max() < 1e-5
+
+
+def test_tree_converges_to_direct_sum(cuda_ok):
+    """The FP64 tree + Ewald form (ChaNGa's algorithm) approaches the direct
+    Ewald sum as the opening angle shrinks, on a clustered periodic set."""
+    from changa_gb300 import gravity, ics, tree
+    p = ics.nfw_halos(32768, ics.rng_for(2), soft=1e-3)
+    idx = np.random.default_rng(4).choice(32768, 1024, replace=False)
+    ew = gravity.EwaldConfig(1.0, 1, 2.6, 2.8)
+    med = {}
+    for theta in (0.7, 0.5, 0.3):
+        L = tree.build_lists(p["pos"], p["mass"], p["soft"], n_bucket=16, theta=theta,
+                             period=1.0)
+        gi = np.argsort(L.perm)[idx].astype(np.int32)  # caller index -> GPU order
+        ds = gravity.DeviceSystem(L, ewald=ew)
+        v = ds.step("fp64").cpu().numpy()[gi]
+        ref = gravity.direct_forces(ds.parts, gi, period=1.0)
+        e = np.linalg.norm(v[:, :3] - ref[:, :3], axis=1) / np.linalg.norm(ref[:, :3], axis=1)
+        med[theta] = float(np.median(e))
+        print("nfw 32k theta %.1f: tree+Ewald vs direct median %.2e p99 %.2e" % (
+            theta, med[theta], np.percentile(e, 99)))
+    assert med[0.7] < 3e-3
+    assert med[0.3] < med[0.5] < med[0.7]
+    assert med[0.3] < med[0.7] / 4
