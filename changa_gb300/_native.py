@@ -99,6 +99,7 @@ CHANGA_ERRORS_RECORD = 1
 CHANGA_FORM_FP32 = 0
 CHANGA_FORM_FP64 = 1
 CHANGA_FORM_MIXED = 2
+CHANGA_STEP_OVERWRITE = 0x100
 CHANGA_MAX_EWH = 256
 
 # kernel ids of changa_gb300_kernel_time
@@ -148,6 +149,7 @@ CUDA_SIGNATURES = {
     "changa_gb300_version": (_I, []),
     "changa_gb300_kernel_launches": (C.c_ulonglong, []),
     "changa_gb300_set_timing": (None, [_I]),
+    "changa_gb300_set_host_chunk_bytes": (None, [_SZ]),
     "changa_gb300_list_variant_count": (_I, []),
     "changa_gb300_set_list_variant": (_I, [_I, _I]),
     "changa_gb300_get_list_variant": (_I, [_I]),

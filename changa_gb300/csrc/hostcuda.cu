@@ -13,6 +13,7 @@
  * or other streams.  Source-array bounds for the kernels' index guards come
  * from cuMemGetAddressRange on the device pointer the request names.
  */
+#include <algorithm>
 #include <atomic>
 #include <climits>
 #include <cstdio>
@@ -783,24 +784,82 @@ int changa_gravity_step(int form, const double* moments, long long n_moments, co
   return rc;
 }
 
+static std::atomic<size_t> g_host_chunk_bytes{size_t(512) << 20};
+
+void changa_gb300_set_host_chunk_bytes(size_t bytes) {
+  g_host_chunk_bytes.store(bytes < 4096 ? 4096 : bytes);
+}
+
+/* The copy stream of the host entry on each device (created once). */
+static cudaStream_t copy_stream() {
+  static cudaStream_t st[64] = {nullptr};
+  static std::mutex mu;
+  int dev = 0;
+  cudaGetDevice(&dev);
+  if (dev < 0 || dev >= 64) dev = 0;
+  std::lock_guard<std::mutex> lk(mu);
+  if (!st[dev] && cudaStreamCreateWithFlags(&st[dev], cudaStreamNonBlocking) != cudaSuccess)
+    st[dev] = nullptr;
+  return st[dev];
+}
+
+/* Host-array evaluation, pipelined: the small arrays go first, then each
+ * interaction list in chunks of about kChunkBytes, on a copy stream; the
+ * compute stream packs, runs Ewald, and launches the list kernel on each
+ * chunk's bucket range as soon as its entries have landed, so the list
+ * stream from host memory overlaps the force arithmetic. */
 int changa_gravity_step_host(int form, const double* moments, long long n_moments,
                              const double* parts, long long n_parts, const ChangaListRequest* cells,
                              const ChangaListRequest* plist, double fperiod,
                              const ChangaEwaldParams* ewald, double* vars, cudaStream_t s) {
+  const bool overwrite = (form & CHANGA_STEP_OVERWRITE) != 0;
+  form &= ~CHANGA_STEP_OVERWRITE;
+  if (form != CHANGA_FORM_FP64 && form != CHANGA_FORM_MIXED)
+    return record_error(CHANGA_E_INVALID_ARG, "gravity_step_host: form", __FILE__, __LINE__);
   if (!moments || !parts || !vars || n_moments < 0 || n_parts < 0)
     return record_error(CHANGA_E_INVALID_ARG, "gravity_step_host: arrays", __FILE__, __LINE__);
   if ((cells && check_req(cells)) || (plist && check_req(plist)))
     return record_error(CHANGA_E_INVALID_ARG, "gravity_step_host: requests", __FILE__, __LINE__);
+  if (ewald && ewald->nEwhLoop > CHANGA_MAX_EWH)
+    return record_error(CHANGA_E_TOO_LARGE, "gravity_step_host: nEwhLoop", __FILE__, __LINE__);
   prepare_pool();
+  const int f = form == CHANGA_FORM_FP64 ? kF64 : kMix;
+  cudaStream_t c = copy_stream();
+  if (!c) return record_error(cudaErrorUnknown, "gravity_step_host: copy stream", __FILE__, __LINE__);
+  const size_t kChunkBytes = g_host_chunk_bytes.load();
+
+  /* chunks: [request][bucket range] by entry bytes */
   const ChangaListRequest* reqs[2] = {cells, plist};
-  size_t off[2][4], sz[2][4];
-  const size_t mb = align256((size_t)n_moments * 12 * sizeof(double));
-  const size_t pb = align256((size_t)n_parts * 5 * sizeof(double));
-  size_t total = mb + pb + pb;  // moments, parts, vars, then the requests
+  std::vector<std::pair<int, int>> chunks[2];
   for (int k = 0; k < 2; ++k) {
     const ChangaListRequest* r = reqs[k];
-    long long ne = r ? r->n_entries : 0;
-    int nb = r ? r->n_buckets : 0;
+    if (!r || r->n_buckets == 0) continue;
+    const long long per = (long long)(kChunkBytes / sizeof(ILCell));
+    int b0 = 0;
+    while (b0 < r->n_buckets) {
+      const int* lo = r->markers + b0 + 1;
+      const int* hi = r->markers + r->n_buckets + 1;
+      const long long want = (long long)r->markers[b0] + per;
+      const int* it = std::upper_bound(lo, hi, (int)std::min<long long>(want, INT_MAX));
+      int b1 = (int)(it - r->markers) - 1;
+      if (b1 <= b0) b1 = b0 + 1;
+      if (b1 > r->n_buckets) b1 = r->n_buckets;
+      chunks[k].push_back({b0, b1});
+      b0 = b1;
+    }
+  }
+
+  /* one device block: FP64 inputs, packed inputs, requests, queue counters */
+  const size_t mb = align256((size_t)n_moments * 12 * sizeof(double));
+  const size_t pb = align256((size_t)n_parts * 5 * sizeof(double));
+  const size_t cpb = f == kMix ? align256((size_t)n_moments * kCellPackF4 * sizeof(float4)) : 0;
+  const size_t ppb = f == kMix ? align256((size_t)n_parts * kPartPackF4 * sizeof(float4)) : 0;
+  size_t off[2][4], sz[2][4];
+  size_t total = mb + pb + pb + cpb + ppb;
+  for (int k = 0; k < 2; ++k) {
+    const ChangaListRequest* r = reqs[k];
+    const long long ne = r ? r->n_entries : 0;
+    const int nb = r ? r->n_buckets : 0;
     sz[k][0] = (size_t)ne * sizeof(ILCell);
     sz[k][1] = (size_t)(nb + 1) * sizeof(int);
     sz[k][2] = (size_t)nb * sizeof(int);
@@ -810,38 +869,112 @@ int changa_gravity_step_host(int form, const double* moments, long long n_moment
       total += align256(sz[k][j]);
     }
   }
+  const size_t qoff = total;
+  total += 256;
   char* block = nullptr;
   CHG_CUDA(cudaMallocAsync((void**)&block, total, s));
   double* d_mom = (double*)block;
   double* d_parts = (double*)(block + mb);
   double* d_vars = (double*)(block + mb + pb);
-  CHG_CUDA(cudaMemcpyAsync(d_mom, moments, (size_t)n_moments * 12 * sizeof(double),
-                           cudaMemcpyHostToDevice, s));
-  CHG_CUDA(cudaMemcpyAsync(d_parts, parts, (size_t)n_parts * 5 * sizeof(double),
-                           cudaMemcpyHostToDevice, s));
-  CHG_CUDA(cudaMemcpyAsync(d_vars, vars, (size_t)n_parts * 5 * sizeof(double),
-                           cudaMemcpyHostToDevice, s));
-  ChangaListRequest dreq[2];
-  for (int k = 0; k < 2; ++k) {
-    const ChangaListRequest* r = reqs[k];
-    dreq[k].list = (const ILCell*)(block + off[k][0]);
-    dreq[k].markers = (const int*)(block + off[k][1]);
-    dreq[k].starts = (const int*)(block + off[k][2]);
-    dreq[k].sizes = (const int*)(block + off[k][3]);
-    dreq[k].n_buckets = r ? r->n_buckets : 0;
-    dreq[k].n_entries = r ? r->n_entries : 0;
-    if (!r || r->n_buckets == 0) continue;
-    const void* src[4] = {r->list, r->markers, r->starts, r->sizes};
-    for (int j = 0; j < 4; ++j)
-      if (sz[k][j]) CHG_CUDA(cudaMemcpyAsync(block + off[k][j], src[j], sz[k][j], cudaMemcpyHostToDevice, s));
-  }
-  int rc = changa_gravity_step(form, d_mom, n_moments, d_parts, n_parts, cells ? &dreq[0] : nullptr,
-                               plist ? &dreq[1] : nullptr, fperiod, ewald, d_vars, s);
+  float4* pc = (float4*)(block + mb + 2 * pb);
+  float4* pp = (float4*)(block + mb + 2 * pb + cpb);
+  unsigned int* q = (unsigned int*)(block + qoff);
+
+  std::vector<cudaEvent_t> evs;
+  auto event = [&](cudaStream_t on) -> cudaEvent_t {
+    cudaEvent_t e = nullptr;
+    if (cudaEventCreateWithFlags(&e, cudaEventDisableTiming) != cudaSuccess) return nullptr;
+    evs.push_back(e);
+    if (cudaEventRecord(e, on) != cudaSuccess) return nullptr;
+    return e;
+  };
+  int rc = 0;
+  cudaError_t e = cudaSuccess;
+  do {
+    cudaEvent_t ready = event(s);  // the block is allocated on s
+    if (!ready || (e = cudaStreamWaitEvent(c, ready, 0)) != cudaSuccess) break;
+    /* small arrays first */
+    if ((e = cudaMemcpyAsync(d_mom, moments, (size_t)n_moments * 12 * sizeof(double),
+                             cudaMemcpyHostToDevice, c)) != cudaSuccess ||
+        (e = cudaMemcpyAsync(d_parts, parts, (size_t)n_parts * 5 * sizeof(double),
+                             cudaMemcpyHostToDevice, c)) != cudaSuccess)
+      break;
+    if (!overwrite && (e = cudaMemcpyAsync(d_vars, vars, (size_t)n_parts * 5 * sizeof(double),
+                                           cudaMemcpyHostToDevice, c)) != cudaSuccess)
+      break;
+    for (int k = 0; k < 2 && e == cudaSuccess; ++k) {
+      const ChangaListRequest* r = reqs[k];
+      if (!r || r->n_buckets == 0) continue;
+      const void* src[3] = {r->markers, r->starts, r->sizes};
+      for (int j = 1; j < 4 && e == cudaSuccess; ++j)
+        e = cudaMemcpyAsync(block + off[k][j], src[j - 1], sz[k][j], cudaMemcpyHostToDevice, c);
+    }
+    if (e != cudaSuccess) break;
+    cudaEvent_t small = event(c);
+    /* the lists, chunk by chunk */
+    std::vector<cudaEvent_t> landed[2];
+    for (int k = 0; k < 2 && e == cudaSuccess; ++k) {
+      const ChangaListRequest* r = reqs[k];
+      for (auto& ch : chunks[k]) {
+        const size_t e0 = (size_t)r->markers[ch.first], e1 = (size_t)r->markers[ch.second];
+        if (e1 > e0 &&
+            (e = cudaMemcpyAsync(block + off[k][0] + e0 * sizeof(ILCell), r->list + e0,
+                                 (e1 - e0) * sizeof(ILCell), cudaMemcpyHostToDevice, c)) !=
+                cudaSuccess)
+          break;
+        landed[k].push_back(event(c));
+      }
+    }
+    if (e != cudaSuccess || !small) break;
+    /* compute stream */
+    if ((e = cudaStreamWaitEvent(s, small, 0)) != cudaSuccess) break;
+    if (overwrite && (e = cudaMemsetAsync(d_vars, 0, (size_t)n_parts * 5 * sizeof(double), s)) !=
+                         cudaSuccess)
+      break;
+    const void* ksrc = d_mom;
+    const void* kpart = d_parts;
+    if (f == kMix) {
+      if ((e = launch_pack_cells(d_mom, n_moments, pc, s)) != cudaSuccess ||
+          (e = launch_pack_parts(d_parts, n_parts, pp, s)) != cudaSuccess)
+        break;
+      ksrc = pc;
+      kpart = pp;
+    }
+    if (ewald && (e = launch_ewald_fp(f, d_parts, n_parts, nullptr, n_parts, *ewald, d_vars, s)) !=
+                     cudaSuccess)
+      break;
+    for (int k = 0; k < 2 && !rc && e == cudaSuccess; ++k) {
+      const ChangaListRequest* r = reqs[k];
+      for (size_t i = 0; i < chunks[k].size() && !rc; ++i) {
+        if (!landed[k][i] || (e = cudaStreamWaitEvent(s, landed[k][i], 0)) != cudaSuccess) break;
+        const int b0 = chunks[k][i].first, b1 = chunks[k][i].second;
+        ChangaListRequest sub;
+        sub.list = (const ILCell*)(block + off[k][0]);
+        sub.markers = (const int*)(block + off[k][1]) + b0;
+        sub.starts = (const int*)(block + off[k][2]) + b0;
+        sub.sizes = (const int*)(block + off[k][3]) + b0;
+        sub.n_buckets = b1 - b0;
+        sub.n_entries = r->markers[b1];
+        rc = k == 0 ? run_fp(f, true, ksrc, n_moments, kpart, n_parts, &sub, fperiod, d_vars, s, q)
+                    : run_fp(f, false, kpart, n_parts, kpart, n_parts, &sub, fperiod, d_vars, s,
+                             q + 32);
+      }
+    }
+    if (rc || e != cudaSuccess) break;
+    e = cudaMemcpyAsync(vars, d_vars, (size_t)n_parts * 5 * sizeof(double), cudaMemcpyDeviceToHost,
+                        s);
+  } while (0);
+  /* the copy stream must be idle before the block goes back to the pool */
+  cudaEvent_t copies_done = event(c);
+  if (copies_done) cudaStreamWaitEvent(s, copies_done, 0);
+  cudaError_t ef = cudaFreeAsync(block, s);
+  cudaError_t es = cudaStreamSynchronize(s);
+  for (cudaEvent_t ev : evs)
+    if (ev) cudaEventDestroy(ev);
   if (rc) return rc;
-  CHG_CUDA(cudaMemcpyAsync(vars, d_vars, (size_t)n_parts * 5 * sizeof(double),
-                           cudaMemcpyDeviceToHost, s));
-  CHG_CUDA(cudaFreeAsync(block, s));
-  CHG_CUDA(cudaStreamSynchronize(s));
+  if (e == cudaSuccess) e = ef;
+  if (e == cudaSuccess) e = es;
+  if (e != cudaSuccess) return record_error((int)e, "gravity_step_host", __FILE__, __LINE__);
   return 0;
 }
 

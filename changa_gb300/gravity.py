@@ -110,14 +110,16 @@ def _host_req(req):
 
 
 def gravity_step_host(lists, form="mixed", ewald: EwaldConfig | None = None, stream=None,
-                      vars=None):
-    """One force evaluation from host arrays; returns vars (N x 5 FP64)."""
+                      vars=None, overwrite=False):
+    """One force evaluation from host arrays; returns vars (N x 5 FP64).
+    Results accumulate into vars unless overwrite (then vars is not read)."""
     lib = N.cuda_lib()
     if vars is None:
-        vars = np.zeros((lists.n, 5))
+        vars = np.empty((lists.n, 5)) if overwrite else np.zeros((lists.n, 5))
     cr, pr = _host_req(lists.cells), _host_req(lists.plist)
     ep = ewald.params(lists.root) if ewald else None
-    rc = lib.changa_gravity_step_host(FORMS[form], _p(lists.moments), lists.moments.shape[0],
+    f = FORMS[form] | (N.CHANGA_STEP_OVERWRITE if overwrite else 0)
+    rc = lib.changa_gravity_step_host(f, _p(lists.moments), lists.moments.shape[0],
                                       _p(lists.parts), lists.n, C.byref(cr), C.byref(pr),
                                       float(lists.period), C.byref(ep) if ep else None, _p(vars),
                                       stream)

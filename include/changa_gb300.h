@@ -159,9 +159,17 @@ int changa_gravity_step(int form, const double *moments, long long n_moments,
 
 /* The same evaluation from HOST arrays: the requests' pointers, moments,
  * parts and the ewt table are host memory (pinned memory copies fastest).
- * Uploads everything on `stream`, runs changa_gravity_step, ACCUMULATES the
- * results into vars (host, n_parts x 5) and returns after the stream has
- * finished, so vars is ready on return. */
+ * The interaction lists are uploaded in chunks on a library-owned copy
+ * stream while the list kernels run on `stream` over the chunks already
+ * landed.  Results ACCUMULATE into vars (host, n_parts x 5); with
+ * form | CHANGA_STEP_OVERWRITE they replace it instead (vars is not read,
+ * so a fresh evaluation needs no zeroed host buffer).  Returns after the
+ * work has finished, so vars is ready on return. */
+#define CHANGA_STEP_OVERWRITE 0x100
+
+/* List bytes per upload chunk of changa_gravity_step_host (default 512 MiB,
+ * at least 4 KiB). */
+void changa_gb300_set_host_chunk_bytes(size_t bytes);
 int changa_gravity_step_host(int form, const double *moments, long long n_moments,
                              const double *parts, long long n_parts,
                              const ChangaListRequest *cells, const ChangaListRequest *plist,
