@@ -577,10 +577,11 @@ __device__ __noinline__ float2 spline_near_f(float r, float dir, float twoh) {
  * (the register cap) x GROUP source chunks per reduction (the list tile). */
 struct Variant {
   int minb, group;
-  bool tp;  // target-parallel kernel (list_kernel_tp); group unused
+  int tp;  // 0 source-parallel, 1 target-parallel (list_kernel_tp), 2 paired (list_kernel_tp2)
 };
-constexpr Variant kVariants[] = {{2, 16, false}, {3, 16, false}, {4, 16, false}, {3, 32, false},
-                                 {2, 32, false}, {2, 0, true},   {3, 0, true},   {4, 0, true}};
+constexpr Variant kVariants[] = {{2, 16, 0}, {3, 16, 0}, {4, 16, 0}, {3, 32, 0}, {2, 32, 0},
+                                 {2, 0, 1},  {3, 0, 1},  {4, 0, 1},  {2, 0, 2},  {3, 0, 2},
+                                 {4, 0, 2}};
 constexpr int kNumVariants = sizeof(kVariants) / sizeof(kVariants[0]);
 
 /* Source-parallel list kernel of the FP32 forms.  Per warp and bucket: the
@@ -1097,6 +1098,309 @@ __global__ void __launch_bounds__(kThreads, MINB) list_kernel_tp(const ListArgs 
   }
 }
 
+/* ------------------------------------------------------------------ */
+/* Paired target-parallel kernel: list_kernel_tp with the FP32 math of  */
+/* two staged sources in one packed instruction (add/mul/fma .f32x2).  */
+/* The list kernels are issue-bound; packed ops issue half as many     */
+/* instructions for the same FMA-pipe work.  Staged records are laid   */
+/* out in pairs ({x0, x1, y0, y1} ...) so each 128-bit shared load     */
+/* yields two ready operand pairs.                                     */
+/* ------------------------------------------------------------------ */
+
+typedef unsigned long long f2;
+
+__device__ __forceinline__ f2 pk2(float a, float b) {
+  f2 r;
+  asm("mov.b64 %0, {%1, %2};" : "=l"(r) : "f"(a), "f"(b));
+  return r;
+}
+__device__ __forceinline__ void up2(f2 v, float& a, float& b) {
+  asm("mov.b64 {%0, %1}, %2;" : "=f"(a), "=f"(b) : "l"(v));
+}
+__device__ __forceinline__ f2 add2(f2 a, f2 b) {
+  f2 r;
+  asm("add.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(a), "l"(b));
+  return r;
+}
+__device__ __forceinline__ f2 sub2(f2 a, f2 b) {
+  f2 r;
+  asm("sub.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(a), "l"(b));
+  return r;
+}
+__device__ __forceinline__ f2 mul2(f2 a, f2 b) {
+  f2 r;
+  asm("mul.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(a), "l"(b));
+  return r;
+}
+__device__ __forceinline__ f2 fma2(f2 a, f2 b, f2 c) {
+  f2 r;
+  asm("fma.rn.f32x2 %0, %1, %2, %3;" : "=l"(r) : "l"(a), "l"(b), "l"(c));
+  return r;
+}
+
+/* float index of field f of pair half h inside a pair block */
+__device__ __forceinline__ int pair_slot(int f, int h) { return 4 * (f >> 1) + 2 * (f & 1) + h; }
+
+template <int FORM, bool CELL, int MINB>
+__global__ void __launch_bounds__(kThreads, MINB) list_kernel_tp2(const ListArgs a) {
+  static_assert(FORM != kF64, "FP32 arithmetic forms only");
+  constexpr int NF = CELL ? 12 : 4;  // fields: x y z m [xx xy xz yy yz zz tr soft]
+  constexpr int PW = NF / 2;         // float4 words per pair
+  __shared__ __align__(16) float4 stage[kWarps][2][16 * PW];
+  __shared__ float ssoft[kWarps][2][32];
+  __shared__ double red[kWarps][5][32];
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+
+  for (;;) {
+    int b = 0;
+    if (lane == 0) b = (int)atomicAdd(a.queue, 1u);
+    b = __shfl_sync(kFull, b, 0);
+    if (b >= a.n_buckets) break;
+    const int e_begin = max(__ldg(a.markers + b), 0);
+    const int e_end = (int)min((long long)__ldg(a.markers + b + 1), a.n_entries);  // memory safety
+    const long long tbase = __ldg(a.starts + b);
+    const int n = __ldg(a.sizes + b);
+    if (n <= 0 || tbase < 0 || tbase + n > a.n_tgt) continue;  // memory safety
+
+    float3 chi = make_float3(0.f, 0.f, 0.f), clo = chi;
+    if constexpr (FORM == kMix) {
+      const float4* tp = static_cast<const float4*>(a.tgt) + kPartPackF4 * tbase;
+      const float4 h = __ldg(tp), l = __ldg(tp + 1);
+      chi = make_float3(h.x, h.y, h.z);
+      clo = make_float3(l.x, l.y, l.z);
+    }
+
+    for (int t0 = 0; t0 < n; t0 += 32) {
+      const int nt = min(32, n - t0);
+      const int G = 32 / nt;
+      const int g = lane / nt;
+      const int t = lane - g * nt;
+      const bool active = g < G;
+      const long long ti = tbase + t0 + t;
+
+      float tx, ty, tz, tsoft, tmass;
+      if constexpr (FORM == kF32) {
+        const CompactPartData* p = static_cast<const CompactPartData*>(a.tgt) + ti;
+        tmass = __ldg(&p->mass);
+        tsoft = __ldg(&p->soft);
+        tx = __ldg(&p->position.x);
+        ty = __ldg(&p->position.y);
+        tz = __ldg(&p->position.z);
+      } else {
+        const float4* p = static_cast<const float4*>(a.tgt) + kPartPackF4 * ti;
+        const float4 h = __ldg(p), l = __ldg(p + 1);
+        tx = (h.x - chi.x) + (l.x - clo.x);
+        ty = (h.y - chi.y) + (l.y - clo.y);
+        tz = (h.z - chi.z) + (l.z - clo.z);
+        tmass = h.w;
+        tsoft = l.w;
+      }
+      const float tsmax = warp_max(active ? tsoft : 0.f);
+      const f2 tx2 = pk2(tx, tx), ty2 = pk2(ty, ty), tz2 = pk2(tz, tz), tm2 = pk2(tmass, tmass);
+
+      float sx = 0.f, sy = 0.f, sz = 0.f, sp = 0.f, idt2 = 0.f;
+      float cx = 0.f, cy = 0.f, cz = 0.f, cp = 0.f;
+
+      RawRec<FORM, CELL> raw;
+      gather_raw<FORM, CELL>(a, e_begin + lane, e_end, raw);
+      int buf = 0;
+      for (int e0 = e_begin; e0 < e_end; e0 += 32, buf ^= 1) {
+        const int ne = min(32, e_end - e0);
+        float4 rec[3];
+        const float ls = finish_raw<FORM, CELL>(a, raw, lane < ne, chi, clo, rec);
+        {
+          /* this lane's record into its half of pair lane/2 */
+          float* pb = reinterpret_cast<float*>(stage[warp][buf] + (lane >> 1) * PW);
+          const int h = lane & 1;
+          pb[pair_slot(0, h)] = rec[0].x;
+          pb[pair_slot(1, h)] = rec[0].y;
+          pb[pair_slot(2, h)] = rec[0].z;
+          pb[pair_slot(3, h)] = rec[0].w;
+          if constexpr (CELL) {
+            // rec[1] {xx, xy, xz, yy}  rec[2] {yz, zz, tr, soft}
+            pb[pair_slot(4, h)] = rec[1].x;
+            pb[pair_slot(5, h)] = rec[1].y;
+            pb[pair_slot(6, h)] = rec[1].z;
+            pb[pair_slot(7, h)] = rec[1].w;
+            pb[pair_slot(8, h)] = rec[2].x;
+            pb[pair_slot(9, h)] = rec[2].y;
+            pb[pair_slot(10, h)] = rec[2].z;
+            pb[pair_slot(11, h)] = rec[2].w;
+          }
+        }
+        ssoft[warp][buf][lane] = ls;
+        const float ss = warp_max(ls) + tsmax;
+        const float near2 = ss * ss;
+        __syncwarp();
+        if (e0 + 32 < e_end) gather_raw<FORM, CELL>(a, e0 + 32 + lane, e_end, raw);
+        const float4* st = stage[warp][buf];
+        f2 ax2 = 0ull, ay2 = 0ull, az2 = 0ull, pot2 = 0ull;  // +0.0f in both halves
+        /* one staged pair on this lane's target */
+        auto body = [&](int p) {
+          const float4 w0 = st[p * PW], w1 = st[p * PW + 1];
+          const f2 px = pk2(w0.x, w0.y), py = pk2(w0.z, w0.w), pz = pk2(w1.x, w1.y),
+                   pm = pk2(w1.z, w1.w);
+          if constexpr (CELL) {
+            /* gravity.h:436-472: r = target - cell */
+            const float4 w2 = st[p * PW + 2], w3 = st[p * PW + 3], w4 = st[p * PW + 4],
+                         w5 = st[p * PW + 5];
+            const f2 xx = pk2(w2.x, w2.y), xy = pk2(w2.z, w2.w), xz = pk2(w3.x, w3.y),
+                     yy = pk2(w3.z, w3.w), yz = pk2(w4.x, w4.y), zz = pk2(w4.z, w4.w),
+                     tr = pk2(w5.x, w5.y);
+            const f2 rx = sub2(tx2, px), ry = sub2(ty2, py), rz = sub2(tz2, pz);
+            const f2 rsq = fma2(rx, rx, fma2(ry, ry, mul2(rz, rz)));
+            float q0, q1;
+            up2(rsq, q0, q1);
+            const f2 dir = pk2(rsqrt_ftz(q0), rsqrt_ftz(q1));
+            const f2 dir2 = mul2(dir, dir);
+            f2 av = dir, bv = mul2(dir2, dir);
+            f2 cv = mul2(bv, mul2(dir2, pk2(3.f, 3.f)));
+            f2 dv = mul2(cv, mul2(dir2, pk2(5.f, 5.f)));
+            if (q0 <= near2 || q1 <= near2) {
+              float a_[2], b_[2], c_[2], d_[2], r_[2] = {q0, q1}, s_[2] = {w5.z, w5.w};
+              up2(av, a_[0], a_[1]);
+              up2(bv, b_[0], b_[1]);
+              up2(cv, c_[0], c_[1]);
+              up2(dv, d_[0], d_[1]);
+#pragma unroll
+              for (int h = 0; h < 2; ++h) {
+                if (r_[h] > near2) continue;
+                const float twoh = s_[h] + tsoft;
+                if (r_[h] == 0.f) {
+                  a_[h] = b_[h] = c_[h] = d_[h] = 0.f;
+                } else if (r_[h] < twoh * twoh) {
+                  const float4 kk = splineq_near_f(a_[h], r_[h], twoh);
+                  a_[h] = kk.x;
+                  b_[h] = kk.y;
+                  c_[h] = kk.z;
+                  d_[h] = kk.w;
+                }
+              }
+              av = pk2(a_[0], a_[1]);
+              bv = pk2(b_[0], b_[1]);
+              cv = pk2(c_[0], c_[1]);
+              dv = pk2(d_[0], d_[1]);
+            }
+            const f2 qirx = fma2(xx, rx, fma2(xy, ry, mul2(xz, rz)));
+            const f2 qiry = fma2(xy, rx, fma2(yy, ry, mul2(yz, rz)));
+            const f2 qirz = fma2(xz, rx, fma2(yz, ry, mul2(zz, rz)));
+            const f2 qir = mul2(pk2(0.5f, 0.5f), fma2(qirx, rx, fma2(qiry, ry, mul2(qirz, rz))));
+            const f2 bM = mul2(bv, pm);
+            const f2 qir3 = fma2(dv, qir, sub2(bM, mul2(cv, tr)));
+            /* pot -= M a + c qir - b tr: accumulated with the opposite sign */
+            pot2 = add2(pot2, sub2(fma2(cv, qir, mul2(pm, av)), mul2(bv, tr)));
+            /* a -= qir3 r - c Q r */
+            ax2 = fma2(cv, qirx, sub2(ax2, mul2(qir3, rx)));
+            ay2 = fma2(cv, qiry, sub2(ay2, mul2(qir3, ry)));
+            az2 = fma2(cv, qirz, sub2(az2, mul2(qir3, rz)));
+            float d0, d1;
+            up2(fma2(tm2, bv, bM), d0, d1);
+            idt2 = fmaxf(idt2, fmaxf(d0, d1));
+          } else {
+            /* gravity.h:276-301: r = source - target */
+            const f2 rx = sub2(px, tx2), ry = sub2(py, ty2), rz = sub2(pz, tz2);
+            const f2 rsq = fma2(rx, rx, fma2(ry, ry, mul2(rz, rz)));
+            float q0, q1;
+            up2(rsq, q0, q1);
+            const f2 dir = pk2(rsqrt_ftz(q0), rsqrt_ftz(q1));
+            f2 av = dir, bv = mul2(mul2(dir, dir), dir);
+            if (q0 <= near2 || q1 <= near2) {
+              float a_[2], b_[2], r_[2] = {q0, q1};
+              up2(av, a_[0], a_[1]);
+              up2(bv, b_[0], b_[1]);
+#pragma unroll
+              for (int h = 0; h < 2; ++h) {
+                if (r_[h] > near2) continue;
+                const float twoh = ssoft[warp][buf][2 * p + h] + tsoft;
+                if (r_[h] == 0.f) {
+                  a_[h] = b_[h] = 0.f;
+                } else {
+                  const float r1 = r_[h] * a_[h];
+                  if (r1 < twoh) {
+                    const float2 kk = spline_near_f(r1, a_[h], twoh);
+                    a_[h] = kk.x;
+                    b_[h] = kk.y;
+                  }
+                }
+              }
+              av = pk2(a_[0], a_[1]);
+              bv = pk2(b_[0], b_[1]);
+            }
+            const f2 bm = mul2(bv, pm);
+            pot2 = fma2(pm, av, pot2);  // opposite sign, negated at the fold
+            ax2 = fma2(rx, bm, ax2);
+            ay2 = fma2(ry, bm, ay2);
+            az2 = fma2(rz, bm, az2);
+            float d0, d1;
+            up2(fma2(tm2, bv, bm), d0, d1);
+            idt2 = fmaxf(idt2, fmaxf(d0, d1));
+          }
+        };
+        if (G == 1) {
+#pragma unroll 4
+          for (int p = 0; p < 16; ++p) body(p);
+        } else if (active) {
+#pragma unroll 2
+          for (int p = g; p < 16; p += G) body(p);
+        }
+        float x0, x1, y0, y1, z0, z1, p0, p1;
+        up2(ax2, x0, x1);
+        up2(ay2, y0, y1);
+        up2(az2, z0, z1);
+        up2(pot2, p0, p1);
+        if constexpr (FORM == kMix) {
+          kahan_add(sx, cx, x0 + x1);
+          kahan_add(sy, cy, y0 + y1);
+          kahan_add(sz, cz, z0 + z1);
+          kahan_add(sp, cp, -(p0 + p1));
+        } else {
+          sx += x0 + x1;
+          sy += y0 + y1;
+          sz += z0 + z1;
+          sp -= p0 + p1;
+        }
+      }
+
+      if (active) {
+        red[warp][0][lane] = (double)sx - (double)cx;
+        red[warp][1][lane] = (double)sy - (double)cy;
+        red[warp][2][lane] = (double)sz - (double)cz;
+        red[warp][3][lane] = (double)sp - (double)cp;
+        red[warp][4][lane] = (double)idt2;
+      }
+      __syncwarp();
+      if (lane < nt) {
+        double rx = 0, ry = 0, rz = 0, rp = 0, ri = 0;
+        for (int gg = 0; gg < G; ++gg) {
+          const int l = gg * nt + lane;
+          rx += red[warp][0][l];
+          ry += red[warp][1][l];
+          rz += red[warp][2][l];
+          rp += red[warp][3][l];
+          ri = fmax(ri, red[warp][4][l]);
+        }
+        const long long to = tbase + t0 + lane;
+        if constexpr (FORM == kF32) {
+          VariablePartData* v = static_cast<VariablePartData*>(a.vars) + to;
+          v->a.x += (float)rx;
+          v->a.y += (float)ry;
+          v->a.z += (float)rz;
+          v->potential += (float)rp;
+          v->dtGrav = fmaxf((float)ri, v->dtGrav);
+        } else {
+          double* v = static_cast<double*>(a.vars) + 5 * to;
+          v[0] += rx;
+          v[1] += ry;
+          v[2] += rz;
+          v[3] += rp;
+          v[4] = fmax(ri, v[4]);
+        }
+      }
+      __syncwarp();
+    }
+  }
+}
+
 __global__ void pack_cells_kernel(const double* __restrict__ m, long long n, float4* __restrict__ out) {
   for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
        i += (long long)gridDim.x * blockDim.x) {
@@ -1124,8 +1428,9 @@ __global__ void pack_parts_kernel(const double* __restrict__ p, long long n, flo
 }
 
 /* The FP64 form runs list_kernel (its cost is the FP64 pipe); the FP32
- * forms run one of the variants below, target-parallel by default (the
- * fastest on every measured workload), source-parallel on request. */
+ * forms run one of the variants below: paired target-parallel by default
+ * (the fastest on the measured workloads), the others on request or by the
+ * autotuner. */
 template <typename K>
 int blocks_per_sm(K kernel, int* cache) {
   if (!*cache) {
@@ -1151,13 +1456,16 @@ cudaError_t launch_kernel(K kernel, int* occ_cache, int kid, const ListArgs& a, 
 }
 
 /* current variant per list kernel id (FP32 forms) */
-int g_variant[6] = {6, 7, 0, 0, 6, 7};
+int g_variant[6] = {8, 9, 0, 0, 8, 9};
 
 template <int FORM, bool CELL, int V>
 cudaError_t launch_variant(const ListArgs& a, cudaStream_t s) {
   static int occ = 0;
   constexpr Variant var = kVariants[V];
-  if constexpr (var.tp)
+  if constexpr (var.tp == 2)
+    return launch_kernel(list_kernel_tp2<FORM, CELL, var.minb>, &occ, list_kernel_id(FORM, CELL),
+                         a, s);
+  else if constexpr (var.tp == 1)
     return launch_kernel(list_kernel_tp<FORM, CELL, var.minb>, &occ, list_kernel_id(FORM, CELL),
                          a, s);
   else

@@ -77,8 +77,11 @@ void changa_gb300_set_timing(int on);
 int changa_gb300_kernel_time(int kernel, double *total_ms, long long *launches);
 
 /* Shape variants of the FP32-form list kernels (kernel ids 0, 1, 4, 5):
- * resident blocks per SM x list entries per reduction tile.  The autotuner
- * (changa_gb300/autotune.py) times them on a workload and selects one. */
+ * 0-4 source-parallel (resident blocks per SM x list chunks per reduction),
+ * 5-7 target-parallel (2/3/4 blocks per SM), 8-10 target-parallel with
+ * paired .f32x2 arithmetic (2/3/4 blocks per SM; defaults 8 for cell lists,
+ * 9 for particle lists).  The autotuner (changa_gb300/autotune.py) times
+ * them on a workload and selects one per kernel. */
 int changa_gb300_list_variant_count(void);
 int changa_gb300_set_list_variant(int kernel, int variant);
 int changa_gb300_get_list_variant(int kernel);
