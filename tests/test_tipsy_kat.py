@@ -1,0 +1,43 @@
+"""Tipsy reader, and the reference's own known answer for its test model
+(teststep/king_soft.bin, the 36000-particle King model; teststep/
+pkdtest.log line 36 gives T = 32.65580 and U = -64.84776 at t = 0 from
+PKDGRAV with hexadecapole moments, nBucket 8, theta 0.7, open boundaries).
+T checks the reader exactly; U is a loose check of the quadrupole tree and
+the oracle's force arithmetic on real data.  The model file is only read
+where the reference tree exists."""
+import os
+
+import numpy as np
+import pytest
+
+from changa_gb300 import tipsy
+
+KING = "/root/reference/teststep/king_soft.bin"
+
+
+def test_roundtrip(tmp_path):
+    rng = np.random.default_rng(0)
+    n = 100
+    pos, vel = rng.normal(size=(n, 3)), rng.normal(size=(n, 3))
+    mass, soft = rng.uniform(1, 2, n) / n, np.full(n, 0.01)
+    p = tmp_path / "t.bin"
+    tipsy.write(str(p), pos, vel, mass, soft, time=0.5)
+    d = tipsy.read(str(p))
+    assert d["n"] == n and d["ndark"] == n and d["time"] == 0.5
+    np.testing.assert_allclose(d["pos"], pos.astype(np.float32), rtol=0, atol=0)
+    np.testing.assert_allclose(d["soft"], np.float32(0.01))
+
+
+@pytest.mark.skipif(not os.path.exists(KING), reason="reference test data not present")
+def test_king_model_energies(built):
+    import oracle
+    from changa_gb300 import tree
+    d = tipsy.read(KING)
+    assert d["n"] == 36000 and d["ndark"] == 36000
+    T = 0.5 * (d["mass"] * (d["vel"] ** 2).sum(1)).sum()
+    assert abs(T / 32.65580 - 1) < 2e-6, T
+    L = tree.build_lists(d["pos"], d["mass"], d["soft"], n_bucket=8, theta=0.7)
+    v = oracle.cell_forces(L.moments, L.parts, L.cells)
+    v = oracle.part_forces(L.parts, L.parts, L.plist, vars=v)
+    U = 0.5 * (L.parts[:, 0] * v[:, 3]).sum()
+    assert abs(U / -64.84776 - 1) < 2e-4, U  # measured 4.0e-5
