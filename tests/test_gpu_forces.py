@@ -261,3 +261,85 @@ def test_every_list_variant(plummer):
     finally:
         for k, s in zip(ids, saved):
             lib.changa_gb300_set_list_variant(k, s)
+
+
+def test_dropin_remote_resume_and_small_phase(plummer):
+    """The other request paths of the drop-in boundary: remote chunks
+    (DataManagerTransferRemoteChunk + *Remote), resume requests carrying the
+    missed nodes / particles on the host (*RemoteResume), the small-phase
+    particle request and TreePieceDataTransferBasic/Cleanup.  Fed the same
+    moments and particles as the local path, each gives the same result."""
+    L, _, _ = plummer
+    lib = N.cuda_lib()
+    rt = gravity._cudart()
+    inp = gravity.DropInInputs(L)
+    try:
+        ref = gravity.dropin_step(inp).copy()
+        d_m, d_p, d_v = C.c_void_p(), C.c_void_p(), C.c_void_p()
+        r_m, r_p = C.c_void_p(), C.c_void_p()
+
+        def fresh():
+            inp.vars.array[...] = 0
+            lib.DataManagerTransferLocalTree(inp.moments.ptr, inp.moments.nbytes, inp.parts.ptr,
+                                             inp.parts.nbytes, inp.vars.ptr, inp.vars.nbytes,
+                                             C.byref(d_m), C.byref(d_p), C.byref(d_v), None, L.n,
+                                             None)
+
+        def request(k, moments=None, parts=None):
+            lst, mk, st, sz, req = inp.reqs[k]
+            r = N.CudaRequest()
+            r.d_localMoments, r.d_localParts, r.d_localVars = d_m, d_p, d_v
+            r.d_remoteMoments, r.d_remoteParts = moments, parts
+            r.list, r.bucketMarkers, r.bucketStarts, r.bucketSizes = lst.ptr, mk.ptr, st.ptr, sz.ptr
+            r.numInteractions = req.n_entries
+            r.numBucketsPlusOne = req.n_buckets + 1
+            r.fperiod = 0.0
+            return r
+
+        def result():
+            lib.TransferParticleVarsBack(inp.out.ptr, inp.out.nbytes, d_v, None, None)
+            rt.cudaStreamSynchronize(None)
+            return inp.out.array.copy()
+
+        def free_all(*ptrs):
+            for q in ptrs:
+                rt.cudaFree(q)
+
+        # remote chunk: the same moments and particles uploaded as remote data
+        fresh()
+        lib.DataManagerTransferRemoteChunk(inp.moments.ptr, inp.moments.nbytes, inp.parts.ptr,
+                                           inp.parts.nbytes, C.byref(r_m), C.byref(r_p), None, None)
+        lib.TreePieceCellListDataTransferRemote(C.byref(request(0, r_m, r_p)))
+        lib.TreePiecePartListDataTransferRemote(C.byref(request(1, r_m, r_p)))
+        assert np.array_equal(result(), ref)
+        free_all(d_m, d_p, d_v, r_m, r_p)
+
+        # resume: the missed nodes / particles travel with the request
+        fresh()
+        rc = request(0)
+        rc.missedNodes, rc.sMissed = inp.moments.ptr, inp.moments.nbytes
+        lib.TreePieceCellListDataTransferRemoteResume(C.byref(rc))
+        rp = request(1)
+        rp.missedParts, rp.sMissed = inp.parts.ptr, inp.parts.nbytes
+        lib.TreePiecePartListDataTransferRemoteResume(C.byref(rp))
+        assert np.array_equal(result(), ref)
+        free_all(d_m, d_p, d_v)
+
+        # small phase: the source particles passed from the host
+        fresh()
+        lib.TreePieceCellListDataTransferLocal(C.byref(request(0)))
+        lib.TreePiecePartListDataTransferLocalSmallPhase(C.byref(request(1)), inp.parts.ptr, L.n)
+        assert np.array_equal(result(), ref)
+        free_all(d_m, d_p, d_v)
+
+        # Basic + Cleanup upload a request's arrays and release them
+        fresh()
+        ptrs = N.CudaDevPtr()
+        lib.TreePieceDataTransferBasic(C.byref(request(0)), C.byref(ptrs))
+        rt.cudaStreamSynchronize(None)
+        assert ptrs.d_list and ptrs.d_bucketMarkers
+        lib.TreePieceDataTransferBasicCleanup(C.byref(ptrs))
+        rt.cudaStreamSynchronize(None)
+        free_all(d_m, d_p, d_v)
+    finally:
+        inp.free()
