@@ -196,6 +196,9 @@ HOST_SIGNATURES = {
     "chg_tree_drop_lists": (None, [_VP]),
     "chg_tree_get_structure": (None, [_VP, _VP, _VP]),
     "chg_tree_get_ranges": (None, [_VP, _VP, _VP]),
+    "chg_tree_set_order": (_I, [_VP, _I]),
+    "chg_tree_soft_lengths": (None, [_VP, _VP]),
+    "chg_tree_get_moments_hex": (None, [_VP, _VP]),
 }
 
 

@@ -88,6 +88,13 @@ struct Tree {
   // walk output per bucket
   std::vector<std::vector<int>> cell_idx, cell_off, part_idx, part_off;
   std::vector<long> n_cells, n_parts;  // per bucket list lengths
+  /* multipole order of the cell interactions: 2 (quadrupole) or 4
+   * (hexadecapole: the walk adds the softening / monopole tests and routes
+   * softened cells to their own per-bucket list) */
+  int order = 2;
+  double theta_mono = 0.0;
+  std::vector<std::vector<int>> soft_idx, soft_off;
+  std::vector<long> n_soft;
 };
 
 /* ---- moments (MultipoleMoments.h:206-352) ---- */
@@ -342,6 +349,57 @@ static inline int open_criterion(const Tree& t, const Node& g, const Node& local
   return f2 <= r2 ? 1 : -1;
 }
 
+/* openSoftening, gravity.h:252-260: the cell's softening sphere (twice its
+ * softening, at cm + offset) meets the bucket's softening sphere or box. */
+static inline bool open_softening(const Tree& t, const Node& g, const Node& local, int off) {
+  double o[3];
+  decode(off, t.period, o);
+  const double c[3] = {g.mom[3] + o[0], g.mom[4] + o[1], g.mom[5] + o[2]};
+  const double r = 2.0 * g.mom[1];
+  double dx = c[0] - local.mom[3], dy = c[1] - local.mom[4], dz = c[2] - local.mom[5];
+  const double rr = r + 2.0 * local.mom[1];
+  if (dx * dx + dy * dy + dz * dz <= rr * rr) return true;
+  const double* b = local.bbox;
+  double d2 = 0.0, d;
+  for (int k = 0; k < 3; ++k) {
+    if ((d = b[k] - c[k]) > 0) d2 += d * d;
+    else if ((d = c[k] - b[3 + k]) > 0) d2 += d * d;
+  }
+  return d2 <= r * r;
+}
+
+/* Hexadecapole form of openCriterionNode (gravity.h:664-722): a
+ * well-separated cell whose softening overlaps the local node is opened
+ * unless it also passes the monopole angle theta_mono. */
+static inline int open_criterion_hex(const Tree& t, const Node& g, const Node& local, int off) {
+  if (g.count <= 6) return 1;
+  double radius = kOpenGeom * g.mom[0] / t.theta;
+  if (radius < g.mom[0]) radius = g.mom[0];
+  double o[3];
+  decode(off, t.period, o);
+  const double c[3] = {g.mom[3] + o[0], g.mom[4] + o[1], g.mom[5] + o[2]};
+  const double* b = local.bbox;
+  double d2 = 0.0, d;
+  for (int k = 0; k < 3; ++k) {
+    if ((d = b[k] - c[k]) > 0) d2 += d * d;
+    else if ((d = c[k] - b[3 + k]) > 0) d2 += d * d;
+  }
+  if (d2 <= radius * radius) {
+    if (local.type == T_BUCKET) return 1;
+    double f2 = 0.0;
+    for (int k = 0; k < 3; ++k) {
+      double a1 = c[k] - b[k], a2 = b[3 + k] - c[k];
+      a1 *= a1;
+      a2 *= a2;
+      f2 += a1 > a2 ? a1 : a2;
+    }
+    return f2 <= radius * radius ? 1 : -1;
+  }
+  if (!open_softening(t, g, local, off)) return 0;
+  const double rm = kOpenGeom * g.mom[0] / t.theta_mono;
+  return d2 <= rm * rm ? 1 : 0;
+}
+
 struct LevelLists {
   std::vector<Entry> clist, plist, und;
 };
@@ -368,12 +426,21 @@ static void emit(WalkCtx& w, int local, int level) {
     co.reserve(nc);
     pi.reserve(np);
     po.reserve(np);
+    const Node& bn = t.nodes[t.bucket_nodes[b]];
     for (int l = 0; l <= level; ++l) {
       for (const Entry& e : w.lv[l].clist) {
-        ci.push_back(t.nodes[e.node].bfs);
         /* reqID = reEncodeOffset(bucket, offset) (TreeWalk.cpp:336); the low
          * 22 bits carry the walking bucket, the kernels read only bits 22+ */
-        co.push_back((e.off << 22) | (ln.first_bucket & 0x3fffff));
+        const int code = (e.off << 22) | (ln.first_bucket & 0x3fffff);
+        if (t.order == 4 && open_softening(t, t.nodes[e.node], bn, e.off)) {
+          /* nodeBucketForce evaluates these as softened point masses
+           * (gravity.h:414-421, Compute.cpp:1683-1698) */
+          t.soft_idx[b].push_back(t.nodes[e.node].bfs);
+          t.soft_off[b].push_back(code);
+          continue;
+        }
+        ci.push_back(t.nodes[e.node].bfs);
+        co.push_back(code);
       }
       for (const Entry& e : w.lv[l].plist) {
         const Node& src = t.nodes[e.node];
@@ -385,6 +452,7 @@ static void emit(WalkCtx& w, int local, int level) {
     }
     t.n_cells[b] = (long)ci.size();
     t.n_parts[b] = (long)pi.size();
+    if (t.order == 4) t.n_soft[b] = (long)t.soft_idx[b].size();
   }
 }
 
@@ -392,7 +460,8 @@ static void process(WalkCtx& w, int local, int level, const Entry& g, std::deque
   Tree& t = *w.t;
   const Node& gn = t.nodes[g.node];
   if (gn.type == T_EMPTY) return;  // DUMP
-  int open = open_criterion(t, gn, t.nodes[local], g.off);
+  int open = t.order == 4 ? open_criterion_hex(t, gn, t.nodes[local], g.off)
+                          : open_criterion(t, gn, t.nodes[local], g.off);
   if (open == 0) {
     w.lv[level].clist.push_back(g);  // COMPUTE
     return;
@@ -618,6 +687,9 @@ int chg_tree_walk(void* h, int nthreads) {
   t->part_off.assign(B, {});
   t->n_cells.assign(B, 0);
   t->n_parts.assign(B, 0);
+  t->soft_idx.assign(t->order == 4 ? B : 0, {});
+  t->soft_off.assign(t->order == 4 ? B : 0, {});
+  t->n_soft.assign(B, 0);
   WalkCtx w;
   w.t = t;
   w.lv.resize(64);
@@ -642,7 +714,94 @@ void chg_tree_list_lengths(void* h, long* n_cells, long* n_parts) {
   if (n_parts) std::memcpy(n_parts, t->n_parts.data(), B * sizeof(long));
 }
 
-/* Serialises one request of kind 0 (cell lists) or 1 (particle lists) for
+/* Adds one particle's reduced (trace-free) scaled moments up to the
+ * hexadecapole to r[21] = {xx xy xz yy yz, xxx xyy xxy yyy xxz yyz xyz,
+ * xxxx xyyy xxxy yyyy xxxz yyyz xxyy xxyz xyyz}, for mass m at (x, y, z)
+ * from the centre of mass in units of the expansion radius: the moments
+ * momEvalFmomrcm consumes (moments.c:772-846 forms the same tensors). */
+static void reduced_moment_add(double* r, double m, double x, double y, double z) {
+  const double x2 = x * x, y2 = y * y, d2 = x2 + y2 + z * z;
+  const double mx2 = m * x2, my2 = m * y2, md2 = m * d2;
+  /* quadrupole: m (r_i r_j - delta_ij d2 / 3), xx and yy stored */
+  const double mxy = m * x * y;
+  r[0] += mx2 - md2 / 3.0;
+  r[1] += mxy;
+  r[2] += m * x * z;
+  r[3] += my2 - md2 / 3.0;
+  r[4] += m * y * z;
+  /* octupole: m (r_i r_j r_k - d2 (delta r) / 5) */
+  const double o = md2 / 5.0;
+  r[5] += (mx2 - 3.0 * o) * x;   // xxx
+  r[6] += (my2 - o) * x;         // xyy
+  r[7] += (mx2 - o) * y;         // xxy
+  r[8] += (my2 - 3.0 * o) * y;   // yyy
+  r[9] += (mx2 - o) * z;         // xxz
+  r[10] += (my2 - o) * z;        // yyz
+  r[11] += mxy * z;              // xyz
+  /* hexadecapole */
+  const double h = md2 / 7.0;
+  const double ax = (mx2 - 3.0 * h) * x, ay = (my2 - 3.0 * h) * y;
+  const double bx = h * (x2 - 0.1 * d2), by = h * (y2 - 0.1 * d2);
+  r[12] += mx2 * x2 - 6.0 * bx;  // xxxx
+  r[13] += ay * x;               // xyyy
+  r[14] += ax * y;               // xxxy
+  r[15] += my2 * y2 - 6.0 * by;  // yyyy
+  r[16] += ax * z;               // xxxz
+  r[17] += ay * z;               // yyyz
+  r[18] += mx2 * y2 - bx - by;   // xxyy
+  r[19] += (mx2 - h) * y * z;    // xxyz
+  r[20] += (my2 - h) * x * z;    // xyyz
+}
+
+/* Hexadecapole moments of every node, breadth-first, 27 doubles each:
+ * {radius, soft, totalMass, cm.xyz, xx xy xz yy yz, xxx xyy xxy yyy xxz yyz
+ * xyz, xxxx xyyy xxxy yyyy xxxz yyyz xxyy xxyz xyyz} (the hexadecapole
+ * CudaMultipoleMoments order, cuda_typedef.h:103-128), the multipole terms
+ * scaled by the node radius.  ChaNGa accumulates them child by child with
+ * shifts and rescales (MultipoleMoments.h:247-262, 318-330, 460-504);
+ * summing each node's particles about its final centre and radius gives
+ * the same tensors. */
+void chg_tree_get_moments_hex(void* h, double* out) {
+  Tree* t = (Tree*)h;
+  const long nm = (long)t->bfs_nodes.size();
+#ifdef _OPENMP
+#pragma omp parallel for schedule(dynamic, 64)
+#endif
+  for (long i = 0; i < nm; ++i) {
+    const Node& nd = t->nodes[t->bfs_nodes[i]];
+    double* o = out + 27 * i;
+    std::memcpy(o, nd.mom, 6 * sizeof(double));
+    double* r = o + 6;
+    for (int k = 0; k < 21; ++k) r[k] = 0.0;
+    const double u = nd.mom[0];
+    if (!(u > 0.0)) continue;
+    const double iu = 1.0 / u;
+    for (int k = nd.first; k < nd.first + nd.count; ++k) {
+      const double* p = &t->pos[3 * (size_t)k];
+      reduced_moment_add(r, t->mass[k], (p[0] - nd.mom[3]) * iu, (p[1] - nd.mom[4]) * iu,
+                         (p[2] - nd.mom[5]) * iu);
+    }
+  }
+}
+
+/* Hexadecapole mode (order 4) or quadrupole (order 2, the default): set
+ * before the walk.  theta_mono = theta^4 (ParallelGravity.cpp:993). */
+int chg_tree_set_order(void* h, int order) {
+  Tree* t = (Tree*)h;
+  if (order != 2 && order != 4) return -1;
+  t->order = order;
+  t->theta_mono = t->theta * t->theta * t->theta * t->theta;
+  return 0;
+}
+
+/* Per-bucket lengths of the softened-cell lists (order 4; zeros else). */
+void chg_tree_soft_lengths(void* h, long* n_soft) {
+  Tree* t = (Tree*)h;
+  std::memcpy(n_soft, t->n_soft.data(), t->bucket_nodes.size() * sizeof(long));
+}
+
+/* Serialises one request of kind 0 (cell lists), 1 (particle lists) or 2
+ * (softened cells of the hexadecapole mode, indices into the moments) for
  * the buckets [b0, b1): list (L x 2 int32), markers (nfilled+1), starts,
  * sizes and the bucket ids (nfilled each).  Only buckets with a non-empty
  * list appear.  Returns nfilled.  index_base is added to every list index
@@ -653,8 +812,11 @@ long chg_tree_serialize(void* h, int kind, long b0, long b1, int* list, int* mar
   long filled = 0;
   long pos = 0;
   for (long b = b0; b < b1; ++b) {
-    const std::vector<int>& ix = kind == 0 ? t->cell_idx[b] : t->part_idx[b];
-    const std::vector<int>& of = kind == 0 ? t->cell_off[b] : t->part_off[b];
+    if (kind == 2 && t->order != 4) break;
+    const std::vector<int>& ix =
+        kind == 0 ? t->cell_idx[b] : (kind == 1 ? t->part_idx[b] : t->soft_idx[b]);
+    const std::vector<int>& of =
+        kind == 0 ? t->cell_off[b] : (kind == 1 ? t->part_off[b] : t->soft_off[b]);
     if (ix.empty()) continue;
     const Node& nd = t->nodes[t->bucket_nodes[b]];
     markers[filled] = (int)pos;

@@ -67,10 +67,15 @@ class TreeLists:
     theta: float
     n_bucket: int
     meta: dict = field(default_factory=dict)
+    order: int = 2
+    softcells: ListRequest | None = None  # order 4: cells evaluated as softened points
 
     @property
     def interactions(self):
-        return self.cells.interactions() + self.plist.interactions()
+        n = self.cells.interactions() + self.plist.interactions()
+        if self.softcells is not None:
+            n += self.softcells.interactions()
+        return n
 
     def abi_moments(self):
         """CudaMultipoleMoments array (M x 12 float32)."""
@@ -96,8 +101,13 @@ def _serialize(lib, h, kind, nb_total, lens):
 
 
 def build_lists(pos, mass, soft, n_bucket=16, theta=0.7, period=0.0, n_replicas=0,
-                nthreads=0) -> TreeLists:
-    """Tree + walk + serialisation for one system (FP64 inputs)."""
+                nthreads=0, order=2) -> TreeLists:
+    """Tree + walk + serialisation for one system (FP64 inputs).  order 2:
+    quadrupole cells (moments M x 12); order 4: hexadecapole cells (moments
+    M x 27, the walk's softening and monopole tests, and the softened cells
+    in their own request, `softcells`, indexing the moments)."""
+    if order not in (2, 4):
+        raise ValueError("order must be 2 or 4")
     lib = host_lib()
     pos = np.ascontiguousarray(pos, dtype=np.float64)
     mass = np.ascontiguousarray(mass, dtype=np.float64)
@@ -115,8 +125,13 @@ def build_lists(pos, mass, soft, n_bucket=16, theta=0.7, period=0.0, n_replicas=
         perm = np.empty(n, dtype=np.int64)
         lib.chg_tree_get_order(h, _ptr(perm))
         nm = lib.chg_tree_num_moments(h)
-        moments = np.empty((nm, 12), dtype=np.float64)
-        lib.chg_tree_get_moments(h, _ptr(moments))
+        if order == 4:
+            lib.chg_tree_set_order(h, 4)
+            moments = np.empty((nm, 27), dtype=np.float64)
+            lib.chg_tree_get_moments_hex(h, _ptr(moments))
+        else:
+            moments = np.empty((nm, 12), dtype=np.float64)
+            lib.chg_tree_get_moments(h, _ptr(moments))
         root = np.empty(12, dtype=np.float64)
         lib.chg_tree_get_root(h, _ptr(root))
         nb = lib.chg_tree_num_buckets(h)
@@ -136,6 +151,11 @@ def build_lists(pos, mass, soft, n_bucket=16, theta=0.7, period=0.0, n_replicas=
         lib.chg_tree_list_lengths(h, _ptr(nc), _ptr(npl))
         cells = _serialize(lib, h, 0, nb, nc)
         plist = _serialize(lib, h, 1, nb, npl)
+        softcells = None
+        if order == 4:
+            ns = np.empty(nb, dtype=np.int64)
+            lib.chg_tree_soft_lengths(h, _ptr(ns))
+            softcells = _serialize(lib, h, 2, nb, ns)
     finally:
         lib.chg_tree_free(h)
     parts = np.empty((n, 5), dtype=np.float64)
@@ -146,7 +166,8 @@ def build_lists(pos, mass, soft, n_bucket=16, theta=0.7, period=0.0, n_replicas=
                      bucket_starts=bstarts, bucket_sizes=bsizes, bucket_bbox=bbox,
                      cells=cells, plist=plist, period=float(period), n_replicas=int(n_replicas),
                      theta=float(theta), n_bucket=int(n_bucket),
-                     meta={"parent": parent, "leaf": leaf, "first": first, "count": count})
+                     meta={"parent": parent, "leaf": leaf, "first": first, "count": count},
+                     order=order, softcells=softcells)
 
 
 def concat_systems(systems):

@@ -19,6 +19,7 @@ import numpy as np
 HERE = os.path.dirname(os.path.abspath(__file__))
 PORT_LIB = os.path.join(HERE, "_build", "libchanga_port.so")
 REF_LIB = os.path.join(HERE, "_ref", "libchanga_ref.so")
+REF_HEX_LIB = os.path.join(HERE, "_ref", "libchanga_ref_hex.so")
 
 _libs = {}
 
@@ -47,8 +48,64 @@ def load(kind="port"):
         for f in (lib.oracle_cell_list_forces, lib.oracle_part_list_forces, lib.oracle_ewald_table,
                   lib.oracle_ewald_forces):
             f.restype = i
+        if kind == "port":
+            _bind_hex(lib)
         _libs[kind] = lib
     return _libs[kind]
+
+
+def _bind_hex(lib):
+    vp, i, l, d = C.c_void_p, C.c_int, C.c_long, C.c_double
+    lib.oracle_cell_list_forces_hex.argtypes = [vp, l, vp, l, vp, vp, vp, vp, i, vp, d, vp, i]
+    lib.oracle_cell_list_forces_hex.restype = i
+
+
+def _load_hex(kind):
+    """The hexadecapole cell-list oracle: the port, or the reference's own
+    gravity.h + moments.c compiled with HEXADECAPOLE (kind "ref")."""
+    if kind == "auto":
+        kind = "ref" if os.path.exists(REF_HEX_LIB) else "port"
+    if kind == "port":
+        return load("port")
+    key = "ref_hex"
+    if key not in _libs:
+        if not os.path.exists(REF_HEX_LIB):
+            build()
+        lib = C.CDLL(REF_HEX_LIB)
+        _bind_hex(lib)
+        _libs[key] = lib
+    return _libs[key]
+
+
+def bucket_geometry(lists, req):
+    """{cm.xyz, soft, bbox lesser xyz, greater xyz} of every bucket of a
+    request (the bucket's own moments and particle box), for the
+    hexadecapole softening test."""
+    ids = np.asarray(req.bucket_ids, dtype=np.int64)
+    mom = lists.moments[lists.meta["leaf"][lists.bucket_starts[ids]]]
+    g = np.empty((len(ids), 10))
+    g[:, 0:3] = mom[:, 3:6]
+    g[:, 3] = mom[:, 1]
+    g[:, 4:10] = lists.bucket_bbox[ids]
+    return g
+
+
+def cell_forces_hex(moments, parts, req, geom, fperiod=0.0, vars=None, kind="port", nthreads=0):
+    """nodeBucketForce of the hexadecapole build over a cell request
+    (moments M x 27; geom from bucket_geometry); returns vars (N x 5)."""
+    lib = _load_hex(kind)
+    moments = _c(moments, np.float64)
+    parts = _c(parts, np.float64)
+    geom = _c(geom, np.float64)
+    if vars is None:
+        vars = np.zeros((parts.shape[0], 5))
+    lst, mk, st, sz = (_c(req.list, np.int32), _c(req.markers, np.int32),
+                       _c(req.starts, np.int32), _c(req.sizes, np.int32))
+    rc = lib.oracle_cell_list_forces_hex(_p(moments), moments.shape[0], _p(parts), parts.shape[0],
+                                         _p(lst), _p(mk), _p(st), _p(sz), len(st), _p(geom),
+                                         float(fperiod), _p(vars), int(nthreads))
+    assert rc == 0
+    return vars
 
 
 def _p(a):

@@ -195,6 +195,129 @@ int oracle_part_list_forces(const double* sources, long n_sources,
   return 0;
 }
 
+/* ---- hexadecapole build ---- */
+
+/* momEvalFmomrcm, moments.c:1469-1525: the scaled reduced moments mo[6..26]
+ * of a cell with radius mo[0] and mass mo[2], evaluated at r = target - cm,
+ * dir = 1/|r|; the same expressions in the same order, so the FP64 results
+ * are those of the reference. */
+static void hex_eval(const double* mo, double dir, double x, double y, double z, double* v) {
+  /* the reference's constant is the single-precision 1/3 (1.0f / 3.0f),
+   * promoted: kept so the FP64 results are bit-identical */
+  const double onethird = (double)(1.0f / 3.0f);
+  const double mxx = mo[6], mxy = mo[7], mxz = mo[8], myy = mo[9], myz = mo[10];
+  const double mxxx = mo[11], mxyy = mo[12], mxxy = mo[13], myyy = mo[14], mxxz = mo[15],
+               myyz = mo[16], mxyz = mo[17];
+  const double mxxxx = mo[18], mxyyy = mo[19], mxxxy = mo[20], myyyy = mo[21], mxxxz = mo[22],
+               myyyz = mo[23], mxxyy = mo[24], mxxyz = mo[25], mxyyz = mo[26];
+  double u = mo[0];
+  u *= dir;
+  double g0 = dir;
+  double g2 = 3 * dir * u * u;
+  double g3 = 5 * g2 * u;
+  double g4 = 7 * g3 * u;
+  x *= dir;
+  y *= dir;
+  z *= dir;
+  double xx = 0.5 * x * x;
+  double xy = x * y;
+  double xz = x * z;
+  double yy = 0.5 * y * y;
+  double yz = y * z;
+  double zz = 0.5 * z * z;
+  double xxx = x * (onethird * xx - zz);
+  double xxz = z * (xx - onethird * zz);
+  double yyy = y * (onethird * yy - zz);
+  double yyz = z * (yy - onethird * zz);
+  xx -= zz;
+  yy -= zz;
+  double xxy = y * xx;
+  double xyy = x * yy;
+  double xyz = xy * z;
+  double tx = g4 * (mxxxx * xxx + mxyyy * yyy + mxxxy * xxy + mxxxz * xxz + mxxyy * xyy +
+                    mxxyz * xyz + mxyyz * yyz);
+  double ty = g4 * (mxyyy * xyy + mxxxy * xxx + myyyy * yyy + myyyz * yyz + mxxyy * xxy +
+                    mxxyz * xxz + mxyyz * xyz);
+  double tz = g4 * (-mxxxx * xxz - (mxyyy + mxxxy) * xyz - myyyy * yyz + mxxxz * xxx +
+                    myyyz * yyy - mxxyy * (xxz + yyz) + mxxyz * xxy + mxyyz * xyy);
+  g4 = 0.25 * (tx * x + ty * y + tz * z);
+  xxx = g3 * (mxxx * xx + mxyy * yy + mxxy * xy + mxxz * xz + mxyz * yz);
+  xxy = g3 * (mxyy * xy + mxxy * xx + myyy * yy + myyz * yz + mxyz * xz);
+  xxz = g3 * (-(mxxx + mxyy) * xz - (mxxy + myyy) * yz + mxxz * xx + myyz * yy + mxyz * xy);
+  g3 = onethird * (xxx * x + xxy * y + xxz * z);
+  xx = g2 * (mxx * x + mxy * y + mxz * z);
+  xy = g2 * (myy * y + mxy * x + myz * z);
+  xz = g2 * (-(mxx + myy) * z + mxz * x + myz * y);
+  g2 = 0.5 * (xx * x + xy * y + xz * z);
+  g0 *= mo[2];
+  v[3] += -(g0 + g2 + g3 + g4);
+  g0 += 5 * g2 + 7 * g3 + 9 * g4;
+  v[0] += dir * (xx + xxx + tx - x * g0);
+  v[1] += dir * (xy + xxy + ty - y * g0);
+  v[2] += dir * (xz + xxz + tz - z * g0);
+}
+
+/* openSoftening, gravity.h:252-260 (closed balls, as the walk uses):
+ * geom = {bucket cm.xyz, bucket soft, bbox lesser xyz, greater xyz}. */
+static int open_softening(const double* mo, const double* off, const double* geom) {
+  const double c0 = mo[3] + off[0], c1 = mo[4] + off[1], c2 = mo[5] + off[2];
+  const double r = 2.0 * mo[1];
+  double dx = geom[0] - c0, dy = geom[1] - c1, dz = geom[2] - c2;
+  const double rr = 2.0 * geom[3] + r;
+  if (dx * dx + dy * dy + dz * dz <= rr * rr) return 1;
+  double d2 = 0.0, d;
+  if ((d = geom[4] - c0) > 0) d2 += d * d;
+  else if ((d = c0 - geom[7]) > 0) d2 += d * d;
+  if ((d = geom[5] - c1) > 0) d2 += d * d;
+  else if ((d = c1 - geom[8]) > 0) d2 += d * d;
+  if ((d = geom[6] - c2) > 0) d2 += d * d;
+  else if ((d = c2 - geom[9]) > 0) d2 += d * d;
+  return d2 <= r * r;
+}
+
+/* nodeBucketForce with HEXADECAPOLE, gravity.h:398-421, 439-446. */
+static void node_bucket_force_hex(const double* mo, const double* off, const double* geom,
+                                  const double* parts, double* vars, int s, int n) {
+  if (open_softening(mo, off, geom)) {
+    const double src[5] = {mo[2], mo[1], mo[3], mo[4], mo[5]};
+    part_bucket_force(src, off, parts, vars, s, n);
+    return;
+  }
+  const double cm0 = mo[3] + off[0], cm1 = mo[4] + off[1], cm2 = mo[5] + off[2];
+  for (int j = s; j < s + n; ++j) {
+    const double* p = parts + 5 * (size_t)j;
+    double* v = vars + 5 * (size_t)j;
+    const double rx = p[2] - cm0, ry = p[3] - cm1, rz = p[4] - cm2;
+    const double rsq = rx * rx + ry * ry + rz * rz;
+    const double dir = 1.0 / sqrt(rsq);
+    hex_eval(mo, dir, rx, ry, rz, v);
+    const double idt2 = (p[0] + mo[2]) * dir * dir * dir;
+    if (idt2 > v[4]) v[4] = idt2;
+  }
+}
+
+int oracle_cell_list_forces_hex(const double* moments, long n_moments, const double* parts,
+                                long n_parts, const int* list, const int* markers,
+                                const int* starts, const int* sizes, int n_buckets,
+                                const double* geom, double fperiod, double* vars, int nthreads) {
+  (void)n_parts;
+#ifdef _OPENMP
+  if (nthreads > 0) omp_set_num_threads(nthreads);
+#pragma omp parallel for schedule(dynamic, 16)
+#endif
+  for (int b = 0; b < n_buckets; ++b) {
+    for (int e = markers[b]; e < markers[b + 1]; ++e) {
+      const int idx = list[2 * (size_t)e];
+      if (idx < 0 || idx >= n_moments) continue;
+      double off[3];
+      decode_offset(list[2 * (size_t)e + 1], fperiod, off);
+      node_bucket_force_hex(moments + 27 * (size_t)idx, off, geom + 10 * (size_t)b, parts, vars,
+                            starts[b], sizes[b]);
+    }
+  }
+  return 0;
+}
+
 /* QEVAL (quadrupole), Ewald.cpp:48-69: evaluates the root expansion with
  * the gamma factors gam[0..3] at (dx, dy, dz). */
 static void qeval(const double* mom, const double gam[6], double dx, double dy, double dz,

@@ -61,6 +61,17 @@ int oracle_ewald_forces(const double* parts, long n_parts, const int* idx, long 
                         const double* root_moments, double L, int nReps,
                         double fEwCut, double dEwhCut, double* vars, int nthreads);
 
+/* Hexadecapole build of the cell lists (nodeBucketForce with
+ * HEXADECAPOLE): moments 27 per node {radius, soft, totalMass, cm.xyz, xx xy
+ * xz yy yz, xxx xyy xxy yyy xxz yyz xyz, xxxx xyyy xxxy yyyy xxxz yyyz xxyy
+ * xxyz xyyz} (scaled reduced moments); geom 10 per request bucket {cm.xyz,
+ * soft, bbox lesser xyz, greater xyz} for the softening test.  Cells whose
+ * softening meets the bucket act as softened point masses. */
+int oracle_cell_list_forces_hex(const double* moments, long n_moments, const double* parts,
+                                long n_parts, const int* list, const int* markers,
+                                const int* starts, const int* sizes, int n_buckets,
+                                const double* geom, double fperiod, double* vars, int nthreads);
+
 #ifdef __cplusplus
 }
 #endif

@@ -67,6 +67,20 @@ struct Sphere {
   Sphere(const Vector3D<T>& o, T r) : origin(o), radius(r) {}
 };
 
+#ifdef HEXADECAPOLE
+#include "moments.h"  /* the reference's own FMOMR and momEvalFmomrcm */
+/* Hexadecapole MultipoleMoments: the members gravity.h reads
+ * (MultipoleMoments.h:182-185 layout with HEXADECAPOLE). */
+struct MultipoleMoments {
+  cosmoType radius;
+  cosmoType soft;
+  cosmoType totalMass;
+  Vector3D<cosmoType> cm;
+  FMOMR mom;
+  MultipoleMoments() : radius(0), soft(0), totalMass(0) { std::memset(&mom, 0, sizeof(mom)); }
+  cosmoType getRadius() const { return radius; }
+};
+#else
 /* Quadrupole MultipoleMoments: the members gravity.h and Ewald.cpp read
  * (MultipoleMoments.h:182-187 layout, non-HEXADECAPOLE). */
 struct MultipoleMoments {
@@ -78,6 +92,7 @@ struct MultipoleMoments {
   MultipoleMoments() : radius(0), soft(0), totalMass(0), xx(0), xy(0), xz(0), yy(0), yz(0), zz(0) {}
   cosmoType getRadius() const { return radius; }
 };
+#endif
 
 class ExternalGravityParticle {
  public:

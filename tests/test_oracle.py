@@ -102,3 +102,49 @@ def test_ewald_single_particle_no_self_force():
     v = oracle.part_forces(L.parts, L.parts, L.plist, fperiod=1.0, vars=v)
     v = oracle.ewald_forces(L.parts, L.root, 1.0, 1, 2.6, 2.8, vars=v)
     assert np.abs(v[0, :3]).max() < 1e-6
+
+
+def _hex_lists(n=8192, soft=0.3, seed=3):
+    from changa_gb300 import ics, tree
+    p = ics.plummer(n, ics.rng_for(seed))
+    p["soft"][:] = soft
+    return tree.build_lists(p["pos"], p["mass"], p["soft"], n_bucket=16, theta=0.7, order=4)
+
+
+@pytest.mark.skipif(not os.path.exists(oracle.REF_HEX_LIB), reason="reference not built here")
+def test_hex_port_bitexact_vs_reference(built):
+    """The port's hexadecapole cell evaluation (momEvalFmomrcm and the
+    openSoftening point-mass path) is bit-identical to the reference's own
+    gravity.h + moments.c built with HEXADECAPOLE, on both lists the
+    hexadecapole walk emits."""
+    L = _hex_lists()
+    assert L.cells.n_entries > 0 and L.softcells.n_entries > 0
+    for req in (L.cells, L.softcells):
+        g = oracle.bucket_geometry(L, req)
+        a = oracle.cell_forces_hex(L.moments, L.parts, req, g, kind="port")
+        b = oracle.cell_forces_hex(L.moments, L.parts, req, g, kind="ref")
+        assert np.array_equal(a, b)
+
+
+def test_hex_more_accurate_than_quadrupole(built):
+    """Same tree, same opening angle: the hexadecapole evaluation sits an
+    order of magnitude closer to the direct sum than the quadrupole one."""
+    from changa_gb300 import ics, tree
+    p = ics.plummer(16384, ics.rng_for(0), soft=0.01)
+    idx = np.random.default_rng(0).choice(16384, 256, replace=False)
+    med = {}
+    for order in (2, 4):
+        L = tree.build_lists(p["pos"], p["mass"], p["soft"], n_bucket=16, theta=0.7, order=order)
+        if order == 4:
+            v = oracle.cell_forces_hex(L.moments, L.parts, L.cells, oracle.bucket_geometry(L, L.cells))
+            if L.softcells.n_buckets:
+                v = oracle.cell_forces_hex(L.moments, L.parts, L.softcells,
+                                           oracle.bucket_geometry(L, L.softcells), vars=v)
+        else:
+            v = oracle.cell_forces(L.moments, L.parts, L.cells)
+        v = oracle.part_forces(L.parts, L.parts, L.plist, vars=v)
+        gi = np.argsort(L.perm)[idx]
+        acc, _ = oracle.direct_sum(L.parts, gi)
+        e = np.linalg.norm(v[gi, :3] - acc, axis=1) / np.linalg.norm(acc, axis=1)
+        med[order] = np.median(e)
+    assert med[4] < med[2] / 4 and med[4] < 3e-4, med
