@@ -175,6 +175,9 @@ CUDA_SIGNATURES = {
     "changa_gravity_graph_destroy": (None, [_VP]),
     "changa_tree_moments": (_I, [_VP, _LL, _VP, _VP, _LL, _VP, _VP]),
     "changa_direct_forces": (_I, [_VP, _LL, _VP, _LL, _D, _D, _VP, _VP]),
+    "changa_gravity_step_hexa": (_I, [_I, _VP, _LL, _VP, _LL, C.POINTER(ChangaListRequest),
+                                      C.POINTER(ChangaListRequest),
+                                      C.POINTER(ChangaListRequest), _D, _VP, _VP]),
     "changa_ewald_forces": (_I, [_I, _VP, _LL, _VP, _LL, C.POINTER(ChangaEwaldParams), _VP, _VP]),
     "changa_ewald_table": (_I, [_VP, _D, _D, _VP, _I]),
 }

@@ -40,6 +40,10 @@ struct ListArgs {
  * hi = (float)x, lo = (float)(x - hi), both exact in FP64. */
 constexpr int kCellPackF4 = 4;
 constexpr int kPartPackF4 = 2;
+/* hexadecapole cell: {hi.xyz, M} {lo.xyz, soft} then the radius and the 21
+ * scaled reduced moments (xx xy xz yy yz, xxx xyy xxy yyy xxz yyz xyz,
+ * xxxx xyyy xxxy yyyy xxxz yyyz xxyy xxyz xyyz) and two zeros */
+constexpr int kCellHexPackF4 = 8;
 
 /* launchers (grav_lists.cu) */
 cudaError_t launch_list(int form, bool cell, const ListArgs& a, cudaStream_t s);
@@ -49,6 +53,12 @@ int get_list_variant(int kernel);
 cudaError_t launch_pack_cells(const double* moments, long long n, float4* out, cudaStream_t s);
 cudaError_t launch_pack_parts(const double* parts, long long n, float4* out, cudaStream_t s);
 cudaError_t launch_zero_vars_f32(VariablePartData* v, long long n, cudaStream_t s);
+/* hexadecapole build: cell lists over 27-double (kF64) or packed (kMix)
+ * moments; the pack; cells as point-mass particles {M, soft, cm} */
+cudaError_t launch_list_hex(int form, const ListArgs& a, cudaStream_t s);
+cudaError_t launch_pack_cells_hex(const double* moments, long long n, float4* out, cudaStream_t s);
+cudaError_t launch_cells_as_parts(const double* moments, int stride, long long n, double* out,
+                                  cudaStream_t s);
 
 /* Ewald (ewald.cu) */
 struct EwaldArgsF32;  // defined in ewald.cu

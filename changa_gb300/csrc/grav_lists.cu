@@ -161,6 +161,69 @@ __device__ __forceinline__ void pp_interact(const T* rec, T tx, T ty, T tz, T ts
   }
 }
 
+/* One hexadecapole cell on one target: momEvalFmomrcm (moments.c:
+ * 1469-1525, CUDAMoments.cu:14-109) for the scaled reduced moments of the
+ * hexadecapole build; no softening (softened cells are evaluated as point
+ * masses from their own list).  rec: {sx, sy, sz, M, radius, xx xy xz yy yz,
+ * xxx xyy xxy yyy xxz yyz xyz, xxxx xyyy xxxy yyyy xxxz yyyz xxyy xxyz xyyz};
+ * r = target - s.  onethird is the reference's single-precision 1/3. */
+template <typename T>
+__device__ __forceinline__ void hex_eval(const T* q, T M, T u, T dir, T x, T y, T z, T& pot,
+                                         T& ax, T& ay, T& az) {
+  const T onethird = T(0.3333333432674408);
+  u *= dir;
+  T g0 = dir;
+  T g2 = T(3) * dir * u * u;
+  T g3 = T(5) * g2 * u;
+  T g4 = T(7) * g3 * u;
+  x *= dir;
+  y *= dir;
+  z *= dir;
+  T xx = T(0.5) * x * x, xy = x * y, xz = x * z, yy = T(0.5) * y * y, yz = y * z,
+    zz = T(0.5) * z * z;
+  T xxx = x * (onethird * xx - zz), xxz = z * (xx - onethird * zz);
+  T yyy = y * (onethird * yy - zz), yyz = z * (yy - onethird * zz);
+  xx -= zz;
+  yy -= zz;
+  T xxy = y * xx, xyy = x * yy, xyz = xy * z;
+  /* q: 0 xx 1 xy 2 xz 3 yy 4 yz 5 xxx 6 xyy 7 xxy 8 yyy 9 xxz 10 yyz 11 xyz
+   *    12 xxxx 13 xyyy 14 xxxy 15 yyyy 16 xxxz 17 yyyz 18 xxyy 19 xxyz 20 xyyz */
+  const T tx = g4 * (q[12] * xxx + q[13] * yyy + q[14] * xxy + q[16] * xxz + q[18] * xyy +
+                     q[19] * xyz + q[20] * yyz);
+  const T ty = g4 * (q[13] * xyy + q[14] * xxx + q[15] * yyy + q[17] * yyz + q[18] * xxy +
+                     q[19] * xxz + q[20] * xyz);
+  const T tz = g4 * (-q[12] * xxz - (q[13] + q[14]) * xyz - q[15] * yyz + q[16] * xxx +
+                     q[17] * yyy - q[18] * (xxz + yyz) + q[19] * xxy + q[20] * xyy);
+  g4 = T(0.25) * (tx * x + ty * y + tz * z);
+  const T o3x = g3 * (q[5] * xx + q[6] * yy + q[7] * xy + q[9] * xz + q[11] * yz);
+  const T o3y = g3 * (q[6] * xy + q[7] * xx + q[8] * yy + q[10] * yz + q[11] * xz);
+  const T o3z = g3 * (-(q[5] + q[6]) * xz - (q[7] + q[8]) * yz + q[9] * xx + q[10] * yy +
+                      q[11] * xy);
+  g3 = onethird * (o3x * x + o3y * y + o3z * z);
+  const T o2x = g2 * (q[0] * x + q[1] * y + q[2] * z);
+  const T o2y = g2 * (q[3] * y + q[1] * x + q[4] * z);
+  const T o2z = g2 * (-(q[0] + q[3]) * z + q[2] * x + q[4] * y);
+  g2 = T(0.5) * (o2x * x + o2y * y + o2z * z);
+  g0 *= M;
+  pot -= g0 + g2 + g3 + g4;
+  g0 += T(5) * g2 + T(7) * g3 + T(9) * g4;
+  ax += dir * (o2x + o3x + tx - x * g0);
+  ay += dir * (o2y + o3y + ty - y * g0);
+  az += dir * (o2z + o3z + tz - z * g0);
+}
+
+template <typename T>
+__device__ __forceinline__ void hex_interact(const T* rec, T tx, T ty, T tz, T tmass,
+                                             Acc<T>& acc) {
+  const T rx = tx - rec[0], ry = ty - rec[1], rz = tz - rec[2];
+  const T rsq = rx * rx + ry * ry + rz * rz;
+  if (rsq != T(0)) {
+    const T dir = rsqrt_t(rsq);
+    hex_eval<T>(rec + 5, rec[3], rec[4], dir, rx, ry, rz, acc.pot, acc.ax, acc.ay, acc.az);
+    acc.idt2 = max_t(acc.idt2, (tmass + rec[3]) * dir * dir * dir);
+  }
+}
+
 __device__ __forceinline__ void kahan_add(float& sum, float& comp, float x) {
   const float y = x - comp;
   const float t = sum + y;
@@ -185,7 +248,7 @@ struct FormT<kMix> {
 };
 
 /* Builds the staged record of list entry e in dst. */
-template <int FORM, bool CELL>
+template <int FORM, bool CELL, bool HEX = false>
 __device__ __forceinline__ void stage_entry(const ListArgs& a, int e, float3 chi, float3 clo,
                                             typename FormT<FORM>::T* dst) {
   const int2 ent = __ldg(a.list + e);
@@ -214,7 +277,17 @@ __device__ __forceinline__ void stage_entry(const ListArgs& a, int e, float3 chi
     }
   } else if constexpr (FORM == kF64) {
     const double fp = a.fperiod_d;
-    if constexpr (CELL) {
+    if constexpr (CELL && HEX) {
+      /* hexadecapole moments: 27 doubles per node */
+      const double* m = static_cast<const double*>(a.src) + 27 * idx;
+      dst[0] = (double)ox * fp + __ldg(m + 3);
+      dst[1] = (double)oy * fp + __ldg(m + 4);
+      dst[2] = (double)oz * fp + __ldg(m + 5);
+      dst[3] = __ldg(m + 2);
+      dst[4] = __ldg(m + 0);
+#pragma unroll
+      for (int k = 0; k < 21; ++k) dst[5 + k] = __ldg(m + 6 + k);
+    } else if constexpr (CELL) {
       const double* m = static_cast<const double*>(a.src) + 12 * idx;
       dst[0] = (double)ox * fp + __ldg(m + 3);
       dst[1] = (double)oy * fp + __ldg(m + 4);
@@ -241,7 +314,21 @@ __device__ __forceinline__ void stage_entry(const ListArgs& a, int e, float3 chi
   } else {  // kMix
     const float fp = a.fperiod_f;
     float4* d4 = reinterpret_cast<float4*>(dst);
-    if constexpr (CELL) {
+    if constexpr (CELL && HEX) {
+      /* packed hexadecapole cell, 8 float4: {hi.xyz, M} {lo.xyz, soft}
+       * {radius, xx, xy, xz} {yy, yz, xxx, xyy} {xxy, yyy, xxz, yyz}
+       * {xyz, xxxx, xyyy, xxxy} {yyyy, xxxz, yyyz, xxyy} {xxyz, xyyz, 0, 0} */
+      const float4* m = static_cast<const float4*>(a.src) + kCellHexPackF4 * idx;
+      const float4 h = __ldg(m), l = __ldg(m + 1);
+      const float sx = ((h.x - chi.x) + (float)ox * fp) + (l.x - clo.x);
+      const float sy = ((h.y - chi.y) + (float)oy * fp) + (l.y - clo.y);
+      const float sz = ((h.z - chi.z) + (float)oz * fp) + (l.z - clo.z);
+      d4[0] = make_float4(sx, sy, sz, h.w);
+      /* rec[4] = radius, rec[5..25] = the 21 moments: the packed words 2..7
+       * carry exactly that sequence */
+#pragma unroll
+      for (int w = 0; w < 6; ++w) d4[1 + w] = __ldg(m + 2 + w);
+    } else if constexpr (CELL) {
       const float4* m = static_cast<const float4*>(a.src) + kCellPackF4 * idx;
       const float4 h = __ldg(m), l = __ldg(m + 1), q0 = __ldg(m + 2), q1 = __ldg(m + 3);
       const float sx = ((h.x - chi.x) + (float)ox * fp) + (l.x - clo.x);
@@ -262,12 +349,13 @@ __device__ __forceinline__ void stage_entry(const ListArgs& a, int e, float3 chi
   }
 }
 
-template <int FORM, bool CELL>
+template <int FORM, bool CELL, bool HEX = false>
 __global__ void __launch_bounds__(kThreads, 2) list_kernel(const ListArgs a) {
   using T = typename FormT<FORM>::T;
   using A = typename FormT<FORM>::A;
-  constexpr int RW = CELL ? 12 : 8;  // record width in T, multiple of 4
-  __shared__ __align__(16) T stage[kWarps][32 * RW];
+  constexpr int RW = CELL ? (HEX ? 28 : 12) : 8;  // record width in T, multiple of 4
+  constexpr int SB = HEX ? 16 : 32;                // entries staged per block
+  __shared__ __align__(16) T stage[kWarps][SB * RW];
   __shared__ A red[kWarps][5][32];
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   T* st = stage[warp];
@@ -328,15 +416,16 @@ __global__ void __launch_bounds__(kThreads, 2) list_kernel(const ListArgs a) {
       T sx = 0, sy = 0, sz = 0, sp = 0, idt2 = 0;
       float cx = 0.f, cy = 0.f, cz = 0.f, cp = 0.f;
 
-      for (int e0 = e_begin; e0 < e_end; e0 += 32) {
-        const int ne = min(32, e_end - e0);
-        if (lane < ne) stage_entry<FORM, CELL>(a, e0 + lane, chi, clo, st + lane * RW);
+      for (int e0 = e_begin; e0 < e_end; e0 += SB) {
+        const int ne = min(SB, e_end - e0);
+        if (lane < ne) stage_entry<FORM, CELL, HEX>(a, e0 + lane, chi, clo, st + lane * RW);
         __syncwarp();
         if (active) {
           Acc<T> acc{T(0), T(0), T(0), T(0), idt2};
 #pragma unroll 4
           for (int k = g; k < ne; k += G) {
-            if constexpr (CELL) pc_interact<T>(st + k * RW, tx, ty, tz, tsoft, tmass, acc);
+            if constexpr (CELL && HEX) hex_interact<T>(st + k * RW, tx, ty, tz, tmass, acc);
+            else if constexpr (CELL) pc_interact<T>(st + k * RW, tx, ty, tz, tsoft, tmass, acc);
             else pp_interact<T>(st + k * RW, tx, ty, tz, tsoft, tmass, acc);
           }
           idt2 = acc.idt2;
@@ -1427,6 +1516,45 @@ __global__ void pack_parts_kernel(const double* __restrict__ p, long long n, flo
   }
 }
 
+/* Packed hexadecapole cells (FP32-mixed form) from 27-double moments. */
+__global__ void pack_cells_hex_kernel(const double* __restrict__ m, long long n,
+                                      float4* __restrict__ out) {
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
+       i += (long long)gridDim.x * blockDim.x) {
+    const double* r = m + 27 * i;
+    const double x = r[3], y = r[4], z = r[5];
+    const float hx = (float)x, hy = (float)y, hz = (float)z;
+    float4* o = out + kCellHexPackF4 * i;
+    o[0] = make_float4(hx, hy, hz, (float)r[2]);
+    o[1] = make_float4((float)(x - (double)hx), (float)(y - (double)hy), (float)(z - (double)hz),
+                       (float)r[1]);
+    float w[24];
+    w[0] = (float)r[0];
+#pragma unroll
+    for (int k = 0; k < 21; ++k) w[1 + k] = (float)r[6 + k];
+    w[22] = 0.f;
+    w[23] = 0.f;
+#pragma unroll
+    for (int k = 0; k < 6; ++k) o[2 + k] = make_float4(w[4 * k], w[4 * k + 1], w[4 * k + 2], w[4 * k + 3]);
+  }
+}
+
+/* Cells as point masses {M, soft, cm} in the particle layout: the sources
+ * of the softened-cell list. */
+__global__ void cells_as_parts_kernel(const double* __restrict__ m, int stride, long long n,
+                                      double* __restrict__ out) {
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
+       i += (long long)gridDim.x * blockDim.x) {
+    const double* r = m + (size_t)stride * i;
+    double* o = out + 5 * i;
+    o[0] = r[2];
+    o[1] = r[1];
+    o[2] = r[3];
+    o[3] = r[4];
+    o[4] = r[5];
+  }
+}
+
 /* The FP64 form runs list_kernel (its cost is the FP64 pipe); the FP32
  * forms run one of the variants below: paired target-parallel by default
  * (the fastest on the measured workloads), the others on request or by the
@@ -1528,6 +1656,35 @@ cudaError_t launch_pack_cells(const double* moments, long long n, float4* out, c
   if (n <= 0) return cudaSuccess;
   TimingScope ts(kKidPack, s);
   pack_cells_kernel<<<grid_for(n, 256), 256, 0, s>>>(moments, n, out);
+  count_launch();
+  return cudaGetLastError();
+}
+
+cudaError_t launch_list_hex(int form, const ListArgs& a, cudaStream_t s) {
+  if (form == kF64) {
+    static int occ = 0;
+    return launch_kernel(list_kernel<kF64, true, true>, &occ, list_kernel_id(kF64, true), a, s);
+  }
+  if (form == kMix) {
+    static int occ = 0;
+    return launch_kernel(list_kernel<kMix, true, true>, &occ, list_kernel_id(kMix, true), a, s);
+  }
+  return cudaErrorInvalidValue;
+}
+
+cudaError_t launch_pack_cells_hex(const double* moments, long long n, float4* out, cudaStream_t s) {
+  if (n <= 0) return cudaSuccess;
+  TimingScope ts(kKidPack, s);
+  pack_cells_hex_kernel<<<grid_for(n, 256), 256, 0, s>>>(moments, n, out);
+  count_launch();
+  return cudaGetLastError();
+}
+
+cudaError_t launch_cells_as_parts(const double* moments, int stride, long long n, double* out,
+                                  cudaStream_t s) {
+  if (n <= 0) return cudaSuccess;
+  TimingScope ts(kKidPack, s);
+  cells_as_parts_kernel<<<grid_for(n, 256), 256, 0, s>>>(moments, stride, n, out);
   count_launch();
   return cudaGetLastError();
 }

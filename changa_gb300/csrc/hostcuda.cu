@@ -784,6 +784,89 @@ int changa_gravity_step(int form, const double* moments, long long n_moments, co
   return rc;
 }
 
+/* Hexadecapole build: cells evaluated with their scaled reduced moments,
+ * softened cells as point masses, particles as usual. */
+int changa_gravity_step_hexa(int form, const double* moments, long long n_moments,
+                             const double* parts, long long n_parts,
+                             const ChangaListRequest* cells, const ChangaListRequest* plist,
+                             const ChangaListRequest* softcells, double fperiod, double* vars,
+                             cudaStream_t s) {
+  if (form != CHANGA_FORM_FP64 && form != CHANGA_FORM_MIXED)
+    return record_error(CHANGA_E_INVALID_ARG, "gravity_step_hexa: form", __FILE__, __LINE__);
+  if (!moments || !parts || !vars || n_moments < 0 || n_parts < 0)
+    return record_error(CHANGA_E_INVALID_ARG, "gravity_step_hexa: arrays", __FILE__, __LINE__);
+  if ((cells && check_req(cells)) || (plist && check_req(plist)) ||
+      (softcells && check_req(softcells)))
+    return record_error(CHANGA_E_INVALID_ARG, "gravity_step_hexa: requests", __FILE__, __LINE__);
+  const int f = form == CHANGA_FORM_FP64 ? kF64 : kMix;
+  prepare_pool();
+  const size_t qb = align256((size_t)n_moments * 5 * sizeof(double));  // cells as particles
+  size_t cb = 0, pb = 0, sb = 0;
+  if (f == kMix) {
+    cb = align256((size_t)n_moments * kCellHexPackF4 * sizeof(float4));
+    pb = align256((size_t)n_parts * kPartPackF4 * sizeof(float4));
+    sb = align256((size_t)n_moments * kPartPackF4 * sizeof(float4));
+  }
+  char* block = nullptr;
+  CHG_CUDA(cudaMallocAsync((void**)&block, qb + cb + pb + sb + 1024, s));
+  double* pseudo = (double*)block;
+  unsigned int* q = (unsigned int*)(block + qb + cb + pb + sb);
+  const void* kcell = moments;
+  const void* kpart = parts;
+  const void* kpseudo = pseudo;
+  int rc = 0;
+  cudaError_t e = cudaSuccess;
+  do {
+    if (softcells && softcells->n_buckets > 0 &&
+        (e = launch_cells_as_parts(moments, 27, n_moments, pseudo, s)) != cudaSuccess)
+      break;
+    if (f == kMix) {
+      float4* pc = (float4*)(block + qb);
+      float4* pp = (float4*)(block + qb + cb);
+      float4* ps = (float4*)(block + qb + cb + pb);
+      if ((e = launch_pack_cells_hex(moments, n_moments, pc, s)) != cudaSuccess ||
+          (e = launch_pack_parts(parts, n_parts, pp, s)) != cudaSuccess)
+        break;
+      if (softcells && softcells->n_buckets > 0 &&
+          (e = launch_pack_parts(pseudo, n_moments, ps, s)) != cudaSuccess)
+        break;
+      kcell = pc;
+      kpart = pp;
+      kpseudo = ps;
+    }
+    if (cells && cells->n_buckets > 0) {
+      ListArgs a;
+      a.src = kcell;
+      a.n_src = n_moments;
+      a.tgt = kpart;
+      a.n_tgt = n_parts;
+      a.vars = vars;
+      a.list = (const int2*)cells->list;
+      a.n_entries = cells->n_entries;
+      a.markers = cells->markers;
+      a.starts = cells->starts;
+      a.sizes = cells->sizes;
+      a.n_buckets = cells->n_buckets;
+      a.fperiod_f = (float)fperiod;
+      a.fperiod_d = fperiod;
+      a.queue = q;
+      if ((e = cudaMemsetAsync(q, 0, sizeof(unsigned int), s)) != cudaSuccess ||
+          (e = launch_list_hex(f, a, s)) != cudaSuccess)
+        break;
+    }
+    if (plist && plist->n_buckets > 0)
+      rc = run_fp(f, false, kpart, n_parts, kpart, n_parts, plist, fperiod, vars, s, q + 64);
+    if (!rc && softcells && softcells->n_buckets > 0)
+      rc = run_fp(f, false, kpseudo, n_moments, kpart, n_parts, softcells, fperiod, vars, s,
+                  q + 128);
+  } while (0);
+  cudaError_t ef = cudaFreeAsync(block, s);
+  if (rc) return rc;
+  if (e == cudaSuccess) e = ef;
+  if (e != cudaSuccess) return record_error((int)e, "gravity_step_hexa", __FILE__, __LINE__);
+  return 0;
+}
+
 static std::atomic<size_t> g_host_chunk_bytes{size_t(512) << 20};
 
 void changa_gb300_set_host_chunk_bytes(size_t bytes) {

@@ -247,7 +247,13 @@ class DeviceSystem:
         self.moments = t(lists.moments)
         self.parts = t(lists.parts)
         self.reqs = []
-        for req in (lists.cells, lists.plist):
+        self.order = getattr(lists, "order", 2)
+        if self.order == 4 and ewald is not None:
+            raise ValueError("the hexadecapole build has no Ewald term here")
+        reqs = [lists.cells, lists.plist]
+        if self.order == 4:
+            reqs.append(lists.softcells)
+        for req in reqs:
             d = dict(list=t(req.list), markers=t(req.markers), starts=t(req.starts), sizes=t(req.sizes))
             r = N.ChangaListRequest()
             r.list = d["list"].data_ptr()
@@ -269,6 +275,14 @@ class DeviceSystem:
         s = stream if stream is not None else torch.cuda.current_stream().cuda_stream
         if zero:
             self.vars.zero_()
+        if self.order == 4:
+            rc = N.cuda_lib().changa_gravity_step_hexa(
+                FORMS[form], self.moments.data_ptr(), self.moments.shape[0],
+                self.parts.data_ptr(), self.n, C.byref(self.reqs[0]["c"]),
+                C.byref(self.reqs[1]["c"]), C.byref(self.reqs[2]["c"]),
+                float(self.lists.period), self.vars.data_ptr(), s)
+            N.check(rc, "changa_gravity_step_hexa")
+            return self.vars
         ep = self.ewald_params
         rc = N.cuda_lib().changa_gravity_step(
             FORMS[form], self.moments.data_ptr(), self.moments.shape[0], self.parts.data_ptr(),

@@ -197,6 +197,22 @@ ChangaGravityGraph *changa_gravity_graph_create(int form, const double *moments,
 int changa_gravity_graph_launch(ChangaGravityGraph *g, cudaStream_t stream);
 void changa_gravity_graph_destroy(ChangaGravityGraph *g);
 
+/* Hexadecapole build (ChaNGa's default configuration, HEXADECAPOLE): one
+ * evaluation with cells in the 27-double hexadecapole layout {radius, soft,
+ * totalMass, cm.xyz, xx xy xz yy yz, xxx xyy xxy yyy xxz yyz xyz, xxxx xyyy
+ * xxxy yyyy xxxz yyyz xxyy xxyz xyyz} (moments scaled by the radius,
+ * reduced: cuda_typedef.h:103-128, moments.h FMOMR), evaluated by
+ * momEvalFmomrcm (gravity.h:439-446) from `cells`; `softcells` lists the
+ * cells whose softening meets the bucket, evaluated as softened point
+ * masses {M, soft, cm} (gravity.h:414-421); `plist` as in
+ * changa_gravity_step.  form: CHANGA_FORM_FP64 or CHANGA_FORM_MIXED;
+ * isolated or periodic lists (fperiod), no Ewald term in this build. */
+int changa_gravity_step_hexa(int form, const double *moments, long long n_moments,
+                             const double *parts, long long n_parts,
+                             const ChangaListRequest *cells, const ChangaListRequest *plist,
+                             const ChangaListRequest *softcells, double fperiod, double *vars,
+                             cudaStream_t stream);
+
 /* Adjoint of the cell + particle list accelerations (FP32-mixed; no
  * reference counterpart): given lam = dL/da (n_parts x 3), ACCUMULATES
  * dL/dx and dL/dm into grad (n_parts x 4 {dx, dy, dz, dm}) through the same
