@@ -343,6 +343,10 @@ def measure_adjoint(leapfrog=True, reps=20, tune=True):
     return out
 
 
+def batched_workload(wl):
+    return hasattr(wl, "systems")
+
+
 def main_ours(args):
     import numpy as np
     import torch
@@ -361,6 +365,13 @@ def main_ours(args):
     t_walk = time.perf_counter() - t0
     ew = wl.ewald_config()
     I = lists.interactions
+    walk_gpu = None
+    if not batched_workload(wl):
+        # the same lists built on the GPU (changa_walk_count/fill), timed
+        from changa_gb300.walk import gpu_walk
+        gpu_walk(lists)
+        walk_gpu = {}
+        gpu_walk(lists, timings=walk_gpu)
     I_c, I_p = lists.cells.interactions(), lists.plist.interactions()
     ds = gravity.DeviceSystem(lists, device="cuda", ewald=ew)
     stream = torch.cuda.current_stream()
@@ -586,7 +597,8 @@ def main_ours(args):
                               l2="inputs larger than L2 (%.2f GB of lists) and a 256 MB flush "
                                  "write between timed steps" %
                                  ((lists.cells.list.nbytes + lists.plist.list.nbytes) / 1e9),
-                              host_walk_s=t_walk, fp64_form=fp64, kernels=kshare,
+                              host_walk_s=t_walk, gpu_walk_s=walk_gpu and walk_gpu.get("walk_s"),
+                              fp64_form=fp64, kernels=kshare,
                               batched_graph=batched, sequential_plain=seq,
                               autotune=tuning,
                               parallelism="replicas x%d" % world),

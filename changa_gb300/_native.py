@@ -89,6 +89,17 @@ class ChangaListRequest(C.Structure):
                 ("sizes", C.c_void_p), ("n_buckets", C.c_int), ("n_entries", C.c_longlong)]
 
 
+class ChangaTreeView(C.Structure):
+    _fields_ = [("geom", C.c_void_p), ("bbox", C.c_void_p), ("info", C.c_void_p),
+                ("parent", C.c_void_p), ("n_nodes", C.c_longlong), ("bucket_node", C.c_void_p),
+                ("n_buckets", C.c_int)]
+
+
+class ChangaWalkParams(C.Structure):
+    _fields_ = [("theta", C.c_double), ("order", C.c_int), ("period", C.c_double),
+                ("n_replicas", C.c_int)]
+
+
 class ChangaEwaldParams(C.Structure):
     _fields_ = [("root", C.c_double * 12), ("L", C.c_double), ("nReps", C.c_int),
                 ("fEwCut", C.c_double), ("nEwhLoop", C.c_int), ("ewt", C.c_void_p)]
@@ -175,6 +186,10 @@ CUDA_SIGNATURES = {
     "changa_gravity_graph_destroy": (None, [_VP]),
     "changa_tree_moments": (_I, [_VP, _LL, _VP, _VP, _LL, _VP, _VP]),
     "changa_direct_forces": (_I, [_VP, _LL, _VP, _LL, _D, _D, _VP, _VP]),
+    "changa_walk_count": (_I, [C.POINTER(ChangaTreeView), C.POINTER(ChangaWalkParams), _VP, _VP,
+                               _VP, _VP]),
+    "changa_walk_fill": (_I, [C.POINTER(ChangaTreeView), C.POINTER(ChangaWalkParams), _VP, _VP,
+                              _VP, _VP, _VP, _VP, _VP]),
     "changa_gravity_step_hexa": (_I, [_I, _VP, _LL, _VP, _LL, C.POINTER(ChangaListRequest),
                                       C.POINTER(ChangaListRequest),
                                       C.POINTER(ChangaListRequest), _D, _VP, _VP]),
@@ -202,6 +217,7 @@ HOST_SIGNATURES = {
     "chg_tree_set_order": (_I, [_VP, _I]),
     "chg_tree_soft_lengths": (None, [_VP, _VP]),
     "chg_tree_get_moments_hex": (None, [_VP, _VP]),
+    "chg_tree_get_nodes": (None, [_VP, _VP, _VP, _VP]),
 }
 
 

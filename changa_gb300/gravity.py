@@ -238,20 +238,24 @@ def dropin_step(inp: DropInInputs, stream=None, cudart=None):
 class DeviceSystem:
     """Device-resident inputs of one force evaluation (torch tensors)."""
 
-    def __init__(self, lists, device="cuda", ewald: EwaldConfig | None = None):
+    def __init__(self, lists, device="cuda", ewald: EwaldConfig | None = None,
+                 device_reqs=None):
+        """device_reqs: requests built on the device (walk.gpu_walk) to use
+        instead of the host lists' (cells, plist[, softcells])."""
         import torch
         self.torch = torch
         self.lists = lists
         self.n = lists.n
-        t = lambda a: torch.from_numpy(np.ascontiguousarray(a)).to(device)
+        t = lambda a: (a.to(device) if isinstance(a, torch.Tensor)
+                       else torch.from_numpy(np.ascontiguousarray(a)).to(device))
         self.moments = t(lists.moments)
         self.parts = t(lists.parts)
         self.reqs = []
         self.order = getattr(lists, "order", 2)
         if self.order == 4 and ewald is not None:
             raise ValueError("the hexadecapole build has no Ewald term here")
-        reqs = [lists.cells, lists.plist]
-        if self.order == 4:
+        reqs = list(device_reqs) if device_reqs is not None else [lists.cells, lists.plist]
+        if self.order == 4 and device_reqs is None:
             reqs.append(lists.softcells)
         for req in reqs:
             d = dict(list=t(req.list), markers=t(req.markers), starts=t(req.starts), sizes=t(req.sizes))

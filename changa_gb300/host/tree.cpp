@@ -784,6 +784,31 @@ void chg_tree_get_moments_hex(void* h, double* out) {
   }
 }
 
+/* Node arrays for a device-side walk, breadth-first like the moments:
+ * geom 6 per node {cm.xyz, radius, soft, mass}, bbox 6 {lesser xyz,
+ * greater xyz} from the node's particles, info 4 {child0, child1, first,
+ * count} with children as moment indices (-1: none; buckets have none). */
+void chg_tree_get_nodes(void* h, double* geom, double* bbox, int* info) {
+  Tree* t = (Tree*)h;
+  for (size_t i = 0; i < t->bfs_nodes.size(); ++i) {
+    const Node& nd = t->nodes[t->bfs_nodes[i]];
+    double* g = geom + 6 * i;
+    g[0] = nd.mom[3];
+    g[1] = nd.mom[4];
+    g[2] = nd.mom[5];
+    g[3] = nd.mom[0];
+    g[4] = nd.mom[1];
+    g[5] = nd.mom[2];
+    std::memcpy(bbox + 6 * i, nd.bbox, 6 * sizeof(double));
+    int* f = info + 4 * i;
+    f[0] = f[1] = -1;
+    if (nd.type == T_INTERNAL)
+      for (int c = 0; c < 2; ++c) f[c] = t->nodes[nd.child[c]].bfs;  // -1 for Empty
+    f[2] = nd.first;
+    f[3] = nd.count;
+  }
+}
+
 /* Hexadecapole mode (order 4) or quadrupole (order 2, the default): set
  * before the walk.  theta_mono = theta^4 (ParallelGravity.cpp:993). */
 int chg_tree_set_order(void* h, int order) {

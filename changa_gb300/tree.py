@@ -138,7 +138,12 @@ def build_lists(pos, mass, soft, n_bucket=16, theta=0.7, period=0.0, n_replicas=
         bstarts = np.empty(nb, dtype=np.int32)
         bsizes = np.empty(nb, dtype=np.int32)
         bbox = np.empty((nb, 6), dtype=np.float64)
-        lib.chg_tree_get_buckets(h, _ptr(bstarts), _ptr(bsizes), _ptr(bbox), None)
+        bnode = np.empty(nb, dtype=np.int32)
+        lib.chg_tree_get_buckets(h, _ptr(bstarts), _ptr(bsizes), _ptr(bbox), _ptr(bnode))
+        ngeom = np.empty((nm, 6), dtype=np.float64)
+        nbbox = np.empty((nm, 6), dtype=np.float64)
+        ninfo = np.empty((nm, 4), dtype=np.int32)
+        lib.chg_tree_get_nodes(h, _ptr(ngeom), _ptr(nbbox), _ptr(ninfo))
         parent = np.empty(nm, dtype=np.int32)
         leaf = np.empty(n, dtype=np.int32)
         lib.chg_tree_get_structure(h, _ptr(parent), _ptr(leaf))
@@ -166,7 +171,9 @@ def build_lists(pos, mass, soft, n_bucket=16, theta=0.7, period=0.0, n_replicas=
                      bucket_starts=bstarts, bucket_sizes=bsizes, bucket_bbox=bbox,
                      cells=cells, plist=plist, period=float(period), n_replicas=int(n_replicas),
                      theta=float(theta), n_bucket=int(n_bucket),
-                     meta={"parent": parent, "leaf": leaf, "first": first, "count": count},
+                     meta={"parent": parent, "leaf": leaf, "first": first, "count": count,
+                           "bucket_node": bnode, "node_geom": ngeom, "node_bbox": nbbox,
+                           "node_info": ninfo},
                      order=order, softcells=softcells)
 
 

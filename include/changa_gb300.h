@@ -249,6 +249,45 @@ int changa_tree_moments(const double *parts, long long n_parts, const int *first
 int changa_direct_forces(const double *parts, long long n_parts, const int *idx, long long n_idx,
                          double L, double rcut_frac, double *out, cudaStream_t stream);
 
+/* Interaction-list walk on the device (no reference counterpart in the
+ * default build; the reference's GPU walk prototype is gpuLocalTreeWalk,
+ * HostCUDA.cu:724-942).  One thread per target bucket reproduces the host
+ * dual walk's per-bucket lists (the same entries, in depth-first order).
+ * Tree arrays in moment (breadth-first) order, device memory:
+ *   geom   n_nodes x 6 {cm.xyz, radius, soft, mass}
+ *   bbox   n_nodes x 6 {lesser xyz, greater xyz} of the node's particles
+ *   info   n_nodes x 4 {child0, child1, first, count} (-1: no child)
+ *   parent n_nodes (-1 at the root); bucket_node: moment index per bucket. */
+typedef struct ChangaTreeView {
+  const double *geom;
+  const double *bbox;
+  const int *info;
+  const int *parent;
+  long long n_nodes;
+  const int *bucket_node;
+  int n_buckets;
+} ChangaTreeView;
+
+typedef struct ChangaWalkParams {
+  double theta;   /* opening angle; the hexadecapole monopole angle is theta^4 */
+  int order;      /* 2 quadrupole, 4 hexadecapole (adds the softened-cell list) */
+  double period;  /* 0 for open boundaries */
+  int n_replicas; /* replica layers on the root check list (0..3) */
+} ChangaWalkParams;
+
+/* Count pass: per-bucket list lengths (device int arrays, n_buckets each;
+ * n_soft only for order 4).  Returns after the stream has finished. */
+int changa_walk_count(const ChangaTreeView *tree, const ChangaWalkParams *p, int *n_cells,
+                      int *n_parts, int *n_soft, cudaStream_t stream);
+/* Fill pass: writes each bucket's entries at its offset (device long long
+ * arrays, exclusive prefix sums of the counts) into the device lists.
+ * Cells and softened cells index the moments, particles index the parts;
+ * offsetID = replica code << 22.  Returns after the stream has finished. */
+int changa_walk_fill(const ChangaTreeView *tree, const ChangaWalkParams *p,
+                     const long long *off_cells, const long long *off_parts,
+                     const long long *off_soft, ILCell *cells, ILCell *parts, ILCell *soft,
+                     cudaStream_t stream);
+
 /* Ewald correction for parts[idx[k]] into vars[idx[k]] (idx == NULL: the
  * first n_idx particles).  form: FP64 or MIXED. */
 int changa_ewald_forces(int form, const double *parts, long long n_parts, const int *idx,
