@@ -100,6 +100,14 @@ class ChangaWalkParams(C.Structure):
                 ("n_replicas", C.c_int)]
 
 
+class ChangaTreeArrays(C.Structure):
+    _fields_ = [("n", C.c_longlong), ("n_nodes", C.c_longlong), ("n_buckets", C.c_int),
+                ("perm", C.c_void_p), ("parts", C.c_void_p), ("moments", C.c_void_p),
+                ("geom", C.c_void_p), ("bbox", C.c_void_p), ("info", C.c_void_p),
+                ("parent", C.c_void_p), ("bucket_node", C.c_void_p), ("leaf", C.c_void_p),
+                ("box", C.c_void_p)]
+
+
 class ChangaEwaldParams(C.Structure):
     _fields_ = [("root", C.c_double * 12), ("L", C.c_double), ("nReps", C.c_int),
                 ("fEwCut", C.c_double), ("nEwhLoop", C.c_int), ("ewt", C.c_void_p)]
@@ -186,6 +194,9 @@ CUDA_SIGNATURES = {
     "changa_gravity_graph_destroy": (None, [_VP]),
     "changa_tree_moments": (_I, [_VP, _LL, _VP, _VP, _LL, _VP, _VP]),
     "changa_direct_forces": (_I, [_VP, _LL, _VP, _LL, _D, _D, _VP, _VP]),
+    "changa_tree_build": (_VP, [_VP, _VP, _VP, _LL, _I, _VP]),
+    "changa_tree_view": (_I, [_VP, C.POINTER(ChangaTreeArrays)]),
+    "changa_tree_free": (None, [_VP]),
     "changa_walk_count": (_I, [C.POINTER(ChangaTreeView), C.POINTER(ChangaWalkParams), _VP, _VP,
                                _VP, _VP]),
     "changa_walk_fill": (_I, [C.POINTER(ChangaTreeView), C.POINTER(ChangaWalkParams), _VP, _VP,

@@ -26,7 +26,8 @@ NVCC = os.path.join(CUDA_HOME, "bin", "nvcc")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 CU_SOURCES = ["grav_lists.cu", "ewald.cu", "hostcuda.cu", "noalloc.cu", "adjoint.cu",
-              "moments.cu", "direct.cu", "walk.cu"]
+              "moments.cu", "direct.cu", "walk.cu",
+              "treebuild.cu"]
 CXX_SOURCES = ["cxx_abi.cpp", "ewald_table.cpp"]
 
 CUDA_LIB = os.path.join(BUILD, "libchanga_gb300.so")

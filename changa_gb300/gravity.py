@@ -270,7 +270,10 @@ class DeviceSystem:
             self.reqs.append(d)
         self.vars = torch.zeros((lists.n, 5), dtype=torch.float64, device=device)
         self.ewald = ewald
-        self.ewald_params = ewald.params(lists.root) if ewald else None
+        root = lists.root
+        if ewald is not None and root is None:  # a device-built tree: the root moments
+            root = self.moments[0].cpu().numpy()
+        self.ewald_params = ewald.params(root) if ewald else None
 
     def step(self, form="mixed", stream=None, zero=True):
         """Enqueues one evaluation on `stream` (torch stream handle or None for

@@ -38,7 +38,8 @@ def gpu_walk(lists, device="cuda", stream=None, timings=None):
     import torch
     lib = N.cuda_lib()
     m = lists.meta
-    t = lambda a: torch.from_numpy(np.ascontiguousarray(a)).to(device)
+    t = lambda a: (a.to(device) if isinstance(a, torch.Tensor)
+                   else torch.from_numpy(np.ascontiguousarray(a)).to(device))
     t0 = time.perf_counter()
     geom, bbox, info = t(m["node_geom"]), t(m["node_bbox"]), t(m["node_info"])
     parent, bnode = t(m["parent"]), t(m["bucket_node"])

@@ -288,6 +288,31 @@ int changa_walk_fill(const ChangaTreeView *tree, const ChangaWalkParams *p,
                      const long long *off_soft, ILCell *cells, ILCell *parts, ILCell *soft,
                      cudaStream_t stream);
 
+/* Tree build on the device (no reference counterpart; restates the host
+ * build, TreePiece.cpp:141-165 box and keys, GenericTreeNode.h:473-599
+ * split, MultipoleMoments.h:206-352, 460-526 moments and radii): positions
+ * (n x 3), masses and softenings are device FP64 arrays.  The handle owns
+ * the device arrays below until changa_tree_free; NULL on error. */
+typedef struct ChangaTree ChangaTree;
+typedef struct ChangaTreeArrays {
+  long long n, n_nodes;
+  int n_buckets;
+  const int *perm;        /* n: GPU (key) order -> input index */
+  const double *parts;    /* n x 5, GPU order */
+  const double *moments;  /* n_nodes x 12, breadth-first */
+  const double *geom;     /* n_nodes x 6 {cm.xyz, radius, soft, mass} */
+  const double *bbox;     /* n_nodes x 6 */
+  const int *info;        /* n_nodes x 4 {child0, child1, first, count} */
+  const int *parent;      /* n_nodes, -1 at the root */
+  const int *bucket_node; /* n_buckets, key order */
+  const int *leaf;        /* n: bucket node of each particle */
+  const double *box;      /* 6: the cubical bounding box */
+} ChangaTreeArrays;
+ChangaTree *changa_tree_build(const double *pos, const double *mass, const double *soft,
+                              long long n, int n_bucket, cudaStream_t stream);
+int changa_tree_view(const ChangaTree *tree, ChangaTreeArrays *out);
+void changa_tree_free(ChangaTree *tree);
+
 /* Ewald correction for parts[idx[k]] into vars[idx[k]] (idx == NULL: the
  * first n_idx particles).  form: FP64 or MIXED. */
 int changa_ewald_forces(int form, const double *parts, long long n_parts, const int *idx,

@@ -28,3 +28,16 @@ def cuda_ok(built):
         pytest.fail("GPU test run without a CUDA device")
     torch.cuda.init()
     return True
+
+
+@pytest.fixture(autouse=True)
+def _record_library_errors(request):
+    """GPU tests run the library with errors recorded rather than aborting
+    the process, so a failing call surfaces as a test failure with its
+    message."""
+    if request.node.get_closest_marker("gpu") is None:
+        yield
+        return
+    from changa_gb300 import _native as N
+    N.cuda_lib().changa_gb300_set_error_mode(N.CHANGA_ERRORS_RECORD)
+    yield
