@@ -29,6 +29,9 @@ CU_SOURCES = ["grav_lists.cu", "ewald.cu", "hostcuda.cu", "noalloc.cu", "adjoint
               "moments.cu", "direct.cu", "walk.cu",
               "treebuild.cu"]
 CXX_SOURCES = ["cxx_abi.cpp", "ewald_table.cpp"]
+# Sources whose FP64 results must equal the host code's bit for bit: no FMA
+# contraction, as the host library is compiled with -ffp-contract=off.
+NO_FMA_SOURCES = {"treebuild.cu": ["-fmad=false"], "walk.cu": ["-fmad=false"]}
 
 CUDA_LIB = os.path.join(BUILD, "libchanga_gb300.so")
 HOST_LIB = os.path.join(BUILD, "libchanga_host.so")
@@ -86,8 +89,10 @@ def build_cuda(force=False, verbose=False):
     for s in CU_SOURCES:
         o = os.path.join(BUILD, "obj", s + ".o")
         objs.append(o)
+        extra = NO_FMA_SOURCES.get(s, [])
         jobs.append([NVCC] + ARCH + ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC",
-                                     "-Xptxas", "-v"] + inc + ["-c", os.path.join(CSRC, s), "-o", o])
+                                     "-Xptxas", "-v"] + extra + inc +
+                    ["-c", os.path.join(CSRC, s), "-o", o])
     for s in CXX_SOURCES:
         o = os.path.join(BUILD, "obj", s + ".o")
         objs.append(o)

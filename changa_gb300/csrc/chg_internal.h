@@ -73,6 +73,9 @@ cudaError_t launch_ewald_fp(int form, const double* parts, long long n_parts, co
 /* runtime helpers (hostcuda.cu) */
 int sm_count();
 void count_launch(unsigned n = 1);
+/* Keeps memory freed with cudaFreeAsync cached in this device's default
+ * pool (a process-local pool attribute, set once per device). */
+void prepare_pool();
 int record_error(int code, const char* what, const char* file, int line);
 
 /* Kernel ids for the optional per-kernel event timing

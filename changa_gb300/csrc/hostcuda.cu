@@ -95,7 +95,7 @@ int sm_count() {
 /* Keeps memory freed with cudaFreeAsync cached in the default pool so
  * per-request allocations do not return to the OS at every synchronise
  * (a process-local pool attribute). */
-static void prepare_pool() {
+void prepare_pool() {
   static bool done[64] = {false};
   static std::mutex mu;
   int dev = 0;

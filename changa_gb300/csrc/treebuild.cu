@@ -15,14 +15,17 @@
  *      empty children dropped (DataManager.cpp:768-858), buckets in key
  *      order;
  *   5. per node: mass, mass-weighted softening and centre of mass, second
- *      moments about the centre of mass (MultipoleMoments.h:206-352 forms
- *      the same sums incrementally), the particle bounding box and the
+ *      moments about the centre of mass, the particle bounding box and the
  *      radius rules (bucket: farthest particle, else half the spatial cell's
  *      diagonal; internal: farthest bounding-box corner;
- *      MultipoleMoments.h:460-526, GenericTreeNode.h:219-255).
+ *      MultipoleMoments.h:206-352, 460-526, GenericTreeNode.h:219-255):
+ *      buckets add their particles one at a time (a thread per bucket),
+ *      then each level's internal nodes add their children, deepest level
+ *      first.
  *
- * The moments are direct sums per node, so they agree with the host's
- * incremental sums to rounding; everything else is exact.
+ * The arithmetic is the host build's, in its order, and this file is
+ * compiled without FMA contraction (as the host code is), so every array
+ * equals the host's bit for bit.
  */
 #include <vector>
 
@@ -306,130 +309,190 @@ __global__ void link_kernel(const LevelNode* __restrict__ nodes, const double* _
   }
 }
 
-/* Moments, box and radius of every node (one warp per node). */
-__device__ __forceinline__ double wsum(double v) {
-#pragma unroll
-  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
-  return v;
-}
-__device__ __forceinline__ double wmin(double v) {
-#pragma unroll
-  for (int o = 16; o > 0; o >>= 1) v = fmin(v, __shfl_xor_sync(0xffffffffu, v, o));
-  return v;
-}
-__device__ __forceinline__ double wmax(double v) {
-#pragma unroll
-  for (int o = 16; o > 0; o >>= 1) v = fmax(v, __shfl_xor_sync(0xffffffffu, v, o));
-  return v;
+/* Moments, box and radius of every node, as the host build forms them:
+ * buckets add their particles one at a time, internal nodes add their
+ * children (MultipoleMoments.h:206-352; the radius rules of
+ * GenericTreeNode.h:219-255 and MultipoleMoments.h:462-476).  The
+ * operations and their order are the host's, and this file is compiled
+ * without FMA contraction as the host code is, so the results are the
+ * host's bit for bit. */
+__device__ __forceinline__ void mom_add_particle(double* m, double pm, double ps, const double* p) {
+  const double m1 = m[2];
+  m[2] += pm;
+  if (m[2] == 0.0) {
+    m[1] = 0.5 * (m[1] + ps);
+    for (int k = 0; k < 3; ++k) m[3 + k] = 0.5 * (m[3 + k] + p[k]);
+    return;
+  }
+  m[1] = (m1 * m[1] + pm * ps) / m[2];
+  const double c0 = m[3], c1 = m[4], c2 = m[5];
+  m[3] = (m1 * c0 + pm * p[0]) / m[2];
+  m[4] = (m1 * c1 + pm * p[1]) / m[2];
+  m[5] = (m1 * c2 + pm * p[2]) / m[2];
+  double d0 = c0 - m[3], d1 = c1 - m[4], d2 = c2 - m[5];
+  m[6] += m1 * d0 * d0;
+  m[9] += m1 * d1 * d1;
+  m[11] += m1 * d2 * d2;
+  m[7] += m1 * d0 * d1;
+  m[8] += m1 * d0 * d2;
+  m[10] += m1 * d1 * d2;
+  d0 = p[0] - m[3];
+  d1 = p[1] - m[4];
+  d2 = p[2] - m[5];
+  m[6] += pm * d0 * d0;
+  m[9] += pm * d1 * d1;
+  m[11] += pm * d2 * d2;
+  m[7] += pm * d0 * d1;
+  m[8] += pm * d0 * d2;
+  m[10] += pm * d1 * d2;
 }
 
-__global__ void node_props_kernel(const double* __restrict__ parts, const int* __restrict__ info,
-                                  const double* __restrict__ cell, long long n_nodes,
-                                  double* __restrict__ moments, double* __restrict__ bbox,
-                                  double* __restrict__ geom) {
-  const int lane = threadIdx.x & 31;
-  const long long warps = (long long)gridDim.x * (blockDim.x >> 5);
-  for (long long node = blockIdx.x * (long long)(blockDim.x >> 5) + (threadIdx.x >> 5);
-       node < n_nodes; node += warps) {
+__device__ __forceinline__ void mom_add_node(double* m, const double* c) {
+  const double m1 = m[2];
+  m[2] += c[2];
+  if (m[2] == 0.0) {
+    m[1] = 0.5 * (m[1] + c[1]);
+    for (int k = 0; k < 3; ++k) m[3 + k] = 0.5 * (m[3 + k] + c[3 + k]);
+    return;
+  }
+  if (m1 == 0.0) {
+    for (int k = 0; k < 12; ++k) m[k] = c[k];
+    return;
+  }
+  if (c[2] == 0.0) return;
+  m[1] = (m1 * m[1] + c[2] * c[1]) / m[2];
+  const double c0 = m[3], c1 = m[4], c2 = m[5];
+  m[3] = (m1 * c0 + c[2] * c[3]) / m[2];
+  m[4] = (m1 * c1 + c[2] * c[4]) / m[2];
+  m[5] = (m1 * c2 + c[2] * c[5]) / m[2];
+  double d0 = c0 - m[3], d1 = c1 - m[4], d2 = c2 - m[5];
+  m[6] += m1 * d0 * d0;
+  m[9] += m1 * d1 * d1;
+  m[11] += m1 * d2 * d2;
+  m[7] += m1 * d0 * d1;
+  m[8] += m1 * d0 * d2;
+  m[10] += m1 * d1 * d2;
+  d0 = c[3] - m[3];
+  d1 = c[4] - m[4];
+  d2 = c[5] - m[5];
+  m[6] += c[6] + c[2] * d0 * d0;
+  m[9] += c[9] + c[2] * d1 * d1;
+  m[11] += c[11] + c[2] * d2 * d2;
+  m[7] += c[7] + c[2] * d0 * d1;
+  m[8] += c[8] + c[2] * d0 * d2;
+  m[10] += c[10] + c[2] * d1 * d2;
+}
+
+__device__ __forceinline__ void store_node(long long node, const double* m, const double* b,
+                                           double* __restrict__ moments, double* __restrict__ bbox,
+                                           double* __restrict__ geom) {
+  double* o = moments + 12 * node;
+#pragma unroll
+  for (int k = 0; k < 12; ++k) o[k] = m[k];
+  double* ob = bbox + 6 * node;
+#pragma unroll
+  for (int k = 0; k < 6; ++k) ob[k] = b[k];
+  double* g = geom + 6 * node;
+  g[0] = m[3];
+  g[1] = m[4];
+  g[2] = m[5];
+  g[3] = m[0];
+  g[4] = m[1];
+  g[5] = m[2];
+}
+
+/* Buckets (one thread each): calculateRadiusBox on the spatial cell, the
+ * particles added in key order, then the farthest particle from the centre
+ * of mass. */
+__global__ void bucket_props_kernel(const double* __restrict__ parts, const int* __restrict__ info,
+                                    const double* __restrict__ cell, long long n_nodes,
+                                    double* __restrict__ moments, double* __restrict__ bbox,
+                                    double* __restrict__ geom) {
+  for (long long node = blockIdx.x * (long long)blockDim.x + threadIdx.x; node < n_nodes;
+       node += (long long)gridDim.x * blockDim.x) {
     const int* f = info + 4 * node;
+    if (f[0] >= 0 || f[1] >= 0) continue;
     const long long first = f[2], count = f[3];
-    const bool bucket = f[0] < 0 && f[1] < 0;
-    double m = 0, ms = 0, mx = 0, my = 0, mz = 0;
-    double lo[3] = {HUGE_VAL, HUGE_VAL, HUGE_VAL}, hi[3] = {-HUGE_VAL, -HUGE_VAL, -HUGE_VAL};
-    for (long long k = first + lane; k < first + count; k += 32) {
-      const double* p = parts + 5 * k;
-      m += p[0];
-      ms += p[0] * p[1];
-      mx += p[0] * p[2];
-      my += p[0] * p[3];
-      mz += p[0] * p[4];
-      for (int a = 0; a < 3; ++a) {
-        lo[a] = fmin(lo[a], p[2 + a]);
-        hi[a] = fmax(hi[a], p[2 + a]);
-      }
-    }
-    m = wsum(m);
-    ms = wsum(ms);
-    mx = wsum(mx);
-    my = wsum(my);
-    mz = wsum(mz);
-    for (int a = 0; a < 3; ++a) {
-      lo[a] = wmin(lo[a]);
-      hi[a] = wmax(hi[a]);
-    }
-    double cx, cy, cz, soft;
-    if (m != 0.0) {
-      cx = mx / m;
-      cy = my / m;
-      cz = mz / m;
-      soft = ms / m;
-    } else {
-      cx = cy = cz = soft = 0.0;
-    }
-    double xx = 0, xy = 0, xz = 0, yy = 0, yz = 0, zz = 0, r2 = 0;
-    for (long long k = first + lane; k < first + count; k += 32) {
-      const double* p = parts + 5 * k;
-      const double dx = p[2] - cx, dy = p[3] - cy, dz = p[4] - cz;
-      xx += p[0] * dx * dx;
-      xy += p[0] * dx * dy;
-      xz += p[0] * dx * dz;
-      yy += p[0] * dy * dy;
-      yz += p[0] * dy * dz;
-      zz += p[0] * dz * dz;
-      const double ex = cx - p[2], ey = cy - p[3], ez = cz - p[4];
-      r2 = fmax(r2, ex * ex + ey * ey + ez * ez);
-    }
-    xx = wsum(xx);
-    xy = wsum(xy);
-    xz = wsum(xz);
-    yy = wsum(yy);
-    yz = wsum(yz);
-    zz = wsum(zz);
-    r2 = wmax(r2);
-    if (lane == 0) {
-      double radius;
-      if (bucket) {
-        const double* sp = cell + 6 * node;
-        const double dx = sp[3] - sp[0], dy = sp[4] - sp[1], dz = sp[5] - sp[2];
-        radius = 0.5 * sqrt(dx * dx + dy * dy + dz * dz);
-        if (count > 1 && r2 > 0.0) radius = sqrt(r2);
-        else if (radius <= 0.0) radius = 1.0;
-      } else {
-        double d1[3];
-        const double c[3] = {cx, cy, cz};
-        for (int a = 0; a < 3; ++a) {
-          const double u = c[a] - lo[a], v = hi[a] - c[a];
-          d1[a] = v > u ? v : u;
+    double m[12];
+#pragma unroll
+    for (int k = 0; k < 12; ++k) m[k] = 0.0;
+    double b[6] = {HUGE_VAL, HUGE_VAL, HUGE_VAL, -HUGE_VAL, -HUGE_VAL, -HUGE_VAL};
+    const double* sp = cell + 6 * node;
+    const double dx = sp[3] - sp[0], dy = sp[4] - sp[1], dz = sp[5] - sp[2];
+    m[0] = 0.5 * sqrt(dx * dx + dy * dy + dz * dz);
+    if (m[0] <= 0.0) {
+      if (count > 1) {
+        const double* p1 = parts + 5 * first + 2;
+        double r2 = 0.0;
+        for (long long i = first + 1; i < first + count; ++i) {
+          const double* p = parts + 5 * i + 2;
+          const double d = (p1[0] - p[0]) * (p1[0] - p[0]) + (p1[1] - p[1]) * (p1[1] - p[1]) +
+                           (p1[2] - p[2]) * (p1[2] - p[2]);
+          if (d > r2) r2 = d;
         }
-        radius = sqrt(d1[0] * d1[0] + d1[1] * d1[1] + d1[2] * d1[2]);
+        if (r2 > 0) m[0] = sqrt(r2);
+      } else {
+        m[0] = 1.0;
       }
-      double* o = moments + 12 * node;
-      o[0] = radius;
-      o[1] = soft;
-      o[2] = m;
-      o[3] = cx;
-      o[4] = cy;
-      o[5] = cz;
-      o[6] = xx;
-      o[7] = xy;
-      o[8] = xz;
-      o[9] = yy;
-      o[10] = yz;
-      o[11] = zz;
-      double* b = bbox + 6 * node;
-      for (int a = 0; a < 3; ++a) {
-        b[a] = lo[a];
-        b[3 + a] = hi[a];
+    }
+    for (long long i = first; i < first + count; ++i) {
+      const double* p = parts + 5 * i;
+      mom_add_particle(m, p[0], p[1], p + 2);
+      for (int k = 0; k < 3; ++k) {
+        if (p[2 + k] < b[k]) b[k] = p[2 + k];
+        if (p[2 + k] > b[3 + k]) b[3 + k] = p[2 + k];
       }
-      double* g = geom + 6 * node;
-      g[0] = cx;
-      g[1] = cy;
-      g[2] = cz;
-      g[3] = radius;
-      g[4] = soft;
-      g[5] = m;
+    }
+    if (count > 1) {
+      double r2 = 0.0;
+      for (long long i = first; i < first + count; ++i) {
+        const double* p = parts + 5 * i + 2;
+        const double d = (m[3] - p[0]) * (m[3] - p[0]) + (m[4] - p[1]) * (m[4] - p[1]) +
+                         (m[5] - p[2]) * (m[5] - p[2]);
+        if (d > r2) r2 = d;
+      }
+      if (r2 > 0.0) m[0] = sqrt(r2);
+    }
+    store_node(node, m, b, moments, bbox, geom);
+  }
+}
+
+/* Internal nodes of one level (one thread each), after the level below:
+ * the children's moments and boxes added in order, then the farthest
+ * corner of the box from the centre of mass. */
+__global__ void internal_props_kernel(const int* __restrict__ info, long long first_node, int width,
+                                      double* __restrict__ moments, double* __restrict__ bbox,
+                                      double* __restrict__ geom) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= width) return;
+  const long long node = first_node + i;
+  const int* f = info + 4 * node;
+  if (f[0] < 0 && f[1] < 0) return;
+  double m[12];
+#pragma unroll
+  for (int k = 0; k < 12; ++k) m[k] = 0.0;
+  double b[6] = {HUGE_VAL, HUGE_VAL, HUGE_VAL, -HUGE_VAL, -HUGE_VAL, -HUGE_VAL};
+  for (int c = 0; c < 2; ++c) {
+    const int ch = f[c];
+    if (ch < 0) continue;
+    double cm[12];
+#pragma unroll
+    for (int k = 0; k < 12; ++k) cm[k] = moments[12 * (size_t)ch + k];
+    mom_add_node(m, cm);
+    const double* cb = bbox + 6 * (size_t)ch;
+    for (int k = 0; k < 3; ++k) {
+      if (cb[k] < b[k]) b[k] = cb[k];
+      if (cb[3 + k] > b[3 + k]) b[3 + k] = cb[3 + k];
     }
   }
+  double d1[3];
+  for (int k = 0; k < 3; ++k) {
+    d1[k] = m[3 + k] - b[k];
+    const double d2 = b[3 + k] - m[3 + k];
+    if (d2 > d1[k]) d1[k] = d2;
+  }
+  m[0] = sqrt(d1[0] * d1[0] + d1[1] * d1[1] + d1[2] * d1[2]);
+  store_node(node, m, b, moments, bbox, geom);
 }
 
 /* Buckets in key order: a bucket starts at particle `first`; every
@@ -509,13 +572,16 @@ struct ChangaTree {
   int* bucket_node = nullptr;    // n_buckets
   int* leaf = nullptr;           // n
   double* box = nullptr;         // 6
-  std::vector<void*> blocks;
+  std::vector<void*> blocks;     // from the device's default pool
 };
 
 extern "C" void changa_tree_free(ChangaTree* t) {
   if (!t) return;
+  /* the arrays may be in use on any stream: wait as cudaFree would, then
+   * hand the blocks back to the pool */
+  cudaDeviceSynchronize();
   for (void* p : t->blocks)
-    if (p) cudaFree(p);
+    if (p) cudaFreeAsync(p, 0);
   delete t;
 }
 
@@ -525,31 +591,49 @@ extern "C" ChangaTree* changa_tree_build(const double* pos, const double* mass, 
     record_error(CHANGA_E_INVALID_ARG, "changa_tree_build: arguments", __FILE__, __LINE__);
     return nullptr;
   }
+  prepare_pool();
   ChangaTree* t = new ChangaTree();
   t->n = n;
   t->n_bucket = n_bucket;
-  auto dmalloc = [&](size_t bytes) -> void* {
+  /* tree arrays live as long as the handle; scratch is freed (back to the
+   * pool, stream-ordered) before the build returns */
+  std::vector<void*> scratch;
+  auto alloc = [&](size_t bytes, bool keep) -> void* {
     void* p = nullptr;
-    if (cudaMalloc(&p, bytes < 256 ? 256 : bytes) != cudaSuccess) return nullptr;
-    t->blocks.push_back(p);
+    if (cudaMallocAsync(&p, bytes < 256 ? 256 : bytes, s) != cudaSuccess) return nullptr;
+    (keep ? t->blocks : scratch).push_back(p);
     return p;
   };
+  auto drop = [&](void* p) {
+    for (auto& b : scratch)
+      if (b == p) {
+        cudaFreeAsync(b, s);
+        b = nullptr;
+      }
+  };
+  auto release_scratch = [&]() {
+    for (void* p : scratch)
+      if (p) cudaFreeAsync(p, s);
+    scratch.clear();
+  };
   auto fail = [&](const char* what) -> ChangaTree* {
-    record_error(cudaGetLastError() != cudaSuccess ? (int)cudaErrorUnknown : CHANGA_E_INVALID_ARG,
-                 what, __FILE__, __LINE__);
+    const cudaError_t e = cudaGetLastError();
+    record_error(e != cudaSuccess ? (int)e : CHANGA_E_INVALID_ARG, what, __FILE__, __LINE__);
+    release_scratch();
     changa_tree_free(t);
     return nullptr;
   };
   /* 1-2: box and keys */
   const int gb = grid_n(n, 256);
-  float* part_box = (float*)dmalloc((size_t)gb * 6 * sizeof(float));
-  t->box = (double*)dmalloc(6 * sizeof(double));
-  unsigned long long* k0 = (unsigned long long*)dmalloc((size_t)n * 8);
-  unsigned long long* k1 = (unsigned long long*)dmalloc((size_t)n * 8);
-  int* v0 = (int*)dmalloc((size_t)n * 4);
-  int* v1 = (int*)dmalloc((size_t)n * 4);
+  float* part_box = (float*)alloc((size_t)gb * 6 * sizeof(float), false);
+  t->box = (double*)alloc(6 * sizeof(double), true);
+  unsigned long long* k0 = (unsigned long long*)alloc((size_t)n * 8, false);
+  unsigned long long* k1 = (unsigned long long*)alloc((size_t)n * 8, false);
+  /* 16 passes: the sorted order ends in the first value buffer */
+  int* v0 = (int*)alloc((size_t)n * 4, true);
+  int* v1 = (int*)alloc((size_t)n * 4, false);
   const int tiles = (int)((n + kSortTile - 1) / kSortTile);
-  int* counts = (int*)dmalloc((size_t)tiles * kDigits * 4);
+  int* counts = (int*)alloc((size_t)tiles * kDigits * 4, false);
   if (!part_box || !t->box || !k0 || !k1 || !v0 || !v1 || !counts) return fail("tree: memory");
   box_partial_kernel<<<gb, 256, 0, s>>>(pos, n, part_box);
   box_final_kernel<<<1, 1, 0, s>>>(part_box, gb, t->box);
@@ -567,7 +651,10 @@ extern "C" ChangaTree* changa_tree_build(const double* pos, const double* mass, 
   }
   if (cudaGetLastError() != cudaSuccess) return fail("tree: sort");
   t->perm = v0;
-  t->parts = (double*)dmalloc((size_t)n * 5 * sizeof(double));
+  drop(k1);
+  drop(v1);
+  drop(counts);
+  t->parts = (double*)alloc((size_t)n * 5 * sizeof(double), true);
   if (!t->parts) return fail("tree: memory");
   gather_parts_kernel<<<grid_n(n, 256), 256, 0, s>>>(pos, mass, soft, t->perm, n, t->parts);
   count_launch();
@@ -575,29 +662,30 @@ extern "C" ChangaTree* changa_tree_build(const double* pos, const double* mass, 
    * so the node count has no tight bound: the node arrays grow by doubling
    * as the levels are built. */
   long long cap = 4 * (n / n_bucket) + 64;
-  t->info = (int*)dmalloc((size_t)cap * 4 * sizeof(int));
-  t->parent = (int*)dmalloc((size_t)cap * sizeof(int));
-  int* levels = (int*)dmalloc((size_t)cap * sizeof(int));
-  double* cell = (double*)dmalloc((size_t)cap * 6 * sizeof(double));
+  t->info = (int*)alloc((size_t)cap * 4 * sizeof(int), true);
+  t->parent = (int*)alloc((size_t)cap * sizeof(int), true);
+  int* levels = (int*)alloc((size_t)cap * sizeof(int), false);
+  double* cell = (double*)alloc((size_t)cap * 6 * sizeof(double), false);
   auto grow = [&](long long need) -> bool {
     long long nc = cap;
     while (nc < need) nc *= 2;
     if (nc == cap) return true;
     void* fields[4] = {t->info, t->parent, levels, cell};
     const size_t width[4] = {4 * sizeof(int), sizeof(int), sizeof(int), 6 * sizeof(double)};
+    const bool keep[4] = {true, true, false, false};
     void* fresh[4];
     for (int k = 0; k < 4; ++k) {
-      fresh[k] = dmalloc((size_t)nc * width[k]);
+      fresh[k] = alloc((size_t)nc * width[k], keep[k]);
       if (!fresh[k]) return false;
       if (cudaMemcpyAsync(fresh[k], fields[k], (size_t)cap * width[k], cudaMemcpyDeviceToDevice,
                           s) != cudaSuccess)
         return false;
     }
-    if (cudaStreamSynchronize(s) != cudaSuccess) return false;
     for (int k = 0; k < 4; ++k) {
-      for (auto& b : t->blocks)
+      auto& list = keep[k] ? t->blocks : scratch;
+      for (auto& b : list)
         if (b == fields[k]) {
-          cudaFree(b);
+          cudaFreeAsync(b, s);
           b = nullptr;
         }
     }
@@ -608,14 +696,15 @@ extern "C" ChangaTree* changa_tree_build(const double* pos, const double* mass, 
     cap = nc;
     return true;
   };
-  LevelNode* lv[2] = {(LevelNode*)dmalloc((size_t)n * sizeof(LevelNode) + 16),
-                      (LevelNode*)dmalloc((size_t)n * sizeof(LevelNode) + 16)};
-  double* sp[2] = {(double*)dmalloc((size_t)n * 6 * sizeof(double) + 64),
-                   (double*)dmalloc((size_t)n * 6 * sizeof(double) + 64)};
-  int* nchild = (int*)dmalloc((size_t)n * sizeof(int) + 16);
-  int* mid = (int*)dmalloc((size_t)n * sizeof(int) + 16);
+  LevelNode* lv[2] = {(LevelNode*)alloc((size_t)n * sizeof(LevelNode) + 16, false),
+                      (LevelNode*)alloc((size_t)n * sizeof(LevelNode) + 16, false)};
+  double* sp[2] = {(double*)alloc((size_t)n * 6 * sizeof(double) + 64, false),
+                   (double*)alloc((size_t)n * 6 * sizeof(double) + 64, false)};
+  int* nchild = (int*)alloc((size_t)n * sizeof(int) + 16, false);
+  int* mid = (int*)alloc((size_t)n * sizeof(int) + 16, false);
+  int* pinned = nullptr;  // per-level read-back: last scan value, mid, node
   if (!t->info || !t->parent || !levels || !cell || !lv[0] || !lv[1] || !sp[0] || !sp[1] ||
-      !nchild || !mid)
+      !nchild || !mid || cudaMallocHost((void**)&pinned, 4 * sizeof(int)) != cudaSuccess)
     return fail("tree: memory");
   {
     const LevelNode root{0, (int)n};
@@ -623,50 +712,69 @@ extern "C" ChangaTree* changa_tree_build(const double* pos, const double* mass, 
     if (cudaMemcpyAsync(lv[0], &root, sizeof(root), cudaMemcpyHostToDevice, s) != cudaSuccess ||
         cudaMemcpyAsync(sp[0], t->box, 6 * sizeof(double), cudaMemcpyDeviceToDevice, s) !=
             cudaSuccess ||
-        cudaMemcpyAsync(t->parent, &minus1, sizeof(int), cudaMemcpyHostToDevice, s) != cudaSuccess)
+        cudaMemcpyAsync(t->parent, &minus1, sizeof(int), cudaMemcpyHostToDevice, s) != cudaSuccess) {
+      cudaFreeHost(pinned);
       return fail("tree: root");
+    }
   }
+  std::vector<long long> level_base;
+  std::vector<int> level_width;
   long long base = 0;
   int width = 1, cur = 0;
   for (int level = 0; width > 0 && level <= 61; ++level) {
     split_kernel<<<(width + 255) / 256, 256, 0, s>>>(k0, lv[cur], width, level, n_bucket, nchild, mid);
     /* exclusive scan of the children counts; the total gives the next width */
     scan_kernel<<<1, 1024, 0, s>>>(nchild, width);
-    int last_scan = 0, last_n = 0, last_mid = 0;
-    LevelNode last_node;
-    cudaMemcpyAsync(&last_scan, nchild + width - 1, sizeof(int), cudaMemcpyDeviceToHost, s);
-    cudaMemcpyAsync(&last_mid, mid + width - 1, sizeof(int), cudaMemcpyDeviceToHost, s);
-    cudaMemcpyAsync(&last_node, lv[cur] + width - 1, sizeof(LevelNode), cudaMemcpyDeviceToHost, s);
-    if (cudaStreamSynchronize(s) != cudaSuccess) return fail("tree: level");
+    cudaMemcpyAsync(pinned, nchild + width - 1, sizeof(int), cudaMemcpyDeviceToHost, s);
+    cudaMemcpyAsync(pinned + 1, mid + width - 1, sizeof(int), cudaMemcpyDeviceToHost, s);
+    cudaMemcpyAsync(pinned + 2, lv[cur] + width - 1, sizeof(LevelNode), cudaMemcpyDeviceToHost, s);
+    if (cudaStreamSynchronize(s) != cudaSuccess) {
+      cudaFreeHost(pinned);
+      return fail("tree: level");
+    }
+    const int last_scan = pinned[0], last_mid = pinned[1];
+    const LevelNode last_node{pinned[2], pinned[3]};
+    int last_n = 0;
     if (last_mid >= 0)
       last_n = (last_mid > last_node.first) + (last_node.first + last_node.count > last_mid);
     const int next_width = last_scan + last_n;
-    if (base + width + next_width > cap && !grow(base + width + next_width))
+    if (base + width + next_width > cap && !grow(base + width + next_width)) {
+      cudaFreeHost(pinned);
       return fail("tree: node memory");
+    }
     link_kernel<<<(width + 255) / 256, 256, 0, s>>>(lv[cur], sp[cur], width, level, (int)base,
                                                     (int)(base + width), nchild, mid, lv[cur ^ 1],
                                                     sp[cur ^ 1], t->info, t->parent, levels, cell);
     count_launch(3);
+    level_base.push_back(base);
+    level_width.push_back(width);
     base += width;
     width = next_width;
     cur ^= 1;
   }
+  cudaFreeHost(pinned);
   if (cudaGetLastError() != cudaSuccess) return fail("tree: levels");
   t->n_nodes = base;
-  /* 5: node properties */
-  t->moments = (double*)dmalloc((size_t)base * 12 * sizeof(double));
-  t->geom = (double*)dmalloc((size_t)base * 6 * sizeof(double));
-  t->bbox = (double*)dmalloc((size_t)base * 6 * sizeof(double));
+  /* 5: node properties, buckets first, then the internal nodes level by
+   * level from the deepest up */
+  t->moments = (double*)alloc((size_t)base * 12 * sizeof(double), true);
+  t->geom = (double*)alloc((size_t)base * 6 * sizeof(double), true);
+  t->bbox = (double*)alloc((size_t)base * 6 * sizeof(double), true);
   if (!t->moments || !t->geom || !t->bbox) return fail("tree: memory");
-  node_props_kernel<<<grid_n((base + 7) / 8, 1, 16), 256, 0, s>>>(t->parts, t->info, cell, base,
-                                                                  t->moments, t->bbox, t->geom);
+  bucket_props_kernel<<<grid_n(base, 128, 16), 128, 0, s>>>(t->parts, t->info, cell, base,
+                                                            t->moments, t->bbox, t->geom);
   count_launch();
+  for (int l = (int)level_base.size() - 1; l >= 0; --l) {
+    internal_props_kernel<<<(level_width[l] + 127) / 128, 128, 0, s>>>(
+        t->info, level_base[l], level_width[l], t->moments, t->bbox, t->geom);
+    count_launch();
+  }
   /* buckets in key order, and each particle's bucket */
-  int* at = (int*)dmalloc((size_t)n * sizeof(int));
-  t->bucket_node = (int*)dmalloc((size_t)n * sizeof(int));
-  t->leaf = (int*)dmalloc((size_t)n * sizeof(int));
+  int* at = (int*)alloc((size_t)n * sizeof(int), false);
+  t->bucket_node = (int*)alloc((size_t)n * sizeof(int), true);
+  t->leaf = (int*)alloc((size_t)n * sizeof(int), true);
   const int ctiles = (int)((n + kCompactTile - 1) / kCompactTile);
-  int* tile_count = (int*)dmalloc((size_t)(ctiles + 1) * sizeof(int));
+  int* tile_count = (int*)alloc((size_t)(ctiles + 1) * sizeof(int), false);
   if (!at || !t->bucket_node || !t->leaf || !tile_count) return fail("tree: memory");
   cudaMemsetAsync(at, 0xff, (size_t)n * sizeof(int), s);
   bucket_mark_kernel<<<grid_n(base, 256), 256, 0, s>>>(t->info, base, at, t->leaf);
@@ -677,6 +785,7 @@ extern "C" ChangaTree* changa_tree_build(const double* pos, const double* mass, 
   count_launch(4);
   int h_nb = 0;
   cudaMemcpyAsync(&h_nb, tile_count + ctiles, sizeof(int), cudaMemcpyDeviceToHost, s);
+  release_scratch();
   if (cudaStreamSynchronize(s) != cudaSuccess) return fail("tree: buckets");
   t->n_buckets = h_nb;
   return t;

@@ -17,8 +17,17 @@
  * instead of level order.
  *
  * Two launches: a count pass (per-bucket list lengths) and, after the
- * caller has turned the counts into offsets, a fill pass.  All geometry is
- * FP64, the same expressions as the host walk, so the decisions agree.
+ * caller has turned the counts into offsets, a fill pass.
+ *
+ * Decisions equal the host walk's FP64 decisions.  GB300 issues FP64 at a
+ * small fraction of its FP32 rate, so each opening test is first made in
+ * FP32 from rounded copies of the node data, with a bound on how far the
+ * FP32 distance can lie from the FP64 one: the clipped box distance and the
+ * farthest-corner distance are 1-Lipschitz in the coordinates, so an input
+ * error of delta moves a squared distance g^2 by at most 2 g delta +
+ * delta^2.  Only tests whose FP32 value lies within that margin of the
+ * threshold are repeated in FP64, with the host's expressions (this file is
+ * compiled without FMA contraction, as the host code is).
  */
 #include "chg_internal.h"
 
@@ -50,7 +59,42 @@ struct WalkArgs {
   int2* parts;
   int2* soft;
   int* error;
+  /* FP32 copies for the screening test */
+  const float4* nodef;  // n_nodes: {cm.xyz, rn32(opening radius^2)}
+  const float4* boxf;   // 2 n_nodes: {lesser.xyz, 0}, {greater.xyz, 0}
+  float period32;
 };
+
+constexpr float kU = 5.9604645e-08f;  // 2^-24, the FP32 unit roundoff
+
+/* FP32 copies of each node's centre, box and opening radius squared, the
+ * last formed in FP64 exactly as open_criterion forms it. */
+__global__ void walk_prep_kernel(const double* __restrict__ geom, const double* __restrict__ bbox,
+                                 long long n_nodes, double theta, float4* __restrict__ nodef,
+                                 float4* __restrict__ boxf) {
+  for (long long g = blockIdx.x * (long long)blockDim.x + threadIdx.x; g < n_nodes;
+       g += (long long)gridDim.x * blockDim.x) {
+    const double* gg = geom + 6 * g;
+    const double kOpenGeom = 2.0 / sqrt(3.0);
+    double radius = kOpenGeom * gg[3] / theta;
+    if (radius < gg[3]) radius = gg[3];
+    nodef[g] = make_float4((float)gg[0], (float)gg[1], (float)gg[2], (float)(radius * radius));
+    const double* b = bbox + 6 * g;
+    boxf[2 * g] = make_float4((float)b[0], (float)b[1], (float)b[2], 0.0f);
+    boxf[2 * g + 1] = make_float4((float)b[3], (float)b[4], (float)b[5], 0.0f);
+  }
+}
+
+/* v <= r2 decided from an FP32 value v within e of the FP64 one and r2 =
+ * rn32 of the FP64 threshold: 1 certainly, 0 certainly not, -1 too close.
+ * The margins carry one extra unit roundoff for the rounding of the two
+ * sums compared here; NaN or infinity give -1. */
+__device__ __forceinline__ int screen_le(float v, float e, float r2) {
+  const float er = 2.0f * kU * r2;
+  if (v + e < r2 - er) return 1;
+  if (v - e > r2 + er) return 0;
+  return -1;
+}
 
 __device__ __forceinline__ void decode(int off, double period, double* o) {
   o[0] = ((off & 7) - 3) * period;
@@ -112,6 +156,56 @@ __device__ int open_criterion(const WalkArgs& a, int g, int local, bool local_bu
   return d2 <= rm * rm ? 1 : 0;
 }
 
+/* open_criterion screened in FP32.  Per axis the FP32 inputs (centre,
+ * replica offset, box faces) and the FP32 sums and differences carry at
+ * most u (3|cm| + 4|o| + 2|b|) of error against the FP64 values; delta =
+ * 6u (|cm| + |o| + |lesser| + |greater|) covers that and the FP64 path's own
+ * rounding (the 1e-30 floor covers conversions that land on FP32
+ * subnormals).  Squares and the three-term sum add 2u of the total,
+ * bounded here by 4u. */
+__device__ int open_criterion_screened(const WalkArgs& a, int g, int local, bool local_bucket,
+                                       int off) {
+  if (a.info[4 * (size_t)g + 3] <= 6) return 1;
+  const float4 nf = a.nodef[g];
+  const float4 lo = a.boxf[2 * (size_t)local], hi = a.boxf[2 * (size_t)local + 1];
+  const float cm[3] = {nf.x, nf.y, nf.z};
+  const float o[3] = {(float)((off & 7) - 3) * a.period32,
+                      (float)(((off >> 3) & 7) - 3) * a.period32,
+                      (float)(((off >> 6) & 7) - 3) * a.period32};
+  const float bl[3] = {lo.x, lo.y, lo.z}, bh[3] = {hi.x, hi.y, hi.z};
+  float c[3], dl[3];
+  float d2 = 0.0f, e = 0.0f;
+#pragma unroll
+  for (int k = 0; k < 3; ++k) {
+    c[k] = cm[k] + o[k];
+    dl[k] = 6.0f * kU * (fabsf(cm[k]) + fabsf(o[k]) + fabsf(bl[k]) + fabsf(bh[k])) + 1e-30f;
+    const float gk = fmaxf(0.0f, fmaxf(bl[k] - c[k], c[k] - bh[k]));
+    d2 += gk * gk;
+    e += 2.0f * gk * dl[k] + 3.0f * dl[k] * dl[k];
+  }
+  e += 4.0f * kU * d2;
+  const int inter = screen_le(d2, e, nf.w);
+  if (inter < 0) return open_criterion(a, g, local, local_bucket, off);
+  if (inter == 1) {
+    if (local_bucket) return 1;
+    float f2 = 0.0f, ef = 0.0f;
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+      const float mk = fmaxf(fabsf(c[k] - bl[k]), fabsf(bh[k] - c[k]));
+      f2 += mk * mk;
+      ef += 2.0f * mk * dl[k] + 3.0f * dl[k] * dl[k];
+    }
+    ef += 4.0f * kU * f2;
+    const int far = screen_le(f2, ef, nf.w);
+    if (far < 0) return open_criterion(a, g, local, local_bucket, off);
+    return far ? 1 : -1;
+  }
+  /* outside the opening sphere: accepted, unless the hexadecapole rules
+   * (softening, monopole radius) open it, which stay in FP64 */
+  if (a.order != 4) return 0;
+  return open_criterion(a, g, local, local_bucket, off);
+}
+
 template <bool FILL>
 __global__ void __launch_bounds__(kWalkThreads) walk_kernel(const WalkArgs a) {
   const int b = blockIdx.x * kWalkThreads + threadIdx.x;
@@ -153,7 +247,7 @@ __global__ void __launch_bounds__(kWalkThreads) walk_kernel(const WalkArgs a) {
     if (g < 0 || g >= a.n_nodes) continue;  // memory safety
     const int local = chain[level];
     const bool local_bucket = level == depth;
-    const int open = open_criterion(a, g, local, local_bucket, code);
+    const int open = open_criterion_screened(a, g, local, local_bucket, code);
     const int* gi = a.info + 4 * (size_t)g;
     if (open == 0) {
       bool softened = false;
@@ -215,9 +309,21 @@ static int walk_launch(const ChangaTreeView* t, const ChangaWalkParams* p, bool 
       p->n_replicas < 0 || p->n_replicas > 3)
     return record_error(CHANGA_E_INVALID_ARG, "walk: arguments", __FILE__, __LINE__);
   if (t->n_buckets == 0) return 0;
-  int* err = nullptr;
-  CHG_CUDA(cudaMallocAsync((void**)&err, sizeof(int), s));
+  prepare_pool();
+  char* block = nullptr;
+  const size_t nn = (size_t)t->n_nodes;
+  CHG_CUDA(cudaMallocAsync((void**)&block, 256 + nn * 3 * sizeof(float4), s));
+  int* err = (int*)block;
+  float4* nodef = (float4*)(block + 256);
+  float4* boxf = nodef + nn;
   CHG_CUDA(cudaMemsetAsync(err, 0, sizeof(int), s));
+  {
+    long long g = (t->n_nodes + 255) / 256;
+    const long long cap = (long long)sm_count() * 8;
+    walk_prep_kernel<<<(int)(g < cap ? g : cap), 256, 0, s>>>(t->geom, t->bbox, t->n_nodes,
+                                                              p->theta, nodef, boxf);
+    count_launch();
+  }
   WalkArgs a;
   a.geom = t->geom;
   a.bbox = t->bbox;
@@ -241,6 +347,9 @@ static int walk_launch(const ChangaTreeView* t, const ChangaWalkParams* p, bool 
   a.parts = (int2*)parts;
   a.soft = (int2*)soft;
   a.error = err;
+  a.nodef = nodef;
+  a.boxf = boxf;
+  a.period32 = (float)p->period;
   const int grid = (t->n_buckets + kWalkThreads - 1) / kWalkThreads;
   if (fill) walk_kernel<true><<<grid, kWalkThreads, 0, s>>>(a);
   else walk_kernel<false><<<grid, kWalkThreads, 0, s>>>(a);
@@ -248,7 +357,7 @@ static int walk_launch(const ChangaTreeView* t, const ChangaWalkParams* p, bool 
   CHG_CUDA(cudaGetLastError());
   int h_err = 0;
   CHG_CUDA(cudaMemcpyAsync(&h_err, err, sizeof(int), cudaMemcpyDeviceToHost, s));
-  CHG_CUDA(cudaFreeAsync(err, s));
+  CHG_CUDA(cudaFreeAsync(block, s));
   CHG_CUDA(cudaStreamSynchronize(s));
   if (h_err)
     return record_error(CHANGA_E_TOO_LARGE, h_err == 1 ? "walk: tree deeper than 64 levels"

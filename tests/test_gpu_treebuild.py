@@ -1,7 +1,7 @@
 """Tree build on the GPU against the host build: same key order, the same
 breadth-first topology, bucket order and particle ranges, the same
-bounding boxes; moments and radii equal to rounding; and the GPU walk over
-the device tree gives the host walk's lists, so forces agree."""
+bounding boxes, moments and radii, bit for bit; and the GPU walk over the
+device tree gives the host walk's lists, so forces agree."""
 import numpy as np
 import pytest
 
@@ -18,7 +18,7 @@ def _dev(a):
     return torch.from_numpy(np.ascontiguousarray(a, dtype=np.float64)).cuda()
 
 
-def _compare(p, n_bucket, theta, period=0.0, ewald=None, degenerate=False):
+def _compare(p, n_bucket, theta, period=0.0, ewald=None):
     L = tree.build_lists(p["pos"], p["mass"], p["soft"], n_bucket=n_bucket, theta=theta,
                          period=period)
     T = DeviceTree(_dev(p["pos"]), _dev(p["mass"]), _dev(p["soft"]), n_bucket=n_bucket,
@@ -32,16 +32,10 @@ def _compare(p, n_bucket, theta, period=0.0, ewald=None, degenerate=False):
         assert np.array_equal(T.meta["leaf"].cpu().numpy(), L.meta["leaf"])
         assert np.array_equal(T.meta["node_bbox"].cpu().numpy(), L.meta["node_bbox"])
         assert np.array_equal(T.parts.cpu().numpy(), L.parts)
-        mo, ref = T.moments.cpu().numpy(), L.moments
-        scale = np.abs(ref).max(axis=0) + 1e-300
-        if degenerate:
-            # a bucket of coincident particles: the host's incremental
-            # centre of mass leaves a 1e-32 spread that its radius rule
-            # turns into a 1e-16 radius, the exact sums give none and keep
-            # the cell radius; every other quantity must agree
-            assert (np.abs(mo - ref)[:, 1:] / scale[1:]).max() < 1e-12
-            return
-        assert (np.abs(mo - ref) / scale).max() < 1e-12
+        # the device sums are the host's, in its order, without FMA
+        # contraction: bit for bit
+        assert np.array_equal(T.moments.cpu().numpy(), L.moments)
+        assert np.array_equal(T.meta["node_geom"].cpu().numpy(), L.meta["node_geom"])
         cells, plist, _ = gpu_walk(T)
         nb = T.n_buckets
         assert same_entries(L.cells, cells, nb) and same_entries(L.plist, plist, nb)
@@ -69,5 +63,5 @@ def test_treebuild_coincident_and_tiny(cuda_ok):
     pos = rng.uniform(-1, 1, (3000, 3))
     pos[1000:1100] = pos[5]
     p = dict(pos=pos, mass=np.full(3000, 1 / 3000), soft=np.full(3000, 0.02))
-    _compare(p, 1, 0.6, degenerate=True)
-    _compare(p, 7, 0.6, degenerate=True)
+    _compare(p, 1, 0.6)
+    _compare(p, 7, 0.6)
