@@ -327,20 +327,58 @@ def measure_adjoint(leapfrog=True, reps=20, tune=True):
            "event_forward_ms": ev[0], "event_vjp_ms": ev[1],
            "event_vjp_over_forward": ev[1] / ev[0]}
     if leapfrog:
-        lf = Leapfrog(m, s, 0.005, 16, theta=wl.theta, n_bucket=wl.n_bucket, checkpoint_every=4)
         w = loss_weights(wl.n, 13)
+        out["leapfrog"] = {"steps": 16, "dt": 0.005, "checkpoint_every": 4}
+        # trees rebuilt every step on the host (build, walk, serialise,
+        # upload) or on the GPU (DeviceTree + gpu_walk)
+        for builder in ("host", "device"):
+            lf = Leapfrog(m, s, 0.005, 16, theta=wl.theta, n_bucket=wl.n_bucket,
+                          checkpoint_every=4, builder=builder)
+            if builder == "device":  # first-use costs (module loads) out of the timing
+                TreeStep(x, m, s, theta=wl.theta, n_bucket=wl.n_bucket, builder="device")
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            lf.forward(x, v)
+            torch.cuda.synchronize()
+            t1 = time.perf_counter()
+            lf.backward(w, torch.zeros_like(w))
+            torch.cuda.synchronize()
+            t2 = time.perf_counter()
+            out["leapfrog"][builder + "_trees"] = {
+                "forward_wall_s": t1 - t0, "reverse_wall_s": t2 - t1,
+                "tree_builds": lf.tree_builds, "force_evals": lf.force_evals}
+    return out
+
+
+def measure_device_pipeline(wl, pts, interactions, reps=3):
+    """Positions already on the device to device-resident lists: the tree
+    built on the GPU (changa_tree_build) and walked there
+    (changa_walk_count/fill); best of `reps` after one untimed run.  The
+    interaction count must equal the host lists'."""
+    import numpy as np
+    import torch
+    from changa_gb300.gputree import DeviceTree
+    from changa_gb300.walk import gpu_walk
+    t = lambda a: torch.from_numpy(np.ascontiguousarray(a, dtype=np.float64)).cuda()
+    pos, m, s = t(pts["pos"]), t(pts["mass"]), t(pts["soft"])
+    best = None
+    for rep in range(reps + 1):
         torch.cuda.synchronize()
         t0 = time.perf_counter()
-        lf.forward(x, v)
+        tree = DeviceTree(pos, m, s, n_bucket=wl.n_bucket, theta=wl.theta, period=wl.period)
         torch.cuda.synchronize()
         t1 = time.perf_counter()
-        lf.backward(w, torch.zeros_like(w))
+        cells, plist, _ = gpu_walk(tree)
         torch.cuda.synchronize()
         t2 = time.perf_counter()
-        out["leapfrog"] = {"steps": 16, "dt": 0.005, "checkpoint_every": 4,
-                           "forward_wall_s": t1 - t0, "reverse_wall_s": t2 - t1,
-                           "tree_builds": lf.tree_builds, "force_evals": lf.force_evals}
-    return out
+        n_int = cells.interactions() + plist.interactions()
+        tree.close()
+        del cells, plist
+        if rep and (best is None or t2 - t0 < best["tree_build_s"] + best["walk_s"]):
+            best = {"tree_build_s": t1 - t0, "walk_s": t2 - t1, "n_nodes": tree.n_nodes,
+                    "n_buckets": tree.n_buckets}
+    best["interactions_match"] = n_int == interactions
+    return best
 
 
 def batched_workload(wl):
@@ -360,18 +398,22 @@ def main_ours(args):
     world, rank, local = dist_setup(args)
     lib = N.cuda_lib()
     wl = WORKLOADS[args.workload]
+    pts = None if batched_workload(wl) else wl.particles()
     t0 = time.perf_counter()
-    lists = wl.lists()
+    lists = wl.lists(particles=pts)
     t_walk = time.perf_counter() - t0
     ew = wl.ewald_config()
     I = lists.interactions
     walk_gpu = None
+    device_pipeline = None
     if not batched_workload(wl):
         # the same lists built on the GPU (changa_walk_count/fill), timed
         from changa_gb300.walk import gpu_walk
         gpu_walk(lists)
         walk_gpu = {}
         gpu_walk(lists, timings=walk_gpu)
+        device_pipeline = measure_device_pipeline(wl, pts, I)
+        del pts
     I_c, I_p = lists.cells.interactions(), lists.plist.interactions()
     ds = gravity.DeviceSystem(lists, device="cuda", ewald=ew)
     stream = torch.cuda.current_stream()
@@ -598,6 +640,7 @@ def main_ours(args):
                                  "write between timed steps" %
                                  ((lists.cells.list.nbytes + lists.plist.list.nbytes) / 1e9),
                               host_walk_s=t_walk, gpu_walk_s=walk_gpu and walk_gpu.get("walk_s"),
+                              device_pipeline=device_pipeline,
                               fp64_form=fp64, kernels=kshare,
                               batched_graph=batched, sequential_plain=seq,
                               autotune=tuning,

@@ -12,8 +12,8 @@ same tree, walk and interaction lists:
   the adjoint differentiates: lists and topology fixed, moments exact.
 * ``Leapfrog``  -- kick-drift-kick integration (the reference's
   Main::advanceBigStep order: half kick, drift, half kick;
-  ParallelGravity.cpp) with the tree rebuilt every step on the host, and
-  its reverse pass with checkpoints every k steps: the forward keeps only
+  ParallelGravity.cpp) with the tree rebuilt every step (on the host, or on
+  the GPU with builder="device"), and its reverse pass with checkpoints every k steps: the forward keeps only
   (x, v) at every k-th step; the reverse pass re-runs each k-step segment
   from its checkpoint (rebuilding the same trees, since the build and the
   forces are deterministic) and walks it backwards.
@@ -37,11 +37,23 @@ from .tree import build_lists
 
 
 class TreeStep:
-    """Tree, lists and device arrays for one set of positions."""
+    """Tree, lists and device arrays for one set of positions.
 
-    def __init__(self, x, mass, soft, theta=0.7, n_bucket=16, device="cuda", nthreads=0):
+    builder "host": the host tree build, walk and serialisation
+    (tree.build_lists), uploaded.  builder "device": the tree built on the
+    GPU (gputree.DeviceTree) and walked there (walk.gpu_walk); the positions
+    never leave the device.  Both give the same tree and the same
+    per-bucket entries."""
+
+    def __init__(self, x, mass, soft, theta=0.7, n_bucket=16, device="cuda", nthreads=0,
+                 builder="host"):
         import torch
         self.torch = torch
+        if builder == "device":
+            self._init_device(x, mass, soft, theta, n_bucket, device)
+            return
+        if builder != "host":
+            raise ValueError("builder must be 'host' or 'device'")
         x_h = x.detach().cpu().numpy() if hasattr(x, "detach") else np.asarray(x)
         m_h = mass.detach().cpu().numpy() if hasattr(mass, "detach") else np.asarray(mass)
         s_h = soft.detach().cpu().numpy() if hasattr(soft, "detach") else np.asarray(soft)
@@ -56,6 +68,25 @@ class TreeStep:
         self.first = t(lists.meta["first"])
         self.count = t(lists.meta["count"])
         self.interactions = lists.interactions
+
+    def _init_device(self, x, mass, soft, theta, n_bucket, device):
+        from .gputree import DeviceTree
+        from .walk import gpu_walk
+        torch = self.torch
+        f = lambda a: torch.as_tensor(a, dtype=torch.float64, device=device).detach()
+        tree = DeviceTree(f(x), f(mass), f(soft), n_bucket=n_bucket, theta=theta)
+        cells, plist, _ = gpu_walk(tree)
+        self.tree = tree
+        self.lists = tree
+        self.n = tree.n
+        self.ds = DeviceSystem(tree, device=device, device_reqs=[cells, plist])
+        self.perm = tree.perm.long()
+        self.parent = tree.meta["parent"]
+        self.leaf = tree.meta["leaf"]
+        info = tree.meta["node_info"]
+        self.first = info[:, 2].contiguous()
+        self.count = info[:, 3].contiguous()
+        self.interactions = cells.interactions() + plist.interactions()
 
     def _stream(self, stream):
         return stream if stream is not None else self.torch.cuda.current_stream().cuda_stream
@@ -107,7 +138,7 @@ class Leapfrog:
     """
 
     def __init__(self, mass, soft, dt, n_steps, theta=0.7, n_bucket=16, checkpoint_every=4,
-                 form="mixed", nthreads=0):
+                 form="mixed", nthreads=0, builder="host"):
         self.mass = mass
         self.soft = soft
         self.dt = float(dt)
@@ -117,6 +148,7 @@ class Leapfrog:
         self.every = max(1, int(checkpoint_every))
         self.form = form
         self.nthreads = nthreads
+        self.builder = builder
         self.checkpoints = {}
         self.trees = None
         self.tree_builds = 0
@@ -129,7 +161,7 @@ class Leapfrog:
             return t
         self.tree_builds += 1
         return TreeStep(x, self.mass, self.soft, self.theta, self.n_bucket, device=x.device,
-                        nthreads=self.nthreads)
+                        nthreads=self.nthreads, builder=self.builder)
 
     def _accel(self, tree):
         self.force_evals += 1

@@ -44,8 +44,8 @@ class Workload:
             return ics.nfw_halos(self.n, rng, soft=self.soft)
         raise ValueError(self.name)
 
-    def lists(self, nthreads=0):
-        p = self.particles()
+    def lists(self, nthreads=0, particles=None):
+        p = particles if particles is not None else self.particles()
         return tree.build_lists(p["pos"], p["mass"], p["soft"], n_bucket=self.n_bucket,
                                 theta=self.theta, period=self.period,
                                 n_replicas=1 if self.period else 0, nthreads=nthreads)
