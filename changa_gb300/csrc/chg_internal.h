@@ -50,6 +50,8 @@ cudaError_t launch_list(int form, bool cell, const ListArgs& a, cudaStream_t s);
 int list_variant_count();
 int set_list_variant(int kernel, int variant);
 int get_list_variant(int kernel);
+int set_hex_variant(int v);
+int get_hex_variant();
 cudaError_t launch_pack_cells(const double* moments, long long n, float4* out, cudaStream_t s);
 cudaError_t launch_pack_parts(const double* parts, long long n, float4* out, cudaStream_t s);
 cudaError_t launch_zero_vars_f32(VariablePartData* v, long long n, cudaStream_t s);

@@ -1490,6 +1490,263 @@ __global__ void __launch_bounds__(kThreads, MINB) list_kernel_tp2(const ListArgs
   }
 }
 
+/* ------------------------------------------------------------------ */
+/* Paired target-parallel kernel for hexadecapole cells (FP32-mixed):  */
+/* list_kernel_tp2's structure with momEvalFmomrcm (hex_eval) on two    */
+/* staged cells per .f32x2 instruction.  Staged pair: 26 fields {x y z */
+/* M radius, 21 moments} of both cells, 13 float4 words; hexadecapole  */
+/* cells carry no softening (softened cells have their own list), so   */
+/* there is no near-field branch.  One staging buffer per warp (the    */
+/* record is 2.2x the quadrupole's); the next block's packed records   */
+/* are loaded into registers while the current block computes.        */
+/* ------------------------------------------------------------------ */
+
+struct RawHex {
+  float4 w[kCellHexPackF4];
+  int code;
+};
+
+__device__ __forceinline__ void gather_hex(const ListArgs& a, int e, int e_end, RawHex& r) {
+  long long idx = 0;
+  r.code = 0x49;  // replica (0, 0, 0)
+  if (e < e_end) {
+    const int2 ent = __ldg(a.list + e);
+    idx = ent.x;
+    if ((unsigned long long)idx >= (unsigned long long)a.n_src) idx = 0;  // memory safety
+    r.code = (ent.y >> 22) & 0x1ff;
+  }
+  const float4* p = static_cast<const float4*>(a.src) + kCellHexPackF4 * idx;
+#pragma unroll
+  for (int k = 0; k < kCellHexPackF4; ++k) r.w[k] = __ldg(p + k);
+}
+
+/* The 26 fields of one record into half h of a staged pair: the position
+ * relative to the bucket's centre with the replica offset (as
+ * stage_entry forms it), M, the radius and the 21 moments; entries past
+ * the list end become massless cells far away (they add exact zeros). */
+__device__ __forceinline__ void stage_hex(const ListArgs& a, const RawHex& r, bool valid,
+                                          float3 chi, float3 clo, float* pb, int h) {
+  const float fp = a.fperiod_f;
+  const float4 hi = r.w[0], lo = r.w[1];
+  float f[26];
+  f[0] = ((hi.x - chi.x) + (float)((r.code & 7) - 3) * fp) + (lo.x - clo.x);
+  f[1] = ((hi.y - chi.y) + (float)(((r.code >> 3) & 7) - 3) * fp) + (lo.y - clo.y);
+  f[2] = ((hi.z - chi.z) + (float)(((r.code >> 6) & 7) - 3) * fp) + (lo.z - clo.z);
+  f[3] = hi.w;
+#pragma unroll
+  for (int w = 0; w < 6; ++w) {
+    const float4 v = r.w[2 + w];
+    if (4 + 4 * w < 26) f[4 + 4 * w] = v.x;
+    if (5 + 4 * w < 26) f[5 + 4 * w] = v.y;
+    if (6 + 4 * w < 26) f[6 + 4 * w] = v.z;
+    if (7 + 4 * w < 26) f[7 + 4 * w] = v.w;
+  }
+  if (!valid) {
+    f[0] = f[1] = f[2] = 1e30f;
+#pragma unroll
+    for (int k = 3; k < 26; ++k) f[k] = 0.f;
+  }
+#pragma unroll
+  for (int k = 0; k < 26; ++k) pb[pair_slot(k, h)] = f[k];
+}
+
+__device__ __forceinline__ f2 lo2(float4 v) { return pk2(v.x, v.y); }
+__device__ __forceinline__ f2 hi2(float4 v) { return pk2(v.z, v.w); }
+
+/* hex_eval on the two cells of staged pair w (13 words) for one target
+ * (r = target - cell).  Field k of the pair sits in word k/2, in its low
+ * half for even k and its high half for odd k. */
+__device__ __forceinline__ void hex_pair(const float4* __restrict__ w, f2 tx2, f2 ty2, f2 tz2,
+                                         f2 tm2, f2& pot2, f2& ax2, f2& ay2, f2& az2,
+                                         float& idt2) {
+  const f2 C3 = pk2(3.f, 3.f), C5 = pk2(5.f, 5.f), C7 = pk2(7.f, 7.f), C9 = pk2(9.f, 9.f);
+  const f2 CH = pk2(0.5f, 0.5f), CMH = pk2(-0.5f, -0.5f), CQ = pk2(0.25f, 0.25f);
+  const float third = 0.3333333432674408f;  // the reference's single-precision 1/3
+  const f2 C13 = pk2(third, third);
+  const float4 w0 = w[0], w1 = w[1], w2 = w[2];
+  const f2 rx = sub2(tx2, lo2(w0)), ry = sub2(ty2, hi2(w0)), rz = sub2(tz2, lo2(w1));
+  const f2 M = hi2(w1);
+  const f2 rsq = fma2(rx, rx, fma2(ry, ry, mul2(rz, rz)));
+  float q0, q1;
+  up2(rsq, q0, q1);
+  /* rsq = 0 (a cell at the target) contributes nothing, as in
+   * hex_interact; the far padding records give rsq = inf and dir = 0 */
+  const f2 dir = pk2(q0 > 0.f ? rsqrt_ftz(q0) : 0.f, q1 > 0.f ? rsqrt_ftz(q1) : 0.f);
+  const f2 u = mul2(lo2(w2), dir);
+  f2 g2 = mul2(mul2(mul2(C3, dir), u), u);
+  f2 g3 = mul2(mul2(C5, g2), u);
+  f2 g4 = mul2(mul2(C7, g3), u);
+  const f2 x = mul2(rx, dir), y = mul2(ry, dir), z = mul2(rz, dir);
+  f2 xx = mul2(mul2(CH, x), x), yy = mul2(mul2(CH, y), y);
+  const f2 xy = mul2(x, y), xz = mul2(x, z), yz = mul2(y, z);
+  const f2 nzz = mul2(mul2(CMH, z), z);  // -zz
+  const f2 xxx = mul2(x, fma2(C13, xx, nzz)), xxz = mul2(z, fma2(C13, nzz, xx));
+  const f2 yyy = mul2(y, fma2(C13, yy, nzz)), yyz = mul2(z, fma2(C13, nzz, yy));
+  xx = add2(xx, nzz);
+  yy = add2(yy, nzz);
+  const f2 xxy = mul2(y, xx), xyy = mul2(x, yy), xyz = mul2(xy, z);
+  const float4 w3 = w[3], w4 = w[4], w5 = w[5], w6 = w[6], w7 = w[7], w8 = w[8], w9 = w[9],
+               w10 = w[10], w11 = w[11], w12 = w[12];
+  /* q[k] is field 5 + k */
+  const f2 Q0 = hi2(w2), Q1 = lo2(w3), Q2 = hi2(w3), Q3 = lo2(w4), Q4 = hi2(w4), Q5 = lo2(w5),
+           Q6 = hi2(w5), Q7 = lo2(w6), Q8 = hi2(w6), Q9 = lo2(w7), Q10 = hi2(w7), Q11 = lo2(w8),
+           Q12 = hi2(w8), Q13 = lo2(w9), Q14 = hi2(w9), Q15 = lo2(w10), Q16 = hi2(w10),
+           Q17 = lo2(w11), Q18 = hi2(w11), Q19 = lo2(w12), Q20 = hi2(w12);
+  f2 t = mul2(Q12, xxx);
+  t = fma2(Q13, yyy, t);
+  t = fma2(Q14, xxy, t);
+  t = fma2(Q16, xxz, t);
+  t = fma2(Q18, xyy, t);
+  t = fma2(Q19, xyz, t);
+  const f2 tx = mul2(g4, fma2(Q20, yyz, t));
+  t = mul2(Q13, xyy);
+  t = fma2(Q14, xxx, t);
+  t = fma2(Q15, yyy, t);
+  t = fma2(Q17, yyz, t);
+  t = fma2(Q18, xxy, t);
+  t = fma2(Q19, xxz, t);
+  const f2 ty = mul2(g4, fma2(Q20, xyz, t));
+  t = mul2(Q16, xxx);
+  t = fma2(Q17, yyy, t);
+  t = fma2(Q19, xxy, t);
+  t = fma2(Q20, xyy, t);
+  f2 sm = mul2(Q12, xxz);
+  sm = fma2(add2(Q13, Q14), xyz, sm);
+  sm = fma2(Q15, yyz, sm);
+  sm = fma2(Q18, add2(xxz, yyz), sm);
+  const f2 tz = mul2(g4, sub2(t, sm));
+  g4 = mul2(CQ, fma2(tx, x, fma2(ty, y, mul2(tz, z))));
+  t = mul2(Q5, xx);
+  t = fma2(Q6, yy, t);
+  t = fma2(Q7, xy, t);
+  t = fma2(Q9, xz, t);
+  const f2 o3x = mul2(g3, fma2(Q11, yz, t));
+  t = mul2(Q6, xy);
+  t = fma2(Q7, xx, t);
+  t = fma2(Q8, yy, t);
+  t = fma2(Q10, yz, t);
+  const f2 o3y = mul2(g3, fma2(Q11, xz, t));
+  t = mul2(Q9, xx);
+  t = fma2(Q10, yy, t);
+  t = fma2(Q11, xy, t);
+  sm = mul2(add2(Q5, Q6), xz);
+  sm = fma2(add2(Q7, Q8), yz, sm);
+  const f2 o3z = mul2(g3, sub2(t, sm));
+  g3 = mul2(C13, fma2(o3x, x, fma2(o3y, y, mul2(o3z, z))));
+  const f2 o2x = mul2(g2, fma2(Q0, x, fma2(Q1, y, mul2(Q2, z))));
+  const f2 o2y = mul2(g2, fma2(Q3, y, fma2(Q1, x, mul2(Q4, z))));
+  const f2 o2z = mul2(g2, sub2(fma2(Q2, x, mul2(Q4, y)), mul2(add2(Q0, Q3), z)));
+  g2 = mul2(CH, fma2(o2x, x, fma2(o2y, y, mul2(o2z, z))));
+  f2 g0 = mul2(dir, M);
+  /* pot -= g0 + g2 + g3 + g4: accumulated with the opposite sign */
+  pot2 = add2(pot2, add2(add2(g0, g2), add2(g3, g4)));
+  g0 = fma2(C5, g2, fma2(C7, g3, fma2(C9, g4, g0)));
+  ax2 = fma2(dir, sub2(add2(add2(o2x, o3x), tx), mul2(x, g0)), ax2);
+  ay2 = fma2(dir, sub2(add2(add2(o2y, o3y), ty), mul2(y, g0)), ay2);
+  az2 = fma2(dir, sub2(add2(add2(o2z, o3z), tz), mul2(z, g0)), az2);
+  float d0, d1;
+  up2(mul2(add2(tm2, M), mul2(dir, mul2(dir, dir))), d0, d1);
+  idt2 = fmaxf(idt2, fmaxf(d0, d1));
+}
+
+template <int MINB>
+__global__ void __launch_bounds__(kThreads, MINB) list_kernel_hex2(const ListArgs a) {
+  constexpr int PW = 13;  // float4 words per staged pair
+  __shared__ __align__(16) float4 stage[kWarps][16 * PW];
+  __shared__ double red[kWarps][5][32];
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+
+  for (;;) {
+    int b = 0;
+    if (lane == 0) b = (int)atomicAdd(a.queue, 1u);
+    b = __shfl_sync(kFull, b, 0);
+    if (b >= a.n_buckets) break;
+    const int e_begin = max(__ldg(a.markers + b), 0);
+    const int e_end = (int)min((long long)__ldg(a.markers + b + 1), a.n_entries);  // memory safety
+    const long long tbase = __ldg(a.starts + b);
+    const int n = __ldg(a.sizes + b);
+    if (n <= 0 || tbase < 0 || tbase + n > a.n_tgt) continue;  // memory safety
+
+    const float4* tp = static_cast<const float4*>(a.tgt) + kPartPackF4 * tbase;
+    const float4 ch = __ldg(tp), cl = __ldg(tp + 1);
+    const float3 chi = make_float3(ch.x, ch.y, ch.z), clo = make_float3(cl.x, cl.y, cl.z);
+
+    for (int t0 = 0; t0 < n; t0 += 32) {
+      const int nt = min(32, n - t0);
+      const int G = 32 / nt;
+      const int g = lane / nt;
+      const int t = lane - g * nt;
+      const bool active = g < G;
+      const long long ti = tbase + t0 + t;
+      const float4* p = static_cast<const float4*>(a.tgt) + kPartPackF4 * ti;
+      const float4 h = __ldg(p), l = __ldg(p + 1);
+      const float tx = (h.x - chi.x) + (l.x - clo.x);
+      const float ty = (h.y - chi.y) + (l.y - clo.y);
+      const float tz = (h.z - chi.z) + (l.z - clo.z);
+      const f2 tx2 = pk2(tx, tx), ty2 = pk2(ty, ty), tz2 = pk2(tz, tz), tm2 = pk2(h.w, h.w);
+
+      float sx = 0.f, sy = 0.f, sz = 0.f, sp = 0.f, idt2 = 0.f;
+      float cx = 0.f, cy = 0.f, cz = 0.f, cp = 0.f;
+      RawHex raw;
+      gather_hex(a, e_begin + lane, e_end, raw);
+      for (int e0 = e_begin; e0 < e_end; e0 += 32) {
+        const int ne = min(32, e_end - e0);
+        stage_hex(a, raw, lane < ne, chi, clo,
+                  reinterpret_cast<float*>(stage[warp] + (lane >> 1) * PW), lane & 1);
+        __syncwarp();
+        if (e0 + 32 < e_end) gather_hex(a, e0 + 32 + lane, e_end, raw);
+        f2 ax2 = 0ull, ay2 = 0ull, az2 = 0ull, pot2 = 0ull;  // +0.0f in both halves
+        const float4* st = stage[warp];
+        if (G == 1) {
+#pragma unroll 2
+          for (int q = 0; q < 16; ++q)
+            hex_pair(st + q * PW, tx2, ty2, tz2, tm2, pot2, ax2, ay2, az2, idt2);
+        } else if (active) {
+          for (int q = g; q < 16; q += G)
+            hex_pair(st + q * PW, tx2, ty2, tz2, tm2, pot2, ax2, ay2, az2, idt2);
+        }
+        __syncwarp();  // the stage is rewritten by the next block
+        float x0, x1, y0, y1, z0, z1, p0, p1;
+        up2(ax2, x0, x1);
+        up2(ay2, y0, y1);
+        up2(az2, z0, z1);
+        up2(pot2, p0, p1);
+        kahan_add(sx, cx, x0 + x1);
+        kahan_add(sy, cy, y0 + y1);
+        kahan_add(sz, cz, z0 + z1);
+        kahan_add(sp, cp, -(p0 + p1));
+      }
+
+      if (active) {
+        red[warp][0][lane] = (double)sx - (double)cx;
+        red[warp][1][lane] = (double)sy - (double)cy;
+        red[warp][2][lane] = (double)sz - (double)cz;
+        red[warp][3][lane] = (double)sp - (double)cp;
+        red[warp][4][lane] = (double)idt2;
+      }
+      __syncwarp();
+      if (lane < nt) {
+        double rx = 0, ry = 0, rz = 0, rp = 0, ri = 0;
+        for (int gg = 0; gg < G; ++gg) {
+          const int l2 = gg * nt + lane;
+          rx += red[warp][0][l2];
+          ry += red[warp][1][l2];
+          rz += red[warp][2][l2];
+          rp += red[warp][3][l2];
+          ri = fmax(ri, red[warp][4][l2]);
+        }
+        double* v = static_cast<double*>(a.vars) + 5 * (tbase + t0 + lane);
+        v[0] += rx;
+        v[1] += ry;
+        v[2] += rz;
+        v[3] += rp;
+        v[4] = fmax(ri, v[4]);
+      }
+      __syncwarp();
+    }
+  }
+}
+
 __global__ void pack_cells_kernel(const double* __restrict__ m, long long n, float4* __restrict__ out) {
   for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
        i += (long long)gridDim.x * blockDim.x) {
@@ -1660,17 +1917,39 @@ cudaError_t launch_pack_cells(const double* moments, long long n, float4* out, c
   return cudaGetLastError();
 }
 
+/* hexadecapole FP32-mixed cell kernel: 0 synchronous staging
+ * (list_kernel<kMix, true, true>), 1/2 paired (list_kernel_hex2, 1/2
+ * resident blocks per SM) */
+int g_hex_variant = 2;
+
 cudaError_t launch_list_hex(int form, const ListArgs& a, cudaStream_t s) {
   if (form == kF64) {
     static int occ = 0;
     return launch_kernel(list_kernel<kF64, true, true>, &occ, list_kernel_id(kF64, true), a, s);
   }
   if (form == kMix) {
+    const int kid = list_kernel_id(kMix, true);
+    if (g_hex_variant == 1) {
+      static int occ = 0;
+      return launch_kernel(list_kernel_hex2<1>, &occ, kid, a, s);
+    }
+    if (g_hex_variant == 2) {
+      static int occ = 0;
+      return launch_kernel(list_kernel_hex2<2>, &occ, kid, a, s);
+    }
     static int occ = 0;
-    return launch_kernel(list_kernel<kMix, true, true>, &occ, list_kernel_id(kMix, true), a, s);
+    return launch_kernel(list_kernel<kMix, true, true>, &occ, kid, a, s);
   }
   return cudaErrorInvalidValue;
 }
+
+int set_hex_variant(int v) {
+  if (v < 0 || v > 2) return -1;
+  g_hex_variant = v;
+  return 0;
+}
+
+int get_hex_variant() { return g_hex_variant; }
 
 cudaError_t launch_pack_cells_hex(const double* moments, long long n, float4* out, cudaStream_t s) {
   if (n <= 0) return cudaSuccess;

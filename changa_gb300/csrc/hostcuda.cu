@@ -614,6 +614,10 @@ int changa_gb300_set_list_variant(int kernel, int variant) {
   return set_list_variant(kernel, variant) ? CHANGA_E_INVALID_ARG : 0;
 }
 int changa_gb300_get_list_variant(int kernel) { return get_list_variant(kernel); }
+int changa_gb300_set_hex_variant(int variant) {
+  return set_hex_variant(variant) ? CHANGA_E_INVALID_ARG : 0;
+}
+int changa_gb300_get_hex_variant(void) { return get_hex_variant(); }
 
 int changa_gb300_kernel_time(int kernel, double* total_ms, long long* launches) {
   if (kernel < 0 || kernel >= kKidCount || !total_ms || !launches) return CHANGA_E_INVALID_ARG;

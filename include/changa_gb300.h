@@ -85,6 +85,10 @@ int changa_gb300_kernel_time(int kernel, double *total_ms, long long *launches);
 int changa_gb300_list_variant_count(void);
 int changa_gb300_set_list_variant(int kernel, int variant);
 int changa_gb300_get_list_variant(int kernel);
+/* The FP32-mixed hexadecapole cell kernel: 0 synchronous staging, 1 / 2
+ * paired .f32x2 arithmetic with 1 / 2 resident blocks per SM (default 2). */
+int changa_gb300_set_hex_variant(int variant);
+int changa_gb300_get_hex_variant(void);
 
 /* ---- device-resident list requests for the extension forms ---- */
 

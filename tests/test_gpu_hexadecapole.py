@@ -7,6 +7,7 @@ import numpy as np
 import pytest
 
 import oracle
+from changa_gb300 import _native as N
 from changa_gb300 import gravity, ics, tree
 from helpers import force_rel_err, pot_rel_err
 
@@ -34,12 +35,23 @@ def test_hex_forms_match_oracle(cuda_ok, soft, n_bucket):
     assert force_rel_err(v64, ref).max() < 1e-6
     assert pot_rel_err(v64, ref).max() < 1e-6
     np.testing.assert_allclose(v64[:, 4], ref[:, 4], rtol=1e-6)
-    vmx = ds.step("mixed").cpu().numpy()
-    e = force_rel_err(vmx, ref)
-    print("hex soft %g: fp64 max %.2e, mixed median %.2e p99 %.2e" % (
-        soft, force_rel_err(v64, ref).max(), np.median(e), np.percentile(e, 99)))
-    assert np.median(e) < 2e-6 and np.percentile(e, 99) < 1e-4
-    assert np.median(pot_rel_err(vmx, ref)) < 2e-6
+    lib = N.cuda_lib()
+    default = lib.changa_gb300_get_hex_variant()
+    try:
+        # every shape of the mixed hexadecapole cell kernel: synchronous
+        # staging (0) and the paired .f32x2 kernel at 1 and 2 blocks per SM
+        for variant in (0, 1, 2):
+            N.check(lib.changa_gb300_set_hex_variant(variant), "set_hex_variant")
+            vmx = ds.step("mixed").cpu().numpy()
+            e = force_rel_err(vmx, ref)
+            print("hex soft %g variant %d: fp64 max %.2e, mixed median %.2e p99 %.2e" % (
+                soft, variant, force_rel_err(v64, ref).max(), np.median(e),
+                np.percentile(e, 99)))
+            assert np.median(e) < 2e-6 and np.percentile(e, 99) < 1e-4
+            assert np.median(pot_rel_err(vmx, ref)) < 2e-6
+            np.testing.assert_allclose(vmx[:, 4], ref[:, 4], rtol=2e-5)
+    finally:
+        lib.changa_gb300_set_hex_variant(default)
 
 
 def test_hex_closer_to_direct_sum_than_quadrupole(cuda_ok):
