@@ -79,6 +79,24 @@ class EwaldReadOnlyData(C.Structure):
                 ("fEwCut2", C.c_float), ("fInner2", C.c_float)]
 
 
+class MultipoleMomentsDataHex(C.Structure):
+    """MultipoleMomentsData of the HEXADECAPOLE build (no quadrupole terms)."""
+    _fields_ = [(n, C.c_float) for n in ("totalMass", "cmx", "cmy", "cmz")]
+
+
+class EwaldReadOnlyDataHex(C.Structure):
+    """EwaldReadOnlyData of the HEXADECAPOLE build."""
+    _fields_ = [("mm", MultipoleMomentsDataHex), ("momcRoot", MomcData),
+                ("n", C.c_int), ("nReps", C.c_int), ("nEwReps", C.c_int), ("nEwhLoop", C.c_int),
+                ("L", C.c_float), ("fEwCut", C.c_float), ("alpha", C.c_float),
+                ("alpha2", C.c_float), ("k1", C.c_float), ("ka", C.c_float),
+                ("fEwCut2", C.c_float), ("fInner2", C.c_float)]
+
+
+# CudaMultipoleMoments: 12 floats (quadrupole build), 27 (HEXADECAPOLE)
+MOMENT_FLOATS = {"quadrupole": 12, "hexadecapole": 27}
+
+
 class EwaldData(C.Structure):
     _fields_ = [("EwaldRange", C.c_int * 2), ("EwaldMarkers", C.c_void_p),
                 ("ewt", C.c_void_p), ("cachedData", C.c_void_p)]
@@ -208,6 +226,7 @@ CUDA_SIGNATURES = {
                                       C.POINTER(ChangaListRequest), _D, _VP, _VP]),
     "changa_ewald_forces": (_I, [_I, _VP, _LL, _VP, _LL, C.POINTER(ChangaEwaldParams), _VP, _VP]),
     "changa_ewald_table": (_I, [_VP, _D, _D, _VP, _I]),
+    "changa_ewald_table_hex": (_I, [_VP, _D, _D, _VP, _I, _VP]),
 }
 
 HOST_SIGNATURES = {
@@ -264,6 +283,23 @@ def cuda_lib():
                                "python changa_gb300/build.py); the GPU path has no fallback")
         _cuda = _bind(C.CDLL(path, mode=C.RTLD_GLOBAL), CUDA_SIGNATURES)
     return _cuda
+
+
+_cuda_hex = None
+
+
+def cuda_lib_hex():
+    """The same library built with -DHEXADECAPOLE: the boundary of ChaNGa's
+    hexadecapole build (108-byte CudaMultipoleMoments, the hexadecapole
+    EwaldReadOnlyData).  Loaded with local symbol scope next to cuda_lib()."""
+    global _cuda_hex
+    if _cuda_hex is None:
+        path = _build.HEX_LIB
+        if not os.path.exists(path):
+            raise RuntimeError("libchanga_gb300_hex.so is not built (run __graft_entry__.build() "
+                               "or python changa_gb300/build.py); the GPU path has no fallback")
+        _cuda_hex = _bind(C.CDLL(path, mode=C.RTLD_LOCAL), CUDA_SIGNATURES)
+    return _cuda_hex
 
 
 def check(rc, what="changa_gb300"):

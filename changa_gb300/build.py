@@ -2,6 +2,8 @@
 
 * ``_build/libchanga_gb300.so`` -- the CUDA library (sm_103a kernels and the
   C-ABI of include/HostCUDA.h, include/EwaldCUDA.h, include/changa_gb300.h).
+* ``_build/libchanga_gb300_hex.so`` -- the same library built with
+  -DHEXADECAPOLE: the boundary of ChaNGa's hexadecapole build.
 * ``_build/libchanga_host.so`` -- host tree build, dual walk and list
   serialisation (the caller side of the boundary).
 
@@ -34,6 +36,10 @@ CXX_SOURCES = ["cxx_abi.cpp", "ewald_table.cpp"]
 NO_FMA_SOURCES = {"treebuild.cu": ["-fmad=false"], "walk.cu": ["-fmad=false"]}
 
 CUDA_LIB = os.path.join(BUILD, "libchanga_gb300.so")
+# the same sources with -DHEXADECAPOLE: the boundary of ChaNGa's default
+# (hexadecapole) build, 108-byte CudaMultipoleMoments and the hexadecapole
+# Ewald root expansion
+HEX_LIB = os.path.join(BUILD, "libchanga_gb300_hex.so")
 HOST_LIB = os.path.join(BUILD, "libchanga_host.so")
 
 
@@ -79,31 +85,37 @@ def build_cuda(force=False, verbose=False):
     headers = [os.path.join(INCLUDE, h) for h in os.listdir(INCLUDE)] + \
               [os.path.join(CSRC, h) for h in os.listdir(CSRC) if h.endswith((".h", ".cuh"))]
     srcs = [os.path.join(CSRC, s) for s in CU_SOURCES + CXX_SOURCES]
-    if not force and _newer(CUDA_LIB, srcs + headers):
+    if not force and _newer(CUDA_LIB, srcs + headers) and _newer(HEX_LIB, srcs + headers):
         return CUDA_LIB
     if not os.path.exists(NVCC):
         raise RuntimeError("nvcc not found at %s" % NVCC)
     inc = ["-I" + INCLUDE, "-I" + CSRC]
     jobs = []
-    objs = []
-    for s in CU_SOURCES:
-        o = os.path.join(BUILD, "obj", s + ".o")
-        objs.append(o)
-        extra = NO_FMA_SOURCES.get(s, [])
-        jobs.append([NVCC] + ARCH + ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC",
-                                     "-Xptxas", "-v"] + extra + inc +
-                    ["-c", os.path.join(CSRC, s), "-o", o])
-    for s in CXX_SOURCES:
-        o = os.path.join(BUILD, "obj", s + ".o")
-        objs.append(o)
-        jobs.append(["g++", "-O2", "-fPIC", "-std=c++17", "-I" + os.path.join(CUDA_HOME, "include")]
-                    + inc + ["-c", os.path.join(CSRC, s), "-o", o])
-    with ThreadPoolExecutor(max_workers=len(jobs)) as ex:
+    objs = {CUDA_LIB: [], HEX_LIB: []}
+    for lib, odir, defs in ((CUDA_LIB, "obj", []), (HEX_LIB, "obj_hex", ["-DHEXADECAPOLE"])):
+        os.makedirs(os.path.join(BUILD, odir), exist_ok=True)
+        for s in CU_SOURCES:
+            o = os.path.join(BUILD, odir, s + ".o")
+            objs[lib].append(o)
+            extra = NO_FMA_SOURCES.get(s, [])
+            jobs.append([NVCC] + ARCH + ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC",
+                                         "-Xptxas", "-v"] + extra + defs + inc +
+                        ["-c", os.path.join(CSRC, s), "-o", o])
+        for s in CXX_SOURCES:
+            o = os.path.join(BUILD, odir, s + ".o")
+            objs[lib].append(o)
+            jobs.append(["g++", "-O2", "-fPIC", "-std=c++17", "-ffp-contract=off",
+                         "-I" + os.path.join(CUDA_HOME, "include")] + defs + inc +
+                        ["-c", os.path.join(CSRC, s), "-o", o])
+    with ThreadPoolExecutor(max_workers=min(len(jobs), (os.cpu_count() or 8) * 2)) as ex:
         outs = list(ex.map(_run, jobs))
     if verbose:
         for o in outs:
             sys.stdout.write(o)
-    _run([NVCC] + ARCH + ["-shared", "-o", CUDA_LIB] + objs)
+    # -Bsymbolic: each library binds its own internal references, so the two
+    # builds (same symbol names) can share one process
+    for lib in (CUDA_LIB, HEX_LIB):
+        _run([NVCC] + ARCH + ["-shared", "-Xlinker", "-Bsymbolic", "-o", lib] + objs[lib])
     with open(os.path.join(BUILD, "ptxas.txt"), "w") as f:
         f.write("".join(outs))
     return CUDA_LIB

@@ -54,7 +54,23 @@ __global__ void __launch_bounds__(128) ewald_f32_kernel(const CompactPartData* _
   }
   const CompactPartData p = parts[id];
   const MultipoleMomentsData& mom = ro.mm;
+#ifdef HEXADECAPOLE
+  /* traces of the complete root moments (Ewald.cpp:99-111) */
+  const MomcData& mc = ro.momcRoot;
+  const float Q4xx = 0.5f * (mc.xxxx + mc.xxyy + mc.xxzz);
+  const float Q4xy = 0.5f * (mc.xxxy + mc.xyyy + mc.xyzz);
+  const float Q4xz = 0.5f * (mc.xxxz + mc.xyyz + mc.xzzz);
+  const float Q4yy = 0.5f * (mc.xxyy + mc.yyyy + mc.yyzz);
+  const float Q4yz = 0.5f * (mc.xxyz + mc.yyyz + mc.yzzz);
+  const float Q4zz = 0.5f * (mc.xxzz + mc.yyzz + mc.zzzz);
+  const float Q4 = 0.25f * (Q4xx + Q4yy + Q4zz);
+  const float Q3x = 0.5f * (mc.xxx + mc.xyy + mc.xzz);
+  const float Q3y = 0.5f * (mc.xxy + mc.yyy + mc.yzz);
+  const float Q3z = 0.5f * (mc.xxz + mc.yyz + mc.zzz);
+  const float Q2 = 0.5f * (mc.xx + mc.yy + mc.zz);
+#else
   const float Q2 = 0.5f * (mom.xx + mom.yy + mom.zz);
+#endif
   float ax = 0.f, ay = 0.f, az = 0.f;
   float fPot = mom.totalMass * ro.k1;
   const float xdif = p.position.x - mom.cmx, ydif = p.position.y - mom.cmy,
@@ -71,7 +87,7 @@ __global__ void __launch_bounds__(128) ewald_f32_kernel(const CompactPartData* _
         const float z = zdif + iz * ro.L;
         float r2 = x * x + y * y + z * z;
         if (r2 > ro.fEwCut2 && !hole) continue;
-        float g0, g1, g2, g3;
+        float g0, g1, g2, g3, g4 = 0.f, g5 = 0.f;
         if (r2 < ro.fInner2) {
           float alphan = ro.ka;
           r2 *= ro.alpha2;
@@ -82,6 +98,12 @@ __global__ void __launch_bounds__(128) ewald_f32_kernel(const CompactPartData* _
           g2 = alphan * ((1.0f / 7.0f) * r2 - (1.0f / 5.0f));
           alphan *= 2.f * ro.alpha2;
           g3 = alphan * ((1.0f / 9.0f) * r2 - (1.0f / 7.0f));
+#ifdef HEXADECAPOLE
+          alphan *= 2.f * ro.alpha2;
+          g4 = alphan * ((1.0f / 11.0f) * r2 - (1.0f / 9.0f));
+          alphan *= 2.f * ro.alpha2;
+          g5 = alphan * ((1.0f / 13.0f) * r2 - (1.0f / 11.0f));
+#endif
         } else {
           const float dir = rsqrtf(r2);
           const float dir2 = dir * dir;
@@ -95,7 +117,53 @@ __global__ void __launch_bounds__(128) ewald_f32_kernel(const CompactPartData* _
           g2 = 3.f * g1 * dir2 + alphan * a;
           alphan *= 2.f * ro.alpha2;
           g3 = 5.f * g2 * dir2 + alphan * a;
+#ifdef HEXADECAPOLE
+          alphan *= 2.f * ro.alpha2;
+          g4 = 7.f * g3 * dir2 + alphan * a;
+          alphan *= 2.f * ro.alpha2;
+          g5 = 9.f * g4 * dir2 + alphan * a;
+#endif
         }
+#ifdef HEXADECAPOLE
+        /* the hexadecapole expansion term (Ewald.cpp:203-240) */
+        const float xx = 0.5f * x * x, yy = 0.5f * y * y, zz = 0.5f * z * z;
+        const float xy = x * y, xz = x * z, yz = y * z, xyz = xy * z;
+        const float xxx = (1.0f / 3.0f) * xx * x, yyy = (1.0f / 3.0f) * yy * y,
+                    zzz = (1.0f / 3.0f) * zz * z;
+        const float xxy = xx * y, xxz = xx * z, xyy = yy * x, yyz = yy * z, xzz = zz * x,
+                    yzz = zz * y;
+        const float Q2mirx = mc.xx * x + mc.xy * y + mc.xz * z;
+        const float Q2miry = mc.xy * x + mc.yy * y + mc.yz * z;
+        const float Q2mirz = mc.xz * x + mc.yz * y + mc.zz * z;
+        const float Q3mirx = mc.xxx * xx + mc.xxy * xy + mc.xxz * xz + mc.xyy * yy +
+                             mc.xyz * yz + mc.xzz * zz;
+        const float Q3miry = mc.xxy * xx + mc.xyy * xy + mc.xyz * xz + mc.yyy * yy +
+                             mc.yyz * yz + mc.yzz * zz;
+        const float Q3mirz = mc.xxz * xx + mc.xyz * xy + mc.xzz * xz + mc.yyz * yy +
+                             mc.yzz * yz + mc.zzz * zz;
+        const float Q4mirx = mc.xxxx * xxx + mc.xxxy * xxy + mc.xxxz * xxz + mc.xxyy * xyy +
+                             mc.xxyz * xyz + mc.xxzz * xzz + mc.xyyy * yyy + mc.xyyz * yyz +
+                             mc.xyzz * yzz + mc.xzzz * zzz;
+        const float Q4miry = mc.xxxy * xxx + mc.xxyy * xxy + mc.xxyz * xxz + mc.xyyy * xyy +
+                             mc.xyyz * xyz + mc.xyzz * xzz + mc.yyyy * yyy + mc.yyyz * yyz +
+                             mc.yyzz * yzz + mc.yzzz * zzz;
+        const float Q4mirz = mc.xxxz * xxx + mc.xxyz * xxy + mc.xxzz * xxz + mc.xyyz * xyy +
+                             mc.xyzz * xyz + mc.xzzz * xzz + mc.yyyz * yyy + mc.yyzz * yyz +
+                             mc.yzzz * yzz + mc.zzzz * zzz;
+        const float Q4x = Q4xx * x + Q4xy * y + Q4xz * z;
+        const float Q4y = Q4xy * x + Q4yy * y + Q4yz * z;
+        const float Q4z = Q4xz * x + Q4yz * y + Q4zz * z;
+        const float Q2mir = 0.5f * (Q2mirx * x + Q2miry * y + Q2mirz * z) -
+                            (Q3x * x + Q3y * y + Q3z * z) + Q4;
+        const float Q3mir = (1.0f / 3.0f) * (Q3mirx * x + Q3miry * y + Q3mirz * z) -
+                            0.5f * (Q4x * x + Q4y * y + Q4z * z);
+        const float Q4mir = 0.25f * (Q4mirx * x + Q4miry * y + Q4mirz * z);
+        const float Qta = g1 * mc.m - g2 * Q2 + g3 * Q2mir + g4 * Q3mir + g5 * Q4mir;
+        fPot -= g0 * mc.m - g1 * Q2 + g2 * Q2mir + g3 * Q3mir + g4 * Q4mir;
+        ax += g2 * (Q2mirx - Q3x) + g3 * (Q3mirx - Q4x) + g4 * Q4mirx - x * Qta;
+        ay += g2 * (Q2miry - Q3y) + g3 * (Q3miry - Q4y) + g4 * Q4miry - y * Qta;
+        az += g2 * (Q2mirz - Q3z) + g3 * (Q3mirz - Q4z) + g4 * Q4mirz - z * Qta;
+#else
         const float Q2mirx = mom.xx * x + mom.xy * y + mom.xz * z;
         const float Q2miry = mom.xy * x + mom.yy * y + mom.yz * z;
         const float Q2mirz = mom.xz * x + mom.yz * y + mom.zz * z;
@@ -105,6 +173,9 @@ __global__ void __launch_bounds__(128) ewald_f32_kernel(const CompactPartData* _
         ax += g2 * Q2mirx - x * Qta;
         ay += g2 * Q2miry - y * Qta;
         az += g2 * Q2mirz - z * Qta;
+        (void)g4;
+        (void)g5;
+#endif
       }
     }
   }

@@ -1506,6 +1506,11 @@ struct RawHex {
   int code;
 };
 
+/* Raw record of entry e: kMix, the packed cell (8 float4); kF32 (the
+ * drop-in of the hexadecapole build), the 108-byte CudaMultipoleMoments
+ * (27 floats, 4-byte aligned) rearranged into the same words with a zero
+ * low part. */
+template <int FORM>
 __device__ __forceinline__ void gather_hex(const ListArgs& a, int e, int e_end, RawHex& r) {
   long long idx = 0;
   r.code = 0x49;  // replica (0, 0, 0)
@@ -1515,23 +1520,54 @@ __device__ __forceinline__ void gather_hex(const ListArgs& a, int e, int e_end, 
     if ((unsigned long long)idx >= (unsigned long long)a.n_src) idx = 0;  // memory safety
     r.code = (ent.y >> 22) & 0x1ff;
   }
-  const float4* p = static_cast<const float4*>(a.src) + kCellHexPackF4 * idx;
+  if constexpr (FORM == kMix) {
+    const float4* p = static_cast<const float4*>(a.src) + kCellHexPackF4 * idx;
 #pragma unroll
-  for (int k = 0; k < kCellHexPackF4; ++k) r.w[k] = __ldg(p + k);
+    for (int k = 0; k < kCellHexPackF4; ++k) r.w[k] = __ldg(p + k);
+  } else {
+#ifdef HEXADECAPOLE
+    /* {radius, soft, totalMass, cm.xyz, then the 21 moments} */
+    const float* m = reinterpret_cast<const float*>(static_cast<const CudaMultipoleMoments*>(a.src) + idx);
+    float v[27];
+#pragma unroll
+    for (int k = 0; k < 27; ++k) v[k] = __ldg(m + k);
+    r.w[0] = make_float4(v[3], v[4], v[5], v[2]);
+    r.w[1] = make_float4(0.f, 0.f, 0.f, v[1]);
+    float q[24];
+    q[0] = v[0];
+#pragma unroll
+    for (int k = 0; k < 21; ++k) q[1 + k] = v[6 + k];
+    q[22] = q[23] = 0.f;
+#pragma unroll
+    for (int w = 0; w < 6; ++w) r.w[2 + w] = make_float4(q[4 * w], q[4 * w + 1], q[4 * w + 2], q[4 * w + 3]);
+#else
+    static_assert(FORM == kMix, "the FP32 hexadecapole drop-in exists in the HEXADECAPOLE build");
+#endif
+  }
 }
 
-/* The 26 fields of one record into half h of a staged pair: the position
- * relative to the bucket's centre with the replica offset (as
- * stage_entry forms it), M, the radius and the 21 moments; entries past
+/* The 26 fields of one record into half h of a staged pair: the source
+ * position with the replica offset (kMix: relative to the bucket's centre,
+ * as stage_entry forms it; kF32: offset + cm as the reference forms it,
+ * HostCUDA.cu:1094-1099), M, the radius and the 21 moments; entries past
  * the list end become massless cells far away (they add exact zeros). */
+template <int FORM>
 __device__ __forceinline__ void stage_hex(const ListArgs& a, const RawHex& r, bool valid,
                                           float3 chi, float3 clo, float* pb, int h) {
   const float fp = a.fperiod_f;
   const float4 hi = r.w[0], lo = r.w[1];
+  const float ox = (float)((r.code & 7) - 3) * fp, oy = (float)(((r.code >> 3) & 7) - 3) * fp,
+              oz = (float)(((r.code >> 6) & 7) - 3) * fp;
   float f[26];
-  f[0] = ((hi.x - chi.x) + (float)((r.code & 7) - 3) * fp) + (lo.x - clo.x);
-  f[1] = ((hi.y - chi.y) + (float)(((r.code >> 3) & 7) - 3) * fp) + (lo.y - clo.y);
-  f[2] = ((hi.z - chi.z) + (float)(((r.code >> 6) & 7) - 3) * fp) + (lo.z - clo.z);
+  if constexpr (FORM == kMix) {
+    f[0] = ((hi.x - chi.x) + ox) + (lo.x - clo.x);
+    f[1] = ((hi.y - chi.y) + oy) + (lo.y - clo.y);
+    f[2] = ((hi.z - chi.z) + oz) + (lo.z - clo.z);
+  } else {
+    f[0] = ox + hi.x;
+    f[1] = oy + hi.y;
+    f[2] = oz + hi.z;
+  }
   f[3] = hi.w;
 #pragma unroll
   for (int w = 0; w < 6; ++w) {
@@ -1649,8 +1685,9 @@ __device__ __forceinline__ void hex_pair(const float4* __restrict__ w, f2 tx2, f
   idt2 = fmaxf(idt2, fmaxf(d0, d1));
 }
 
-template <int MINB>
+template <int FORM, int MINB>
 __global__ void __launch_bounds__(kThreads, MINB) list_kernel_hex2(const ListArgs a) {
+  static_assert(FORM == kMix || FORM == kF32, "FP32 arithmetic forms only");
   constexpr int PW = 13;  // float4 words per staged pair
   __shared__ __align__(16) float4 stage[kWarps][16 * PW];
   __shared__ double red[kWarps][5][32];
@@ -1667,9 +1704,13 @@ __global__ void __launch_bounds__(kThreads, MINB) list_kernel_hex2(const ListArg
     const int n = __ldg(a.sizes + b);
     if (n <= 0 || tbase < 0 || tbase + n > a.n_tgt) continue;  // memory safety
 
-    const float4* tp = static_cast<const float4*>(a.tgt) + kPartPackF4 * tbase;
-    const float4 ch = __ldg(tp), cl = __ldg(tp + 1);
-    const float3 chi = make_float3(ch.x, ch.y, ch.z), clo = make_float3(cl.x, cl.y, cl.z);
+    float3 chi = make_float3(0.f, 0.f, 0.f), clo = chi;
+    if constexpr (FORM == kMix) {
+      const float4* tp = static_cast<const float4*>(a.tgt) + kPartPackF4 * tbase;
+      const float4 ch = __ldg(tp), cl = __ldg(tp + 1);
+      chi = make_float3(ch.x, ch.y, ch.z);
+      clo = make_float3(cl.x, cl.y, cl.z);
+    }
 
     for (int t0 = 0; t0 < n; t0 += 32) {
       const int nt = min(32, n - t0);
@@ -1678,23 +1719,33 @@ __global__ void __launch_bounds__(kThreads, MINB) list_kernel_hex2(const ListArg
       const int t = lane - g * nt;
       const bool active = g < G;
       const long long ti = tbase + t0 + t;
-      const float4* p = static_cast<const float4*>(a.tgt) + kPartPackF4 * ti;
-      const float4 h = __ldg(p), l = __ldg(p + 1);
-      const float tx = (h.x - chi.x) + (l.x - clo.x);
-      const float ty = (h.y - chi.y) + (l.y - clo.y);
-      const float tz = (h.z - chi.z) + (l.z - clo.z);
-      const f2 tx2 = pk2(tx, tx), ty2 = pk2(ty, ty), tz2 = pk2(tz, tz), tm2 = pk2(h.w, h.w);
+      float tx, ty, tz, tmass;
+      if constexpr (FORM == kMix) {
+        const float4* p = static_cast<const float4*>(a.tgt) + kPartPackF4 * ti;
+        const float4 h = __ldg(p), l = __ldg(p + 1);
+        tx = (h.x - chi.x) + (l.x - clo.x);
+        ty = (h.y - chi.y) + (l.y - clo.y);
+        tz = (h.z - chi.z) + (l.z - clo.z);
+        tmass = h.w;
+      } else {
+        const CompactPartData* p = static_cast<const CompactPartData*>(a.tgt) + ti;
+        tmass = __ldg(&p->mass);
+        tx = __ldg(&p->position.x);
+        ty = __ldg(&p->position.y);
+        tz = __ldg(&p->position.z);
+      }
+      const f2 tx2 = pk2(tx, tx), ty2 = pk2(ty, ty), tz2 = pk2(tz, tz), tm2 = pk2(tmass, tmass);
 
       float sx = 0.f, sy = 0.f, sz = 0.f, sp = 0.f, idt2 = 0.f;
       float cx = 0.f, cy = 0.f, cz = 0.f, cp = 0.f;
       RawHex raw;
-      gather_hex(a, e_begin + lane, e_end, raw);
+      gather_hex<FORM>(a, e_begin + lane, e_end, raw);
       for (int e0 = e_begin; e0 < e_end; e0 += 32) {
         const int ne = min(32, e_end - e0);
-        stage_hex(a, raw, lane < ne, chi, clo,
-                  reinterpret_cast<float*>(stage[warp] + (lane >> 1) * PW), lane & 1);
+        stage_hex<FORM>(a, raw, lane < ne, chi, clo,
+                        reinterpret_cast<float*>(stage[warp] + (lane >> 1) * PW), lane & 1);
         __syncwarp();
-        if (e0 + 32 < e_end) gather_hex(a, e0 + 32 + lane, e_end, raw);
+        if (e0 + 32 < e_end) gather_hex<FORM>(a, e0 + 32 + lane, e_end, raw);
         f2 ax2 = 0ull, ay2 = 0ull, az2 = 0ull, pot2 = 0ull;  // +0.0f in both halves
         const float4* st = stage[warp];
         if (G == 1) {
@@ -1711,10 +1762,17 @@ __global__ void __launch_bounds__(kThreads, MINB) list_kernel_hex2(const ListArg
         up2(ay2, y0, y1);
         up2(az2, z0, z1);
         up2(pot2, p0, p1);
-        kahan_add(sx, cx, x0 + x1);
-        kahan_add(sy, cy, y0 + y1);
-        kahan_add(sz, cz, z0 + z1);
-        kahan_add(sp, cp, -(p0 + p1));
+        if constexpr (FORM == kMix) {
+          kahan_add(sx, cx, x0 + x1);
+          kahan_add(sy, cy, y0 + y1);
+          kahan_add(sz, cz, z0 + z1);
+          kahan_add(sp, cp, -(p0 + p1));
+        } else {
+          sx += x0 + x1;
+          sy += y0 + y1;
+          sz += z0 + z1;
+          sp -= p0 + p1;
+        }
       }
 
       if (active) {
@@ -1735,12 +1793,22 @@ __global__ void __launch_bounds__(kThreads, MINB) list_kernel_hex2(const ListArg
           rp += red[warp][3][l2];
           ri = fmax(ri, red[warp][4][l2]);
         }
-        double* v = static_cast<double*>(a.vars) + 5 * (tbase + t0 + lane);
-        v[0] += rx;
-        v[1] += ry;
-        v[2] += rz;
-        v[3] += rp;
-        v[4] = fmax(ri, v[4]);
+        const long long to = tbase + t0 + lane;
+        if constexpr (FORM == kF32) {
+          VariablePartData* v = static_cast<VariablePartData*>(a.vars) + to;
+          v->a.x += (float)rx;
+          v->a.y += (float)ry;
+          v->a.z += (float)rz;
+          v->potential += (float)rp;
+          v->dtGrav = fmaxf((float)ri, v->dtGrav);
+        } else {
+          double* v = static_cast<double*>(a.vars) + 5 * to;
+          v[0] += rx;
+          v[1] += ry;
+          v[2] += rz;
+          v[3] += rp;
+          v[4] = fmax(ri, v[4]);
+        }
       }
       __syncwarp();
     }
@@ -1865,11 +1933,24 @@ cudaError_t launch_src(int v, const ListArgs& a, cudaStream_t s, std::integer_se
   return e;
 }
 
+/* the drop-in cell lists of the hexadecapole build: momEvalFmomrcm on the
+ * 108-byte CudaMultipoleMoments (nodeGravityComputation with HEXADECAPOLE,
+ * HostCUDA.cu:1106-1112); the quadrupole build's FP32 cell kernels are not
+ * instantiated there */
+#ifdef HEXADECAPOLE
+constexpr bool kHexDropIn = true;
+#else
+constexpr bool kHexDropIn = false;
+#endif
+
 template <int FORM, bool CELL>
 cudaError_t launch_t(const ListArgs& a, cudaStream_t s) {
   if constexpr (FORM == kF64) {
     static int occ = 0;
     return launch_kernel(list_kernel<FORM, CELL>, &occ, list_kernel_id(FORM, CELL), a, s);
+  } else if constexpr (kHexDropIn && FORM == kF32 && CELL) {
+    static int occ = 0;
+    return launch_kernel(list_kernel_hex2<kF32, 2>, &occ, list_kernel_id(kF32, true), a, s);
   } else {
     return launch_src<FORM, CELL>(g_variant[list_kernel_id(FORM, CELL)], a, s,
                                   std::make_integer_sequence<int, kNumVariants>{});
@@ -1931,11 +2012,11 @@ cudaError_t launch_list_hex(int form, const ListArgs& a, cudaStream_t s) {
     const int kid = list_kernel_id(kMix, true);
     if (g_hex_variant == 1) {
       static int occ = 0;
-      return launch_kernel(list_kernel_hex2<1>, &occ, kid, a, s);
+      return launch_kernel(list_kernel_hex2<kMix, 1>, &occ, kid, a, s);
     }
     if (g_hex_variant == 2) {
       static int occ = 0;
-      return launch_kernel(list_kernel_hex2<2>, &occ, kid, a, s);
+      return launch_kernel(list_kernel_hex2<kMix, 2>, &occ, kid, a, s);
     }
     static int occ = 0;
     return launch_kernel(list_kernel<kMix, true, true>, &occ, kid, a, s);

@@ -74,6 +74,32 @@ class EwaldConfig:
         p._keep = tb
         return p
 
+    def table_hex(self, root):
+        """The hexadecapole build's table for a 27-value root, and the root's
+        complete moments (MomcData order)."""
+        out = np.zeros((N.CHANGA_MAX_EWH, 5))
+        momc = np.zeros(32)
+        n = N.cuda_lib().changa_ewald_table_hex(_p(np.ascontiguousarray(root, np.float64)), self.L,
+                                                self.dEwhCut, _p(out), N.CHANGA_MAX_EWH, _p(momc))
+        if n < 0:
+            raise ValueError("Ewald h-table larger than %d rows" % N.CHANGA_MAX_EWH)
+        return out[:n].copy(), momc
+
+    def readonly_f32_hex(self, root, n_active, momc):
+        """EwaldReadOnlyData of the hexadecapole build as TreePiece::EwaldGPU
+        fills it (Ewald.cpp:452-516): the complete root moments, mass and
+        centre rounded to float."""
+        q = self.readonly_f32(np.concatenate([root[:6], np.zeros(6)]), n_active)
+        ro = N.EwaldReadOnlyDataHex()
+        for f, _ in N.EwaldReadOnlyDataHex._fields_:
+            if f not in ("mm", "momcRoot"):
+                setattr(ro, f, getattr(q, f))
+        ro.mm.totalMass = q.mm.totalMass
+        ro.mm.cmx, ro.mm.cmy, ro.mm.cmz = q.mm.cmx, q.mm.cmy, q.mm.cmz
+        for k, (f, _) in enumerate(N.MomcData._fields_):
+            setattr(ro.momcRoot, f, float(np.float32(momc[k])))
+        return ro
+
     def readonly_f32(self, root, n_active):
         """EwaldReadOnlyData as TreePiece::EwaldGPU fills it (Ewald.cpp:470-516)."""
         ro = N.EwaldReadOnlyData()
@@ -149,11 +175,16 @@ class PinnedArray:
 
 class DropInInputs:
     """The host buffers ChaNGa would hand the drop-in boundary for one
-    force evaluation (pinned, FP32 ABI structs), built once."""
+    force evaluation (pinned, FP32 ABI structs), built once.  Lists of
+    order 4 go to the HEXADECAPOLE build of the library (108-byte moments,
+    the hexadecapole Ewald data); their softened cells are the caller's
+    (ChaNGa evaluates them on the CPU, Compute.cpp:1683-1698)."""
 
     def __init__(self, lists, ewald: EwaldConfig | None = None):
         self.lists = lists
         self.n = lists.n
+        self.hex = getattr(lists, "order", 2) == 4
+        self.lib = N.cuda_lib_hex() if self.hex else N.cuda_lib()
         self.moments = PinnedArray(lists.abi_moments())
         self.parts = PinnedArray(lists.abi_parts())
         self.vars = PinnedArray(np.zeros((lists.n, 5), np.float32))
@@ -166,13 +197,19 @@ class DropInInputs:
         self.ewald_data = None
         if ewald is not None:
             ed = N.EwaldData()
-            lib = N.cuda_lib()
+            lib = self.lib
             lib.EwaldHostMemorySetup(C.byref(ed), self.n, N.CHANGA_MAX_EWH, 1)
-            tb = ewald.table(lists.root)
+            if self.hex:
+                tb, momc = ewald.table_hex(lists.moments[0])
+            else:
+                tb = ewald.table(lists.root)
             ewt = (N.EwtData * tb.shape[0]).from_address(ed.ewt)
             for i in range(tb.shape[0]):
                 ewt[i].hx, ewt[i].hy, ewt[i].hz, ewt[i].hCfac, ewt[i].hSfac = [float(np.float32(x)) for x in tb[i]]
-            ro = ewald.readonly_f32(lists.root, self.n)
+            if self.hex:
+                ro = ewald.readonly_f32_hex(lists.moments[0], self.n, momc)
+            else:
+                ro = ewald.readonly_f32(lists.root, self.n)
             ro.nEwhLoop = tb.shape[0]
             C.memmove(ed.cachedData, C.byref(ro), C.sizeof(ro))
             mk = (C.c_int * self.n).from_address(ed.EwaldMarkers)
@@ -192,7 +229,7 @@ class DropInInputs:
             for a in r[:4]:
                 a.free()
         if self.ewald_data is not None:
-            N.cuda_lib().EwaldHostMemoryFree(C.byref(self.ewald_data), 1)
+            self.lib.EwaldHostMemoryFree(C.byref(self.ewald_data), 1)
             self.ewald_data = None
 
 
@@ -200,7 +237,7 @@ def dropin_step(inp: DropInInputs, stream=None, cudart=None):
     """Runs one force evaluation through the reference-facing boundary and
     returns the VariablePartData rows (N x 5 float32, a view of pinned
     memory, valid until the next call).  All device memory is released."""
-    lib = N.cuda_lib()
+    lib = inp.lib
     rt = cudart or _cudart()
     d_m, d_p, d_v = C.c_void_p(), C.c_void_p(), C.c_void_p()
     lib.DataManagerTransferLocalTree(inp.moments.ptr, inp.moments.nbytes, inp.parts.ptr,

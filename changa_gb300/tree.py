@@ -78,7 +78,8 @@ class TreeLists:
         return n
 
     def abi_moments(self):
-        """CudaMultipoleMoments array (M x 12 float32)."""
+        """CudaMultipoleMoments array: M x 12 float32 (quadrupole build) or
+        M x 27 float32 (order 4: the HEXADECAPOLE build's 108-byte struct)."""
         return np.ascontiguousarray(self.moments, dtype=np.float32)
 
     def abi_parts(self):

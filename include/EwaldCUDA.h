@@ -3,8 +3,9 @@
  *
  * Replaces the reference's EwaldCUDA.h (declarations at EwaldCUDA.h:59-62,
  * implementation in HostCUDA.cu:1887-2192).  Struct layouts are identical
- * (quadrupole build: MultipoleMomentsData carries xx..zz).  C linkage, with
- * the reference's C++-mangled names exported as well (see HostCUDA.h).
+ * in both builds (HEXADECAPOLE defined or not, as the reference's own
+ * header).  C linkage, with the reference's C++-mangled names exported as
+ * well (see HostCUDA.h).
  *
  * Difference on purpose: the reference copies EwaldReadOnlyData and the
  * h-table into __constant__ symbols per call (HostCUDA.cu:1934-1935), which
@@ -25,15 +26,18 @@ typedef struct {
   cudatype hCfac, hSfac;
 } EwtData;
 
-/** Root quadrupole moments (reference: EwaldCUDA.h:18-24). */
+/** Root mass and centre, with the quadrupole moments in the quadrupole
+ *  build (reference: EwaldCUDA.h:18-24). */
 typedef struct {
+#ifndef HEXADECAPOLE
   cudatype xx, xy, xz, yy, yz, zz;
+#endif
   cudatype totalMass;
   cudatype cmx, cmy, cmz;
 } MultipoleMomentsData;
 
-/** Complete root moments of the hexadecapole build (reference:
- *  EwaldCUDA.h:28-36); carried for layout compatibility. */
+/** Complete root moments, the hexadecapole build's Ewald expansion
+ *  (reference: EwaldCUDA.h:28-36; unused by the quadrupole build). */
 typedef struct {
   cudatype m;
   cudatype xx, yy, xy, xz, yz;

@@ -326,6 +326,14 @@ int changa_ewald_forces(int form, const double *parts, long long n_parts, const 
 /* Host restatement of TreePiece::EwaldInit (Ewald.cpp:285-383): fills up to
  * max_h rows of ewt; returns nEwhLoop, or -1 if max_h is too small. */
 int changa_ewald_table(const double *root, double L, double dEwhCut, double *ewt, int max_h);
+/* The hexadecapole build's table (TreePiece::EwaldInit with HEXADECAPOLE,
+ * Ewald.cpp:285-383): root holds the 27 hexadecapole moment values
+ * {radius, soft, M, cm, 21 scaled reduced moments}; the rows are as above
+ * (hSfac now carries the octupole).  momc, if not NULL, receives the root's
+ * complete moments in MomcData order (32 doubles), the values
+ * EwaldReadOnlyData.momcRoot carries in that build. */
+int changa_ewald_table_hex(const double *root, double L, double dEwhCut, double *ewt,
+                           int max_h, double *momc);
 
 #ifdef __cplusplus
 }

@@ -32,15 +32,24 @@ typedef struct CudaVector3D {
   cudatype x, y, z;
 } CudaVector3D;
 
-/** Quadrupole moments of one tree node, 48 bytes
- *  (reference: cuda_typedef.h:104-177, !HEXADECAPOLE, !GPU_LOCAL_TREE_WALK).
- *  xx..zz are the raw second moments sum m dx dx about cm (not trace-free). */
+/** Multipole moments of one tree node (reference: cuda_typedef.h:104-177,
+ *  !GPU_LOCAL_TREE_WALK).
+ *  Quadrupole build, 48 bytes: xx..zz are the raw second moments
+ *  sum m dx dx about cm (not trace-free).
+ *  HEXADECAPOLE build, 108 bytes: the scaled reduced (trace-free) moments
+ *  up to fourth order of moments.h's FMOMR, in units of the node radius. */
 typedef struct CudaMultipoleMoments {
   cudatype radius;
   cudatype soft;
   cudatype totalMass;
   CudaVector3D cm;
+#ifdef HEXADECAPOLE
+  cudatype xx, xy, xz, yy, yz;
+  cudatype xxx, xyy, xxy, yyy, xxz, yyz, xyz;
+  cudatype xxxx, xyyy, xxxy, yyyy, xxxz, yyyz, xxyy, xxyz, xyyz;
+#else
   cudatype xx, xy, xz, yy, yz, zz;
+#endif
 } CudaMultipoleMoments;
 
 /** A bucket of source particles on an interaction list

@@ -57,7 +57,11 @@ def load(kind="port"):
 def _bind_hex(lib):
     vp, i, l, d = C.c_void_p, C.c_int, C.c_long, C.c_double
     lib.oracle_cell_list_forces_hex.argtypes = [vp, l, vp, l, vp, vp, vp, vp, i, vp, d, vp, i]
-    lib.oracle_cell_list_forces_hex.restype = i
+    lib.oracle_ewald_table_hex.argtypes = [vp, d, d, vp, i, vp]
+    lib.oracle_ewald_forces_hex.argtypes = [vp, l, vp, l, vp, d, i, d, d, vp, i]
+    for f in (lib.oracle_cell_list_forces_hex, lib.oracle_ewald_table_hex,
+              lib.oracle_ewald_forces_hex):
+        f.restype = i
 
 
 def _load_hex(kind):
@@ -176,6 +180,36 @@ def ewald_forces(parts, root, L, nReps, fEwCut, dEwhCut, idx=None, vars=None, ki
         vars = np.zeros((n_idx, 5))
     rc = lib.oracle_ewald_forces(_p(parts), parts.shape[0], _p(idx), n_idx, _p(root), float(L),
                                  int(nReps), float(fEwCut), float(dEwhCut), _p(vars), int(nthreads))
+    assert rc == 0
+    return vars
+
+
+def ewald_table_hex(root, L, dEwhCut, kind="port"):
+    """EwaldInit of the hexadecapole build for a 27-value root: (h-table rows,
+    the root's complete moments in MomcData order)."""
+    lib = _load_hex(kind)
+    root = _c(root, np.float64)
+    out = np.zeros((4096, 5))
+    momc = np.zeros(32)
+    n = lib.oracle_ewald_table_hex(_p(root), float(L), float(dEwhCut), _p(out), 4096, _p(momc))
+    assert n >= 0
+    return out[:n].copy(), momc
+
+
+def ewald_forces_hex(parts, root, L, nReps, fEwCut, dEwhCut, idx=None, vars=None, kind="port",
+                     nthreads=0):
+    """BucketEwald of the hexadecapole build for parts[idx]; returns vars
+    rows in idx order."""
+    lib = _load_hex(kind)
+    parts = _c(parts, np.float64)
+    root = _c(root, np.float64)
+    idx = _c(idx, np.int32)
+    n_idx = parts.shape[0] if idx is None else len(idx)
+    if vars is None:
+        vars = np.zeros((n_idx, 5))
+    rc = lib.oracle_ewald_forces_hex(_p(parts), parts.shape[0], _p(idx), n_idx, _p(root),
+                                     float(L), int(nReps), float(fEwCut), float(dEwhCut),
+                                     _p(vars), int(nthreads))
     assert rc == 0
     return vars
 

@@ -478,3 +478,318 @@ int oracle_ewald_forces(const double* parts, long n_parts, const int* idx, long 
   }
   return 0;
 }
+
+/* ---- hexadecapole build of the Ewald correction ---- */
+
+/* Complete moments (moments.h MOMC) of a hexadecapole root given as 27
+ * doubles {radius, soft, M, cm.xyz, xx xy xz yy yz, xxx xyy xxy yyy xxz yyz
+ * xyz, xxxx xyyy xxxy yyyy xxxz yyyz xxyy xxyz xyyz}: momRescaleFmomr to
+ * unit scale (moments.c:238-267, f = radius) then momFmomr2Momc
+ * (moments.c:1563-1597), as EwaldInit does (Ewald.cpp:291-296). */
+typedef struct {
+  double m, xx, yy, xy, xz, yz;
+  double xxx, xyy, xxy, yyy, xxz, yyz, xyz;
+  double xxxx, xyyy, xxxy, yyyy, xxxz, yyyz, xxyy, xxyz, xyyz;
+  double zz, xzz, yzz, zzz, xxzz, xyzz, xzzz, yyzz, yzzz, zzzz;
+} momc_t;
+
+static void momc_from_root(const double* r, momc_t* c) {
+  double f = r[0] / 1.0, s = f;
+  s *= f;
+  c->m = r[2];
+  c->xx = r[6] * s;
+  c->xy = r[7] * s;
+  c->xz = r[8] * s;
+  c->yy = r[9] * s;
+  c->yz = r[10] * s;
+  s *= f;
+  c->xxx = r[11] * s;
+  c->xyy = r[12] * s;
+  c->xxy = r[13] * s;
+  c->yyy = r[14] * s;
+  c->xxz = r[15] * s;
+  c->yyz = r[16] * s;
+  c->xyz = r[17] * s;
+  s *= f;
+  c->xxxx = r[18] * s;
+  c->xyyy = r[19] * s;
+  c->xxxy = r[20] * s;
+  c->yyyy = r[21] * s;
+  c->xxxz = r[22] * s;
+  c->yyyz = r[23] * s;
+  c->xxyy = r[24] * s;
+  c->xxyz = r[25] * s;
+  c->xyyz = r[26] * s;
+  c->zz = -(c->xx + c->yy);
+  c->xzz = -(c->xxx + c->xyy);
+  c->yzz = -(c->xxy + c->yyy);
+  c->zzz = -(c->xxz + c->yyz);
+  c->xxzz = -(c->xxxx + c->xxyy);
+  c->xyzz = -(c->xxxy + c->xyyy);
+  c->xzzz = -(c->xxxz + c->xyyz);
+  c->yyzz = -(c->xxyy + c->yyyy);
+  c->yzzz = -(c->xxyz + c->yyyz);
+  c->zzzz = -(c->xxzz + c->yyzz);
+}
+
+/* QEVAL (hexadecapole), Ewald.cpp:6-46: the root expansion of complete
+ * moments with gamma factors gam[0..5] at (dx, dy, dz). */
+static void qeval_hex(const momc_t* mom, const double gam[6], double dx, double dy, double dz,
+                      double* ax, double* ay, double* az, double* fPot) {
+  double Qmirx, Qmiry, Qmirz, Qmir, Qta = 0.0;
+  Qmirx = (1.0 / 6.0) * (mom->xzzz * dz * dz * dz + 3 * mom->xyzz * dy * dz * dz +
+                         3 * mom->xyyz * dy * dy * dz + mom->xyyy * dy * dy * dy +
+                         3 * mom->xxzz * dx * dz * dz + 6 * mom->xxyz * dx * dy * dz +
+                         3 * mom->xxyy * dx * dy * dy + 3 * mom->xxxz * dx * dx * dz +
+                         3 * mom->xxxy * dx * dx * dy + mom->xxxx * dx * dx * dx);
+  Qmiry = (1.0 / 6.0) * (mom->yzzz * dz * dz * dz + 3 * mom->xyzz * dx * dz * dz +
+                         3 * mom->xxyz * dx * dx * dz + mom->xxxy * dx * dx * dx +
+                         3 * mom->yyzz * dy * dz * dz + 6 * mom->xyyz * dx * dy * dz +
+                         3 * mom->xxyy * dx * dx * dy + 3 * mom->yyyz * dy * dy * dz +
+                         3 * mom->xyyy * dx * dy * dy + mom->yyyy * dy * dy * dy);
+  Qmirz = (1.0 / 6.0) * (mom->yyyz * dy * dy * dy + 3 * mom->xyyz * dx * dy * dy +
+                         3 * mom->xxyz * dx * dx * dy + mom->xxxz * dx * dx * dx +
+                         3 * mom->yyzz * dy * dy * dz + 6 * mom->xyzz * dx * dy * dz +
+                         3 * mom->xxzz * dx * dx * dz + 3 * mom->yzzz * dy * dz * dz +
+                         3 * mom->xzzz * dx * dz * dz + mom->zzzz * dz * dz * dz);
+  Qmir = (1.0 / 4.0) * (Qmirx * dx + Qmiry * dy + Qmirz * dz);
+  *fPot -= gam[4] * Qmir;
+  Qta += gam[5] * Qmir;
+  *ax += gam[4] * Qmirx;
+  *ay += gam[4] * Qmiry;
+  *az += gam[4] * Qmirz;
+  Qmirx = (1.0 / 2.0) * (mom->xzz * dz * dz + 2 * mom->xyz * dy * dz + mom->xyy * dy * dy +
+                         2 * mom->xxz * dx * dz + 2 * mom->xxy * dx * dy + mom->xxx * dx * dx);
+  Qmiry = (1.0 / 2.0) * (mom->yzz * dz * dz + 2 * mom->xyz * dx * dz + mom->xxy * dx * dx +
+                         2 * mom->yyz * dy * dz + 2 * mom->xyy * dx * dy + mom->yyy * dy * dy);
+  Qmirz = (1.0 / 2.0) * (mom->yyz * dy * dy + 2 * mom->xyz * dx * dy + mom->xxz * dx * dx +
+                         2 * mom->yzz * dy * dz + 2 * mom->xzz * dx * dz + mom->zzz * dz * dz);
+  Qmir = (1.0 / 3.0) * (Qmirx * dx + Qmiry * dy + Qmirz * dz);
+  *fPot -= gam[3] * Qmir;
+  Qta += gam[4] * Qmir;
+  *ax += gam[3] * Qmirx;
+  *ay += gam[3] * Qmiry;
+  *az += gam[3] * Qmirz;
+  Qmirx = (1.0 / 1.0) * (mom->xz * dz + mom->xy * dy + mom->xx * dx);
+  Qmiry = (1.0 / 1.0) * (mom->yz * dz + mom->xy * dx + mom->yy * dy);
+  Qmirz = (1.0 / 1.0) * (mom->yz * dy + mom->xz * dx + mom->zz * dz);
+  Qmir = (1.0 / 2.0) * (Qmirx * dx + Qmiry * dy + Qmirz * dz);
+  *fPot -= gam[2] * Qmir;
+  Qta += gam[3] * Qmir;
+  *ax += gam[2] * Qmirx;
+  *ay += gam[2] * Qmiry;
+  *az += gam[2] * Qmirz;
+  *fPot -= gam[0] * mom->m;
+  Qta += gam[1] * mom->m;
+  *ax -= dx * Qta;
+  *ay -= dy * Qta;
+  *az -= dz * Qta;
+}
+
+static void momc_out(const momc_t* c, double* o) {
+  /* EwaldCUDA.h MomcData order */
+  const double v[32] = {c->m,    c->xx,   c->yy,   c->xy,   c->xz,   c->yz,   c->xxx,  c->xyy,
+                        c->xxy,  c->yyy,  c->xxz,  c->yyz,  c->xyz,  c->xxxx, c->xyyy, c->xxxy,
+                        c->yyyy, c->xxxz, c->yyyz, c->xxyy, c->xxyz, c->xyyz, c->zz,   c->xzz,
+                        c->yzz,  c->zzz,  c->xxzz, c->xyzz, c->xzzz, c->yyzz, c->yzzz, c->zzzz};
+  for (int k = 0; k < 32; ++k) o[k] = v[k];
+}
+
+/* TreePiece::EwaldInit h-table, Ewald.cpp:285-383 (hexadecapole). */
+int oracle_ewald_table_hex(const double* root, double L, double dEwhCut, double* ewt, int max_h,
+                           double* momc) {
+  momc_t c;
+  momc_from_root(root, &c);
+  if (momc) momc_out(&c, momc);
+  int hReps = (int)ceil(dEwhCut);
+  double alpha = 2.0 / L;
+  double k4 = M_PI * M_PI / (alpha * alpha * L * L);
+  int i = 0;
+  for (int hx = -hReps; hx <= hReps; ++hx)
+    for (int hy = -hReps; hy <= hReps; ++hy)
+      for (int hz = -hReps; hz <= hReps; ++hz) {
+        int h2 = hx * hx + hy * hy + hz * hz;
+        if (h2 == 0) continue;
+        if (h2 > dEwhCut * dEwhCut) continue;
+        if (i >= max_h) return -1;
+        double gam[6], ax = 0, ay = 0, az = 0, mfacc = 0.0, mfacs = 0.0;
+        gam[0] = exp(-k4 * h2) / (M_PI * h2 * L);
+        gam[1] = 2 * M_PI / L * gam[0];
+        gam[2] = -2 * M_PI / L * gam[1];
+        gam[3] = 2 * M_PI / L * gam[2];
+        gam[4] = -2 * M_PI / L * gam[3];
+        gam[5] = 2 * M_PI / L * gam[4];
+        gam[1] = 0.0; gam[3] = 0.0; gam[5] = 0.0;
+        qeval_hex(&c, gam, hx, hy, hz, &ax, &ay, &az, &mfacc);
+        gam[0] = exp(-k4 * h2) / (M_PI * h2 * L);
+        gam[1] = 2 * M_PI / L * gam[0];
+        gam[2] = -2 * M_PI / L * gam[1];
+        gam[3] = 2 * M_PI / L * gam[2];
+        gam[4] = -2 * M_PI / L * gam[3];
+        gam[5] = 2 * M_PI / L * gam[4];
+        gam[0] = 0.0; gam[2] = 0.0; gam[4] = 0.0;
+        ax = ay = az = 0.0;
+        qeval_hex(&c, gam, hx, hy, hz, &ax, &ay, &az, &mfacs);
+        ewt[5 * i + 0] = 2 * M_PI / L * hx;
+        ewt[5 * i + 1] = 2 * M_PI / L * hy;
+        ewt[5 * i + 2] = 2 * M_PI / L * hz;
+        ewt[5 * i + 3] = mfacc;
+        ewt[5 * i + 4] = mfacs;
+        ++i;
+      }
+  return i;
+}
+
+/* TreePiece::BucketEwald (hexadecapole), Ewald.cpp:72-281 for one
+ * particle: the complete root moments to fourth order, g0..g5. */
+static void ewald_one_hex(const double* p, const double* root, const momc_t* mom, double L,
+                          int nReps, double fEwCut, const double* ewt, int nEwhLoop, double* v) {
+  const double onethird = 1.0 / 3.0;
+  double Q4xx = 0.5 * (mom->xxxx + mom->xxyy + mom->xxzz);
+  double Q4xy = 0.5 * (mom->xxxy + mom->xyyy + mom->xyzz);
+  double Q4xz = 0.5 * (mom->xxxz + mom->xyyz + mom->xzzz);
+  double Q4yy = 0.5 * (mom->xxyy + mom->yyyy + mom->yyzz);
+  double Q4yz = 0.5 * (mom->xxyz + mom->yyyz + mom->yzzz);
+  double Q4zz = 0.5 * (mom->xxzz + mom->yyzz + mom->zzzz);
+  double Q4 = 0.25 * (Q4xx + Q4yy + Q4zz);
+  double Q3x = 0.5 * (mom->xxx + mom->xyy + mom->xzz);
+  double Q3y = 0.5 * (mom->xxy + mom->yyy + mom->yzz);
+  double Q3z = 0.5 * (mom->xxz + mom->yyz + mom->zzz);
+  double Q2 = 0.5 * (mom->xx + mom->yy + mom->zz);
+  int nEwReps = (int)ceil(fEwCut);
+  double fEwCut2 = fEwCut * fEwCut * L * L;
+  double fInner2 = 1.2e-3 * L * L;
+  if (nReps > nEwReps) nEwReps = nReps;
+  double alpha = 2.0 / L;
+  double alpha2 = alpha * alpha;
+  double k1 = M_PI / (alpha2 * L * L * L);
+  double ka = 2.0 * alpha / sqrt(M_PI);
+  double fPot = root[2] * k1, ax = 0.0, ay = 0.0, az = 0.0;
+  double dx = p[2] - root[3], dy = p[3] - root[4], dz = p[4] - root[5];
+  for (int ix = -nEwReps; ix <= nEwReps; ++ix) {
+    int bInHolex = (ix >= -nReps && ix <= nReps);
+    double x = dx + ix * L;
+    for (int iy = -nEwReps; iy <= nEwReps; ++iy) {
+      int bInHolexy = (bInHolex && iy >= -nReps && iy <= nReps);
+      double y = dy + iy * L;
+      for (int iz = -nEwReps; iz <= nEwReps; ++iz) {
+        int bInHole = (bInHolexy && iz >= -nReps && iz <= nReps);
+        double z = dz + iz * L;
+        double r2 = x * x + y * y + z * z;
+        if (r2 > fEwCut2 && !bInHole) continue;
+        double g0, g1, g2, g3, g4, g5, alphan;
+        if (r2 < fInner2) {
+          alphan = ka;
+          r2 *= alpha2;
+          g0 = alphan * ((1.0 / 3.0) * r2 - 1.0);
+          alphan *= 2 * alpha2;
+          g1 = alphan * ((1.0 / 5.0) * r2 - (1.0 / 3.0));
+          alphan *= 2 * alpha2;
+          g2 = alphan * ((1.0 / 7.0) * r2 - (1.0 / 5.0));
+          alphan *= 2 * alpha2;
+          g3 = alphan * ((1.0 / 9.0) * r2 - (1.0 / 7.0));
+          alphan *= 2 * alpha2;
+          g4 = alphan * ((1.0 / 11.0) * r2 - (1.0 / 9.0));
+          alphan *= 2 * alpha2;
+          g5 = alphan * ((1.0 / 13.0) * r2 - (1.0 / 11.0));
+        } else {
+          double dir = 1 / sqrt(r2);
+          double dir2 = dir * dir;
+          double a = exp(-r2 * alpha2);
+          a *= ka * dir2;
+          if (bInHole) g0 = -erf(alpha / dir);
+          else g0 = erfc(alpha / dir);
+          g0 *= dir;
+          g1 = g0 * dir2 + a;
+          alphan = 2 * alpha2;
+          g2 = 3 * g1 * dir2 + alphan * a;
+          alphan *= 2 * alpha2;
+          g3 = 5 * g2 * dir2 + alphan * a;
+          alphan *= 2 * alpha2;
+          g4 = 7 * g3 * dir2 + alphan * a;
+          alphan *= 2 * alpha2;
+          g5 = 9 * g4 * dir2 + alphan * a;
+        }
+        double xx = 0.5 * x * x;
+        double xxx = onethird * xx * x;
+        double xxy = xx * y;
+        double xxz = xx * z;
+        double yy = 0.5 * y * y;
+        double yyy = onethird * yy * y;
+        double xyy = yy * x;
+        double yyz = yy * z;
+        double zz = 0.5 * z * z;
+        double zzz = onethird * zz * z;
+        double xzz = zz * x;
+        double yzz = zz * y;
+        double xy = x * y;
+        double xyz = xy * z;
+        double xz = x * z;
+        double yz = y * z;
+        double Q2mirx = mom->xx * x + mom->xy * y + mom->xz * z;
+        double Q2miry = mom->xy * x + mom->yy * y + mom->yz * z;
+        double Q2mirz = mom->xz * x + mom->yz * y + mom->zz * z;
+        double Q3mirx = mom->xxx * xx + mom->xxy * xy + mom->xxz * xz + mom->xyy * yy +
+                        mom->xyz * yz + mom->xzz * zz;
+        double Q3miry = mom->xxy * xx + mom->xyy * xy + mom->xyz * xz + mom->yyy * yy +
+                        mom->yyz * yz + mom->yzz * zz;
+        double Q3mirz = mom->xxz * xx + mom->xyz * xy + mom->xzz * xz + mom->yyz * yy +
+                        mom->yzz * yz + mom->zzz * zz;
+        double Q4mirx = mom->xxxx * xxx + mom->xxxy * xxy + mom->xxxz * xxz + mom->xxyy * xyy +
+                        mom->xxyz * xyz + mom->xxzz * xzz + mom->xyyy * yyy + mom->xyyz * yyz +
+                        mom->xyzz * yzz + mom->xzzz * zzz;
+        double Q4miry = mom->xxxy * xxx + mom->xxyy * xxy + mom->xxyz * xxz + mom->xyyy * xyy +
+                        mom->xyyz * xyz + mom->xyzz * xzz + mom->yyyy * yyy + mom->yyyz * yyz +
+                        mom->yyzz * yzz + mom->yzzz * zzz;
+        double Q4mirz = mom->xxxz * xxx + mom->xxyz * xxy + mom->xxzz * xxz + mom->xyyz * xyy +
+                        mom->xyzz * xyz + mom->xzzz * xzz + mom->yyyz * yyy + mom->yyzz * yyz +
+                        mom->yzzz * yzz + mom->zzzz * zzz;
+        double Q4x = Q4xx * x + Q4xy * y + Q4xz * z;
+        double Q4y = Q4xy * x + Q4yy * y + Q4yz * z;
+        double Q4z = Q4xz * x + Q4yz * y + Q4zz * z;
+        double Q2mir = 0.5 * (Q2mirx * x + Q2miry * y + Q2mirz * z) - (Q3x * x + Q3y * y + Q3z * z) + Q4;
+        double Q3mir = onethird * (Q3mirx * x + Q3miry * y + Q3mirz * z) - 0.5 * (Q4x * x + Q4y * y + Q4z * z);
+        double Q4mir = 0.25 * (Q4mirx * x + Q4miry * y + Q4mirz * z);
+        double Qta = g1 * mom->m - g2 * Q2 + g3 * Q2mir + g4 * Q3mir + g5 * Q4mir;
+        fPot -= g0 * mom->m - g1 * Q2 + g2 * Q2mir + g3 * Q3mir + g4 * Q4mir;
+        ax += g2 * (Q2mirx - Q3x) + g3 * (Q3mirx - Q4x) + g4 * Q4mirx - x * Qta;
+        ay += g2 * (Q2miry - Q3y) + g3 * (Q3miry - Q4y) + g4 * Q4miry - y * Qta;
+        az += g2 * (Q2mirz - Q3z) + g3 * (Q3mirz - Q4z) + g4 * Q4mirz - z * Qta;
+      }
+    }
+  }
+  for (int i = 0; i < nEwhLoop; ++i) {
+    const double* e = ewt + 5 * i;
+    double hdotx = e[0] * dx + e[1] * dy + e[2] * dz;
+    double c = cos(hdotx), s = sin(hdotx);
+    fPot += e[3] * c + e[4] * s;
+    ax += e[0] * (e[3] * s - e[4] * c);
+    ay += e[1] * (e[3] * s - e[4] * c);
+    az += e[2] * (e[3] * s - e[4] * c);
+  }
+  v[3] += fPot;
+  v[0] += ax;
+  v[1] += ay;
+  v[2] += az;
+}
+
+int oracle_ewald_forces_hex(const double* parts, long n_parts, const int* idx, long n_idx,
+                            const double* root, double L, int nReps, double fEwCut,
+                            double dEwhCut, double* vars, int nthreads) {
+  (void)n_parts;
+  double ewt[5 * 4096];
+  momc_t c;
+  momc_from_root(root, &c);
+  int nh = oracle_ewald_table_hex(root, L, dEwhCut, ewt, 4096, NULL);
+  if (nh < 0) return -1;
+#ifdef _OPENMP
+  if (nthreads > 0) omp_set_num_threads(nthreads);
+#pragma omp parallel for schedule(dynamic, 64)
+#endif
+  for (long k = 0; k < n_idx; ++k) {
+    long j = idx ? idx[k] : k;
+    ewald_one_hex(parts + 5 * (size_t)j, root, &c, L, nReps, fEwCut, ewt, nh,
+                  vars + 5 * (size_t)k);
+  }
+  return 0;
+}

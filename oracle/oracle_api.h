@@ -72,6 +72,16 @@ int oracle_cell_list_forces_hex(const double* moments, long n_moments, const dou
                                 const int* starts, const int* sizes, int n_buckets,
                                 const double* geom, double fperiod, double* vars, int nthreads);
 
+/* Hexadecapole build of the Ewald correction: root_moments holds the 27
+ * hexadecapole values of the root (layout as above).  The table function
+ * also returns the root's complete moments (MomcData order, 32 doubles) in
+ * momc when it is not NULL. */
+int oracle_ewald_table_hex(const double* root_moments, double L, double dEwhCut, double* ewt,
+                           int max_h, double* momc);
+int oracle_ewald_forces_hex(const double* parts, long n_parts, const int* idx, long n_idx,
+                            const double* root_moments, double L, int nReps, double fEwCut,
+                            double dEwhCut, double* vars, int nthreads);
+
 #ifdef __cplusplus
 }
 #endif

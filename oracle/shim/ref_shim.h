@@ -176,6 +176,9 @@ class TreePiece {
   bool bBucketsInited;
   int thisIndex, numTreePieces, numChunks;
   ShimTreePieceProxy thisProxy;
+#ifdef HEXADECAPOLE
+  MOMC momcRoot; /* ParallelGravity.h: the root's complete moments */
+#endif
   TreePiece()
       : myParticles(0), root(0), nReplicas(0), fEwCut(0), dEwhCut(0), ewt(0),
         nMaxEwhLoop(100), nEwhLoop(0), activeRung(0), bBucketsInited(true),

@@ -27,21 +27,26 @@ def _declared(header):
     return sorted(set(n for n in names if not n.startswith("_")))
 
 
-def _exported():
-    out = subprocess.run(["nm", "-D", "--defined-only", N._build.CUDA_LIB], capture_output=True,
-                         text=True, check=True).stdout
+def _exported(path=None):
+    out = subprocess.run(["nm", "-D", "--defined-only", path or N._build.CUDA_LIB],
+                         capture_output=True, text=True, check=True).stdout
     return set(l.split()[-1] for l in out.splitlines() if " T " in l)
 
 
+@pytest.mark.parametrize("build", ["quadrupole", "hexadecapole"])
 @pytest.mark.parametrize("header", ["HostCUDA.h", "EwaldCUDA.h", "changa_gb300.h"])
-def test_every_declared_symbol_exported(lib, header):
+def test_every_declared_symbol_exported(lib, header, build):
+    """Both builds of the library (the quadrupole one and the HEXADECAPOLE
+    one) export the whole boundary."""
     names = _declared(header)
     assert len(names) >= 3
-    exported = _exported()
+    hexa = build == "hexadecapole"
+    exported = _exported(N._build.HEX_LIB if hexa else None)
     missing = [n for n in names if n not in exported]
     assert not missing, missing
+    loaded = N.cuda_lib_hex() if hexa else lib
     for n in names:
-        assert hasattr(lib, n)
+        assert hasattr(loaded, n)
 
 
 def test_reference_mangled_names_exported(lib):
@@ -109,6 +114,75 @@ def test_struct_layouts(tmp_path):
     assert N.CudaRequest.fperiod.offset == got["CudaRequest.fperiod"]
     assert N.CudaRequest.remote.offset == got["CudaRequest.remote"]
     assert N.CudaRequest.cb.offset == got["CudaRequest.cb"]
+
+
+LAYOUT_PROBE_HEX = r"""
+#include <stdio.h>
+#include <stddef.h>
+#include "HostCUDA.h"
+#include "EwaldCUDA.h"
+#define P(T) printf(#T " %zu\n", sizeof(T))
+#define O(T, f) printf(#T "." #f " %zu\n", offsetof(T, f))
+int main(void) {
+  P(CudaMultipoleMoments); P(MultipoleMomentsData); P(MomcData); P(EwaldReadOnlyData);
+  O(CudaMultipoleMoments, xx); O(CudaMultipoleMoments, xxx); O(CudaMultipoleMoments, xxxx);
+  O(CudaMultipoleMoments, xyyz); O(EwaldReadOnlyData, momcRoot); O(EwaldReadOnlyData, n);
+  O(EwaldReadOnlyData, fInner2);
+  return 0;
+}
+"""
+
+
+def test_struct_layouts_hexadecapole(tmp_path):
+    """The boundary headers compiled with -DHEXADECAPOLE give the reference's
+    hexadecapole layouts (cuda_typedef.h:104-128, EwaldCUDA.h:18-47)."""
+    src = tmp_path / "probe_hex.c"
+    src.write_text(LAYOUT_PROBE_HEX)
+    exe = tmp_path / "probe_hex"
+    cuda_inc = os.path.join(os.environ.get("CUDA_HOME", "/usr/local/cuda"), "include")
+    subprocess.run(["gcc", "-DHEXADECAPOLE", "-I", INCLUDE, "-I", cuda_inc, str(src), "-o",
+                    str(exe)], check=True)
+    got = dict(l.rsplit(" ", 1) for l in subprocess.run([str(exe)], capture_output=True, text=True,
+                                                        check=True).stdout.splitlines())
+    got = {k: int(v) for k, v in got.items()}
+    assert got["CudaMultipoleMoments"] == 108
+    assert got["CudaMultipoleMoments.xx"] == 24
+    assert got["CudaMultipoleMoments.xxx"] == 44
+    assert got["CudaMultipoleMoments.xxxx"] == 72
+    assert got["CudaMultipoleMoments.xyyz"] == 104
+    assert got["MultipoleMomentsData"] == 16
+    assert got["MomcData"] == 128
+    assert got["EwaldReadOnlyData"] == 16 + 128 + 16 + 32
+    assert got["EwaldReadOnlyData.momcRoot"] == 16
+    import ctypes as C
+    assert C.sizeof(N.EwaldReadOnlyDataHex) == got["EwaldReadOnlyData"]
+    assert N.EwaldReadOnlyDataHex.n.offset == got["EwaldReadOnlyData.n"]
+    assert N.EwaldReadOnlyDataHex.fInner2.offset == got["EwaldReadOnlyData.fInner2"]
+
+
+def _hex_root():
+    from changa_gb300 import ics, tree
+    p = ics.nfw_halos(8000, ics.rng_for(2), soft=1e-3)
+    L = tree.build_lists(p["pos"], p["mass"], p["soft"], n_bucket=16, theta=0.7, period=1.0,
+                         order=4)
+    return L.moments[0].copy()
+
+
+def test_ewald_table_hex_matches_oracle(lib):
+    """changa_ewald_table_hex (our restatement of EwaldInit with
+    HEXADECAPOLE) against the oracle: the complete root moments exactly, the
+    table to rounding (the contractions are summed in another order)."""
+    import oracle
+    from changa_gb300.gravity import EwaldConfig
+    root = _hex_root()
+    tb, momc = EwaldConfig(1.0, 1, 2.6, 2.8).table_hex(root)
+    ref, ref_momc = oracle.ewald_table_hex(root, 1.0, 2.8)
+    assert tb.shape == (80, 5)
+    np.testing.assert_array_equal(momc, ref_momc)
+    np.testing.assert_array_equal(tb[:, :3], ref[:, :3])
+    scale = np.abs(ref[:, 3:]).max(axis=0)
+    assert (np.abs(tb[:, 3:] - ref[:, 3:]).max(axis=0) <= 1e-14 * scale).all()
+    assert np.abs(ref[:, 4]).max() > 0  # the octupole gives a sine term
 
 
 def test_ewald_table_matches_oracle(lib):

@@ -9,7 +9,7 @@ import pytest
 import oracle
 from changa_gb300 import _native as N
 from changa_gb300 import gravity, ics, tree
-from helpers import force_rel_err, pot_rel_err
+from helpers import force_rel_err, force_rms_err, pot_rel_err
 
 pytestmark = pytest.mark.gpu
 
@@ -69,3 +69,84 @@ def test_hex_closer_to_direct_sum_than_quadrupole(cuda_ok):
         print("plummer64k theta 0.7 order %d: median %.2e p99 %.2e" % (
             order, med[order], np.percentile(e, 99)))
     assert med[4] < med[2] / 4
+
+
+def _f32(a):
+    return np.asarray(a, np.float32).astype(np.float64)
+
+
+def _dropin_reference(L, ewald=None):
+    """What the HEXADECAPOLE drop-in computes, by the oracle on the FP32
+    inputs it receives: the cell list (cells whose softening misses the
+    bucket; ChaNGa evaluates the softened ones on the CPU) with
+    momEvalFmomrcm, the particle list, and the hexadecapole Ewald term."""
+    mom, parts = _f32(L.moments), _f32(L.parts)
+    v = oracle.cell_forces_hex(mom, parts, L.cells, oracle.bucket_geometry(L, L.cells),
+                               fperiod=L.period)
+    v = oracle.part_forces(parts, parts, L.plist, fperiod=L.period, vars=v)
+    if ewald is not None:
+        v = oracle.ewald_forces_hex(parts, L.moments[0], ewald.L, ewald.n_reps, ewald.fEwCut,
+                                    ewald.dEwhCut, vars=v)
+    return v
+
+
+def test_hex_dropin_matches_oracle(cuda_ok):
+    """The boundary of ChaNGa's hexadecapole build (libchanga_gb300_hex.so:
+    108-byte CudaMultipoleMoments through DataManagerTransferLocalTree and
+    TreePieceCellListDataTransferLocal) against the oracle."""
+    p = ics.plummer(32768, ics.rng_for(0), soft=0.01)
+    L = tree.build_lists(p["pos"], p["mass"], p["soft"], n_bucket=16, theta=0.7, order=4)
+    ref = _dropin_reference(L)
+    inp = gravity.DropInInputs(L)
+    try:
+        assert inp.moments.nbytes == 108 * L.moments.shape[0]
+        v = gravity.dropin_step(inp).astype(np.float64)
+    finally:
+        inp.free()
+    e = force_rel_err(v, ref)
+    print("hex drop-in: median %.2e p99 %.2e" % (np.median(e), np.percentile(e, 99)))
+    assert np.median(e) < 2e-6 and np.percentile(e, 99) < 1e-4
+    assert np.median(pot_rel_err(v, ref)) < 2e-6
+    np.testing.assert_allclose(v[:, 4], ref[:, 4], rtol=1e-4)
+
+
+def test_hex_dropin_ewald(cuda_ok):
+    """EwaldHost of the hexadecapole build (the root's complete moments in
+    EwaldReadOnlyData.momcRoot, octupole sine terms in the h-table) on a
+    clustered periodic box, with the tree replicas, against the oracle."""
+    p = ics.nfw_halos(32768, ics.rng_for(2), soft=1e-3)
+    L = tree.build_lists(p["pos"], p["mass"], p["soft"], n_bucket=16, theta=0.7, period=1.0,
+                         order=4)
+    ew = gravity.EwaldConfig(1.0, 1, 2.6, 2.8)
+    ref = _dropin_reference(L, ew)
+    inp = gravity.DropInInputs(L, ewald=ew)
+    try:
+        v = gravity.dropin_step(inp).astype(np.float64)
+    finally:
+        inp.free()
+    e = force_rms_err(v, ref)
+    dpot = np.abs(v[:, 3] - ref[:, 3])
+    # the quadrupole build's drop-in on the same box, for scale
+    Lq = tree.build_lists(p["pos"], p["mass"], p["soft"], n_bucket=16, theta=0.7, period=1.0)
+    mq, pq = _f32(Lq.moments), _f32(Lq.parts)
+    refq = oracle.cell_forces(mq, pq, Lq.cells, fperiod=1.0)
+    refq = oracle.part_forces(pq, pq, Lq.plist, fperiod=1.0, vars=refq)
+    refq = oracle.ewald_forces(pq, _f32(Lq.root), 1.0, 1, 2.6, 2.8, vars=refq)
+    inq = gravity.DropInInputs(Lq, ewald=ew)
+    try:
+        vq = gravity.dropin_step(inq).astype(np.float64)
+    finally:
+        inq.free()
+    dpot_q = np.abs(vq[:, 3] - refq[:, 3])
+    worst = int(np.argmax(dpot))
+    r2 = ((L.parts[worst, 2:5] - L.moments[0, 3:6]) ** 2).sum()
+    print("hex drop-in with Ewald: median %.2e max %.2e; pot max %.2e (r^2 to the root %.2e), "
+          "quadrupole build pot max %.2e" % (np.median(e), e.max(), dpot.max(), r2, dpot_q.max()))
+    # FP32 rounding of O(10) hole and replica terms of size G M / L = 1
+    # against the rms force, as for the quadrupole drop-in
+    assert np.median(e) < 5e-5 and e.max() < 2e-3
+    # the potential carries the reference's single-precision two-term series
+    # inside fInner2 = 1.1e-2 L^2 (Ewald.cpp:508-516), where the dropped
+    # (alpha r)^4 term of g0 alone reaches ka (alpha r)^4 / 10 = 4.5e-4 of
+    # G M / L; the oracle (CPU constants) switches at 1.2e-3 L^2
+    assert dpot.max() < 1e-3 and dpot_q.max() < 1e-3

@@ -148,3 +148,39 @@ def test_hex_more_accurate_than_quadrupole(built):
         e = np.linalg.norm(v[gi, :3] - acc, axis=1) / np.linalg.norm(acc, axis=1)
         med[order] = np.median(e)
     assert med[4] < med[2] / 4 and med[4] < 3e-4, med
+
+
+@pytest.mark.skipif(not os.path.exists(oracle.REF_HEX_LIB), reason="reference not built here")
+def test_hex_ewald_port_bitexact_vs_reference(built):
+    """The port's hexadecapole Ewald (EwaldInit's complete root moments and
+    h-table, BucketEwald to fourth order) is bit-identical to the reference's
+    Ewald.cpp built with HEXADECAPOLE, on a clustered periodic root with
+    sizeable octupole and hexadecapole moments."""
+    p = ics.nfw_halos(16384, ics.rng_for(2), soft=1e-3)
+    L = tree.build_lists(p["pos"], p["mass"], p["soft"], n_bucket=16, theta=0.7, period=1.0,
+                         order=4)
+    root = L.moments[0]
+    tp, mp = oracle.ewald_table_hex(root, 1.0, 2.8, kind="port")
+    tr, mr = oracle.ewald_table_hex(root, 1.0, 2.8, kind="ref")
+    assert np.array_equal(tp, tr) and np.array_equal(mp, mr)
+    assert np.abs(tr[:, 4]).max() > 0
+    idx = np.arange(0, L.n, 61).astype(np.int32)
+    a = oracle.ewald_forces_hex(L.parts, root, 1.0, 1, 2.6, 2.8, idx=idx, kind="port")
+    b = oracle.ewald_forces_hex(L.parts, root, 1.0, 1, 2.6, 2.8, idx=idx, kind="ref")
+    assert np.array_equal(a, b)
+
+
+def test_hex_ewald_single_particle_no_self_force():
+    """Hexadecapole build: a lone particle feels no force from its own
+    replicas, tree replicas plus the Ewald correction."""
+    p = dict(pos=np.array([[0.3, 0.6, 0.45]]), mass=np.array([1.0]), soft=np.array([1e-3]))
+    L = tree.build_lists(p["pos"], p["mass"], p["soft"], n_bucket=16, theta=0.7, period=1.0,
+                         order=4)
+    v = np.zeros((1, 5))
+    for req in (L.cells, L.softcells):
+        if req.n_buckets:
+            v = oracle.cell_forces_hex(L.moments, L.parts, req, oracle.bucket_geometry(L, req),
+                                       fperiod=1.0, vars=v)
+    v = oracle.part_forces(L.parts, L.parts, L.plist, fperiod=1.0, vars=v)
+    v = oracle.ewald_forces_hex(L.parts, L.moments[0], 1.0, 1, 2.6, 2.8, vars=v)
+    assert np.abs(v[0, :3]).max() < 1e-6
