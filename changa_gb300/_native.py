@@ -128,7 +128,8 @@ class ChangaTreeArrays(C.Structure):
 
 class ChangaEwaldParams(C.Structure):
     _fields_ = [("root", C.c_double * 12), ("L", C.c_double), ("nReps", C.c_int),
-                ("fEwCut", C.c_double), ("nEwhLoop", C.c_int), ("ewt", C.c_void_p)]
+                ("fEwCut", C.c_double), ("nEwhLoop", C.c_int), ("ewt", C.c_void_p),
+                ("momc", C.c_void_p)]
 
 
 CHANGA_ERRORS_ABORT = 0
@@ -223,7 +224,8 @@ CUDA_SIGNATURES = {
                               _VP, _VP, _VP, _VP, _VP]),
     "changa_gravity_step_hexa": (_I, [_I, _VP, _LL, _VP, _LL, C.POINTER(ChangaListRequest),
                                       C.POINTER(ChangaListRequest),
-                                      C.POINTER(ChangaListRequest), _D, _VP, _VP]),
+                                      C.POINTER(ChangaListRequest), _D,
+                                      C.POINTER(ChangaEwaldParams), _VP, _VP]),
     "changa_ewald_forces": (_I, [_I, _VP, _LL, _VP, _LL, C.POINTER(ChangaEwaldParams), _VP, _VP]),
     "changa_ewald_table": (_I, [_VP, _D, _D, _VP, _I]),
     "changa_ewald_table_hex": (_I, [_VP, _D, _D, _VP, _I, _VP]),

@@ -68,9 +68,10 @@ cudaError_t launch_ewald_f32(const CompactPartData* parts, VariablePartData* var
                              const int* markers, int largephase, int first, int last,
                              const EwaldReadOnlyData& ro, const EwtData* ewt,
                              cudaStream_t s);
+/* hex: the hexadecapole build's expansion (p.momc required) */
 cudaError_t launch_ewald_fp(int form, const double* parts, long long n_parts, const int* idx,
                             long long n_idx, const ChangaEwaldParams& p, double* vars,
-                            cudaStream_t s);
+                            cudaStream_t s, bool hex = false);
 
 /* runtime helpers (hostcuda.cu) */
 int sm_count();

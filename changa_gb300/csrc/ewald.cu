@@ -196,20 +196,92 @@ __global__ void __launch_bounds__(128) ewald_f32_kernel(const CompactPartData* _
   v.a.z += az;
   v.potential += fPot;
 }
+/* The hexadecapole build's root for the extension forms: complete moments
+ * (EwaldCUDA.h MomcData order) and their traces (Ewald.cpp:99-111). */
+template <typename T>
+struct HexRoot {
+  T c[32];
+  T Q4xx, Q4xy, Q4xz, Q4yy, Q4yz, Q4zz, Q4, Q3x, Q3y, Q3z, Q2;
+};
+
+template <typename T>
+void fill_hex_root(const double* mc, HexRoot<T>& R) {
+  for (int k = 0; k < 32; ++k) R.c[k] = (T)mc[k];
+  R.Q4xx = (T)(0.5 * (mc[13] + mc[19] + mc[26]));
+  R.Q4xy = (T)(0.5 * (mc[15] + mc[14] + mc[27]));
+  R.Q4xz = (T)(0.5 * (mc[17] + mc[21] + mc[28]));
+  R.Q4yy = (T)(0.5 * (mc[19] + mc[16] + mc[29]));
+  R.Q4yz = (T)(0.5 * (mc[20] + mc[18] + mc[30]));
+  R.Q4zz = (T)(0.5 * (mc[26] + mc[29] + mc[31]));
+  R.Q4 = (T)(0.25 * (0.5 * (mc[13] + mc[19] + mc[26]) + 0.5 * (mc[19] + mc[16] + mc[29]) +
+                     0.5 * (mc[26] + mc[29] + mc[31])));
+  R.Q3x = (T)(0.5 * (mc[6] + mc[7] + mc[23]));
+  R.Q3y = (T)(0.5 * (mc[8] + mc[9] + mc[24]));
+  R.Q3z = (T)(0.5 * (mc[10] + mc[11] + mc[25]));
+  R.Q2 = (T)(0.5 * (mc[1] + mc[2] + mc[22]));
+}
+
+/* One real-space term of the hexadecapole expansion about the root
+ * (Ewald.cpp:203-240) at offset (x, y, z) with g0..g5.  MomcData indices:
+ * 0 m; 1 xx 2 yy 3 xy 4 xz 5 yz; 6 xxx 7 xyy 8 xxy 9 yyy 10 xxz 11 yyz
+ * 12 xyz; 13 xxxx 14 xyyy 15 xxxy 16 yyyy 17 xxxz 18 yyyz 19 xxyy 20 xxyz
+ * 21 xyyz; 22 zz; 23 xzz 24 yzz 25 zzz; 26 xxzz 27 xyzz 28 xzzz 29 yyzz
+ * 30 yzzz 31 zzzz. */
+template <typename T>
+__device__ __forceinline__ void hex_ewald_term(const HexRoot<T>& R, T x, T y, T z, T g0, T g1,
+                                               T g2, T g3, T g4, T g5, T& fPot, T& ax, T& ay,
+                                               T& az) {
+  const T* c = R.c;
+  const T third = T(1) / T(3);
+  const T xx = T(0.5) * x * x, yy = T(0.5) * y * y, zz = T(0.5) * z * z;
+  const T xy = x * y, xz = x * z, yz = y * z, xyz = xy * z;
+  const T xxx = third * xx * x, yyy = third * yy * y, zzz = third * zz * z;
+  const T xxy = xx * y, xxz = xx * z, xyy = yy * x, yyz = yy * z, xzz = zz * x, yzz = zz * y;
+  const T Q2mirx = c[1] * x + c[3] * y + c[4] * z;
+  const T Q2miry = c[3] * x + c[2] * y + c[5] * z;
+  const T Q2mirz = c[4] * x + c[5] * y + c[22] * z;
+  const T Q3mirx = c[6] * xx + c[8] * xy + c[10] * xz + c[7] * yy + c[12] * yz + c[23] * zz;
+  const T Q3miry = c[8] * xx + c[7] * xy + c[12] * xz + c[9] * yy + c[11] * yz + c[24] * zz;
+  const T Q3mirz = c[10] * xx + c[12] * xy + c[23] * xz + c[11] * yy + c[24] * yz + c[25] * zz;
+  const T Q4mirx = c[13] * xxx + c[15] * xxy + c[17] * xxz + c[19] * xyy + c[20] * xyz +
+                   c[26] * xzz + c[14] * yyy + c[21] * yyz + c[27] * yzz + c[28] * zzz;
+  const T Q4miry = c[15] * xxx + c[19] * xxy + c[20] * xxz + c[14] * xyy + c[21] * xyz +
+                   c[27] * xzz + c[16] * yyy + c[18] * yyz + c[29] * yzz + c[30] * zzz;
+  const T Q4mirz = c[17] * xxx + c[20] * xxy + c[26] * xxz + c[21] * xyy + c[27] * xyz +
+                   c[28] * xzz + c[18] * yyy + c[29] * yyz + c[30] * yzz + c[31] * zzz;
+  const T Q4x = R.Q4xx * x + R.Q4xy * y + R.Q4xz * z;
+  const T Q4y = R.Q4xy * x + R.Q4yy * y + R.Q4yz * z;
+  const T Q4z = R.Q4xz * x + R.Q4yz * y + R.Q4zz * z;
+  const T Q2mir = T(0.5) * (Q2mirx * x + Q2miry * y + Q2mirz * z) -
+                  (R.Q3x * x + R.Q3y * y + R.Q3z * z) + R.Q4;
+  const T Q3mir = third * (Q3mirx * x + Q3miry * y + Q3mirz * z) -
+                  T(0.5) * (Q4x * x + Q4y * y + Q4z * z);
+  const T Q4mir = T(0.25) * (Q4mirx * x + Q4miry * y + Q4mirz * z);
+  const T M = c[0];
+  const T Qta = g1 * M - g2 * R.Q2 + g3 * Q2mir + g4 * Q3mir + g5 * Q4mir;
+  fPot -= g0 * M - g1 * R.Q2 + g2 * Q2mir + g3 * Q3mir + g4 * Q4mir;
+  ax += g2 * (Q2mirx - R.Q3x) + g3 * (Q3mirx - Q4x) + g4 * Q4mirx - x * Qta;
+  ay += g2 * (Q2miry - R.Q3y) + g3 * (Q3miry - Q4y) + g4 * Q4miry - y * Qta;
+  az += g2 * (Q2mirz - R.Q3z) + g3 * (Q3mirz - Q4z) + g4 * Q4mirz - z * Qta;
+}
+
 struct EwaldFpArgs {
   double mom[12];
+  HexRoot<double> hex;  // the hexadecapole build's root (HEX kernels only)
   double L, fEwCut2, alpha, alpha2, k1, ka;
   int nReps, nEwReps, nEwhLoop;
   double ewt[CHANGA_MAX_EWH][5];
 };
 
-/* FP64 real-space term (Ewald.cpp:137-196, quadrupole). */
+/* FP64 real-space term (Ewald.cpp:137-240): quadrupole, or with HEX the
+ * hexadecapole expansion of the complete root moments (g4, g5 added). */
+template <bool HEX>
 __device__ __forceinline__ void ewald_term_f64(const EwaldFpArgs& P, double x, double y, double z,
                                                bool hole, double fInner2, double& fPot,
                                                double& ax, double& ay, double& az) {
   const double* mom = P.mom;
   double r2 = x * x + y * y + z * z;
-  double g0, g1, g2, g3;
+  double g0, g1, g2, g3, g4 = 0.0, g5 = 0.0;
   if (r2 < fInner2) {
     double alphan = P.ka;
     r2 *= P.alpha2;
@@ -220,6 +292,12 @@ __device__ __forceinline__ void ewald_term_f64(const EwaldFpArgs& P, double x, d
     g2 = alphan * ((1.0 / 7.0) * r2 - (1.0 / 5.0));
     alphan *= 2 * P.alpha2;
     g3 = alphan * ((1.0 / 9.0) * r2 - (1.0 / 7.0));
+    if constexpr (HEX) {
+      alphan *= 2 * P.alpha2;
+      g4 = alphan * ((1.0 / 11.0) * r2 - (1.0 / 9.0));
+      alphan *= 2 * P.alpha2;
+      g5 = alphan * ((1.0 / 13.0) * r2 - (1.0 / 11.0));
+    }
   } else {
     const double dir = rsqrt(r2);
     const double dir2 = dir * dir;
@@ -233,6 +311,16 @@ __device__ __forceinline__ void ewald_term_f64(const EwaldFpArgs& P, double x, d
     g2 = 3 * g1 * dir2 + alphan * a;
     alphan *= 2 * P.alpha2;
     g3 = 5 * g2 * dir2 + alphan * a;
+    if constexpr (HEX) {
+      alphan *= 2 * P.alpha2;
+      g4 = 7 * g3 * dir2 + alphan * a;
+      alphan *= 2 * P.alpha2;
+      g5 = 9 * g4 * dir2 + alphan * a;
+    }
+  }
+  if constexpr (HEX) {
+    hex_ewald_term<double>(P.hex, x, y, z, g0, g1, g2, g3, g4, g5, fPot, ax, ay, az);
+    return;
   }
   const double Q2 = 0.5 * (mom[6] + mom[9] + mom[11]);
   const double Q2mirx = mom[6] * x + mom[7] * y + mom[8] * z;
@@ -247,6 +335,7 @@ __device__ __forceinline__ void ewald_term_f64(const EwaldFpArgs& P, double x, d
 }
 
 
+template <bool HEX>
 __global__ void __launch_bounds__(128) ewald_f64_kernel(const double* __restrict__ parts,
                                                         long long n_parts,
                                                         const int* __restrict__ idx,
@@ -272,7 +361,7 @@ __global__ void __launch_bounds__(128) ewald_f64_kernel(const double* __restrict
         const double z = dzd + iz * P.L;
         const double r2 = x * x + y * y + z * z;
         if (r2 > P.fEwCut2 && !hole) continue;
-        ewald_term_f64(P, x, y, z, hole, fInner2, fPot, ax, ay, az);
+        ewald_term_f64<HEX>(P, x, y, z, hole, fInner2, fPot, ax, ay, az);
       }
     }
   }
@@ -303,6 +392,7 @@ constexpr int kMixWarps = 4;
 struct EwaldMixArgs {
   double cm[3];
   float M, xx, xy, xz, yy, yz, zz, Q2;
+  HexRoot<float> hex;  // the hexadecapole build's root (HEX kernels only)
   float L, alpha2, ka, cut2, k1M, twopi_over_L;
   int nReps, nEwReps, nEwhLoop;
   float4 h[CHANGA_MAX_EWH];  // integer h as floats, hCfac
@@ -361,6 +451,7 @@ __device__ __forceinline__ float erfc_nr(float x, float x2) {
   return t * __expf(p - x2);
 }
 
+template <bool HEX>
 __global__ void __launch_bounds__(kMixWarps * 32) ewald_mix_kernel(
     const double* __restrict__ parts, long long n_parts, const int* __restrict__ idx,
     long long n_idx, double* __restrict__ vars, const __grid_constant__ EwaldMixArgs P) {
@@ -430,12 +521,16 @@ __global__ void __launch_bounds__(kMixWarps * 32) ewald_mix_kernel(
     const float r2 = x * x + y * y + z * z;
     if (r2 > P.cut2 && !hole) continue;
     const float s = a2 * r2;
-    float g0, g1, g2, g3;
+    float g0, g1, g2, g3, g4 = 0.f, g5 = 0.f;
     if (hole && s < 1.0f) {
       g0 = -ka * hole_series<0>(s);
       g1 = -twoa2 * ka * hole_series<1>(s);
       g2 = -foura4 * ka * hole_series<2>(s);
       g3 = -foura4 * twoa2 * ka * hole_series<3>(s);
+      if constexpr (HEX) {
+        g4 = -foura4 * foura4 * ka * hole_series<4>(s);
+        g5 = -foura4 * foura4 * twoa2 * ka * hole_series<5>(s);
+      }
     } else {
       const float dir = rsqrtf(r2);
       const float dir2 = dir * dir;
@@ -447,6 +542,14 @@ __global__ void __launch_bounds__(kMixWarps * 32) ewald_mix_kernel(
       g1 = fmaf(g0, dir2, a);
       g2 = fmaf(3.f * g1, dir2, twoa2 * a);
       g3 = fmaf(5.f * g2, dir2, foura4 * a);
+      if constexpr (HEX) {
+        g4 = fmaf(7.f * g3, dir2, foura4 * twoa2 * a);
+        g5 = fmaf(9.f * g4, dir2, foura4 * foura4 * a);
+      }
+    }
+    if constexpr (HEX) {
+      hex_ewald_term<float>(P.hex, x, y, z, g0, g1, g2, g3, g4, g5, fp, fx, fy, fz);
+      continue;
     }
     const float Q2mirx = P.xx * x + P.xy * y + P.xz * z;
     const float Q2miry = P.xy * x + P.yy * y + P.yz * z;
@@ -505,9 +608,10 @@ cudaError_t launch_ewald_f32(const CompactPartData* parts, VariablePartData* var
 
 cudaError_t launch_ewald_fp(int form, const double* parts, long long n_parts, const int* idx,
                             long long n_idx, const ChangaEwaldParams& p, double* vars,
-                            cudaStream_t s) {
+                            cudaStream_t s, bool hex) {
   if (n_idx <= 0) return cudaSuccess;
-  if (p.nEwhLoop < 0 || p.nEwhLoop > CHANGA_MAX_EWH || (p.nEwhLoop > 0 && !p.ewt) || !(p.L > 0))
+  if (p.nEwhLoop < 0 || p.nEwhLoop > CHANGA_MAX_EWH || (p.nEwhLoop > 0 && !p.ewt) || !(p.L > 0) ||
+      (hex && !p.momc))
     return cudaErrorInvalidValue;
   const double L = p.L;
   const double alpha = 2.0 / L, alpha2 = alpha * alpha;
@@ -527,9 +631,11 @@ cudaError_t launch_ewald_fp(int form, const double* parts, long long n_parts, co
     P.nEwhLoop = p.nEwhLoop;
     for (int i = 0; i < p.nEwhLoop; ++i)
       for (int k = 0; k < 5; ++k) P.ewt[i][k] = p.ewt[5 * i + k];
+    if (hex) fill_hex_root(p.momc, P.hex);
     int blocks = (int)((n_idx + 127) / 128);
     TimingScope ts(kKidEwaldF64, s);
-    ewald_f64_kernel<<<blocks, 128, 0, s>>>(parts, n_parts, idx, n_idx, vars, P);
+    if (hex) ewald_f64_kernel<true><<<blocks, 128, 0, s>>>(parts, n_parts, idx, n_idx, vars, P);
+    else ewald_f64_kernel<false><<<blocks, 128, 0, s>>>(parts, n_parts, idx, n_idx, vars, P);
     count_launch();
     return cudaGetLastError();
   }
@@ -560,10 +666,12 @@ cudaError_t launch_ewald_fp(int form, const double* parts, long long n_parts, co
                          (float)e[3]);
     P.hs[i] = (float)e[4];
   }
+  if (hex) fill_hex_root(p.momc, P.hex);
   int threads = kMixWarps * 32;
   int blocks = (int)((n_idx + threads - 1) / threads);
   TimingScope ts(kKidEwaldMix, s);
-  ewald_mix_kernel<<<blocks, threads, 0, s>>>(parts, n_parts, idx, n_idx, vars, P);
+  if (hex) ewald_mix_kernel<true><<<blocks, threads, 0, s>>>(parts, n_parts, idx, n_idx, vars, P);
+  else ewald_mix_kernel<false><<<blocks, threads, 0, s>>>(parts, n_parts, idx, n_idx, vars, P);
   count_launch();
   return cudaGetLastError();
 }

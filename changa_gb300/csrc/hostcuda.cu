@@ -793,8 +793,8 @@ int changa_gravity_step(int form, const double* moments, long long n_moments, co
 int changa_gravity_step_hexa(int form, const double* moments, long long n_moments,
                              const double* parts, long long n_parts,
                              const ChangaListRequest* cells, const ChangaListRequest* plist,
-                             const ChangaListRequest* softcells, double fperiod, double* vars,
-                             cudaStream_t s) {
+                             const ChangaListRequest* softcells, double fperiod,
+                             const ChangaEwaldParams* ewald, double* vars, cudaStream_t s) {
   if (form != CHANGA_FORM_FP64 && form != CHANGA_FORM_MIXED)
     return record_error(CHANGA_E_INVALID_ARG, "gravity_step_hexa: form", __FILE__, __LINE__);
   if (!moments || !parts || !vars || n_moments < 0 || n_parts < 0)
@@ -863,6 +863,12 @@ int changa_gravity_step_hexa(int form, const double* moments, long long n_moment
     if (!rc && softcells && softcells->n_buckets > 0)
       rc = run_fp(f, false, kpseudo, n_moments, kpart, n_parts, softcells, fperiod, vars, s,
                   q + 128);
+    if (!rc && ewald) {
+      e = launch_ewald_fp(f, parts, n_parts, nullptr, n_parts, *ewald, vars, s, true);
+      if (e != cudaSuccess)
+        rc = record_error((int)e, "gravity_step_hexa: ewald", __FILE__, __LINE__);
+      e = cudaSuccess;
+    }
   } while (0);
   cudaError_t ef = cudaFreeAsync(block, s);
   if (rc) return rc;

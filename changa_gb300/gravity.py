@@ -74,6 +74,24 @@ class EwaldConfig:
         p._keep = tb
         return p
 
+    def params_hex(self, root):
+        """ChangaEwaldParams of the hexadecapole build for a 27-value root:
+        mass and centre in root[2..5], the complete moments in momc."""
+        p = N.ChangaEwaldParams()
+        for i in range(6):
+            p.root[i] = float(root[i])
+        p.L = self.L
+        p.nReps = self.n_reps
+        p.fEwCut = self.fEwCut
+        tb, momc = self.table_hex(root)
+        tb = np.ascontiguousarray(tb)
+        momc = np.ascontiguousarray(momc)
+        p.nEwhLoop = tb.shape[0]
+        p.ewt = tb.ctypes.data
+        p.momc = momc.ctypes.data
+        p._keep = (tb, momc)
+        return p
+
     def table_hex(self, root):
         """The hexadecapole build's table for a 27-value root, and the root's
         complete moments (MomcData order)."""
@@ -289,8 +307,6 @@ class DeviceSystem:
         self.parts = t(lists.parts)
         self.reqs = []
         self.order = getattr(lists, "order", 2)
-        if self.order == 4 and ewald is not None:
-            raise ValueError("the hexadecapole build has no Ewald term here")
         reqs = list(device_reqs) if device_reqs is not None else [lists.cells, lists.plist]
         if self.order == 4 and device_reqs is None:
             reqs.append(lists.softcells)
@@ -308,9 +324,15 @@ class DeviceSystem:
         self.vars = torch.zeros((lists.n, 5), dtype=torch.float64, device=device)
         self.ewald = ewald
         root = lists.root
-        if ewald is not None and root is None:  # a device-built tree: the root moments
+        if ewald is not None and (root is None or self.order == 4):
+            # a device-built tree or the hexadecapole build: the root moments
             root = self.moments[0].cpu().numpy()
-        self.ewald_params = ewald.params(root) if ewald else None
+        if ewald is None:
+            self.ewald_params = None
+        elif self.order == 4:
+            self.ewald_params = ewald.params_hex(root)
+        else:
+            self.ewald_params = ewald.params(root)
 
     def step(self, form="mixed", stream=None, zero=True):
         """Enqueues one evaluation on `stream` (torch stream handle or None for
@@ -324,7 +346,9 @@ class DeviceSystem:
                 FORMS[form], self.moments.data_ptr(), self.moments.shape[0],
                 self.parts.data_ptr(), self.n, C.byref(self.reqs[0]["c"]),
                 C.byref(self.reqs[1]["c"]), C.byref(self.reqs[2]["c"]),
-                float(self.lists.period), self.vars.data_ptr(), s)
+                float(self.lists.period),
+                C.byref(self.ewald_params) if self.ewald_params else None,
+                self.vars.data_ptr(), s)
             N.check(rc, "changa_gravity_step_hexa")
             return self.vars
         ep = self.ewald_params
@@ -341,6 +365,8 @@ class GravityGraph:
     (changa_gravity_graph_create) and replayed with one launch."""
 
     def __init__(self, ds: DeviceSystem, form="mixed"):
+        if ds.order != 2:
+            raise ValueError("the graph form captures the quadrupole evaluation")
         self.ds = ds
         ep = ds.ewald_params
         self.handle = N.cuda_lib().changa_gravity_graph_create(

@@ -154,6 +154,10 @@ typedef struct ChangaEwaldParams {
   double fEwCut;     /* real-space cut in periods */
   int nEwhLoop;      /* rows in ewt, at most CHANGA_MAX_EWH */
   const double *ewt; /* HOST: nEwhLoop x 5 {hx, hy, hz, hCfac, hSfac} */
+  const double *momc; /* HOST: the root's complete moments (MomcData order,
+                         32 values, changa_ewald_table_hex); read only by
+                         changa_gravity_step_hexa, which then takes M and cm
+                         from root[2..5] */
 } ChangaEwaldParams;
 
 #define CHANGA_MAX_EWH 256
@@ -210,12 +214,15 @@ void changa_gravity_graph_destroy(ChangaGravityGraph *g);
  * cells whose softening meets the bucket, evaluated as softened point
  * masses {M, soft, cm} (gravity.h:414-421); `plist` as in
  * changa_gravity_step.  form: CHANGA_FORM_FP64 or CHANGA_FORM_MIXED;
- * isolated or periodic lists (fperiod), no Ewald term in this build. */
+ * isolated or periodic lists (fperiod).  ewald (may be NULL): the
+ * hexadecapole Ewald correction (BucketEwald with HEXADECAPOLE,
+ * Ewald.cpp:72-281) about the root with complete moments ewald->momc and
+ * the table of changa_ewald_table_hex. */
 int changa_gravity_step_hexa(int form, const double *moments, long long n_moments,
                              const double *parts, long long n_parts,
                              const ChangaListRequest *cells, const ChangaListRequest *plist,
-                             const ChangaListRequest *softcells, double fperiod, double *vars,
-                             cudaStream_t stream);
+                             const ChangaListRequest *softcells, double fperiod,
+                             const ChangaEwaldParams *ewald, double *vars, cudaStream_t stream);
 
 /* Adjoint of the cell + particle list accelerations (FP32-mixed; no
  * reference counterpart): given lam = dL/da (n_parts x 3), ACCUMULATES

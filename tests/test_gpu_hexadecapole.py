@@ -150,3 +150,35 @@ def test_hex_dropin_ewald(cuda_ok):
     # (alpha r)^4 term of g0 alone reaches ka (alpha r)^4 / 10 = 4.5e-4 of
     # G M / L; the oracle (CPU constants) switches at 1.2e-3 L^2
     assert dpot.max() < 1e-3 and dpot_q.max() < 1e-3
+
+
+def test_hex_forms_with_ewald(cuda_ok):
+    """changa_gravity_step_hexa with its Ewald term (the root's complete
+    moments to fourth order) on a clustered periodic box: the FP64 form
+    against the oracle per particle, the FP32-mixed form as the quadrupole
+    mixed Ewald is judged (rms|a| and G M / L units)."""
+    p = ics.nfw_halos(32768, ics.rng_for(2), soft=1e-3)
+    L = tree.build_lists(p["pos"], p["mass"], p["soft"], n_bucket=16, theta=0.7, period=1.0,
+                         order=4)
+    ew = gravity.EwaldConfig(1.0, 1, 2.6, 2.8)
+    ref = np.zeros((L.n, 5))
+    for req in (L.cells, L.softcells):
+        if req.n_buckets:
+            ref = oracle.cell_forces_hex(L.moments, L.parts, req, oracle.bucket_geometry(L, req),
+                                         fperiod=1.0, vars=ref)
+    ref = oracle.part_forces(L.parts, L.parts, L.plist, fperiod=1.0, vars=ref)
+    ref = oracle.ewald_forces_hex(L.parts, L.moments[0], 1.0, 1, 2.6, 2.8, vars=ref)
+    ds = gravity.DeviceSystem(L, ewald=ew)
+    v64 = ds.step("fp64").cpu().numpy()
+    e64 = force_rel_err(v64, ref)
+    vmx = ds.step("mixed").cpu().numpy()
+    e = force_rms_err(vmx, ref)
+    print("hex + Ewald: fp64 max %.2e, pot max %.2e; mixed rms median %.2e max %.2e, rel median "
+          "%.2e, pot max %.2e" % (e64.max(), np.abs(v64[:, 3] - ref[:, 3]).max(), np.median(e),
+                                  e.max(), np.median(force_rel_err(vmx, ref)),
+                                  np.abs(vmx[:, 3] - ref[:, 3]).max()))
+    assert e64.max() < 1e-6
+    assert np.abs(v64[:, 3] - ref[:, 3]).max() < 1e-9
+    assert np.median(e) < 5e-5 and e.max() < 2e-3
+    assert np.median(force_rel_err(vmx, ref)) < 1e-4
+    assert np.abs(vmx[:, 3] - ref[:, 3]).max() < 5e-5
