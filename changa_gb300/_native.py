@@ -118,6 +118,12 @@ class ChangaWalkParams(C.Structure):
                 ("n_replicas", C.c_int)]
 
 
+class ChangaWalkLists(C.Structure):
+    _fields_ = [("n_buckets", C.c_int), ("order", C.c_int), ("passes", C.c_int),
+                ("n_entries", C.c_longlong * 3), ("list", C.c_void_p * 3),
+                ("markers", C.c_void_p * 3)]
+
+
 class ChangaTreeArrays(C.Structure):
     _fields_ = [("n", C.c_longlong), ("n_nodes", C.c_longlong), ("n_buckets", C.c_int),
                 ("perm", C.c_void_p), ("parts", C.c_void_p), ("moments", C.c_void_p),
@@ -222,6 +228,10 @@ CUDA_SIGNATURES = {
                                _VP, _VP]),
     "changa_walk_fill": (_I, [C.POINTER(ChangaTreeView), C.POINTER(ChangaWalkParams), _VP, _VP,
                               _VP, _VP, _VP, _VP, _VP]),
+    "changa_walk": (_I, [C.POINTER(ChangaTreeView), C.POINTER(ChangaWalkParams),
+                         C.POINTER(ChangaWalkLists), _VP]),
+    "changa_walk_lists_free": (None, [C.POINTER(ChangaWalkLists)]),
+    "changa_walk_set_pool_factor": (None, [_D]),
     "changa_gravity_step_hexa": (_I, [_I, _VP, _LL, _VP, _LL, C.POINTER(ChangaListRequest),
                                       C.POINTER(ChangaListRequest),
                                       C.POINTER(ChangaListRequest), _D,

@@ -87,7 +87,10 @@ __global__ void __launch_bounds__(128) ewald_f32_kernel(const CompactPartData* _
         const float z = zdif + iz * ro.L;
         float r2 = x * x + y * y + z * z;
         if (r2 > ro.fEwCut2 && !hole) continue;
-        float g0, g1, g2, g3, g4 = 0.f, g5 = 0.f;
+        float g0, g1, g2, g3;
+#ifdef HEXADECAPOLE
+        float g4, g5;
+#endif
         if (r2 < ro.fInner2) {
           float alphan = ro.ka;
           r2 *= ro.alpha2;
@@ -173,8 +176,6 @@ __global__ void __launch_bounds__(128) ewald_f32_kernel(const CompactPartData* _
         ax += g2 * Q2mirx - x * Qta;
         ay += g2 * Q2miry - y * Qta;
         az += g2 * Q2mirz - z * Qta;
-        (void)g4;
-        (void)g5;
 #endif
       }
     }

@@ -9,15 +9,22 @@
  * opened into its particles when it is a bucket, or deferred to the next
  * local level when undecided (openCriterionNode, gravity.h:652-723).
  * Which entries a bucket finally holds depends only on the tests against
- * the local nodes on the path from the root to that bucket.  So one thread
- * per target bucket reproduces the same per-bucket sets with a depth-first
- * stack of (source node, local level, replica) entries: it tests against
- * the local node of its level and pushes deferred entries one level down.
- * The lists hold the same entries as the host walk's, in depth-first
- * instead of level order.
+ * the local nodes on the path from the root to that bucket, not on the
+ * order of the tests.  So one warp per target bucket reproduces the same
+ * per-bucket sets from a stack of (source node, local level, replica)
+ * entries in shared memory: each step pops up to 32 entries, tests each on
+ * its own lane against the local node of its level, and pushes opened
+ * children (or, when undecided, the entry one level down) back in lane
+ * order.  The lanes keep 32 independent tests in flight per bucket, where a
+ * thread per bucket would chain thousands of dependent loads; the stack
+ * stays within a few hundred entries (a 32-wide last-in-first-out frontier)
+ * and its capacity is checked.  The lists hold the same entries as the host
+ * walk's, in this traversal's order, and each list's entries of one step
+ * are written contiguously.
  *
  * Two launches: a count pass (per-bucket list lengths) and, after the
- * caller has turned the counts into offsets, a fill pass.
+ * counts have become offsets, a fill pass; changa_walk runs both and the
+ * prefix sums in between.
  *
  * Decisions equal the host walk's FP64 decisions.  GB300 issues FP64 at a
  * small fraction of its FP32 rate, so each opening test is first made in
@@ -29,13 +36,20 @@
  * threshold are repeated in FP64, with the host's expressions (this file is
  * compiled without FMA contraction, as the host code is).
  */
+#include <atomic>
+#include <cstring>
+#include <vector>
+
 #include "chg_internal.h"
 
 namespace chg {
 namespace {
 
-constexpr int kWalkThreads = 128;
-constexpr int kStack = 256;
+constexpr int kWalkWarps = 4;      // warps (buckets) per block
+constexpr int kWarpStack = 1024;   // stack entries per warp
+constexpr int kChunk = 256;        // entries per pool chunk of the append pass
+constexpr int kMaxChunks = 128;    // chunks per bucket and list in the append pass
+enum { kCount = 0, kFill = 1, kAppend = 2 };
 
 struct WalkArgs {
   const double* geom;  // n_nodes x 6 {cm.xyz, radius, soft, mass}
@@ -59,26 +73,49 @@ struct WalkArgs {
   int2* parts;
   int2* soft;
   int* error;
-  /* FP32 copies for the screening test */
-  const float4* nodef;  // n_nodes: {cm.xyz, rn32(opening radius^2)}
+  /* append pass: per list a pool of kChunk-entry chunks, each chunk's
+   * bucket and rank in that bucket's list; bucket_stride > 1 walks every
+   * bucket_stride-th bucket only (the sampled count pass) and writes its
+   * counts at b / bucket_stride */
+  int2* pool[3];
+  int* chunk_bucket[3];
+  int* chunk_rank[3];
+  unsigned int* pool_next;
+  long long pool_chunks[3];
+  int* overflow;
+  int bucket_stride;
+  /* per node, one 32-byte record for the traversal (see WalkNode) */
+  const struct WalkNode* nodes;
   const float4* boxf;   // 2 n_nodes: {lesser.xyz, 0}, {greater.xyz, 0}
   float period32;
 };
 
+/* What the traversal reads of a source node, in one 32-byte record (two
+ * 16-byte loads from one sector): FP32 centre and opening radius^2 for the
+ * screened test, then {child0, child1, first, count}. */
+struct __align__(32) WalkNode {
+  float4 geo;
+  int4 link;
+};
+
+
 constexpr float kU = 5.9604645e-08f;  // 2^-24, the FP32 unit roundoff
 
-/* FP32 copies of each node's centre, box and opening radius squared, the
- * last formed in FP64 exactly as open_criterion forms it. */
+/* Each node's traversal record (FP32 centre and opening radius squared,
+ * the latter formed in FP64 exactly as open_criterion forms it, and its
+ * links) and its FP32 box. */
 __global__ void walk_prep_kernel(const double* __restrict__ geom, const double* __restrict__ bbox,
-                                 long long n_nodes, double theta, float4* __restrict__ nodef,
-                                 float4* __restrict__ boxf) {
+                                 const int* __restrict__ info, long long n_nodes, double theta,
+                                 WalkNode* __restrict__ nodes, float4* __restrict__ boxf) {
   for (long long g = blockIdx.x * (long long)blockDim.x + threadIdx.x; g < n_nodes;
        g += (long long)gridDim.x * blockDim.x) {
     const double* gg = geom + 6 * g;
     const double kOpenGeom = 2.0 / sqrt(3.0);
     double radius = kOpenGeom * gg[3] / theta;
     if (radius < gg[3]) radius = gg[3];
-    nodef[g] = make_float4((float)gg[0], (float)gg[1], (float)gg[2], (float)(radius * radius));
+    const int* f = info + 4 * g;
+    nodes[g].geo = make_float4((float)gg[0], (float)gg[1], (float)gg[2], (float)(radius * radius));
+    nodes[g].link = make_int4(f[0], f[1], f[2], f[3]);
     const double* b = bbox + 6 * g;
     boxf[2 * g] = make_float4((float)b[0], (float)b[1], (float)b[2], 0.0f);
     boxf[2 * g + 1] = make_float4((float)b[3], (float)b[4], (float)b[5], 0.0f);
@@ -163,10 +200,10 @@ __device__ int open_criterion(const WalkArgs& a, int g, int local, bool local_bu
  * rounding (the 1e-30 floor covers conversions that land on FP32
  * subnormals).  Squares and the three-term sum add 2u of the total,
  * bounded here by 4u. */
-__device__ int open_criterion_screened(const WalkArgs& a, int g, int local, bool local_bucket,
-                                       int off) {
-  if (a.info[4 * (size_t)g + 3] <= 6) return 1;
-  const float4 nf = a.nodef[g];
+__device__ int open_criterion_screened(const WalkArgs& a, const WalkNode& nd, int g, int local,
+                                       bool local_bucket, int off) {
+  if (nd.link.w <= 6) return 1;
+  const float4 nf = nd.geo;
   const float4 lo = a.boxf[2 * (size_t)local], hi = a.boxf[2 * (size_t)local + 1];
   const float cm[3] = {nf.x, nf.y, nf.z};
   const float o[3] = {(float)((off & 7) - 3) * a.period32,
@@ -206,92 +243,282 @@ __device__ int open_criterion_screened(const WalkArgs& a, int g, int local, bool
   return open_criterion(a, g, local, local_bucket, off);
 }
 
-template <bool FILL>
-__global__ void __launch_bounds__(kWalkThreads) walk_kernel(const WalkArgs a) {
-  const int b = blockIdx.x * kWalkThreads + threadIdx.x;
-  if (b >= a.n_buckets) return;
+__device__ __forceinline__ int warp_excl_scan(int v, int& total) {
+  const int lane = threadIdx.x & 31;
+  int x = v;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const int y = __shfl_up_sync(0xffffffffu, x, o);
+    if (lane >= o) x += y;
+  }
+  total = __shfl_sync(0xffffffffu, x, 31);
+  return x - v;
+}
+
+/* Append pass: this step's t entries of list k (this lane's at bucket-list
+ * positions q0 .. q0 + n - 1, q0 = cnt + its exclusive offset) go to the
+ * bucket's chunks; chunks are taken from the pool as the list grows (lane 0,
+ * one atomic per step that needs any) and recorded in the warp's table. */
+__device__ __forceinline__ void append_step(const WalkArgs& a, int k, int b, int* tab, int& nalloc,
+                                            long long cnt, int total, long long q0, int n,
+                                            int first_index, int code) {
+  const int need = (int)((cnt + total + kChunk - 1) / kChunk);
+  if (need > nalloc) {  // uniform over the warp
+    if ((threadIdx.x & 31) == 0) {
+      const int m = need - nalloc;
+      long long c0 = -1;
+      if (need <= kMaxChunks) {
+        c0 = atomicAdd(a.pool_next + k, (unsigned)m);
+        if (c0 + m > a.pool_chunks[k]) c0 = -1;
+      }
+      if (c0 < 0) atomicExch(a.overflow, 1);
+      for (int i = 0; i < m && nalloc + i < kMaxChunks; ++i) {
+        tab[nalloc + i] = c0 < 0 ? -1 : (int)(c0 + i);
+        if (c0 >= 0) {
+          a.chunk_bucket[k][c0 + i] = b;
+          a.chunk_rank[k][c0 + i] = nalloc + i;
+        }
+      }
+    }
+    nalloc = need;
+    __syncwarp();
+  }
+  for (int j = 0; j < n; ++j) {
+    const long long q = q0 + j;
+    const long long r = q / kChunk;
+    const int c = r < kMaxChunks ? tab[r] : -1;
+    if (c >= 0) a.pool[k][(size_t)c * kChunk + (q - r * kChunk)] = make_int2(first_index + j, code << 22);
+  }
+}
+
+template <int MODE>
+__global__ void __launch_bounds__(kWalkWarps * 32) walk_kernel(const WalkArgs a) {
+  constexpr bool FILL = MODE == kFill;
+  __shared__ int2 stk[kWalkWarps][kWarpStack];
+  __shared__ int chain[kWalkWarps][64];
+  __shared__ int ctab[MODE == kAppend ? kWalkWarps : 1][3][MODE == kAppend ? kMaxChunks : 1];
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const unsigned full = 0xffffffffu;
+  const long long bl = ((long long)blockIdx.x * kWalkWarps + warp) * a.bucket_stride;
+  if (bl >= a.n_buckets) return;  // the whole warp
+  const int b = (int)bl;
   const int bn = a.bucket_node[b];
   if (bn < 0 || bn >= a.n_nodes) return;
   /* local nodes from the root down to this bucket */
-  int chain[64];
   int depth = 0;
-  {
-    int tmp[64];
+  if (lane == 0) {
     int n = 0;
-    for (int x = bn; x >= 0 && x < a.n_nodes && n < 64; x = a.parent[x]) tmp[n++] = x;
-    if (n >= 64 || tmp[n - 1] != 0) {
-      atomicExch(a.error, 1);
-      return;
+    for (int x = bn; x >= 0 && x < a.n_nodes && n < 65; x = a.parent[x]) ++n;
+    if (n > 64) {
+      depth = -1;
+    } else {
+      int k = n - 1;
+      for (int x = bn; k >= 0; x = a.parent[x]) chain[warp][k--] = x;
+      depth = chain[warp][0] == 0 ? n - 1 : -1;
     }
-    for (int i = 0; i < n; ++i) chain[i] = tmp[n - 1 - i];
-    depth = n - 1;  // chain[depth] == bn
   }
-  int nc = 0, np = 0, ns = 0;
+  depth = __shfl_sync(full, depth, 0);
+  if (depth < 0) {
+    if (lane == 0) atomicExch(a.error, 1);
+    return;
+  }
   long long oc = 0, op = 0, os = 0;
   if (FILL) {
     oc = a.off_cells[b];
     op = a.off_parts[b];
     os = a.off_soft ? a.off_soft[b] : 0;
   }
-  /* stack entries: node, level << 16 | replica code */
-  int2 st[kStack];
-  int sp = 0;
-  const int nr = a.n_replicas;
-  for (int x = -nr; x <= nr; ++x)
-    for (int y = -nr; y <= nr; ++y)
-      for (int z = -nr; z <= nr; ++z)
-        if (sp < kStack) st[sp++] = make_int2(0, (x + 3) | ((y + 3) << 3) | ((z + 3) << 6));
-  while (sp > 0) {
-    const int2 e = st[--sp];
-    const int g = e.x, level = e.y >> 16, code = e.y & 0xffff;
-    if (g < 0 || g >= a.n_nodes) continue;  // memory safety
-    const int local = chain[level];
-    const bool local_bucket = level == depth;
-    const int open = open_criterion_screened(a, g, local, local_bucket, code);
-    const int* gi = a.info + 4 * (size_t)g;
-    if (open == 0) {
-      bool softened = false;
-      if (a.order == 4) {
-        double o[3];
-        decode(code, a.period, o);
-        const double* gg = a.geom + 6 * (size_t)g;
-        const double c[3] = {gg[0] + o[0], gg[1] + o[1], gg[2] + o[2]};
-        softened = open_softening(a, g, bn, c);
-      }
-      if (softened) {
-        if (FILL) a.soft[os + ns] = make_int2(g, code << 22);
-        ++ns;
-      } else {
-        if (FILL) a.cells[oc + nc] = make_int2(g, code << 22);
-        ++nc;
-      }
-      continue;
-    }
-    if (gi[0] < 0 && gi[1] < 0) {  // a source bucket: its particles
-      if (FILL)
-        for (int k = 0; k < gi[3]; ++k) a.parts[op + np + k] = make_int2(gi[2] + k, code << 22);
-      np += gi[3];
-      continue;
-    }
-    if (open == 1 || local_bucket) {
-      if (sp + 2 > kStack) {
-        atomicExch(a.error, 2);
-        break;
-      }
-      if (gi[1] >= 0) st[sp++] = make_int2(gi[1], (level << 16) | code);
-      if (gi[0] >= 0) st[sp++] = make_int2(gi[0], (level << 16) | code);
-    } else {
-      if (sp + 1 > kStack) {
-        atomicExch(a.error, 2);
-        break;
-      }
-      st[sp++] = make_int2(g, ((level + 1) << 16) | code);
-    }
+  /* the root of every replica on the check list */
+  const int nr = a.n_replicas, side = 2 * nr + 1, nrep = side * side * side;
+  for (int r = lane; r < nrep; r += 32) {
+    const int x = r / (side * side) - nr, y = (r / side) % side - nr, z = r % side - nr;
+    stk[warp][r] = make_int2(0, (x + 3) | ((y + 3) << 3) | ((z + 3) << 6));
   }
-  if (!FILL) {
-    a.n_cells[b] = nc;
-    a.n_parts[b] = np;
-    if (a.n_soft) a.n_soft[b] = ns;
+  int sp = nrep;
+  long long nc = 0, np = 0, ns = 0;
+  int na[3] = {0, 0, 0};  // append pass: chunks taken per list
+  __syncwarp();
+  while (sp > 0) {
+    const int n = sp < 32 ? sp : 32;
+    const int top = sp - n;
+    int2 e = make_int2(-1, 0);
+    if (lane < n) e = stk[warp][top + lane];
+    sp = top;
+    __syncwarp();  // popped before anything is pushed over them
+    /* kind: 0 cell, 1 softened cell, 2 particles, 3 open, 4 defer, -1 none */
+    int kind = -1, c0 = -1, c1 = -1, pfirst = 0, pcount = 0;
+    const int g = e.x, level = e.y >> 16, code = e.y & 0xffff;
+    if (g >= 0 && g < a.n_nodes) {  // memory safety
+      const int local = chain[warp][level];
+      const bool local_bucket = level == depth;
+      const WalkNode nd = a.nodes[g];
+      const int open = open_criterion_screened(a, nd, g, local, local_bucket, code);
+      if (open == 0) {
+        bool softened = false;
+        if (a.order == 4) {
+          double o[3];
+          decode(code, a.period, o);
+          const double* gg = a.geom + 6 * (size_t)g;
+          const double c[3] = {gg[0] + o[0], gg[1] + o[1], gg[2] + o[2]};
+          softened = open_softening(a, g, bn, c);
+        }
+        kind = softened ? 1 : 0;
+      } else if (nd.link.x < 0 && nd.link.y < 0) {  // a source bucket: its particles
+        kind = 2;
+        pfirst = nd.link.z;
+        pcount = nd.link.w;
+      } else if (open == 1 || local_bucket) {
+        kind = 3;
+        c0 = nd.link.x;
+        c1 = nd.link.y;
+      } else {
+        kind = 4;
+      }
+    }
+    /* pushes, in lane order; within a lane child 1 below child 0 */
+    const int npush = kind == 3 ? (c0 >= 0) + (c1 >= 0) : (kind == 4 ? 1 : 0);
+    int tpush;
+    int pos = sp + warp_excl_scan(npush, tpush);
+    if (sp + tpush > kWarpStack) {  // uniform: every lane sees tpush
+      if (lane == 0) atomicExch(a.error, 2);
+      break;
+    }
+    if (kind == 3) {
+      if (c1 >= 0) stk[warp][pos++] = make_int2(c1, (level << 16) | code);
+      if (c0 >= 0) stk[warp][pos++] = make_int2(c0, (level << 16) | code);
+    } else if (kind == 4) {
+      stk[warp][pos] = make_int2(g, ((level + 1) << 16) | code);
+    }
+    sp += tpush;
+    /* accepted cells, softened cells and particles, contiguous per step */
+    const unsigned below = (1u << lane) - 1u;
+    const unsigned mc = __ballot_sync(full, kind == 0), ms = __ballot_sync(full, kind == 1);
+    int tpart;
+    const int ppos = warp_excl_scan(kind == 2 ? pcount : 0, tpart);
+    if (FILL) {
+      if (kind == 0) a.cells[oc + nc + __popc(mc & below)] = make_int2(g, code << 22);
+      if (kind == 1) a.soft[os + ns + __popc(ms & below)] = make_int2(g, code << 22);
+      if (kind == 2)
+        for (int k = 0; k < pcount; ++k) a.parts[op + np + ppos + k] = make_int2(pfirst + k, code << 22);
+    } else if (MODE == kAppend) {
+      if (mc)
+        append_step(a, 0, b, ctab[warp][0], na[0], nc, __popc(mc), nc + __popc(mc & below),
+                     kind == 0, g, code);
+      if (ms)
+        append_step(a, 2, b, ctab[warp][2], na[2], ns, __popc(ms), ns + __popc(ms & below),
+                     kind == 1, g, code);
+      if (tpart)
+        append_step(a, 1, b, ctab[warp][1], na[1], np, tpart, np + ppos, kind == 2 ? pcount : 0,
+                    pfirst, code);
+    }
+    nc += __popc(mc);
+    ns += __popc(ms);
+    np += tpart;
+    __syncwarp();  // pushes visible to the next pops
+  }
+  if (!FILL && lane == 0) {
+    const int i = b / a.bucket_stride;
+    a.n_cells[i] = (int)nc;
+    a.n_parts[i] = (int)np;
+    if (a.n_soft) a.n_soft[i] = (int)ns;
+  }
+}
+
+/* The append pass's chunks into CSR order: entry j of chunk c (rank r of
+ * bucket b) goes to off[b] + r kChunk + j when it lies inside b's list. */
+__global__ void gather_chunks_kernel(const int2* __restrict__ pool, const int* __restrict__ cb,
+                                     const int* __restrict__ cr, long long n_chunks,
+                                     const long long* __restrict__ off, int2* __restrict__ out) {
+  const long long total = n_chunks * kChunk;
+  for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < total;
+       t += (long long)gridDim.x * blockDim.x) {
+    const long long c = t / kChunk;
+    const int j = (int)(t - c * kChunk);
+    const int b = cb[c];
+    const long long pos = (long long)cr[c] * kChunk + j;
+    if (off[b] + pos < off[b + 1]) out[off[b] + pos] = pool[t];
+  }
+}
+
+/* Exclusive scan of n int counts into off64[0..n] and off32[0..n]: per-tile
+ * sums, a one-block scan of the tile sums, then per-tile scans. */
+constexpr int kScanThreads = 1024, kScanPer = 4, kScanTile = kScanThreads * kScanPer;
+
+__global__ void scan_tile_sums_kernel(const int* __restrict__ in, int n, long long* __restrict__ ts) {
+  __shared__ long long part[kScanThreads / 32];
+  const long long base = (long long)blockIdx.x * kScanTile + threadIdx.x * kScanPer;
+  long long v = 0;
+  for (int k = 0; k < kScanPer; ++k)
+    if (base + k < n) v += in[base + k];
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  if ((threadIdx.x & 31) == 0) part[threadIdx.x >> 5] = v;
+  __syncthreads();
+  if (threadIdx.x < 32) {
+    long long w = part[threadIdx.x];
+    for (int o = 16; o > 0; o >>= 1) w += __shfl_xor_sync(0xffffffffu, w, o);
+    if (threadIdx.x == 0) ts[blockIdx.x] = w;
+  }
+}
+
+__device__ long long block_exclusive_scan(long long v, long long* sh, long long& total) {
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  long long x = v;
+  for (int o = 1; o < 32; o <<= 1) {
+    const long long y = __shfl_up_sync(0xffffffffu, x, o);
+    if (lane >= o) x += y;
+  }
+  if (lane == 31) sh[w] = x;
+  __syncthreads();
+  if (w == 0) {
+    long long z = sh[lane];
+    for (int o = 1; o < 32; o <<= 1) {
+      const long long y = __shfl_up_sync(0xffffffffu, z, o);
+      if (lane >= o) z += y;
+    }
+    sh[lane] = z;
+  }
+  __syncthreads();
+  total = sh[31];
+  const long long before = w ? sh[w - 1] : 0;
+  __syncthreads();
+  return before + x - v;
+}
+
+__global__ void scan_tiles_kernel(long long* __restrict__ ts, int nt) {
+  __shared__ long long sh[32];
+  long long carry = 0;
+  for (int b0 = 0; b0 < nt; b0 += kScanThreads) {
+    const int i = b0 + threadIdx.x;
+    const long long v = i < nt ? ts[i] : 0;
+    long long tot;
+    const long long ex = block_exclusive_scan(v, sh, tot);
+    if (i < nt) ts[i] = carry + ex;
+    carry += tot;
+  }
+}
+
+__global__ void scan_apply_kernel(const int* __restrict__ in, int n, const long long* __restrict__ ts,
+                                  long long* __restrict__ off64, int* __restrict__ off32) {
+  __shared__ long long sh[32];
+  const long long base = (long long)blockIdx.x * kScanTile + threadIdx.x * kScanPer;
+  int v[kScanPer];
+  long long sum = 0;
+  for (int k = 0; k < kScanPer; ++k) {
+    v[k] = base + k < n ? in[base + k] : 0;
+    sum += v[k];
+  }
+  long long tot;
+  long long run = ts[blockIdx.x] + block_exclusive_scan(sum, sh, tot);
+  for (int k = 0; k < kScanPer; ++k) {
+    if (base + k < n) {
+      off64[base + k] = run;
+      off32[base + k] = (int)run;
+    }
+    run += v[k];
+    if (base + k == n - 1) {
+      off64[n] = run;
+      off32[n] = (int)run;
+    }
   }
 }
 
@@ -300,31 +527,29 @@ __global__ void __launch_bounds__(kWalkThreads) walk_kernel(const WalkArgs a) {
 
 using namespace chg;
 
-static int walk_launch(const ChangaTreeView* t, const ChangaWalkParams* p, bool fill, int* nc,
-                       int* np, int* ns, const long long* oc, const long long* op,
-                       const long long* os, ILCell* cells, ILCell* parts, ILCell* soft,
-                       cudaStream_t s) {
-  if (!t || !p || !t->geom || !t->bbox || !t->info || !t->parent || !t->bucket_node ||
-      t->n_nodes <= 0 || t->n_buckets < 0 || p->theta <= 0 || (p->order != 2 && p->order != 4) ||
-      p->n_replicas < 0 || p->n_replicas > 3)
-    return record_error(CHANGA_E_INVALID_ARG, "walk: arguments", __FILE__, __LINE__);
-  if (t->n_buckets == 0) return 0;
+static bool walk_args_ok(const ChangaTreeView* t, const ChangaWalkParams* p) {
+  return t && p && t->geom && t->bbox && t->info && t->parent && t->bucket_node &&
+         t->n_nodes > 0 && t->n_buckets >= 0 && p->theta > 0 && (p->order == 2 || p->order == 4) &&
+         p->n_replicas >= 0 && p->n_replicas <= 3;
+}
+
+/* Node records and boxes for the screened tests (stream-ordered scratch,
+ * freed by the caller). */
+static int walk_setup(const ChangaTreeView* t, const ChangaWalkParams* p, WalkArgs& a, char** block,
+                      cudaStream_t s) {
   prepare_pool();
-  char* block = nullptr;
   const size_t nn = (size_t)t->n_nodes;
-  CHG_CUDA(cudaMallocAsync((void**)&block, 256 + nn * 3 * sizeof(float4), s));
-  int* err = (int*)block;
-  float4* nodef = (float4*)(block + 256);
-  float4* boxf = nodef + nn;
+  CHG_CUDA(cudaMallocAsync((void**)block, 256 + nn * (sizeof(WalkNode) + 2 * sizeof(float4)), s));
+  int* err = (int*)*block;
+  WalkNode* nodes = (WalkNode*)(*block + 256);
+  float4* boxf = (float4*)(nodes + nn);
   CHG_CUDA(cudaMemsetAsync(err, 0, sizeof(int), s));
-  {
-    long long g = (t->n_nodes + 255) / 256;
-    const long long cap = (long long)sm_count() * 8;
-    walk_prep_kernel<<<(int)(g < cap ? g : cap), 256, 0, s>>>(t->geom, t->bbox, t->n_nodes,
-                                                              p->theta, nodef, boxf);
-    count_launch();
-  }
-  WalkArgs a;
+  long long g = (t->n_nodes + 255) / 256;
+  const long long cap = (long long)sm_count() * 8;
+  walk_prep_kernel<<<(int)(g < cap ? g : cap), 256, 0, s>>>(t->geom, t->bbox, t->info, t->n_nodes,
+                                                            p->theta, nodes, boxf);
+  count_launch();
+  a = WalkArgs{};
   a.geom = t->geom;
   a.bbox = t->bbox;
   a.info = t->info;
@@ -337,6 +562,39 @@ static int walk_launch(const ChangaTreeView* t, const ChangaWalkParams* p, bool 
   a.period = p->period;
   a.order = p->order;
   a.n_replicas = p->n_replicas;
+  a.error = err;
+  a.nodes = nodes;
+  a.boxf = boxf;
+  a.period32 = (float)p->period;
+  a.bucket_stride = 1;
+  return 0;
+}
+
+static void walk_run(const WalkArgs& a, int mode, cudaStream_t s) {
+  const long long warps = ((long long)a.n_buckets + a.bucket_stride - 1) / a.bucket_stride;
+  const int grid = (int)((warps + kWalkWarps - 1) / kWalkWarps);
+  if (mode == kFill) walk_kernel<kFill><<<grid, kWalkWarps * 32, 0, s>>>(a);
+  else if (mode == kAppend) walk_kernel<kAppend><<<grid, kWalkWarps * 32, 0, s>>>(a);
+  else walk_kernel<kCount><<<grid, kWalkWarps * 32, 0, s>>>(a);
+  count_launch();
+}
+
+static int walk_error(int h_err) {
+  return record_error(CHANGA_E_TOO_LARGE, h_err == 1 ? "walk: tree deeper than 64 levels"
+                                                     : "walk: traversal stack exhausted",
+                      __FILE__, __LINE__);
+}
+
+static int walk_launch(const ChangaTreeView* t, const ChangaWalkParams* p, bool fill, int* nc,
+                       int* np, int* ns, const long long* oc, const long long* op,
+                       const long long* os, ILCell* cells, ILCell* parts, ILCell* soft,
+                       cudaStream_t s) {
+  if (!walk_args_ok(t, p))
+    return record_error(CHANGA_E_INVALID_ARG, "walk: arguments", __FILE__, __LINE__);
+  if (t->n_buckets == 0) return 0;
+  WalkArgs a;
+  char* block = nullptr;
+  if (int rc = walk_setup(t, p, a, &block, s)) return rc;
   a.n_cells = nc;
   a.n_parts = np;
   a.n_soft = ns;
@@ -346,24 +604,13 @@ static int walk_launch(const ChangaTreeView* t, const ChangaWalkParams* p, bool 
   a.cells = (int2*)cells;
   a.parts = (int2*)parts;
   a.soft = (int2*)soft;
-  a.error = err;
-  a.nodef = nodef;
-  a.boxf = boxf;
-  a.period32 = (float)p->period;
-  const int grid = (t->n_buckets + kWalkThreads - 1) / kWalkThreads;
-  if (fill) walk_kernel<true><<<grid, kWalkThreads, 0, s>>>(a);
-  else walk_kernel<false><<<grid, kWalkThreads, 0, s>>>(a);
-  count_launch();
+  walk_run(a, fill ? kFill : kCount, s);
   CHG_CUDA(cudaGetLastError());
   int h_err = 0;
-  CHG_CUDA(cudaMemcpyAsync(&h_err, err, sizeof(int), cudaMemcpyDeviceToHost, s));
+  CHG_CUDA(cudaMemcpyAsync(&h_err, a.error, sizeof(int), cudaMemcpyDeviceToHost, s));
   CHG_CUDA(cudaFreeAsync(block, s));
   CHG_CUDA(cudaStreamSynchronize(s));
-  if (h_err)
-    return record_error(CHANGA_E_TOO_LARGE, h_err == 1 ? "walk: tree deeper than 64 levels"
-                                                       : "walk: traversal stack exhausted",
-                        __FILE__, __LINE__);
-  return 0;
+  return h_err ? walk_error(h_err) : 0;
 }
 
 extern "C" int changa_walk_count(const ChangaTreeView* tree, const ChangaWalkParams* p,
@@ -383,4 +630,174 @@ extern "C" int changa_walk_fill(const ChangaTreeView* tree, const ChangaWalkPara
     return record_error(CHANGA_E_INVALID_ARG, "walk_fill: outputs", __FILE__, __LINE__);
   return walk_launch(tree, p, true, nullptr, nullptr, nullptr, off_cells, off_parts, off_soft,
                      cells, parts, soft, s);
+}
+
+/* ---- both passes and the prefix sums, lists owned by the result ---- */
+
+/* append-pass pool size over the sampled estimate of the entries */
+static std::atomic<double> g_pool_factor{1.2};
+
+extern "C" void changa_walk_set_pool_factor(double f) { g_pool_factor.store(f > 0 ? f : 0.0); }
+
+static void release_lists(ChangaWalkLists* out) {
+  for (int k = 0; k < 3; ++k) {
+    if (out->list[k]) cudaFreeAsync(out->list[k], 0);
+    if (out->markers[k]) cudaFreeAsync(out->markers[k], 0);
+    out->list[k] = nullptr;
+    out->markers[k] = nullptr;
+  }
+}
+
+extern "C" void changa_walk_lists_free(ChangaWalkLists* out) {
+  if (!out) return;
+  cudaDeviceSynchronize();  // the lists may be in use on any stream
+  release_lists(out);
+  std::memset(out, 0, sizeof(*out));
+}
+
+extern "C" int changa_walk(const ChangaTreeView* t, const ChangaWalkParams* p,
+                           ChangaWalkLists* out, cudaStream_t s) {
+  if (!out) return record_error(CHANGA_E_INVALID_ARG, "walk: output", __FILE__, __LINE__);
+  std::memset(out, 0, sizeof(*out));
+  if (!walk_args_ok(t, p))
+    return record_error(CHANGA_E_INVALID_ARG, "walk: arguments", __FILE__, __LINE__);
+  const int nb = t->n_buckets;
+  out->n_buckets = nb;
+  out->order = p->order;
+  if (nb == 0) return 0;
+  const int nl = p->order == 4 ? 3 : 2;
+  WalkArgs a;
+  char* block = nullptr;
+  if (int rc = walk_setup(t, p, a, &block, s)) return rc;
+  std::vector<void*> scratch{block};
+  auto finish = [&](int rc) {
+    for (void* q : scratch) cudaFreeAsync(q, s);
+    scratch.clear();
+    if (rc) {
+      cudaStreamSynchronize(s);
+      release_lists(out);
+    }
+    return rc;
+  };
+  auto alloc = [&](size_t bytes) -> void* {
+    void* q = nullptr;
+    if (cudaMallocAsync(&q, bytes < 256 ? 256 : bytes, s) != cudaSuccess) return nullptr;
+    scratch.push_back(q);
+    return q;
+  };
+  int* cnt = (int*)alloc((size_t)3 * nb * sizeof(int));
+  const int tiles = (nb + kScanTile - 1) / kScanTile;
+  long long* ts = (long long*)alloc((size_t)tiles * sizeof(long long));
+  long long* off = (long long*)alloc((size_t)3 * (nb + 1) * sizeof(long long));
+  unsigned int* ctr = (unsigned int*)alloc(64);
+  if (!cnt || !ts || !off || !ctr)
+    return finish(record_error(cudaErrorMemoryAllocation, "walk: memory", __FILE__, __LINE__));
+  int h_err = 0;
+  /* Large trees: one traversal appends the entries into pools of chunks
+   * sized from a sampled count (every 16th bucket); small trees (where the
+   * sample's fixed costs dominate) count, then fill. */
+  bool appended = false;
+  long long chunks[3] = {0, 0, 0};
+  if (nb >= 16384) {
+    const int stride = 16, nsamp = (nb + stride - 1) / stride;
+    int* samp = (int*)alloc((size_t)3 * nsamp * sizeof(int));
+    if (!samp)
+      return finish(record_error(cudaErrorMemoryAllocation, "walk: memory", __FILE__, __LINE__));
+    a.n_cells = samp;
+    a.n_parts = samp + nsamp;
+    a.n_soft = nl == 3 ? samp + 2 * nsamp : nullptr;
+    a.bucket_stride = stride;
+    walk_run(a, kCount, s);
+    a.bucket_stride = 1;
+    std::vector<int> hs((size_t)nl * nsamp);
+    if (cudaMemcpyAsync(hs.data(), samp, hs.size() * sizeof(int), cudaMemcpyDeviceToHost, s) !=
+            cudaSuccess ||
+        cudaStreamSynchronize(s) != cudaSuccess)
+      return finish(record_error((int)cudaGetLastError(), "walk: sample", __FILE__, __LINE__));
+    bool ok = true;
+    for (int k = 0; k < nl && ok; ++k) {
+      double sum = 0;
+      for (int i = 0; i < nsamp; ++i) sum += hs[(size_t)k * nsamp + i];
+      chunks[k] = (long long)(sum * ((double)nb / nsamp) * g_pool_factor.load() / kChunk) + nb + 256;
+      a.pool[k] = (int2*)alloc((size_t)chunks[k] * kChunk * sizeof(int2));
+      a.chunk_bucket[k] = (int*)alloc((size_t)chunks[k] * sizeof(int));
+      a.chunk_rank[k] = (int*)alloc((size_t)chunks[k] * sizeof(int));
+      a.pool_chunks[k] = chunks[k];
+      ok = a.pool[k] && a.chunk_bucket[k] && a.chunk_rank[k];
+    }
+    if (ok && cudaMemsetAsync(ctr, 0, 64, s) == cudaSuccess) {
+      a.pool_next = ctr;
+      a.overflow = reinterpret_cast<int*>(ctr + 8);
+      a.n_cells = cnt;
+      a.n_parts = cnt + nb;
+      a.n_soft = nl == 3 ? cnt + 2 * (size_t)nb : nullptr;
+      walk_run(a, kAppend, s);
+      appended = true;
+    } else {
+      cudaGetLastError();  // a pool that did not fit: count and fill instead
+    }
+  }
+  if (!appended) {
+    a.n_cells = cnt;
+    a.n_parts = cnt + nb;
+    a.n_soft = nl == 3 ? cnt + 2 * (size_t)nb : nullptr;
+    walk_run(a, kCount, s);
+  }
+  /* offsets (and the int32 markers) of every list */
+  for (int k = 0; k < nl; ++k) {
+    if (cudaMallocAsync((void**)&out->markers[k], (size_t)(nb + 1) * sizeof(int), s) != cudaSuccess)
+      return finish(record_error(cudaErrorMemoryAllocation, "walk: markers", __FILE__, __LINE__));
+    scan_tile_sums_kernel<<<tiles, kScanThreads, 0, s>>>(cnt + (size_t)k * nb, nb, ts);
+    scan_tiles_kernel<<<1, kScanThreads, 0, s>>>(ts, tiles);
+    scan_apply_kernel<<<tiles, kScanThreads, 0, s>>>(cnt + (size_t)k * nb, nb, ts,
+                                                     off + (size_t)k * (nb + 1), out->markers[k]);
+    count_launch(3);
+  }
+  long long tot[3] = {0, 0, 0};
+  unsigned int hc[16] = {0};
+  for (int k = 0; k < nl; ++k)
+    cudaMemcpyAsync(&tot[k], off + (size_t)k * (nb + 1) + nb, sizeof(long long),
+                    cudaMemcpyDeviceToHost, s);
+  cudaMemcpyAsync(hc, ctr, 64, cudaMemcpyDeviceToHost, s);
+  cudaMemcpyAsync(&h_err, a.error, sizeof(int), cudaMemcpyDeviceToHost, s);
+  if (cudaStreamSynchronize(s) != cudaSuccess)
+    return finish(record_error((int)cudaGetLastError(), "walk: count", __FILE__, __LINE__));
+  if (h_err) return finish(walk_error(h_err));
+  for (int k = 0; k < nl; ++k) {
+    if (tot[k] >= (1LL << 31) - 1)
+      return finish(record_error(CHANGA_E_TOO_LARGE, "walk: list exceeds int32 markers", __FILE__,
+                                 __LINE__));
+    out->n_entries[k] = tot[k];
+    if (cudaMallocAsync((void**)&out->list[k], (size_t)(tot[k] > 0 ? tot[k] : 1) * sizeof(ILCell),
+                        s) != cudaSuccess)
+      return finish(record_error(cudaErrorMemoryAllocation, "walk: lists", __FILE__, __LINE__));
+  }
+  const bool overflow = appended && hc[8] != 0;
+  if (appended && !overflow) {
+    for (int k = 0; k < nl; ++k) {
+      const long long used = (long long)hc[k] < chunks[k] ? (long long)hc[k] : chunks[k];
+      if (used == 0) continue;
+      long long g = (used * kChunk + 255) / 256;
+      const long long cap = (long long)sm_count() * 16;
+      gather_chunks_kernel<<<(int)(g < cap ? g : cap), 256, 0, s>>>(
+          a.pool[k], a.chunk_bucket[k], a.chunk_rank[k], used, off + (size_t)k * (nb + 1),
+          (int2*)out->list[k]);
+      count_launch();
+    }
+  } else {
+    /* entries by a second traversal (small trees, or pools that ran short) */
+    a.off_cells = off;
+    a.off_parts = off + (nb + 1);
+    a.off_soft = nl == 3 ? off + 2 * (size_t)(nb + 1) : nullptr;
+    a.cells = (int2*)out->list[0];
+    a.parts = (int2*)out->list[1];
+    a.soft = nl == 3 ? (int2*)out->list[2] : nullptr;
+    walk_run(a, kFill, s);
+    cudaMemcpyAsync(&h_err, a.error, sizeof(int), cudaMemcpyDeviceToHost, s);
+  }
+  out->passes = appended ? (overflow ? 3 : 1) : 2;
+  if (cudaStreamSynchronize(s) != cudaSuccess)
+    return finish(record_error((int)cudaGetLastError(), "walk: entries", __FILE__, __LINE__));
+  if (h_err) return finish(walk_error(h_err));
+  return finish(0);
 }

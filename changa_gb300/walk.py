@@ -32,9 +32,26 @@ class DeviceListRequest:
         return self.list.cpu().numpy(), self.markers.cpu().numpy()
 
 
-def gpu_walk(lists, device="cuda", stream=None, timings=None):
+class _WalkLists:
+    """Owns the device lists of one changa_walk call until collected."""
+
+    def __init__(self, lib, res):
+        self.lib, self.res = lib, res
+
+    def __del__(self):
+        try:
+            self.lib.changa_walk_lists_free(C.byref(self.res))
+        except Exception:
+            pass
+
+
+def gpu_walk(lists, device="cuda", stream=None, timings=None, method="single"):
     """Walks lists' tree on the GPU; returns (cells, plist, softcells or None)
-    as DeviceListRequests over all buckets (bucket b at position b)."""
+    as DeviceListRequests over all buckets (bucket b at position b).
+
+    method "single": one library call (changa_walk: counts, prefix sums and
+    entries, library-owned lists); "two_pass": changa_walk_count, torch
+    prefix sums, changa_walk_fill into torch-owned lists."""
     import torch
     lib = N.cuda_lib()
     m = lists.meta
@@ -50,6 +67,29 @@ def gpu_walk(lists, device="cuda", stream=None, timings=None):
                             int(lists.n_replicas))
     s = stream if stream is not None else torch.cuda.current_stream().cuda_stream
     nb = int(bnode.shape[0])
+    if method == "single":
+        from .gputree import _view
+        torch.cuda.synchronize()
+        t1 = time.perf_counter()
+        res = N.ChangaWalkLists()
+        N.check(lib.changa_walk(C.byref(tv), C.byref(wp), C.byref(res), s), "changa_walk")
+        owner = _WalkLists(lib, res)
+        t2 = time.perf_counter()
+        starts = info[bnode.long(), 2].contiguous()
+        sizes = info[bnode.long(), 3].contiguous()
+        reqs = []
+        for k in range(3 if order == 4 else 2):
+            n = int(res.n_entries[k])
+            lst = _view(res.list[k], (n, 2), "<i4")
+            mk = _view(res.markers[k], (nb + 1,), "<i4")
+            r = DeviceListRequest(lst, mk, starts, sizes)
+            r._owner = owner
+            reqs.append(r)
+        if timings is not None:
+            timings.update(upload_s=t1 - t0, walk_s=t2 - t1, passes=int(res.passes))
+        return reqs[0], reqs[1], (reqs[2] if order == 4 else None)
+    if method != "two_pass":
+        raise ValueError("method must be 'single' or 'two_pass'")
     counts = [torch.zeros(nb, dtype=torch.int32, device=device) for _ in range(3)]
     torch.cuda.synchronize()
     t1 = time.perf_counter()

@@ -299,6 +299,33 @@ int changa_walk_fill(const ChangaTreeView *tree, const ChangaWalkParams *p,
                      const long long *off_soft, ILCell *cells, ILCell *parts, ILCell *soft,
                      cudaStream_t stream);
 
+/* The whole walk in one call.  Trees of 16384 buckets or more take one
+ * traversal: a count of every 16th bucket sizes pools of 256-entry chunks,
+ * one pass counts every bucket's lists and appends their entries chunk by
+ * chunk, and a gather puts the chunks in list order (a fill pass replaces
+ * the gather if a pool ran short).  Smaller trees count, then fill.  The
+ * lists and markers are device arrays owned by the result until
+ * changa_walk_lists_free: list k (0 cells, 1 particles, 2 softened cells
+ * when order is 4) holds n_entries[k] ILCells, bucket b's entries at
+ * markers[k][b] .. markers[k][b + 1], in the same order as count + fill
+ * write them.  passes: 1 (append + gather), 2 (count + fill), 3 (append,
+ * then fill).  Returns after the stream has finished. */
+typedef struct ChangaWalkLists {
+  int n_buckets;
+  int order;
+  int passes;
+  long long n_entries[3];
+  ILCell *list[3];
+  int *markers[3];
+} ChangaWalkLists;
+int changa_walk(const ChangaTreeView *tree, const ChangaWalkParams *p, ChangaWalkLists *out,
+                cudaStream_t stream);
+void changa_walk_lists_free(ChangaWalkLists *out);
+/* Append-pass pool capacity as a multiple of the sampled estimate of the
+ * entries (default 1.2; 0 leaves one chunk per bucket and list, so lists
+ * longer than one chunk end in the fill pass). */
+void changa_walk_set_pool_factor(double factor);
+
 /* Tree build on the device (no reference counterpart; restates the host
  * build, TreePiece.cpp:141-165 box and keys, GenericTreeNode.h:473-599
  * split, MultipoleMoments.h:206-352, 460-526 moments and radii): positions

@@ -13,8 +13,19 @@ from helpers import force_rel_err, force_rms_err
 pytestmark = pytest.mark.gpu
 
 
+def _identical(a, b):
+    """Two device requests hold the same arrays (entries in the same order)."""
+    la, ma = a.to_host()
+    lb, mb = b.to_host()
+    return np.array_equal(la, lb) and np.array_equal(ma, mb)
+
+
 def _check(L, ewald=None):
     cells, plist, soft = gpu_walk(L)
+    # changa_walk writes exactly what count + fill write
+    two = gpu_walk(L, method="two_pass")
+    for k in range(3 if L.order == 4 else 2):
+        assert _identical((cells, plist, soft)[k], two[k])
     nb = len(L.bucket_starts)
     assert same_entries(L.cells, cells, nb)
     assert same_entries(L.plist, plist, nb)
@@ -54,3 +65,30 @@ def test_walk_hexadecapole_softened(cuda_ok):
 def test_walk_ragged_buckets(cuda_ok, nb):
     p = ics.plummer(3000, ics.rng_for(5), soft=0.05)
     _check(tree.build_lists(p["pos"], p["mass"], p["soft"], n_bucket=nb, theta=0.6))
+
+
+def test_walk_single_traversal_path(cuda_ok):
+    """A tree of more than 16384 buckets takes changa_walk's single
+    traversal (sampled pool sizes, append, gather): the same arrays as count
+    + fill, the host walk's entries; and with pools too small it falls back
+    to the fill pass with the same result."""
+    from changa_gb300 import _native as N
+    p = ics.plummer(65536, ics.rng_for(6), soft=0.01)
+    L = tree.build_lists(p["pos"], p["mass"], p["soft"], n_bucket=2, theta=0.7)
+    nb = len(L.bucket_starts)
+    assert nb >= 16384
+    tm = {}
+    one = gpu_walk(L, timings=tm)
+    assert tm["passes"] == 1
+    two = gpu_walk(L, method="two_pass")
+    lib = N.cuda_lib()
+    lib.changa_walk_set_pool_factor(0.0)
+    try:
+        tm3 = {}
+        short = gpu_walk(L, timings=tm3)
+    finally:
+        lib.changa_walk_set_pool_factor(1.2)
+    assert tm3["passes"] == 3
+    for k in range(2):
+        assert _identical(one[k], two[k]) and _identical(short[k], two[k])
+    assert same_entries(L.cells, one[0], nb) and same_entries(L.plist, one[1], nb)
