@@ -343,3 +343,48 @@ def test_dropin_remote_resume_and_small_phase(plummer):
         free_all(d_m, d_p, d_v)
     finally:
         inp.free()
+
+
+def test_dropin_concurrent_streams(plummer, lattice):
+    """ChaNGa calls the boundary from several PE threads at once, each
+    TreePiece on its own stream (TreePiece.cpp:5380).  Four threads with
+    their own streams and host buffers, mixing cell/particle lists with
+    Ewald requests, call the drop-in concurrently (ctypes releases the GIL);
+    every result equals its serial result bit for bit (no shared mutable
+    state on the path; the Ewald parameters travel with each launch)."""
+    import threading
+    import torch
+    L, _, _ = plummer
+    Ll, ew, _ = lattice
+    cases = [(L, None), (Ll, ew), (L, None), (Ll, ew)]
+    serial = []
+    for Lc, e in cases:
+        inp = gravity.DropInInputs(Lc, ewald=e)
+        try:
+            serial.append(gravity.dropin_step(inp).copy())
+        finally:
+            inp.free()
+    inputs = [gravity.DropInInputs(Lc, ewald=e) for Lc, e in cases]
+    streams = [torch.cuda.Stream() for _ in cases]
+    out = [None] * len(cases)
+    errors = []
+
+    def run(i):
+        try:
+            for _ in range(3):
+                out[i] = gravity.dropin_step(inputs[i], stream=streams[i].cuda_stream).copy()
+        except Exception as ex:  # reported below
+            errors.append(ex)
+
+    threads = [threading.Thread(target=run, args=(i,)) for i in range(len(cases))]
+    try:
+        for t in threads:
+            t.start()
+        for t in threads:
+            t.join()
+    finally:
+        for inp in inputs:
+            inp.free()
+    assert not errors, errors
+    for i in range(len(cases)):
+        assert np.array_equal(out[i], serial[i]), i
