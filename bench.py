@@ -67,6 +67,8 @@ def parse():
     ap.add_argument("--no-adjoint-leapfrog", dest="adjoint_leapfrog", action="store_false")
     ap.add_argument("--no-direct", dest="direct", action="store_false",
                     help="skip the direct-sum error of the sampled particles")
+    ap.add_argument("--no-hexadecapole", dest="hexadecapole", action="store_false",
+                    help="skip the hexadecapole-build measurement on the same particles")
     ap.add_argument("--variants", default=None,
                     help="CELL,PART list-kernel shape variants to use instead of the autotuner")
     return ap.parse_args()
@@ -381,6 +383,63 @@ def measure_device_pipeline(wl, pts, interactions, reps=3):
     return best
 
 
+def measure_hexadecapole(wl, pts, samp=None, dsum=None, steps=5):
+    """ChaNGa's default build on the same particles: the hexadecapole lists
+    (host tree and walk, order 4) evaluated in the FP32-mixed form with the
+    hexadecapole Ewald term; same timing rules as the headline (warm-up, a
+    256 MB flush between steps, CUDA events on the stream).  The tree and
+    particle order are the quadrupole build's, so the sampled particles'
+    direct sums compare directly."""
+    import numpy as np
+    import torch
+    from changa_gb300 import _native as N
+    from changa_gb300 import gravity, tree
+    lib = N.cuda_lib()
+    t0 = time.perf_counter()
+    L = tree.build_lists(pts["pos"], pts["mass"], pts["soft"], n_bucket=wl.n_bucket,
+                         theta=wl.theta, period=wl.period, n_replicas=1 if wl.period else 0,
+                         order=4)
+    host_s = time.perf_counter() - t0
+    ds = gravity.DeviceSystem(L, device="cuda", ewald=wl.ewald_config())
+    stream = torch.cuda.current_stream()
+    flush = torch.empty(256 * 2 ** 20 // 4, dtype=torch.float32, device="cuda")
+    for _ in range(3):
+        ds.step("mixed")
+    torch.cuda.synchronize()
+    lib.changa_gb300_set_timing(1)
+    for k in N.KERNEL_IDS:
+        N.kernel_time(k)
+    evs = []
+    for _ in range(steps):
+        flush.fill_(1.0)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        ds.step("mixed")
+        e1.record(stream)
+        evs.append((e0, e1))
+    torch.cuda.synchronize()
+    kt = {k: N.kernel_time(k)[0] / steps for k in ("list_mixed_cell", "list_mixed_part",
+                                                   "ewald_mixed", "pack")}
+    lib.changa_gb300_set_timing(0)
+    ms = sum(a.elapsed_time(b) for a, b in evs) / steps
+    Ic, Ip, Is = (L.cells.interactions(), L.plist.interactions(), L.softcells.interactions())
+    I = Ic + Ip + Is
+    out = {"moments": "hexadecapole (scaled reduced, to fourth order)", "form": "FP32-mixed",
+           "interactions": I, "cell_interactions": Ic, "particle_interactions": Ip,
+           "softened_cell_interactions": Is, "ms_per_step": ms,
+           "interactions_per_s": I / (ms / 1e3), "kernel_ms": kt,
+           "cell_tflops_counted": Ic * 196 / (kt["list_mixed_cell"] / 1e3) / 1e12,
+           "host_tree_walk_s": host_s}
+    if samp is not None and dsum is not None:
+        v = ds.vars.cpu().numpy()[samp]
+        e = np.linalg.norm(v[:, :3] - dsum[:, :3], axis=1) / np.linalg.norm(dsum[:, :3], axis=1)
+        out.update({"median_rel_force_err_vs_direct": float(np.median(e)),
+                    "p99_rel_force_err_vs_direct": float(np.percentile(e, 99))})
+    del ds, L
+    torch.cuda.empty_cache()
+    return out
+
+
 def batched_workload(wl):
     return hasattr(wl, "systems")
 
@@ -413,7 +472,6 @@ def main_ours(args):
         walk_gpu = {}
         gpu_walk(lists, timings=walk_gpu)
         device_pipeline = measure_device_pipeline(wl, pts, I)
-        del pts
     I_c, I_p = lists.cells.interactions(), lists.plist.interactions()
     ds = gravity.DeviceSystem(lists, device="cuda", ewald=ew)
     stream = torch.cuda.current_stream()
@@ -534,6 +592,14 @@ def main_ours(args):
         for k in N.KERNEL_IDS:
             N.kernel_time(k)
 
+    # ChaNGa's default build (hexadecapole) on the same particles
+    hexa = None
+    if args.hexadecapole and pts is not None:
+        samp_h = samp if fp64 is not None else None
+        dsum_h = dsum if (fp64 is not None and args.direct) else None
+        hexa = measure_hexadecapole(wl, pts, samp_h, dsum_h)
+    pts = None
+
     # end to end through the public C-ABI with pinned host buffers
     e2e = None
     if args.e2e_steps > 0:
@@ -640,7 +706,7 @@ def main_ours(args):
                                  "write between timed steps" %
                                  ((lists.cells.list.nbytes + lists.plist.list.nbytes) / 1e9),
                               host_walk_s=t_walk, gpu_walk_s=walk_gpu and walk_gpu.get("walk_s"),
-                              device_pipeline=device_pipeline,
+                              device_pipeline=device_pipeline, hexadecapole=hexa,
                               fp64_form=fp64, kernels=kshare,
                               batched_graph=batched, sequential_plain=seq,
                               autotune=tuning,

@@ -8,7 +8,8 @@ leaving the device.
     acc = vars[:, :3][tree.inverse_perm()]                      # caller order
 
 The arrays stay owned by the library handle; torch tensors view them
-(CUDA array interface) until close().
+(CUDA array interface), and every view keeps the handle alive, so the
+device memory outlives the last view (or an explicit close()).
 """
 from __future__ import annotations
 
@@ -18,14 +19,36 @@ from . import _native as N
 
 
 class _CudaArray:
-    def __init__(self, ptr, shape, typestr):
+    """A CUDA array interface provider; torch keeps the provider (and so
+    `owner`, the holder of the memory) alive as long as the tensor."""
+
+    def __init__(self, ptr, shape, typestr, owner):
+        self.owner = owner
         self.__cuda_array_interface__ = {"shape": tuple(shape), "typestr": typestr,
                                          "data": (int(ptr), False), "version": 3}
 
 
-def _view(ptr, shape, typestr):
+def _view(ptr, shape, typestr, owner):
     import torch
-    return torch.as_tensor(_CudaArray(ptr, shape, typestr), device="cuda")
+    return torch.as_tensor(_CudaArray(ptr, shape, typestr, owner), device="cuda")
+
+
+class _TreeHandle:
+    """Owns one changa_tree_build result; frees it once."""
+
+    def __init__(self, handle):
+        self.handle = handle
+
+    def free(self):
+        if self.handle:
+            N.cuda_lib().changa_tree_free(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.free()
+        except Exception:
+            pass
 
 
 class DeviceTree:
@@ -40,28 +63,30 @@ class DeviceTree:
         soft = soft.contiguous().to(torch.float64)
         self._keep = (pos, mass, soft)
         s = stream if stream is not None else torch.cuda.current_stream().cuda_stream
-        self.handle = lib.changa_tree_build(pos.data_ptr(), mass.data_ptr(), soft.data_ptr(),
-                                            pos.shape[0], int(n_bucket), s)
-        if not self.handle:
+        handle = lib.changa_tree_build(pos.data_ptr(), mass.data_ptr(), soft.data_ptr(),
+                                       pos.shape[0], int(n_bucket), s)
+        if not handle:
             N.check(lib.changa_gb300_last_error() or N.CHANGA_ERRORS_RECORD, "changa_tree_build")
+        self._h = _TreeHandle(handle)
         a = N.ChangaTreeArrays()
-        N.check(lib.changa_tree_view(self.handle, C.byref(a)), "changa_tree_view")
+        N.check(lib.changa_tree_view(handle, C.byref(a)), "changa_tree_view")
+        h = self._h
         n, nm, nb = int(a.n), int(a.n_nodes), int(a.n_buckets)
         self.n, self.n_nodes, self.n_buckets = n, nm, nb
         self.n_bucket, self.theta = int(n_bucket), float(theta)
         self.period, self.n_replicas = float(period), int(n_replicas if period else 0)
         if period and not self.n_replicas:
             self.n_replicas = 1
-        self.perm = _view(a.perm, (n,), "<i4")
-        self.parts = _view(a.parts, (n, 5), "<f8")
-        self.moments = _view(a.moments, (nm, 12), "<f8")
-        self.meta = {"node_geom": _view(a.geom, (nm, 6), "<f8"),
-                     "node_bbox": _view(a.bbox, (nm, 6), "<f8"),
-                     "node_info": _view(a.info, (nm, 4), "<i4"),
-                     "parent": _view(a.parent, (nm,), "<i4"),
-                     "bucket_node": _view(a.bucket_node, (nb,), "<i4"),
-                     "leaf": _view(a.leaf, (n,), "<i4")}
-        self.box = _view(a.box, (6,), "<f8")
+        self.perm = _view(a.perm, (n,), "<i4", h)
+        self.parts = _view(a.parts, (n, 5), "<f8", h)
+        self.moments = _view(a.moments, (nm, 12), "<f8", h)
+        self.meta = {"node_geom": _view(a.geom, (nm, 6), "<f8", h),
+                     "node_bbox": _view(a.bbox, (nm, 6), "<f8", h),
+                     "node_info": _view(a.info, (nm, 4), "<i4", h),
+                     "parent": _view(a.parent, (nm,), "<i4", h),
+                     "bucket_node": _view(a.bucket_node, (nb,), "<i4", h),
+                     "leaf": _view(a.leaf, (n,), "<i4", h)}
+        self.box = _view(a.box, (6,), "<f8", h)
         self.root = None
 
     def inverse_perm(self):
@@ -71,13 +96,10 @@ class DeviceTree:
         inv[self.perm.long()] = torch.arange(self.n, device=self.perm.device)
         return inv
 
-    def close(self):
-        if getattr(self, "handle", None):
-            N.cuda_lib().changa_tree_free(self.handle)
-            self.handle = None
+    @property
+    def handle(self):
+        return self._h.handle
 
-    def __del__(self):
-        try:
-            self.close()
-        except Exception:
-            pass
+    def close(self):
+        """Frees the device arrays now (the views must not be used after)."""
+        self._h.free()

@@ -80,11 +80,10 @@ def gpu_walk(lists, device="cuda", stream=None, timings=None, method="single"):
         reqs = []
         for k in range(3 if order == 4 else 2):
             n = int(res.n_entries[k])
-            lst = _view(res.list[k], (n, 2), "<i4")
-            mk = _view(res.markers[k], (nb + 1,), "<i4")
-            r = DeviceListRequest(lst, mk, starts, sizes)
-            r._owner = owner
-            reqs.append(r)
+            # the views keep `owner` (and so the lists) alive
+            lst = _view(res.list[k], (n, 2), "<i4", owner)
+            mk = _view(res.markers[k], (nb + 1,), "<i4", owner)
+            reqs.append(DeviceListRequest(lst, mk, starts, sizes))
         if timings is not None:
             timings.update(upload_s=t1 - t0, walk_s=t2 - t1, passes=int(res.passes))
         return reqs[0], reqs[1], (reqs[2] if order == 4 else None)

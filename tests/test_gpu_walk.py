@@ -92,3 +92,27 @@ def test_walk_single_traversal_path(cuda_ok):
     for k in range(2):
         assert _identical(one[k], two[k]) and _identical(short[k], two[k])
     assert same_entries(L.cells, one[0], nb) and same_entries(L.plist, one[1], nb)
+
+
+def test_device_lists_outlive_their_call(cuda_ok):
+    """Tree arrays and lists come back as torch views of library memory;
+    each view keeps its owner alive.  Five trees built one after another
+    (only their DeviceSystems kept), each evaluated after all were built,
+    give the host-built trees' FP64 forces: no tree's memory was handed on
+    to the next build while still in use."""
+    import torch
+    from changa_gb300.gputree import DeviceTree
+    p = ics.plummer(65536, ics.rng_for(4), soft=0.01)
+    systems, hosts = [], []
+    for k in range(5):
+        pos = p["pos"] * (1.0 + 0.01 * k)
+        t = lambda a: torch.from_numpy(np.ascontiguousarray(a, dtype=np.float64)).cuda()
+        T = DeviceTree(t(pos), t(p["mass"]), t(p["soft"]), n_bucket=16, theta=0.7)
+        cells, plist, _ = gpu_walk(T)
+        systems.append(gravity.DeviceSystem(T, device_reqs=[cells, plist]))
+        del T, cells, plist
+        hosts.append(tree.build_lists(pos, p["mass"], p["soft"], n_bucket=16, theta=0.7))
+    for ds, L in zip(systems, hosts):
+        dev = ds.step("fp64").cpu().numpy()
+        host = gravity.DeviceSystem(L).step("fp64").cpu().numpy()
+        assert force_rel_err(dev, host).max() < 1e-10
