@@ -255,13 +255,11 @@ __device__ __forceinline__ int warp_excl_scan(int v, int& total) {
   return x - v;
 }
 
-/* Append pass: this step's t entries of list k (this lane's at bucket-list
- * positions q0 .. q0 + n - 1, q0 = cnt + its exclusive offset) go to the
- * bucket's chunks; chunks are taken from the pool as the list grows (lane 0,
- * one atomic per step that needs any) and recorded in the warp's table. */
-__device__ __forceinline__ void append_step(const WalkArgs& a, int k, int b, int* tab, int& nalloc,
-                                            long long cnt, int total, long long q0, int n,
-                                            int first_index, int code) {
+/* Append pass: before a step adds `total` entries to list k (cnt so far),
+ * the bucket's chunks are extended to hold them (lane 0, one atomic; the
+ * warp's table maps list ranks to chunks; -1 once the pool is short). */
+__device__ __forceinline__ void ensure_chunks(const WalkArgs& a, int k, int b, int* tab, int& nalloc,
+                                              long long cnt, int total) {
   const int need = (int)((cnt + total + kChunk - 1) / kChunk);
   if (need > nalloc) {  // uniform over the warp
     if ((threadIdx.x & 31) == 0) {
@@ -283,12 +281,14 @@ __device__ __forceinline__ void append_step(const WalkArgs& a, int k, int b, int
     nalloc = need;
     __syncwarp();
   }
-  for (int j = 0; j < n; ++j) {
-    const long long q = q0 + j;
-    const long long r = q / kChunk;
-    const int c = r < kMaxChunks ? tab[r] : -1;
-    if (c >= 0) a.pool[k][(size_t)c * kChunk + (q - r * kChunk)] = make_int2(first_index + j, code << 22);
-  }
+}
+
+/* Entry q of list k of this bucket into its chunk. */
+__device__ __forceinline__ void append_at(const WalkArgs& a, int k, const int* tab, long long q,
+                                          int2 e) {
+  const long long r = q / kChunk;
+  const int c = r < kMaxChunks ? tab[r] : -1;
+  if (c >= 0) a.pool[k][(size_t)c * kChunk + (q - r * kChunk)] = e;
 }
 
 template <int MODE>
@@ -395,21 +395,41 @@ __global__ void __launch_bounds__(kWalkWarps * 32) walk_kernel(const WalkArgs a)
     const unsigned mc = __ballot_sync(full, kind == 0), ms = __ballot_sync(full, kind == 1);
     int tpart;
     const int ppos = warp_excl_scan(kind == 2 ? pcount : 0, tpart);
-    if (FILL) {
-      if (kind == 0) a.cells[oc + nc + __popc(mc & below)] = make_int2(g, code << 22);
-      if (kind == 1) a.soft[os + ns + __popc(ms & below)] = make_int2(g, code << 22);
-      if (kind == 2)
-        for (int k = 0; k < pcount; ++k) a.parts[op + np + ppos + k] = make_int2(pfirst + k, code << 22);
-    } else if (MODE == kAppend) {
-      if (mc)
-        append_step(a, 0, b, ctab[warp][0], na[0], nc, __popc(mc), nc + __popc(mc & below),
-                     kind == 0, g, code);
-      if (ms)
-        append_step(a, 2, b, ctab[warp][2], na[2], ns, __popc(ms), ns + __popc(ms & below),
-                     kind == 1, g, code);
-      if (tpart)
-        append_step(a, 1, b, ctab[warp][1], na[1], np, tpart, np + ppos, kind == 2 ? pcount : 0,
-                    pfirst, code);
+    if (MODE == kAppend) {
+      if (mc) ensure_chunks(a, 0, b, ctab[warp][0], na[0], nc, __popc(mc));
+      if (ms) ensure_chunks(a, 2, b, ctab[warp][2], na[2], ns, __popc(ms));
+      if (tpart) ensure_chunks(a, 1, b, ctab[warp][1], na[1], np, tpart);
+    }
+    if (kind == 0) {
+      const long long q = nc + __popc(mc & below);
+      if (FILL) a.cells[oc + q] = make_int2(g, code << 22);
+      if (MODE == kAppend) append_at(a, 0, ctab[warp][0], q, make_int2(g, code << 22));
+    }
+    if (kind == 1) {
+      const long long q = ns + __popc(ms & below);
+      if (FILL) a.soft[os + q] = make_int2(g, code << 22);
+      if (MODE == kAppend) append_at(a, 2, ctab[warp][2], q, make_int2(g, code << 22));
+    }
+    if (MODE != kCount && tpart) {
+      /* the step's particle entries, 32 at a time: entry j belongs to the
+       * first lane whose run ends after j (a binary search over the lanes'
+       * inclusive ends), which lies ppos(owner) into that lane's run */
+      const int incl = ppos + (kind == 2 ? pcount : 0);
+      for (int j0 = 0; j0 < tpart; j0 += 32) {
+        const int j = j0 + lane;
+        int owner = 0;
+#pragma unroll
+        for (int bit = 16; bit > 0; bit >>= 1)
+          if (__shfl_sync(full, incl, owner + bit - 1) <= j) owner += bit;
+        const int o_pos = __shfl_sync(full, ppos, owner);
+        const int o_first = __shfl_sync(full, pfirst, owner);
+        const int o_code = __shfl_sync(full, code, owner);
+        if (j < tpart) {
+          const int2 e = make_int2(o_first + (j - o_pos), o_code << 22);
+          if (FILL) a.parts[op + np + j] = e;
+          if (MODE == kAppend) append_at(a, 1, ctab[warp][1], np + j, e);
+        }
+      }
     }
     nc += __popc(mc);
     ns += __popc(ms);
