@@ -31,6 +31,7 @@
  *         rounding of the *relative* vector, and per-tile FP32 partial sums
  *         are folded into Kahan-compensated per-particle totals.
  */
+#include <cuda.h>
 #include <type_traits>
 #include <utility>
 
@@ -666,11 +667,13 @@ __device__ __noinline__ float2 spline_near_f(float r, float dir, float twoh) {
  * (the register cap) x GROUP source chunks per reduction (the list tile). */
 struct Variant {
   int minb, group;
-  int tp;  // 0 source-parallel, 1 target-parallel (list_kernel_tp), 2 paired (list_kernel_tp2)
+  int tp;  // 0 source-parallel, 1 target-parallel (list_kernel_tp), 2 paired (list_kernel_tp2),
+           // 3 paired with TMA-staged cell records (list_kernel_tma; FP32-mixed cell lists,
+           //   list_kernel_tp2 for the others)
 };
 constexpr Variant kVariants[] = {{2, 16, 0}, {3, 16, 0}, {4, 16, 0}, {3, 32, 0}, {2, 32, 0},
                                  {2, 0, 1},  {3, 0, 1},  {4, 0, 1},  {2, 0, 2},  {3, 0, 2},
-                                 {4, 0, 2}};
+                                 {4, 0, 2},  {2, 0, 3},  {1, 0, 3}};
 constexpr int kNumVariants = sizeof(kVariants) / sizeof(kVariants[0]);
 
 /* Source-parallel list kernel of the FP32 forms.  Per warp and bucket: the
@@ -1230,6 +1233,73 @@ __device__ __forceinline__ f2 fma2(f2 a, f2 b, f2 c) {
 /* float index of field f of pair half h inside a pair block */
 __device__ __forceinline__ int pair_slot(int f, int h) { return 4 * (f >> 1) + 2 * (f & 1) + h; }
 
+/* One staged pair of quadrupole cells on one target, FP32 (gravity.h:
+ * 436-472, r = target - cell), for the paired kernels: w holds the pair's
+ * six words {x0 x1 y0 y1} {z0 z1 M0 M1} {xx xy} {xz yy} {yz zz} {tr soft}
+ * (each two-field word as pair halves); results accumulate with the
+ * potential's sign reversed. */
+__device__ __forceinline__ void pc_pair(const float4* __restrict__ w, f2 tx2, f2 ty2, f2 tz2, f2 tm2,
+                                        float tsoft, float near2, f2& pot2, f2& ax2, f2& ay2,
+                                        f2& az2, float& idt2) {
+  const float4 w0 = w[0], w1 = w[1];
+  const f2 px = pk2(w0.x, w0.y), py = pk2(w0.z, w0.w), pz = pk2(w1.x, w1.y), pm = pk2(w1.z, w1.w);
+  const float4 w2 = w[2], w3 = w[3], w4 = w[4],
+               w5 = w[5];
+  const f2 xx = pk2(w2.x, w2.y), xy = pk2(w2.z, w2.w), xz = pk2(w3.x, w3.y),
+           yy = pk2(w3.z, w3.w), yz = pk2(w4.x, w4.y), zz = pk2(w4.z, w4.w),
+           tr = pk2(w5.x, w5.y);
+  const f2 rx = sub2(tx2, px), ry = sub2(ty2, py), rz = sub2(tz2, pz);
+  const f2 rsq = fma2(rx, rx, fma2(ry, ry, mul2(rz, rz)));
+  float q0, q1;
+  up2(rsq, q0, q1);
+  const f2 dir = pk2(rsqrt_ftz(q0), rsqrt_ftz(q1));
+  const f2 dir2 = mul2(dir, dir);
+  f2 av = dir, bv = mul2(dir2, dir);
+  f2 cv = mul2(bv, mul2(dir2, pk2(3.f, 3.f)));
+  f2 dv = mul2(cv, mul2(dir2, pk2(5.f, 5.f)));
+  if (q0 <= near2 || q1 <= near2) {
+    float a_[2], b_[2], c_[2], d_[2], r_[2] = {q0, q1}, s_[2] = {w5.z, w5.w};
+    up2(av, a_[0], a_[1]);
+    up2(bv, b_[0], b_[1]);
+    up2(cv, c_[0], c_[1]);
+    up2(dv, d_[0], d_[1]);
+#pragma unroll
+    for (int h = 0; h < 2; ++h) {
+      if (r_[h] > near2) continue;
+      const float twoh = s_[h] + tsoft;
+      if (r_[h] == 0.f) {
+        a_[h] = b_[h] = c_[h] = d_[h] = 0.f;
+      } else if (r_[h] < twoh * twoh) {
+        const float4 kk = splineq_near_f(a_[h], r_[h], twoh);
+        a_[h] = kk.x;
+        b_[h] = kk.y;
+        c_[h] = kk.z;
+        d_[h] = kk.w;
+      }
+    }
+    av = pk2(a_[0], a_[1]);
+    bv = pk2(b_[0], b_[1]);
+    cv = pk2(c_[0], c_[1]);
+    dv = pk2(d_[0], d_[1]);
+  }
+  const f2 qirx = fma2(xx, rx, fma2(xy, ry, mul2(xz, rz)));
+  const f2 qiry = fma2(xy, rx, fma2(yy, ry, mul2(yz, rz)));
+  const f2 qirz = fma2(xz, rx, fma2(yz, ry, mul2(zz, rz)));
+  const f2 qir = mul2(pk2(0.5f, 0.5f), fma2(qirx, rx, fma2(qiry, ry, mul2(qirz, rz))));
+  const f2 bM = mul2(bv, pm);
+  const f2 qir3 = fma2(dv, qir, sub2(bM, mul2(cv, tr)));
+  /* pot -= M a + c qir - b tr: accumulated with the opposite sign */
+  pot2 = add2(pot2, sub2(fma2(cv, qir, mul2(pm, av)), mul2(bv, tr)));
+  /* a -= qir3 r - c Q r */
+  ax2 = fma2(cv, qirx, sub2(ax2, mul2(qir3, rx)));
+  ay2 = fma2(cv, qiry, sub2(ay2, mul2(qir3, ry)));
+  az2 = fma2(cv, qirz, sub2(az2, mul2(qir3, rz)));
+  float d0, d1;
+  up2(fma2(tm2, bv, bM), d0, d1);
+  idt2 = fmaxf(idt2, fmaxf(d0, d1));
+}
+
+
 template <int FORM, bool CELL, int MINB>
 __global__ void __launch_bounds__(kThreads, MINB) list_kernel_tp2(const ListArgs a) {
   static_assert(FORM != kF64, "FP32 arithmetic forms only");
@@ -1326,66 +1396,12 @@ __global__ void __launch_bounds__(kThreads, MINB) list_kernel_tp2(const ListArgs
         f2 ax2 = 0ull, ay2 = 0ull, az2 = 0ull, pot2 = 0ull;  // +0.0f in both halves
         /* one staged pair on this lane's target */
         auto body = [&](int p) {
-          const float4 w0 = st[p * PW], w1 = st[p * PW + 1];
-          const f2 px = pk2(w0.x, w0.y), py = pk2(w0.z, w0.w), pz = pk2(w1.x, w1.y),
-                   pm = pk2(w1.z, w1.w);
           if constexpr (CELL) {
-            /* gravity.h:436-472: r = target - cell */
-            const float4 w2 = st[p * PW + 2], w3 = st[p * PW + 3], w4 = st[p * PW + 4],
-                         w5 = st[p * PW + 5];
-            const f2 xx = pk2(w2.x, w2.y), xy = pk2(w2.z, w2.w), xz = pk2(w3.x, w3.y),
-                     yy = pk2(w3.z, w3.w), yz = pk2(w4.x, w4.y), zz = pk2(w4.z, w4.w),
-                     tr = pk2(w5.x, w5.y);
-            const f2 rx = sub2(tx2, px), ry = sub2(ty2, py), rz = sub2(tz2, pz);
-            const f2 rsq = fma2(rx, rx, fma2(ry, ry, mul2(rz, rz)));
-            float q0, q1;
-            up2(rsq, q0, q1);
-            const f2 dir = pk2(rsqrt_ftz(q0), rsqrt_ftz(q1));
-            const f2 dir2 = mul2(dir, dir);
-            f2 av = dir, bv = mul2(dir2, dir);
-            f2 cv = mul2(bv, mul2(dir2, pk2(3.f, 3.f)));
-            f2 dv = mul2(cv, mul2(dir2, pk2(5.f, 5.f)));
-            if (q0 <= near2 || q1 <= near2) {
-              float a_[2], b_[2], c_[2], d_[2], r_[2] = {q0, q1}, s_[2] = {w5.z, w5.w};
-              up2(av, a_[0], a_[1]);
-              up2(bv, b_[0], b_[1]);
-              up2(cv, c_[0], c_[1]);
-              up2(dv, d_[0], d_[1]);
-#pragma unroll
-              for (int h = 0; h < 2; ++h) {
-                if (r_[h] > near2) continue;
-                const float twoh = s_[h] + tsoft;
-                if (r_[h] == 0.f) {
-                  a_[h] = b_[h] = c_[h] = d_[h] = 0.f;
-                } else if (r_[h] < twoh * twoh) {
-                  const float4 kk = splineq_near_f(a_[h], r_[h], twoh);
-                  a_[h] = kk.x;
-                  b_[h] = kk.y;
-                  c_[h] = kk.z;
-                  d_[h] = kk.w;
-                }
-              }
-              av = pk2(a_[0], a_[1]);
-              bv = pk2(b_[0], b_[1]);
-              cv = pk2(c_[0], c_[1]);
-              dv = pk2(d_[0], d_[1]);
-            }
-            const f2 qirx = fma2(xx, rx, fma2(xy, ry, mul2(xz, rz)));
-            const f2 qiry = fma2(xy, rx, fma2(yy, ry, mul2(yz, rz)));
-            const f2 qirz = fma2(xz, rx, fma2(yz, ry, mul2(zz, rz)));
-            const f2 qir = mul2(pk2(0.5f, 0.5f), fma2(qirx, rx, fma2(qiry, ry, mul2(qirz, rz))));
-            const f2 bM = mul2(bv, pm);
-            const f2 qir3 = fma2(dv, qir, sub2(bM, mul2(cv, tr)));
-            /* pot -= M a + c qir - b tr: accumulated with the opposite sign */
-            pot2 = add2(pot2, sub2(fma2(cv, qir, mul2(pm, av)), mul2(bv, tr)));
-            /* a -= qir3 r - c Q r */
-            ax2 = fma2(cv, qirx, sub2(ax2, mul2(qir3, rx)));
-            ay2 = fma2(cv, qiry, sub2(ay2, mul2(qir3, ry)));
-            az2 = fma2(cv, qirz, sub2(az2, mul2(qir3, rz)));
-            float d0, d1;
-            up2(fma2(tm2, bv, bM), d0, d1);
-            idt2 = fmaxf(idt2, fmaxf(d0, d1));
+            pc_pair(st + p * PW, tx2, ty2, tz2, tm2, tsoft, near2, pot2, ax2, ay2, az2, idt2);
           } else {
+            const float4 w0 = st[p * PW], w1 = st[p * PW + 1];
+            const f2 px = pk2(w0.x, w0.y), py = pk2(w0.z, w0.w), pz = pk2(w1.x, w1.y),
+                     pm = pk2(w1.z, w1.w);
             /* gravity.h:276-301: r = source - target */
             const f2 rx = sub2(px, tx2), ry = sub2(py, ty2), rz = sub2(pz, tz2);
             const f2 rsq = fma2(rx, rx, fma2(ry, ry, mul2(rz, rz)));
@@ -1484,6 +1500,227 @@ __global__ void __launch_bounds__(kThreads, MINB) list_kernel_tp2(const ListArgs
           v[3] += rp;
           v[4] = fmax(ri, v[4]);
         }
+      }
+      __syncwarp();
+    }
+  }
+}
+
+/* ------------------------------------------------------------------ */
+/* Paired cell kernel with TMA staging (FP32-mixed form): the packed    */
+/* cell records (64 bytes, one row of a 2-D tensor map) of each         */
+/* 32-entry block arrive in shared memory by eight tile::gather4 bulk   */
+/* tensor copies (four rows by index each) on a per-warp mbarrier; the  */
+/* next block's copy runs while the current block computes.  Each lane  */
+/* then turns its raw record into its half of a staged pair, and the    */
+/* arithmetic is list_kernel_tp2's (pc_pair).                           */
+/* ------------------------------------------------------------------ */
+
+__device__ int g_tma_timeouts = 0;  // mbarrier waits that gave up (results then invalid)
+
+__device__ __forceinline__ unsigned smem_u32(const void* p) {
+  return (unsigned)__cvta_generic_to_shared(p);
+}
+
+/* Waits for phase `parity` of the mbarrier, at most 2^22 polls. */
+__device__ __forceinline__ bool mbar_wait(unsigned bar, unsigned parity) {
+  for (int it = 0; it < (1 << 22); ++it) {
+    unsigned done;
+    asm volatile(
+        "{ .reg .pred p; mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2; "
+        "selp.u32 %0, 1, 0, p; }"
+        : "=r"(done)
+        : "r"(bar), "r"(parity)
+        : "memory");
+    if (done) return true;
+  }
+  return false;
+}
+
+/* Lane 0: the 32 rows of one block (row indices from the lanes) into raw. */
+__device__ __forceinline__ void tma_issue_block(const CUtensorMap* tmap, unsigned raw, unsigned bar,
+                                                int row) {
+  const unsigned full = 0xffffffffu;
+  int r[32];
+#pragma unroll
+  for (int l = 0; l < 32; ++l) r[l] = __shfl_sync(full, row, l);
+  if ((threadIdx.x & 31) == 0) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar), "r"(32 * 64)
+                 : "memory");
+#pragma unroll
+    for (int q = 0; q < 8; ++q)
+      asm volatile(
+          "cp.async.bulk.tensor.2d.shared::cluster.global.tile::gather4.mbarrier::complete_tx::bytes"
+          " [%0], [%1, {%2, %3, %4, %5, %6}], [%7];" ::"r"(raw + q * 256),
+          "l"(tmap), "r"(0), "r"(r[4 * q]), "r"(r[4 * q + 1]), "r"(r[4 * q + 2]), "r"(r[4 * q + 3]),
+          "r"(bar)
+          : "memory");
+  }
+}
+
+template <int MINB>
+__global__ void __launch_bounds__(kThreads, MINB) list_kernel_tma(const ListArgs a,
+                                                                  const __grid_constant__ CUtensorMap tmap) {
+  constexpr int PW = 6;  // float4 words per staged pair
+  __shared__ __align__(1024) float4 raw[kWarps][32 * kCellPackF4];
+  __shared__ __align__(16) float4 stage[kWarps][16 * PW];
+  __shared__ __align__(8) unsigned long long bars[kWarps];
+  __shared__ double red[kWarps][5][32];
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const unsigned full = 0xffffffffu;
+  const unsigned bar = smem_u32(&bars[warp]), rawa = smem_u32(raw[warp]);
+  if (lane == 0) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(bar) : "memory");
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+  }
+  __syncwarp();
+  unsigned phase = 0;
+  bool ok = true;
+
+  for (;;) {
+    int b = 0;
+    if (lane == 0) b = (int)atomicAdd(a.queue, 1u);
+    b = __shfl_sync(full, b, 0);
+    if (b >= a.n_buckets || !ok) break;
+    const int e_begin = max(__ldg(a.markers + b), 0);
+    const int e_end = (int)min((long long)__ldg(a.markers + b + 1), a.n_entries);  // memory safety
+    const long long tbase = __ldg(a.starts + b);
+    const int n = __ldg(a.sizes + b);
+    if (n <= 0 || tbase < 0 || tbase + n > a.n_tgt) continue;  // memory safety
+
+    const float4* tp0 = static_cast<const float4*>(a.tgt) + kPartPackF4 * tbase;
+    const float4 ch = __ldg(tp0), cl = __ldg(tp0 + 1);
+    const float3 chi = make_float3(ch.x, ch.y, ch.z), clo = make_float3(cl.x, cl.y, cl.z);
+
+    for (int t0 = 0; t0 < n && ok; t0 += 32) {
+      const int nt = min(32, n - t0);
+      const int G = 32 / nt;
+      const int g = lane / nt;
+      const int t = lane - g * nt;
+      const bool active = g < G;
+      const long long ti = tbase + t0 + t;
+      const float4* pp = static_cast<const float4*>(a.tgt) + kPartPackF4 * ti;
+      const float4 h = __ldg(pp), l = __ldg(pp + 1);
+      const float tx = (h.x - chi.x) + (l.x - clo.x);
+      const float ty = (h.y - chi.y) + (l.y - clo.y);
+      const float tz = (h.z - chi.z) + (l.z - clo.z);
+      const float tmass = h.w, tsoft = l.w;
+      const float tsmax = warp_max(active ? tsoft : 0.f);
+      const f2 tx2 = pk2(tx, tx), ty2 = pk2(ty, ty), tz2 = pk2(tz, tz), tm2 = pk2(tmass, tmass);
+
+      float sx = 0.f, sy = 0.f, sz = 0.f, sp = 0.f, idt2 = 0.f;
+      float cx = 0.f, cy = 0.f, cz = 0.f, cp = 0.f;
+      /* this lane's entry of the first block: its row and replica code */
+      auto entry = [&](int e, int& row, int& code) {
+        row = 0;
+        code = 0x49;  // replica (0, 0, 0)
+        if (e < e_end) {
+          const int2 ent = __ldg(a.list + e);
+          row = ent.x;
+          if ((unsigned long long)row >= (unsigned long long)a.n_src) row = 0;  // memory safety
+          code = (ent.y >> 22) & 0x1ff;
+        }
+      };
+      int row = 0, code = 0x49;
+      if (e_begin < e_end) {  // uniform; every issued block is waited for below
+        entry(e_begin + lane, row, code);
+        tma_issue_block(&tmap, rawa, bar, row);
+      }
+      for (int e0 = e_begin; e0 < e_end; e0 += 32) {
+        const int ne = min(32, e_end - e0);
+        if (!mbar_wait(bar, phase)) {
+          if (lane == 0) atomicAdd(&g_tma_timeouts, 1);
+          mbar_wait(bar, phase);  // once more (bounded) for the copy in flight
+          ok = false;
+          break;
+        }
+        phase ^= 1u;
+        /* this lane's raw record into its half of pair lane/2 */
+        {
+          const float4* rr = raw[warp] + lane * kCellPackF4;
+          const float4 w0 = rr[0], w1 = rr[1], w2 = rr[2], w3 = rr[3];
+          const float fp = a.fperiod_f;
+          const float ox = (float)((code & 7) - 3) * fp, oy = (float)(((code >> 3) & 7) - 3) * fp,
+                      oz = (float)(((code >> 6) & 7) - 3) * fp;
+          const bool valid = lane < ne;
+          float f[12];
+          f[0] = valid ? ((w0.x - chi.x) + ox) + (w1.x - clo.x) : 1e30f;
+          f[1] = valid ? ((w0.y - chi.y) + oy) + (w1.y - clo.y) : 1e30f;
+          f[2] = valid ? ((w0.z - chi.z) + oz) + (w1.z - clo.z) : 1e30f;
+          f[3] = valid ? w0.w : 0.f;
+          f[4] = valid ? w2.x : 0.f;
+          f[5] = valid ? w2.y : 0.f;
+          f[6] = valid ? w2.z : 0.f;
+          f[7] = valid ? w2.w : 0.f;
+          f[8] = valid ? w3.x : 0.f;
+          f[9] = valid ? w3.y : 0.f;
+          f[10] = valid ? w3.z : 0.f;
+          f[11] = valid ? w1.w : 0.f;  // softening
+          float* pb = reinterpret_cast<float*>(stage[warp] + (lane >> 1) * PW);
+#pragma unroll
+          for (int k = 0; k < 12; ++k) pb[pair_slot(k, lane & 1)] = f[k];
+          const float ls = valid ? w1.w : 0.f;
+          const float ss = warp_max(ls) + tsmax;
+          /* the raw buffer is free again: order the reads above before the
+           * next block's bulk copies into it */
+          __syncwarp();
+          if (lane == 0) asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+          __syncwarp();
+          if (e0 + 32 < e_end) {
+            entry(e0 + 32 + lane, row, code);
+            tma_issue_block(&tmap, rawa, bar, row);
+          }
+          const float near2 = ss * ss;
+          const float4* st = stage[warp];
+          f2 ax2 = 0ull, ay2 = 0ull, az2 = 0ull, pot2 = 0ull;
+          if (G == 1) {
+#pragma unroll 4
+            for (int q = 0; q < 16; ++q)
+              pc_pair(st + q * PW, tx2, ty2, tz2, tm2, tsoft, near2, pot2, ax2, ay2, az2, idt2);
+          } else if (active) {
+#pragma unroll 2
+            for (int q = g; q < 16; q += G)
+              pc_pair(st + q * PW, tx2, ty2, tz2, tm2, tsoft, near2, pot2, ax2, ay2, az2, idt2);
+          }
+          __syncwarp();  // the stage is rewritten by the next block
+          float x0, x1, y0, y1, z0, z1, p0, p1;
+          up2(ax2, x0, x1);
+          up2(ay2, y0, y1);
+          up2(az2, z0, z1);
+          up2(pot2, p0, p1);
+          kahan_add(sx, cx, x0 + x1);
+          kahan_add(sy, cy, y0 + y1);
+          kahan_add(sz, cz, z0 + z1);
+          kahan_add(sp, cp, -(p0 + p1));
+        }
+      }
+      if (!ok) break;
+
+      if (active) {
+        red[warp][0][lane] = (double)sx - (double)cx;
+        red[warp][1][lane] = (double)sy - (double)cy;
+        red[warp][2][lane] = (double)sz - (double)cz;
+        red[warp][3][lane] = (double)sp - (double)cp;
+        red[warp][4][lane] = (double)idt2;
+      }
+      __syncwarp();
+      if (lane < nt) {
+        double rx = 0, ry = 0, rz = 0, rp = 0, ri = 0;
+        for (int gg = 0; gg < G; ++gg) {
+          const int l2 = gg * nt + lane;
+          rx += red[warp][0][l2];
+          ry += red[warp][1][l2];
+          rz += red[warp][2][l2];
+          rp += red[warp][3][l2];
+          ri = fmax(ri, red[warp][4][l2]);
+        }
+        double* v = static_cast<double*>(a.vars) + 5 * (tbase + t0 + lane);
+        v[0] += rx;
+        v[1] += ry;
+        v[2] += rz;
+        v[3] += rp;
+        v[4] = fmax(ri, v[4]);
       }
       __syncwarp();
     }
@@ -1911,11 +2148,68 @@ cudaError_t launch_kernel(K kernel, int* occ_cache, int kid, const ListArgs& a, 
 /* current variant per list kernel id (FP32 forms) */
 int g_variant[6] = {8, 9, 0, 0, 8, 9};
 
+/* cuTensorMapEncodeTiled, resolved through the runtime (the library
+ * loads on machines without a driver). */
+typedef CUresult (*EncodeTiledFn)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*,
+                                  const cuuint64_t*, const cuuint64_t*, const cuuint32_t*,
+                                  const cuuint32_t*, CUtensorMapInterleave, CUtensorMapSwizzle,
+                                  CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+static EncodeTiledFn encode_tiled_fn() {
+  static EncodeTiledFn fn = nullptr;
+  static bool tried = false;
+  if (!tried) {
+    void* f = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &f, 12000, cudaEnableDefault,
+                                         &q) == cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      fn = (EncodeTiledFn)f;
+    else
+      cudaGetLastError();
+    tried = true;
+  }
+  return fn;
+}
+
+/* The packed cell records as a 2-D tensor: rows of 16 floats (64 bytes),
+ * one row per box (tile::gather4 takes one-row boxes). */
+static bool make_cell_tmap(const void* base, long long rows, CUtensorMap* tm) {
+  EncodeTiledFn enc = encode_tiled_fn();
+  if (!enc || !base || rows <= 0 || rows > 0x7fffffffLL || ((uintptr_t)base & 15)) return false;
+  const cuuint64_t dims[2] = {16, (cuuint64_t)rows};
+  const cuuint64_t strides[1] = {16 * sizeof(float)};
+  const cuuint32_t box[2] = {16, 1};
+  const cuuint32_t estr[2] = {1, 1};
+  return enc(tm, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2, const_cast<void*>(base), dims, strides, box,
+             estr, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
+             CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+}
+
+template <int MINB>
+cudaError_t launch_tma(const ListArgs& a, const CUtensorMap& tm, cudaStream_t s) {
+  static int occ = 0;
+  if (a.n_buckets <= 0) return cudaSuccess;
+  long long want = ((long long)a.n_buckets + kWarps - 1) / kWarps;
+  long long cap = (long long)sm_count() * blocks_per_sm(list_kernel_tma<MINB>, &occ);
+  int grid = (int)(want < cap ? want : cap);
+  TimingScope ts(list_kernel_id(kMix, true), s);
+  list_kernel_tma<MINB><<<grid, kThreads, 0, s>>>(a, tm);
+  count_launch();
+  return cudaGetLastError();
+}
+
 template <int FORM, bool CELL, int V>
 cudaError_t launch_variant(const ListArgs& a, cudaStream_t s) {
   static int occ = 0;
   constexpr Variant var = kVariants[V];
-  if constexpr (var.tp == 2)
+  if constexpr (var.tp == 3) {
+    if constexpr (FORM == kMix && CELL) {
+      CUtensorMap tm;
+      if (make_cell_tmap(a.src, a.n_src, &tm)) return launch_tma<var.minb>(a, tm, s);
+    }
+    return launch_kernel(list_kernel_tp2<FORM, CELL, var.minb>, &occ, list_kernel_id(FORM, CELL),
+                         a, s);
+  } else if constexpr (var.tp == 2)
     return launch_kernel(list_kernel_tp2<FORM, CELL, var.minb>, &occ, list_kernel_id(FORM, CELL),
                          a, s);
   else if constexpr (var.tp == 1)

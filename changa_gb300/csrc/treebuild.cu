@@ -277,7 +277,7 @@ __global__ void link_kernel(const LevelNode* __restrict__ nodes, const double* _
                             int n_nodes, int level, int base, int next_base,
                             const int* __restrict__ nchild_scan, const int* __restrict__ mid,
                             LevelNode* __restrict__ next, double* __restrict__ next_split,
-                            int* __restrict__ info, int* __restrict__ parent, int* __restrict__ levels,
+                            int* __restrict__ info, int* __restrict__ parent,
                             double* __restrict__ cell) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n_nodes) return;
@@ -287,7 +287,6 @@ __global__ void link_kernel(const LevelNode* __restrict__ nodes, const double* _
   f[0] = f[1] = -1;
   f[2] = nd.first;
   f[3] = nd.count;
-  levels[me] = level;
   const double* sp = split + 6 * (size_t)i;
   for (int k = 0; k < 6; ++k) cell[6 * (size_t)me + k] = sp[k];
   if (mid[i] < 0) return;
@@ -664,24 +663,23 @@ extern "C" ChangaTree* changa_tree_build(const double* pos, const double* mass, 
   long long cap = 4 * (n / n_bucket) + 64;
   t->info = (int*)alloc((size_t)cap * 4 * sizeof(int), true);
   t->parent = (int*)alloc((size_t)cap * sizeof(int), true);
-  int* levels = (int*)alloc((size_t)cap * sizeof(int), false);
   double* cell = (double*)alloc((size_t)cap * 6 * sizeof(double), false);
   auto grow = [&](long long need) -> bool {
     long long nc = cap;
     while (nc < need) nc *= 2;
     if (nc == cap) return true;
-    void* fields[4] = {t->info, t->parent, levels, cell};
-    const size_t width[4] = {4 * sizeof(int), sizeof(int), sizeof(int), 6 * sizeof(double)};
-    const bool keep[4] = {true, true, false, false};
-    void* fresh[4];
-    for (int k = 0; k < 4; ++k) {
+    void* fields[3] = {t->info, t->parent, cell};
+    const size_t width[3] = {4 * sizeof(int), sizeof(int), 6 * sizeof(double)};
+    const bool keep[3] = {true, true, false};
+    void* fresh[3];
+    for (int k = 0; k < 3; ++k) {
       fresh[k] = alloc((size_t)nc * width[k], keep[k]);
       if (!fresh[k]) return false;
       if (cudaMemcpyAsync(fresh[k], fields[k], (size_t)cap * width[k], cudaMemcpyDeviceToDevice,
                           s) != cudaSuccess)
         return false;
     }
-    for (int k = 0; k < 4; ++k) {
+    for (int k = 0; k < 3; ++k) {
       auto& list = keep[k] ? t->blocks : scratch;
       for (auto& b : list)
         if (b == fields[k]) {
@@ -691,8 +689,7 @@ extern "C" ChangaTree* changa_tree_build(const double* pos, const double* mass, 
     }
     t->info = (int*)fresh[0];
     t->parent = (int*)fresh[1];
-    levels = (int*)fresh[2];
-    cell = (double*)fresh[3];
+    cell = (double*)fresh[2];
     cap = nc;
     return true;
   };
@@ -703,7 +700,7 @@ extern "C" ChangaTree* changa_tree_build(const double* pos, const double* mass, 
   int* nchild = (int*)alloc((size_t)n * sizeof(int) + 16, false);
   int* mid = (int*)alloc((size_t)n * sizeof(int) + 16, false);
   int* pinned = nullptr;  // per-level read-back: last scan value, mid, node
-  if (!t->info || !t->parent || !levels || !cell || !lv[0] || !lv[1] || !sp[0] || !sp[1] ||
+  if (!t->info || !t->parent || !cell || !lv[0] || !lv[1] || !sp[0] || !sp[1] ||
       !nchild || !mid || cudaMallocHost((void**)&pinned, 4 * sizeof(int)) != cudaSuccess)
     return fail("tree: memory");
   {
@@ -744,7 +741,7 @@ extern "C" ChangaTree* changa_tree_build(const double* pos, const double* mass, 
     }
     link_kernel<<<(width + 255) / 256, 256, 0, s>>>(lv[cur], sp[cur], width, level, (int)base,
                                                     (int)(base + width), nchild, mid, lv[cur ^ 1],
-                                                    sp[cur ^ 1], t->info, t->parent, levels, cell);
+                                                    sp[cur ^ 1], t->info, t->parent, cell);
     count_launch(3);
     level_base.push_back(base);
     level_width.push_back(width);

@@ -9,6 +9,7 @@ import pytest
 import oracle
 from changa_gb300 import _native as N
 from changa_gb300 import gravity, ics, tree
+from changa_gb300.walk import gpu_walk
 from helpers import (FIXTURES, force_rel_err, force_rms_err, load_golden, lists_from_golden,
                      pot_rel_err, pot_rms_err)
 
@@ -226,9 +227,11 @@ def test_empty_request_and_validation(cuda_ok):
 
 
 def test_every_list_variant(plummer):
-    """Every shape variant of the FP32-form list kernels (source-parallel
-    and target-parallel), on the Plummer lists and on ragged buckets, holds
-    the same tolerances as the default one."""
+    """Every shape variant of the FP32-form list kernels (source-parallel,
+    target-parallel, paired, and paired with TMA-staged cell records), on
+    the Plummer lists, on ragged buckets and on GPU-walk lists (every
+    bucket, some lists empty), holds the same tolerances as the default
+    one."""
     L, ref, ref32 = plummer
     lib = N.cuda_lib()
     ids = [N.KERNEL_IDS[k] for k in ("list_f32_cell", "list_f32_part", "list_mixed_cell",
@@ -258,6 +261,11 @@ def test_every_list_variant(plummer):
                 vm = gravity.DeviceSystem(R).step("mixed").cpu().numpy()
                 assert np.median(force_rel_err(vm, rr)) < MIX_MEDIAN_TOL, (var, R.n_bucket)
                 assert np.percentile(force_rel_err(vm, rr), 99) < MIX_P99_TOL, (var, R.n_bucket)
+            # lists from the GPU walk hold every bucket, some with empty lists
+            cells, plist, _ = gpu_walk(ragged[0])
+            vd = gravity.DeviceSystem(ragged[0], device_reqs=[cells, plist]).step("mixed")
+            e = force_rel_err(vd.cpu().numpy(), ragged_ref[0])
+            assert np.median(e) < MIX_MEDIAN_TOL and np.percentile(e, 99) < MIX_P99_TOL, var
     finally:
         for k, s in zip(ids, saved):
             lib.changa_gb300_set_list_variant(k, s)
