@@ -19,7 +19,8 @@
  *   ewald_mix_kernel  FP32-mixed: d = x - cm in FP64 rounded once; each warp
  *                     first culls the replica lattice against the bounding box
  *                     of its 32 particles (so threads loop over ~90 candidate
- *                     replicas, not 343); hole terms with alpha^2 r^2 < 1 use
+ *                     replicas, not 343, each kept as packed offsets and its
+ *                     hole flag); hole terms with alpha^2 r^2 < 1 use
  *                     the convergent power series of the g_n (no cancellation
  *                     between -erf(ar)/r and the 1/r^k terms); other terms use
  *                     a rational erfc with fractional error < 1.2e-7 (Press et
@@ -505,7 +506,15 @@ __global__ void __launch_bounds__(kMixWarps * 32) ewald_mix_kernel(
       keep = hole || d2 <= P.cut2 * 1.0001f;
     }
     const unsigned bal = __ballot_sync(0xffffffffu, keep);
-    if (keep) repl[warp][count + __popc(bal & ((1u << lane) - 1u))] = (short)r;
+    if (keep) {
+      /* the replica as packed offsets (each + 8 in four bits) and its hole
+       * flag, so the term loop decodes it with shifts instead of integer
+       * divisions */
+      const int ix = r / (side * side) - nE, iy = (r / side) % side - nE, iz = r % side - nE;
+      const bool hole = ix >= -nR && ix <= nR && iy >= -nR && iy <= nR && iz >= -nR && iz <= nR;
+      repl[warp][count + __popc(bal & ((1u << lane) - 1u))] =
+          (short)((ix + 8) | ((iy + 8) << 4) | ((iz + 8) << 8) | ((int)hole << 12));
+    }
     count += __popc(bal);
   }
   __syncwarp();
@@ -515,9 +524,9 @@ __global__ void __launch_bounds__(kMixWarps * 32) ewald_mix_kernel(
   const float M = P.M, Q2 = P.Q2;
   float fp = P.k1M, fx = 0.f, fy = 0.f, fz = 0.f;
   for (int q = 0; q < count; ++q) {
-    const int r = repl[warp][q];
-    const int ix = r / (side * side) - nE, iy = (r / side) % side - nE, iz = r % side - nE;
-    const bool hole = ix >= -nR && ix <= nR && iy >= -nR && iy <= nR && iz >= -nR && iz <= nR;
+    const int pk = repl[warp][q];
+    const int ix = (pk & 15) - 8, iy = ((pk >> 4) & 15) - 8, iz = ((pk >> 8) & 15) - 8;
+    const bool hole = (pk >> 12) & 1;
     const float x = dx + ix * L, y = dy + iy * L, z = dz + iz * L;
     const float r2 = x * x + y * y + z * z;
     if (r2 > P.cut2 && !hole) continue;
