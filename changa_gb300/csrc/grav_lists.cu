@@ -934,6 +934,43 @@ __device__ __forceinline__ void gather_raw(const ListArgs& a, int e, int e_end,
   }
 }
 
+/* List entry e (a massless entry at replica (0, 0, 0) past the end), and the
+ * raw record of a loaded entry: gather_raw in two steps, so the entries can
+ * be loaded a block ahead of their records. */
+__device__ __forceinline__ int2 load_entry(const ListArgs& a, int e, int e_end) {
+  return e < e_end ? __ldg(a.list + e) : make_int2(0, 0x49 << 22);
+}
+
+template <int FORM, bool CELL>
+__device__ __forceinline__ void gather_raw_entry(const ListArgs& a, int2 ent,
+                                                 RawRec<FORM, CELL>& r) {
+  long long idx = ent.x;
+  if ((unsigned long long)idx >= (unsigned long long)a.n_src) idx = 0;  // memory safety
+  r.code = (ent.y >> 22) & 0x1ff;
+  if constexpr (FORM == kF32) {
+    if constexpr (CELL) {
+      const float4* m = reinterpret_cast<const float4*>(
+          static_cast<const CudaMultipoleMoments*>(a.src) + idx);
+      r.w0 = __ldg(m);
+      r.w1 = __ldg(m + 1);
+      r.w2 = __ldg(m + 2);
+    } else {
+      const CompactPartData* p = static_cast<const CompactPartData*>(a.src) + idx;
+      r.w0 = make_float4(__ldg(&p->position.x), __ldg(&p->position.y), __ldg(&p->position.z),
+                         __ldg(&p->mass));
+      r.f4 = __ldg(&p->soft);
+    }
+  } else {
+    const float4* p = static_cast<const float4*>(a.src) + (CELL ? kCellPackF4 : kPartPackF4) * idx;
+    r.w0 = __ldg(p);
+    r.w1 = __ldg(p + 1);
+    if constexpr (CELL) {
+      r.w2 = __ldg(p + 2);
+      r.w3 = __ldg(p + 3);
+    }
+  }
+}
+
 /* Finished record words: cells {x, y, z, M} {xx, xy, xz, yy} {yz, zz, tr,
  * soft}; particles {x, y, z, m} and the softening.  Entries past the list
  * end become massless records far away (they add exact zeros). */
@@ -1233,6 +1270,14 @@ __device__ __forceinline__ f2 fma2(f2 a, f2 b, f2 c) {
 /* float index of field f of pair half h inside a pair block */
 __device__ __forceinline__ int pair_slot(int f, int h) { return 4 * (f >> 1) + 2 * (f & 1) + h; }
 
+/* max of three (one instruction on sm_100 and later; NaN operands are
+ * ignored as fmaxf ignores them) */
+__device__ __forceinline__ float fmax3(float a, float b, float c) {
+  float d;
+  asm("max.f32 %0, %1, %2, %3;" : "=f"(d) : "f"(a), "f"(b), "f"(c));
+  return d;
+}
+
 /* One staged pair of quadrupole cells on one target, FP32 (gravity.h:
  * 436-472, r = target - cell), for the paired kernels: w holds the pair's
  * six words {x0 x1 y0 y1} {z0 z1 M0 M1} {xx xy} {xz yy} {yz zz} {tr soft}
@@ -1257,7 +1302,7 @@ __device__ __forceinline__ void pc_pair(const float4* __restrict__ w, f2 tx2, f2
   f2 av = dir, bv = mul2(dir2, dir);
   f2 cv = mul2(bv, mul2(dir2, pk2(3.f, 3.f)));
   f2 dv = mul2(cv, mul2(dir2, pk2(5.f, 5.f)));
-  if (q0 <= near2 || q1 <= near2) {
+  if (fminf(q0, q1) <= near2) {
     float a_[2], b_[2], c_[2], d_[2], r_[2] = {q0, q1}, s_[2] = {w5.z, w5.w};
     up2(av, a_[0], a_[1]);
     up2(bv, b_[0], b_[1]);
@@ -1296,7 +1341,7 @@ __device__ __forceinline__ void pc_pair(const float4* __restrict__ w, f2 tx2, f2
   az2 = fma2(cv, qirz, sub2(az2, mul2(qir3, rz)));
   float d0, d1;
   up2(fma2(tm2, bv, bM), d0, d1);
-  idt2 = fmaxf(idt2, fmaxf(d0, d1));
+  idt2 = fmax3(idt2, d0, d1);
 }
 
 
@@ -1360,8 +1405,11 @@ __global__ void __launch_bounds__(kThreads, MINB) list_kernel_tp2(const ListArgs
       float sx = 0.f, sy = 0.f, sz = 0.f, sp = 0.f, idt2 = 0.f;
       float cx = 0.f, cy = 0.f, cz = 0.f, cp = 0.f;
 
+      /* records one block ahead, their list entries two blocks ahead */
       RawRec<FORM, CELL> raw;
-      gather_raw<FORM, CELL>(a, e_begin + lane, e_end, raw);
+      int2 ent = load_entry(a, e_begin + lane, e_end);
+      gather_raw_entry<FORM, CELL>(a, ent, raw);
+      ent = load_entry(a, e_begin + 32 + lane, e_end);
       int buf = 0;
       for (int e0 = e_begin; e0 < e_end; e0 += 32, buf ^= 1) {
         const int ne = min(32, e_end - e0);
@@ -1391,7 +1439,10 @@ __global__ void __launch_bounds__(kThreads, MINB) list_kernel_tp2(const ListArgs
         const float ss = warp_max(ls) + tsmax;
         const float near2 = ss * ss;
         __syncwarp();
-        if (e0 + 32 < e_end) gather_raw<FORM, CELL>(a, e0 + 32 + lane, e_end, raw);
+        if (e0 + 32 < e_end) {
+          gather_raw_entry<FORM, CELL>(a, ent, raw);
+          ent = load_entry(a, e0 + 64 + lane, e_end);
+        }
         const float4* st = stage[warp][buf];
         f2 ax2 = 0ull, ay2 = 0ull, az2 = 0ull, pot2 = 0ull;  // +0.0f in both halves
         /* one staged pair on this lane's target */
@@ -1409,7 +1460,7 @@ __global__ void __launch_bounds__(kThreads, MINB) list_kernel_tp2(const ListArgs
             up2(rsq, q0, q1);
             const f2 dir = pk2(rsqrt_ftz(q0), rsqrt_ftz(q1));
             f2 av = dir, bv = mul2(mul2(dir, dir), dir);
-            if (q0 <= near2 || q1 <= near2) {
+            if (fminf(q0, q1) <= near2) {
               float a_[2], b_[2], r_[2] = {q0, q1};
               up2(av, a_[0], a_[1]);
               up2(bv, b_[0], b_[1]);
@@ -1438,7 +1489,7 @@ __global__ void __launch_bounds__(kThreads, MINB) list_kernel_tp2(const ListArgs
             az2 = fma2(rz, bm, az2);
             float d0, d1;
             up2(fma2(tm2, bv, bm), d0, d1);
-            idt2 = fmaxf(idt2, fmaxf(d0, d1));
+            idt2 = fmax3(idt2, d0, d1);
           }
         };
         if (G == 1) {
@@ -1919,7 +1970,7 @@ __device__ __forceinline__ void hex_pair(const float4* __restrict__ w, f2 tx2, f
   az2 = fma2(dir, sub2(add2(add2(o2z, o3z), tz), mul2(z, g0)), az2);
   float d0, d1;
   up2(mul2(add2(tm2, M), mul2(dir, mul2(dir, dir))), d0, d1);
-  idt2 = fmaxf(idt2, fmaxf(d0, d1));
+  idt2 = fmax3(idt2, d0, d1);
 }
 
 template <int FORM, int MINB>
