@@ -644,8 +644,9 @@ def main_ours(args):
                "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(lists.parts.nbytes),
                "ms_per_step": 1e3 * t_e2e,
                "api": "changa_gravity_step_host (include/changa_gb300.h), pinned host "
-                      "buffers, CHANGA_STEP_OVERWRITE; lists uploaded in 512 MiB chunks on a "
-                      "copy stream overlapping the list kernels"}
+                      "buffers, CHANGA_STEP_OVERWRITE; lists uploaded in 512 MiB chunks (halving "
+                      "toward the end) on a copy stream overlapping the list kernels; each "
+                      "chunk's particles read back on a second copy stream once final"}
         for a in list(pin.values()) + [out]:
             a.free()
 

@@ -883,24 +883,81 @@ void changa_gb300_set_host_chunk_bytes(size_t bytes) {
   g_host_chunk_bytes.store(bytes < 4096 ? 4096 : bytes);
 }
 
-/* The copy stream of the host entry on each device (created once). */
-static cudaStream_t copy_stream() {
-  static cudaStream_t st[64] = {nullptr};
+/* The copy streams of the host entry on each device (created once):
+ * which 0 carries the uploads, which 1 the read-backs, so the two
+ * directions of the host link run at once. */
+static cudaStream_t copy_stream(int which = 0) {
+  static cudaStream_t st[64][2] = {{nullptr}};
   static std::mutex mu;
   int dev = 0;
   cudaGetDevice(&dev);
   if (dev < 0 || dev >= 64) dev = 0;
   std::lock_guard<std::mutex> lk(mu);
-  if (!st[dev] && cudaStreamCreateWithFlags(&st[dev], cudaStreamNonBlocking) != cudaSuccess)
-    st[dev] = nullptr;
-  return st[dev];
+  cudaStream_t& x = st[dev][which & 1];
+  if (!x && cudaStreamCreateWithFlags(&x, cudaStreamNonBlocking) != cudaSuccess) x = nullptr;
+  return x;
+}
+
+/* Bucket ranges [b0, b1) of a request, about `per` list entries each; with
+ * shrink, the last 2 per entries go in halving chunks (down to per / 16),
+ * so little arithmetic is left once the final entries have landed. */
+static void list_chunks(const ChangaListRequest* r, long long per, bool shrink,
+                        std::vector<std::pair<int, int>>& out) {
+  const long long total = r->markers[r->n_buckets];
+  const long long floor_ = std::max<long long>(1, per / 16);
+  int b0 = 0;
+  while (b0 < r->n_buckets) {
+    const long long left = total - r->markers[b0];
+    long long want_n = per;
+    if (shrink && left <= 2 * per) want_n = std::max(floor_, left / 2);
+    const int* lo = r->markers + b0 + 1;
+    const int* hi = r->markers + r->n_buckets + 1;
+    const long long want = (long long)r->markers[b0] + want_n;
+    const int* it = std::upper_bound(lo, hi, (int)std::min<long long>(want, INT_MAX));
+    int b1 = (int)(it - r->markers) - 1;
+    if (b1 <= b0) b1 = b0 + 1;
+    if (b1 > r->n_buckets) b1 = r->n_buckets;
+    out.push_back({b0, b1});
+    b0 = b1;
+  }
+}
+
+/* Page-locked (or registered) host memory: a read-back into it returns at
+ * once, so it can be enqueued between launches without stalling them. */
+static bool host_pinned(const void* p) {
+  cudaPointerAttributes at;
+  if (cudaPointerGetAttributes(&at, p) != cudaSuccess) {
+    cudaGetLastError();
+    return false;
+  }
+  return at.type == cudaMemoryTypeHost;
+}
+
+/* Particle range [lo, hi) that the buckets [b0, b1) of r write (clamped to
+ * [0, n); empty when lo >= hi). */
+static std::pair<long long, long long> target_range(const ChangaListRequest* r, int b0, int b1,
+                                                    long long n) {
+  long long lo = LLONG_MAX, hi = LLONG_MIN;
+  for (int b = b0; b < b1; ++b) {
+    const long long st = r->starts[b], sz = r->sizes[b];
+    if (sz <= 0 || st < 0 || st + sz > n) continue;  // the kernel skips these buckets
+    lo = std::min(lo, st);
+    hi = std::max(hi, st + sz);
+  }
+  if (lo >= hi) return {0, 0};
+  return {lo, hi};
 }
 
 /* Host-array evaluation, pipelined: the small arrays go first, then each
  * interaction list in chunks of about kChunkBytes, on a copy stream; the
  * compute stream packs, runs Ewald, and launches the list kernel on each
  * chunk's bucket range as soon as its entries have landed, so the list
- * stream from host memory overlaps the force arithmetic. */
+ * stream from host memory overlaps the force arithmetic.  The last list's
+ * chunks shrink toward its end, and when their particle ranges are
+ * disjoint and vars is page-locked, each range's results go back on a
+ * second copy stream as soon as its kernel is done (every other
+ * contribution to those particles is ordered before it), so the read-back
+ * overlaps the remaining uploads. */
 int changa_gravity_step_host(int form, const double* moments, long long n_moments,
                              const double* parts, long long n_parts, const ChangaListRequest* cells,
                              const ChangaListRequest* plist, double fperiod,
@@ -921,25 +978,19 @@ int changa_gravity_step_host(int form, const double* moments, long long n_moment
   if (!c) return record_error(cudaErrorUnknown, "gravity_step_host: copy stream", __FILE__, __LINE__);
   const size_t kChunkBytes = g_host_chunk_bytes.load();
 
+  cudaStream_t rb = copy_stream(1);
+  if (!rb) return record_error(cudaErrorUnknown, "gravity_step_host: copy stream", __FILE__, __LINE__);
+
   /* chunks: [request][bucket range] by entry bytes */
   const ChangaListRequest* reqs[2] = {cells, plist};
+  int last = -1;  // the request evaluated last
+  for (int k = 0; k < 2; ++k)
+    if (reqs[k] && reqs[k]->n_buckets > 0) last = k;
   std::vector<std::pair<int, int>> chunks[2];
   for (int k = 0; k < 2; ++k) {
     const ChangaListRequest* r = reqs[k];
     if (!r || r->n_buckets == 0) continue;
-    const long long per = (long long)(kChunkBytes / sizeof(ILCell));
-    int b0 = 0;
-    while (b0 < r->n_buckets) {
-      const int* lo = r->markers + b0 + 1;
-      const int* hi = r->markers + r->n_buckets + 1;
-      const long long want = (long long)r->markers[b0] + per;
-      const int* it = std::upper_bound(lo, hi, (int)std::min<long long>(want, INT_MAX));
-      int b1 = (int)(it - r->markers) - 1;
-      if (b1 <= b0) b1 = b0 + 1;
-      if (b1 > r->n_buckets) b1 = r->n_buckets;
-      chunks[k].push_back({b0, b1});
-      b0 = b1;
-    }
+    list_chunks(r, (long long)(kChunkBytes / sizeof(ILCell)), k == last, chunks[k]);
   }
 
   /* one device block: FP64 inputs, packed inputs, requests, queue counters */
@@ -1019,6 +1070,36 @@ int changa_gravity_step_host(int form, const double* moments, long long n_moment
       }
     }
     if (e != cudaSuccess || !small) break;
+    /* the last list's particle ranges (host work while the copies run):
+     * per-chunk read-backs when they are disjoint */
+    std::vector<std::pair<long long, long long>> ranges, gaps;
+    bool early = last >= 0 && host_pinned(vars);
+    if (early) {
+      for (auto& ch : chunks[last])
+        ranges.push_back(target_range(reqs[last], ch.first, ch.second, n_parts));
+      std::vector<std::pair<long long, long long>> sorted;
+      for (auto& g : ranges)
+        if (g.first < g.second) sorted.push_back(g);
+      std::sort(sorted.begin(), sorted.end());
+      for (size_t i = 1; i < sorted.size() && early; ++i)
+        early = sorted[i - 1].second <= sorted[i].first;
+      /* the particles no chunk of the last list writes: final before it */
+      long long at = 0;
+      for (auto& g : sorted) {
+        if (g.first > at) gaps.push_back({at, g.first});
+        at = g.second;
+      }
+      if (at < n_parts) gaps.push_back({at, n_parts});
+    }
+    auto read_back = [&](long long lo, long long hi) -> cudaError_t {
+      if (lo >= hi) return cudaSuccess;
+      cudaEvent_t done = event(s);
+      if (!done) return cudaErrorUnknown;
+      cudaError_t x = cudaStreamWaitEvent(rb, done, 0);
+      if (x != cudaSuccess) return x;
+      return cudaMemcpyAsync(vars + 5 * lo, d_vars + 5 * lo, (size_t)(hi - lo) * 5 * sizeof(double),
+                             cudaMemcpyDeviceToHost, rb);
+    };
     /* compute stream */
     if ((e = cudaStreamWaitEvent(s, small, 0)) != cudaSuccess) break;
     if (overwrite && (e = cudaMemsetAsync(d_vars, 0, (size_t)n_parts * 5 * sizeof(double), s)) !=
@@ -1038,7 +1119,12 @@ int changa_gravity_step_host(int form, const double* moments, long long n_moment
       break;
     for (int k = 0; k < 2 && !rc && e == cudaSuccess; ++k) {
       const ChangaListRequest* r = reqs[k];
-      for (size_t i = 0; i < chunks[k].size() && !rc; ++i) {
+      if (k == last && early) {
+        for (size_t i = 0; i < gaps.size() && e == cudaSuccess; ++i)
+          e = read_back(gaps[i].first, gaps[i].second);
+        if (e != cudaSuccess) break;
+      }
+      for (size_t i = 0; i < chunks[k].size() && !rc && e == cudaSuccess; ++i) {
         if (!landed[k][i] || (e = cudaStreamWaitEvent(s, landed[k][i], 0)) != cudaSuccess) break;
         const int b0 = chunks[k][i].first, b1 = chunks[k][i].second;
         ChangaListRequest sub;
@@ -1051,15 +1137,19 @@ int changa_gravity_step_host(int form, const double* moments, long long n_moment
         rc = k == 0 ? run_fp(f, true, ksrc, n_moments, kpart, n_parts, &sub, fperiod, d_vars, s, q)
                     : run_fp(f, false, kpart, n_parts, kpart, n_parts, &sub, fperiod, d_vars, s,
                              q + 32);
+        if (!rc && k == last && early) e = read_back(ranges[i].first, ranges[i].second);
       }
     }
     if (rc || e != cudaSuccess) break;
-    e = cudaMemcpyAsync(vars, d_vars, (size_t)n_parts * 5 * sizeof(double), cudaMemcpyDeviceToHost,
-                        s);
+    if (!early)
+      e = cudaMemcpyAsync(vars, d_vars, (size_t)n_parts * 5 * sizeof(double),
+                          cudaMemcpyDeviceToHost, s);
   } while (0);
-  /* the copy stream must be idle before the block goes back to the pool */
+  /* both copy streams must be idle before the block goes back to the pool */
   cudaEvent_t copies_done = event(c);
   if (copies_done) cudaStreamWaitEvent(s, copies_done, 0);
+  cudaEvent_t reads_done = event(rb);
+  if (reads_done) cudaStreamWaitEvent(s, reads_done, 0);
   cudaError_t ef = cudaFreeAsync(block, s);
   cudaError_t es = cudaStreamSynchronize(s);
   for (cudaEvent_t ev : evs)

@@ -116,6 +116,56 @@ def test_host_entry_pipelined_chunks(plummer, lattice):
         lib.changa_gb300_set_host_chunk_bytes(512 << 20)
 
 
+def _reordered(req, order):
+    """The request with its buckets taken in `order` (a subset or a
+    permutation of the bucket indices), entries moved with them."""
+    seg = [req.list[req.markers[b]:req.markers[b + 1]] for b in order]
+    lst = np.concatenate(seg) if seg else req.list[:0]
+    markers = np.zeros(len(order) + 1, dtype=np.int32)
+    markers[1:] = np.cumsum([len(x) for x in seg])
+    return tree.ListRequest(np.ascontiguousarray(lst, dtype=np.int32), markers,
+                            np.ascontiguousarray(req.starts[order]),
+                            np.ascontiguousarray(req.sizes[order]),
+                            np.ascontiguousarray(req.bucket_ids[order]))
+
+
+def test_host_entry_early_readback(plummer, lattice):
+    """Host-array entry into page-locked vars, where each chunk's particles
+    are read back as soon as their last kernel is done: bit-identical to
+    the device-resident evaluation for the particle list as built, for one
+    with every other bucket dropped (particles no chunk writes), and for one
+    with its buckets shuffled (overlapping chunk ranges: one read-back at
+    the end), each chunked finely and with Ewald."""
+    import dataclasses
+    lib = N.cuda_lib()
+    rng = np.random.Generator(np.random.PCG64(7))
+    lib.changa_gb300_set_host_chunk_bytes(16 * 1024)
+    try:
+        for (L0, ew) in ((plummer[0], None), (lattice[0], lattice[1])):
+            nb = L0.plist.n_buckets
+            for order in (np.arange(nb), np.arange(0, nb, 2), rng.permutation(nb)):
+                L = dataclasses.replace(L0, plist=_reordered(L0.plist, order))
+                for form in ("mixed", "fp64"):
+                    dev = gravity.DeviceSystem(L, ewald=ew).step(form).cpu().numpy()
+                    out = gravity.PinnedArray(np.zeros((L.n, 5)))
+                    try:
+                        host = gravity.gravity_step_host(L, form, ewald=ew, vars=out.array,
+                                                         overwrite=True)
+                        if ew is None:
+                            assert np.array_equal(host, dev), form
+                        else:
+                            np.testing.assert_allclose(host, dev, rtol=1e-12,
+                                                       atol=1e-13 * np.abs(dev).max())
+                        out.array[...] = 1.0
+                        acc = gravity.gravity_step_host(L, form, ewald=ew, vars=out.array)
+                        np.testing.assert_allclose(acc[:, :4], dev[:, :4] + 1.0, rtol=1e-12,
+                                                   atol=1e-12)
+                    finally:
+                        out.free()
+    finally:
+        lib.changa_gb300_set_host_chunk_bytes(512 << 20)
+
+
 @pytest.mark.parametrize("name", FIXTURES)
 def test_fp64_form_matches_golden(cuda_ok, name):
     g = load_golden(name)
