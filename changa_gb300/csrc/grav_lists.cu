@@ -1278,70 +1278,102 @@ __device__ __forceinline__ float fmax3(float a, float b, float c) {
   return d;
 }
 
+__device__ __forceinline__ float fmin3(float a, float b, float c) {
+  float d;
+  asm("min.f32 %0, %1, %2, %3;" : "=f"(d) : "f"(a), "f"(b), "f"(c));
+  return d;
+}
+
+/* One lane's cell record into its half h of a staged pair (pc_pair's
+ * layout): {x0 x1 y0 y1} {z0 z1 -M0 -M1} {Sxx Sxy} {Sxz Syy} {Syz Szz}
+ * {tr tr3} with S = 3Q and tr3 = 3 tr (each two-field word as pair halves);
+ * the softening goes to a side array. */
+__device__ __forceinline__ void stage_cell_half(float* pb, int h, float4 p, float4 q1, float4 q2) {
+  // p {x, y, z, M}  q1 {xx, xy, xz, yy}  q2 {yz, zz, tr, soft}
+  pb[pair_slot(0, h)] = p.x;
+  pb[pair_slot(1, h)] = p.y;
+  pb[pair_slot(2, h)] = p.z;
+  pb[pair_slot(3, h)] = -p.w;
+  pb[pair_slot(4, h)] = 3.f * q1.x;
+  pb[pair_slot(5, h)] = 3.f * q1.y;
+  pb[pair_slot(6, h)] = 3.f * q1.z;
+  pb[pair_slot(7, h)] = 3.f * q1.w;
+  pb[pair_slot(8, h)] = 3.f * q2.x;
+  pb[pair_slot(9, h)] = 3.f * q2.y;
+  pb[pair_slot(10, h)] = q2.z;
+  pb[pair_slot(11, h)] = 3.f * q2.z;
+}
+
 /* One staged pair of quadrupole cells on one target, FP32 (gravity.h:
- * 436-472, r = target - cell), for the paired kernels: w holds the pair's
- * six words {x0 x1 y0 y1} {z0 z1 M0 M1} {xx xy} {xz yy} {yz zz} {tr soft}
- * (each two-field word as pair halves); results accumulate with the
- * potential's sign reversed. */
-__device__ __forceinline__ void pc_pair(const float4* __restrict__ w, f2 tx2, f2 ty2, f2 tz2, f2 tm2,
-                                        float tsoft, float near2, f2& pot2, f2& ax2, f2& ay2,
-                                        f2& az2, float& idt2) {
+ * 436-472, r = target - cell), for the paired kernels, on records staged by
+ * stage_cell_half.  With s = 1/r^2, c3 = c/3 and u = d/15 (far field:
+ * c3 = b s, u = c3 s), q = S r = 3 Q r and w = r.q = 6 qir, the terms of
+ * the reference read
+ *   c Q r = c3 q,  2 c qir = c3 w,  d qir = 2.5 u w,  c tr = c3 tr3,
+ * so no constant factor is applied per pair.  Accumulators: pa2 gets
+ * -M a + b tr and pw2 gets c3 w (the potential is pa2 - pw2 / 2), the
+ * acceleration adds c Q r - qir3 r (qir3 = b M + d qir - c tr), and idtn
+ * keeps the minimum of -(m_t b + M b) (dtGrav's maximum, negated).  sft
+ * holds the pair's two softenings. */
+__device__ __forceinline__ void pc_pair(const float4* __restrict__ w, const float* __restrict__ sft,
+                                        f2 tx2, f2 ty2, f2 tz2, f2 tmn2, float tsoft, float near2,
+                                        f2& pa2, f2& pw2, f2& ax2, f2& ay2, f2& az2, float& idtn) {
   const float4 w0 = w[0], w1 = w[1];
-  const f2 px = pk2(w0.x, w0.y), py = pk2(w0.z, w0.w), pz = pk2(w1.x, w1.y), pm = pk2(w1.z, w1.w);
+  const f2 px = pk2(w0.x, w0.y), py = pk2(w0.z, w0.w), pz = pk2(w1.x, w1.y), mn = pk2(w1.z, w1.w);
   const float4 w2 = w[2], w3 = w[3], w4 = w[4],
                w5 = w[5];
-  const f2 xx = pk2(w2.x, w2.y), xy = pk2(w2.z, w2.w), xz = pk2(w3.x, w3.y),
-           yy = pk2(w3.z, w3.w), yz = pk2(w4.x, w4.y), zz = pk2(w4.z, w4.w),
-           tr = pk2(w5.x, w5.y);
+  const f2 sxx = pk2(w2.x, w2.y), sxy = pk2(w2.z, w2.w), sxz = pk2(w3.x, w3.y),
+           syy = pk2(w3.z, w3.w), syz = pk2(w4.x, w4.y), szz = pk2(w4.z, w4.w),
+           tr = pk2(w5.x, w5.y), tr3 = pk2(w5.z, w5.w);
   const f2 rx = sub2(tx2, px), ry = sub2(ty2, py), rz = sub2(tz2, pz);
   const f2 rsq = fma2(rx, rx, fma2(ry, ry, mul2(rz, rz)));
   float q0, q1;
   up2(rsq, q0, q1);
-  const f2 dir = pk2(rsqrt_ftz(q0), rsqrt_ftz(q1));
-  const f2 dir2 = mul2(dir, dir);
-  f2 av = dir, bv = mul2(dir2, dir);
-  f2 cv = mul2(bv, mul2(dir2, pk2(3.f, 3.f)));
-  f2 dv = mul2(cv, mul2(dir2, pk2(5.f, 5.f)));
+  f2 av = pk2(rsqrt_ftz(q0), rsqrt_ftz(q1));
+  const f2 s2 = mul2(av, av);
+  f2 bv = mul2(s2, av);
+  f2 cv = mul2(bv, s2);  // c / 3
+  f2 uv = mul2(cv, s2);  // d / 15
   if (fminf(q0, q1) <= near2) {
-    float a_[2], b_[2], c_[2], d_[2], r_[2] = {q0, q1}, s_[2] = {w5.z, w5.w};
+    float a_[2], b_[2], c_[2], u_[2], r_[2] = {q0, q1};
     up2(av, a_[0], a_[1]);
     up2(bv, b_[0], b_[1]);
     up2(cv, c_[0], c_[1]);
-    up2(dv, d_[0], d_[1]);
+    up2(uv, u_[0], u_[1]);
 #pragma unroll
     for (int h = 0; h < 2; ++h) {
       if (r_[h] > near2) continue;
-      const float twoh = s_[h] + tsoft;
+      const float twoh = sft[h] + tsoft;
       if (r_[h] == 0.f) {
-        a_[h] = b_[h] = c_[h] = d_[h] = 0.f;
+        a_[h] = b_[h] = c_[h] = u_[h] = 0.f;
       } else if (r_[h] < twoh * twoh) {
         const float4 kk = splineq_near_f(a_[h], r_[h], twoh);
         a_[h] = kk.x;
         b_[h] = kk.y;
-        c_[h] = kk.z;
-        d_[h] = kk.w;
+        c_[h] = kk.z * (1.f / 3.f);
+        u_[h] = kk.w * (1.f / 15.f);
       }
     }
     av = pk2(a_[0], a_[1]);
     bv = pk2(b_[0], b_[1]);
     cv = pk2(c_[0], c_[1]);
-    dv = pk2(d_[0], d_[1]);
+    uv = pk2(u_[0], u_[1]);
   }
-  const f2 qirx = fma2(xx, rx, fma2(xy, ry, mul2(xz, rz)));
-  const f2 qiry = fma2(xy, rx, fma2(yy, ry, mul2(yz, rz)));
-  const f2 qirz = fma2(xz, rx, fma2(yz, ry, mul2(zz, rz)));
-  const f2 qir = mul2(pk2(0.5f, 0.5f), fma2(qirx, rx, fma2(qiry, ry, mul2(qirz, rz))));
-  const f2 bM = mul2(bv, pm);
-  const f2 qir3 = fma2(dv, qir, sub2(bM, mul2(cv, tr)));
-  /* pot -= M a + c qir - b tr: accumulated with the opposite sign */
-  pot2 = add2(pot2, sub2(fma2(cv, qir, mul2(pm, av)), mul2(bv, tr)));
-  /* a -= qir3 r - c Q r */
-  ax2 = fma2(cv, qirx, sub2(ax2, mul2(qir3, rx)));
-  ay2 = fma2(cv, qiry, sub2(ay2, mul2(qir3, ry)));
-  az2 = fma2(cv, qirz, sub2(az2, mul2(qir3, rz)));
+  const f2 qx = fma2(sxx, rx, fma2(sxy, ry, mul2(sxz, rz)));
+  const f2 qy = fma2(sxy, rx, fma2(syy, ry, mul2(syz, rz)));
+  const f2 qz = fma2(sxz, rx, fma2(syz, ry, mul2(szz, rz)));
+  const f2 wq = fma2(qx, rx, fma2(qy, ry, mul2(qz, rz)));
+  const f2 bmn = mul2(bv, mn);  // -b M
+  /* -qir3 = -b M - 2.5 u w + c3 tr3 */
+  const f2 nq3 = fma2(uv, mul2(wq, pk2(-2.5f, -2.5f)), fma2(cv, tr3, bmn));
+  pa2 = fma2(bv, tr, fma2(mn, av, pa2));
+  pw2 = fma2(cv, wq, pw2);
+  ax2 = fma2(cv, qx, fma2(nq3, rx, ax2));
+  ay2 = fma2(cv, qy, fma2(nq3, ry, ay2));
+  az2 = fma2(cv, qz, fma2(nq3, rz, az2));
   float d0, d1;
-  up2(fma2(tm2, bv, bM), d0, d1);
-  idt2 = fmax3(idt2, d0, d1);
+  up2(fma2(tmn2, bv, bmn), d0, d1);
+  idtn = fmin3(idtn, d0, d1);
 }
 
 
@@ -1400,7 +1432,8 @@ __global__ void __launch_bounds__(kThreads, MINB) list_kernel_tp2(const ListArgs
         tsoft = l.w;
       }
       const float tsmax = warp_max(active ? tsoft : 0.f);
-      const f2 tx2 = pk2(tx, tx), ty2 = pk2(ty, ty), tz2 = pk2(tz, tz), tm2 = pk2(tmass, tmass);
+      const float tms = CELL ? -tmass : tmass;  // pc_pair takes the target mass negated
+      const f2 tx2 = pk2(tx, tx), ty2 = pk2(ty, ty), tz2 = pk2(tz, tz), tm2 = pk2(tms, tms);
 
       float sx = 0.f, sy = 0.f, sz = 0.f, sp = 0.f, idt2 = 0.f;
       float cx = 0.f, cy = 0.f, cz = 0.f, cp = 0.f;
@@ -1419,20 +1452,13 @@ __global__ void __launch_bounds__(kThreads, MINB) list_kernel_tp2(const ListArgs
           /* this lane's record into its half of pair lane/2 */
           float* pb = reinterpret_cast<float*>(stage[warp][buf] + (lane >> 1) * PW);
           const int h = lane & 1;
-          pb[pair_slot(0, h)] = rec[0].x;
-          pb[pair_slot(1, h)] = rec[0].y;
-          pb[pair_slot(2, h)] = rec[0].z;
-          pb[pair_slot(3, h)] = rec[0].w;
           if constexpr (CELL) {
-            // rec[1] {xx, xy, xz, yy}  rec[2] {yz, zz, tr, soft}
-            pb[pair_slot(4, h)] = rec[1].x;
-            pb[pair_slot(5, h)] = rec[1].y;
-            pb[pair_slot(6, h)] = rec[1].z;
-            pb[pair_slot(7, h)] = rec[1].w;
-            pb[pair_slot(8, h)] = rec[2].x;
-            pb[pair_slot(9, h)] = rec[2].y;
-            pb[pair_slot(10, h)] = rec[2].z;
-            pb[pair_slot(11, h)] = rec[2].w;
+            stage_cell_half(pb, h, rec[0], rec[1], rec[2]);
+          } else {
+            pb[pair_slot(0, h)] = rec[0].x;
+            pb[pair_slot(1, h)] = rec[0].y;
+            pb[pair_slot(2, h)] = rec[0].z;
+            pb[pair_slot(3, h)] = rec[0].w;
           }
         }
         ssoft[warp][buf][lane] = ls;
@@ -1445,10 +1471,12 @@ __global__ void __launch_bounds__(kThreads, MINB) list_kernel_tp2(const ListArgs
         }
         const float4* st = stage[warp][buf];
         f2 ax2 = 0ull, ay2 = 0ull, az2 = 0ull, pot2 = 0ull;  // +0.0f in both halves
+        f2 pw2 = 0ull;
         /* one staged pair on this lane's target */
         auto body = [&](int p) {
           if constexpr (CELL) {
-            pc_pair(st + p * PW, tx2, ty2, tz2, tm2, tsoft, near2, pot2, ax2, ay2, az2, idt2);
+            pc_pair(st + p * PW, &ssoft[warp][buf][2 * p], tx2, ty2, tz2, tm2, tsoft, near2, pot2,
+                    pw2, ax2, ay2, az2, idt2);
           } else {
             const float4 w0 = st[p * PW], w1 = st[p * PW + 1];
             const f2 px = pk2(w0.x, w0.y), py = pk2(w0.z, w0.w), pz = pk2(w1.x, w1.y),
@@ -1504,16 +1532,24 @@ __global__ void __launch_bounds__(kThreads, MINB) list_kernel_tp2(const ListArgs
         up2(ay2, y0, y1);
         up2(az2, z0, z1);
         up2(pot2, p0, p1);
+        float pb_;  // this block's potential
+        if constexpr (CELL) {
+          float w0_, w1_;
+          up2(pw2, w0_, w1_);
+          pb_ = (p0 + p1) - 0.5f * (w0_ + w1_);
+        } else {
+          pb_ = -(p0 + p1);
+        }
         if constexpr (FORM == kMix) {
           kahan_add(sx, cx, x0 + x1);
           kahan_add(sy, cy, y0 + y1);
           kahan_add(sz, cz, z0 + z1);
-          kahan_add(sp, cp, -(p0 + p1));
+          kahan_add(sp, cp, pb_);
         } else {
           sx += x0 + x1;
           sy += y0 + y1;
           sz += z0 + z1;
-          sp -= p0 + p1;
+          sp += pb_;
         }
       }
 
@@ -1522,7 +1558,7 @@ __global__ void __launch_bounds__(kThreads, MINB) list_kernel_tp2(const ListArgs
         red[warp][1][lane] = (double)sy - (double)cy;
         red[warp][2][lane] = (double)sz - (double)cz;
         red[warp][3][lane] = (double)sp - (double)cp;
-        red[warp][4][lane] = (double)idt2;
+        red[warp][4][lane] = CELL ? -(double)idt2 : (double)idt2;
       }
       __syncwarp();
       if (lane < nt) {
@@ -1615,6 +1651,7 @@ __global__ void __launch_bounds__(kThreads, MINB) list_kernel_tma(const ListArgs
   constexpr int PW = 6;  // float4 words per staged pair
   __shared__ __align__(1024) float4 raw[kWarps][32 * kCellPackF4];
   __shared__ __align__(16) float4 stage[kWarps][16 * PW];
+  __shared__ float ssoft[kWarps][32];
   __shared__ __align__(8) unsigned long long bars[kWarps];
   __shared__ double red[kWarps][5][32];
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -1658,7 +1695,7 @@ __global__ void __launch_bounds__(kThreads, MINB) list_kernel_tma(const ListArgs
       const float tz = (h.z - chi.z) + (l.z - clo.z);
       const float tmass = h.w, tsoft = l.w;
       const float tsmax = warp_max(active ? tsoft : 0.f);
-      const f2 tx2 = pk2(tx, tx), ty2 = pk2(ty, ty), tz2 = pk2(tz, tz), tm2 = pk2(tmass, tmass);
+      const f2 tx2 = pk2(tx, tx), ty2 = pk2(ty, ty), tz2 = pk2(tz, tz), tm2 = pk2(-tmass, -tmass);
 
       float sx = 0.f, sy = 0.f, sz = 0.f, sp = 0.f, idt2 = 0.f;
       float cx = 0.f, cy = 0.f, cz = 0.f, cp = 0.f;
@@ -1695,23 +1732,17 @@ __global__ void __launch_bounds__(kThreads, MINB) list_kernel_tma(const ListArgs
           const float ox = (float)((code & 7) - 3) * fp, oy = (float)(((code >> 3) & 7) - 3) * fp,
                       oz = (float)(((code >> 6) & 7) - 3) * fp;
           const bool valid = lane < ne;
-          float f[12];
-          f[0] = valid ? ((w0.x - chi.x) + ox) + (w1.x - clo.x) : 1e30f;
-          f[1] = valid ? ((w0.y - chi.y) + oy) + (w1.y - clo.y) : 1e30f;
-          f[2] = valid ? ((w0.z - chi.z) + oz) + (w1.z - clo.z) : 1e30f;
-          f[3] = valid ? w0.w : 0.f;
-          f[4] = valid ? w2.x : 0.f;
-          f[5] = valid ? w2.y : 0.f;
-          f[6] = valid ? w2.z : 0.f;
-          f[7] = valid ? w2.w : 0.f;
-          f[8] = valid ? w3.x : 0.f;
-          f[9] = valid ? w3.y : 0.f;
-          f[10] = valid ? w3.z : 0.f;
-          f[11] = valid ? w1.w : 0.f;  // softening
+          const float4 p = valid ? make_float4(((w0.x - chi.x) + ox) + (w1.x - clo.x),
+                                               ((w0.y - chi.y) + oy) + (w1.y - clo.y),
+                                               ((w0.z - chi.z) + oz) + (w1.z - clo.z), w0.w)
+                                 : make_float4(1e30f, 1e30f, 1e30f, 0.f);
+          const float4 zero = make_float4(0.f, 0.f, 0.f, 0.f);
+          // w2 {xx, xy, xz, yy}  w3 {yz, zz, tr, 0}
+          const float4 q1 = valid ? w2 : zero, q2 = valid ? make_float4(w3.x, w3.y, w3.z, 0.f) : zero;
           float* pb = reinterpret_cast<float*>(stage[warp] + (lane >> 1) * PW);
-#pragma unroll
-          for (int k = 0; k < 12; ++k) pb[pair_slot(k, lane & 1)] = f[k];
+          stage_cell_half(pb, lane & 1, p, q1, q2);
           const float ls = valid ? w1.w : 0.f;
+          ssoft[warp][lane] = ls;
           const float ss = warp_max(ls) + tsmax;
           /* the raw buffer is free again: order the reads above before the
            * next block's bulk copies into it */
@@ -1724,15 +1755,17 @@ __global__ void __launch_bounds__(kThreads, MINB) list_kernel_tma(const ListArgs
           }
           const float near2 = ss * ss;
           const float4* st = stage[warp];
-          f2 ax2 = 0ull, ay2 = 0ull, az2 = 0ull, pot2 = 0ull;
+          f2 ax2 = 0ull, ay2 = 0ull, az2 = 0ull, pot2 = 0ull, pw2 = 0ull;
           if (G == 1) {
 #pragma unroll 4
             for (int q = 0; q < 16; ++q)
-              pc_pair(st + q * PW, tx2, ty2, tz2, tm2, tsoft, near2, pot2, ax2, ay2, az2, idt2);
+              pc_pair(st + q * PW, &ssoft[warp][2 * q], tx2, ty2, tz2, tm2, tsoft, near2, pot2,
+                      pw2, ax2, ay2, az2, idt2);
           } else if (active) {
 #pragma unroll 2
             for (int q = g; q < 16; q += G)
-              pc_pair(st + q * PW, tx2, ty2, tz2, tm2, tsoft, near2, pot2, ax2, ay2, az2, idt2);
+              pc_pair(st + q * PW, &ssoft[warp][2 * q], tx2, ty2, tz2, tm2, tsoft, near2, pot2,
+                      pw2, ax2, ay2, az2, idt2);
           }
           __syncwarp();  // the stage is rewritten by the next block
           float x0, x1, y0, y1, z0, z1, p0, p1;
@@ -1740,10 +1773,12 @@ __global__ void __launch_bounds__(kThreads, MINB) list_kernel_tma(const ListArgs
           up2(ay2, y0, y1);
           up2(az2, z0, z1);
           up2(pot2, p0, p1);
+          float w0_, w1_;
+          up2(pw2, w0_, w1_);
           kahan_add(sx, cx, x0 + x1);
           kahan_add(sy, cy, y0 + y1);
           kahan_add(sz, cz, z0 + z1);
-          kahan_add(sp, cp, -(p0 + p1));
+          kahan_add(sp, cp, (p0 + p1) - 0.5f * (w0_ + w1_));
         }
       }
       if (!ok) break;
@@ -1753,7 +1788,7 @@ __global__ void __launch_bounds__(kThreads, MINB) list_kernel_tma(const ListArgs
         red[warp][1][lane] = (double)sy - (double)cy;
         red[warp][2][lane] = (double)sz - (double)cz;
         red[warp][3][lane] = (double)sp - (double)cp;
-        red[warp][4][lane] = (double)idt2;
+        red[warp][4][lane] = -(double)idt2;  // pc_pair keeps dtGrav negated
       }
       __syncwarp();
       if (lane < nt) {
