@@ -1030,6 +1030,11 @@ __device__ __forceinline__ float warp_max(float v) {
   for (int o = 16; o > 0; o >>= 1) v = fmaxf(v, __shfl_xor_sync(kFull, v, o));
   return v;
 }
+__device__ __forceinline__ float warp_min(float v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v = fminf(v, __shfl_xor_sync(kFull, v, o));
+  return v;
+}
 
 template <int FORM, bool CELL, int MINB>
 __global__ void __launch_bounds__(kThreads, MINB) list_kernel_tp(const ListArgs a) {
@@ -1234,6 +1239,12 @@ __global__ void __launch_bounds__(kThreads, MINB) list_kernel_tp(const ListArgs 
 /* instructions for the same FMA-pipe work.  Staged records are laid   */
 /* out in pairs ({x0, x1, y0, y1} ...) so each 128-bit shared load     */
 /* yields two ready operand pairs.                                     */
+/* Particle lists: a block whose sources all lie beyond the softening  */
+/* bound of the targets' bounding box runs a loop with no softening    */
+/* test; in the other blocks the pairs within the bound are zeroed by  */
+/* selects and marked, and each lane evaluates its marked sources with */
+/* the spline after the block.  Neither loop branches per pair, so the */
+/* compiler overlaps consecutive pairs.                                */
 /* ------------------------------------------------------------------ */
 
 typedef unsigned long long f2;
@@ -1432,6 +1443,15 @@ __global__ void __launch_bounds__(kThreads, MINB) list_kernel_tp2(const ListArgs
         tsoft = l.w;
       }
       const float tsmax = warp_max(active ? tsoft : 0.f);
+      /* particles: the targets' bounding box, against which each block's
+       * sources are tested for the softening bound */
+      float3 blo = make_float3(0.f, 0.f, 0.f), bhi = blo;
+      if constexpr (!CELL) {
+        blo = make_float3(warp_min(active ? tx : 3.4e38f), warp_min(active ? ty : 3.4e38f),
+                          warp_min(active ? tz : 3.4e38f));
+        bhi = make_float3(warp_max(active ? tx : -3.4e38f), warp_max(active ? ty : -3.4e38f),
+                          warp_max(active ? tz : -3.4e38f));
+      }
       const float tms = CELL ? -tmass : tmass;  // pc_pair takes the target mass negated
       const f2 tx2 = pk2(tx, tx), ty2 = pk2(ty, ty), tz2 = pk2(tz, tz), tm2 = pk2(tms, tms);
 
@@ -1464,6 +1484,16 @@ __global__ void __launch_bounds__(kThreads, MINB) list_kernel_tp2(const ListArgs
         ssoft[warp][buf][lane] = ls;
         const float ss = warp_max(ls) + tsmax;
         const float near2 = ss * ss;
+        /* particles: no source of the block within the softening bound of
+         * the targets' box (then no pair of the block is softened; the
+         * margin covers the rounding of the box distance) */
+        bool far_block = false;
+        if constexpr (!CELL) {
+          const float bx = fmaxf(fmaxf(blo.x - rec[0].x, rec[0].x - bhi.x), 0.f);
+          const float by = fmaxf(fmaxf(blo.y - rec[0].y, rec[0].y - bhi.y), 0.f);
+          const float bz = fmaxf(fmaxf(blo.z - rec[0].z, rec[0].z - bhi.z), 0.f);
+          far_block = __all_sync(kFull, fmaf(bx, bx, fmaf(by, by, bz * bz)) > near2 * 1.0001f);
+        }
         __syncwarp();
         if (e0 + 32 < e_end) {
           gather_raw_entry<FORM, CELL>(a, ent, raw);
@@ -1472,60 +1502,97 @@ __global__ void __launch_bounds__(kThreads, MINB) list_kernel_tp2(const ListArgs
         const float4* st = stage[warp][buf];
         f2 ax2 = 0ull, ay2 = 0ull, az2 = 0ull, pot2 = 0ull;  // +0.0f in both halves
         f2 pw2 = 0ull;
-        /* one staged pair on this lane's target */
+        unsigned nmask = 0;  // particles: sources left for the softened pass
+        /* one staged cell pair on this lane's target */
         auto body = [&](int p) {
-          if constexpr (CELL) {
-            pc_pair(st + p * PW, &ssoft[warp][buf][2 * p], tx2, ty2, tz2, tm2, tsoft, near2, pot2,
-                    pw2, ax2, ay2, az2, idt2);
-          } else {
-            const float4 w0 = st[p * PW], w1 = st[p * PW + 1];
-            const f2 px = pk2(w0.x, w0.y), py = pk2(w0.z, w0.w), pz = pk2(w1.x, w1.y),
-                     pm = pk2(w1.z, w1.w);
-            /* gravity.h:276-301: r = source - target */
-            const f2 rx = sub2(px, tx2), ry = sub2(py, ty2), rz = sub2(pz, tz2);
-            const f2 rsq = fma2(rx, rx, fma2(ry, ry, mul2(rz, rz)));
-            float q0, q1;
-            up2(rsq, q0, q1);
-            const f2 dir = pk2(rsqrt_ftz(q0), rsqrt_ftz(q1));
-            f2 av = dir, bv = mul2(mul2(dir, dir), dir);
-            if (fminf(q0, q1) <= near2) {
-              float a_[2], b_[2], r_[2] = {q0, q1};
-              up2(av, a_[0], a_[1]);
-              up2(bv, b_[0], b_[1]);
-#pragma unroll
-              for (int h = 0; h < 2; ++h) {
-                if (r_[h] > near2) continue;
-                const float twoh = ssoft[warp][buf][2 * p + h] + tsoft;
-                if (r_[h] == 0.f) {
-                  a_[h] = b_[h] = 0.f;
-                } else {
-                  const float r1 = r_[h] * a_[h];
-                  if (r1 < twoh) {
-                    const float2 kk = spline_near_f(r1, a_[h], twoh);
-                    a_[h] = kk.x;
-                    b_[h] = kk.y;
-                  }
-                }
-              }
-              av = pk2(a_[0], a_[1]);
-              bv = pk2(b_[0], b_[1]);
-            }
-            const f2 bm = mul2(bv, pm);
-            pot2 = fma2(pm, av, pot2);  // opposite sign, negated at the fold
-            ax2 = fma2(rx, bm, ax2);
-            ay2 = fma2(ry, bm, ay2);
-            az2 = fma2(rz, bm, az2);
-            float d0, d1;
-            up2(fma2(tm2, bv, bm), d0, d1);
-            idt2 = fmax3(idt2, d0, d1);
-          }
+          pc_pair(st + p * PW, &ssoft[warp][buf][2 * p], tx2, ty2, tz2, tm2, tsoft, near2, pot2,
+                  pw2, ax2, ay2, az2, idt2);
         };
-        if (G == 1) {
+        /* a staged particle pair without branches: with MARK, halves within
+         * the softening bound get a = b = 0 (selects) and their bit in nmask,
+         * for the softened pass after the block */
+        auto part_body = [&](int p, auto mark) {
+          const float4 w0 = st[p * PW], w1 = st[p * PW + 1];
+          const f2 pm = pk2(w1.z, w1.w);
+          /* gravity.h:276-301: r = source - target */
+          const f2 rx = sub2(pk2(w0.x, w0.y), tx2), ry = sub2(pk2(w0.z, w0.w), ty2),
+                   rz = sub2(pk2(w1.x, w1.y), tz2);
+          const f2 rsq = fma2(rx, rx, fma2(ry, ry, mul2(rz, rz)));
+          float q0, q1;
+          up2(rsq, q0, q1);
+          float a0 = rsqrt_ftz(q0), a1 = rsqrt_ftz(q1);
+          if constexpr (decltype(mark)::value) {
+            const bool n0 = q0 <= near2, n1 = q1 <= near2;
+            nmask |= ((n0 ? 1u : 0u) | (n1 ? 2u : 0u)) << (2 * p);
+            a0 = n0 ? 0.f : a0;
+            a1 = n1 ? 0.f : a1;
+          }
+          const f2 av = pk2(a0, a1);
+          const f2 bv = mul2(mul2(av, av), av);
+          const f2 bm = mul2(bv, pm);
+          pot2 = fma2(pm, av, pot2);  // opposite sign, negated at the fold
+          ax2 = fma2(rx, bm, ax2);
+          ay2 = fma2(ry, bm, ay2);
+          az2 = fma2(rz, bm, az2);
+          float d0, d1;
+          up2(fma2(tm2, bv, bm), d0, d1);
+          idt2 = fmax3(idt2, d0, d1);
+        };
+        using Far = std::integral_constant<bool, false>;
+        using Mark = std::integral_constant<bool, true>;
+        if constexpr (CELL) {
+          if (G == 1) {
 #pragma unroll 4
-          for (int p = 0; p < 16; ++p) body(p);
-        } else if (active) {
+            for (int p = 0; p < 16; ++p) body(p);
+          } else if (active) {
 #pragma unroll 2
-          for (int p = g; p < 16; p += G) body(p);
+            for (int p = g; p < 16; p += G) body(p);
+          }
+        } else if (far_block) {
+          if (G == 1) {
+#pragma unroll 4
+            for (int p = 0; p < 16; ++p) part_body(p, Far{});
+          } else if (active) {
+#pragma unroll 2
+            for (int p = g; p < 16; p += G) part_body(p, Far{});
+          }
+        } else {
+          if (G == 1) {
+#pragma unroll 4
+            for (int p = 0; p < 16; ++p) part_body(p, Mark{});
+          } else if (active) {
+#pragma unroll 2
+            for (int p = g; p < 16; p += G) part_body(p, Mark{});
+          }
+        }
+        /* the marked sources (within the softening bound of the block),
+         * each lane its own, all lanes at once: gravity.h:276-301 with the
+         * spline inside 2h, zero at r = 0 */
+        float ex = 0.f, ey = 0.f, ez = 0.f, ep = 0.f;
+        if constexpr (!CELL) {
+          while (nmask) {
+            const int jb = __ffs(nmask) - 1;
+            nmask &= nmask - 1u;
+            const float* pb = reinterpret_cast<const float*>(st + (jb >> 1) * PW);
+            const int h = jb & 1;
+            const float dx = pb[pair_slot(0, h)] - tx, dy = pb[pair_slot(1, h)] - ty,
+                        dz = pb[pair_slot(2, h)] - tz, sm = pb[pair_slot(3, h)];
+            const float q = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
+            float av = 0.f, bv = 0.f;
+            if (q != 0.f) {
+              av = rsqrt_ftz(q);
+              bv = (av * av) * av;
+              const float twoh = ssoft[warp][buf][jb] + tsoft;
+              const float r1 = q * av;
+              if (r1 < twoh) spline_near(r1, av, twoh, av, bv);
+            }
+            const float bm = bv * sm;
+            ep = fmaf(sm, av, ep);
+            ex = fmaf(dx, bm, ex);
+            ey = fmaf(dy, bm, ey);
+            ez = fmaf(dz, bm, ez);
+            idt2 = fmaxf(idt2, fmaf(tmass, bv, bm));
+          }
         }
         float x0, x1, y0, y1, z0, z1, p0, p1;
         up2(ax2, x0, x1);
@@ -1538,17 +1605,17 @@ __global__ void __launch_bounds__(kThreads, MINB) list_kernel_tp2(const ListArgs
           up2(pw2, w0_, w1_);
           pb_ = (p0 + p1) - 0.5f * (w0_ + w1_);
         } else {
-          pb_ = -(p0 + p1);
+          pb_ = -((p0 + p1) + ep);
         }
         if constexpr (FORM == kMix) {
-          kahan_add(sx, cx, x0 + x1);
-          kahan_add(sy, cy, y0 + y1);
-          kahan_add(sz, cz, z0 + z1);
+          kahan_add(sx, cx, (x0 + x1) + ex);
+          kahan_add(sy, cy, (y0 + y1) + ey);
+          kahan_add(sz, cz, (z0 + z1) + ez);
           kahan_add(sp, cp, pb_);
         } else {
-          sx += x0 + x1;
-          sy += y0 + y1;
-          sz += z0 + z1;
+          sx += (x0 + x1) + ex;
+          sy += (y0 + y1) + ey;
+          sz += (z0 + z1) + ez;
           sp += pb_;
         }
       }
