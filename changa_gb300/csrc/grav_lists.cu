@@ -1325,7 +1325,9 @@ __device__ __forceinline__ void stage_cell_half(float* pb, int h, float4 p, floa
  * -M a + b tr and pw2 gets c3 w (the potential is pa2 - pw2 / 2), the
  * acceleration adds c Q r - qir3 r (qir3 = b M + d qir - c tr), and idtn
  * keeps the minimum of -(m_t b + M b) (dtGrav's maximum, negated).  sft
- * holds the pair's two softenings. */
+ * holds the pair's two softenings.  NEAR = false leaves out the softening
+ * test (for blocks whose cells all lie beyond the softening bound). */
+template <bool NEAR = true>
 __device__ __forceinline__ void pc_pair(const float4* __restrict__ w, const float* __restrict__ sft,
                                         f2 tx2, f2 ty2, f2 tz2, f2 tmn2, float tsoft, float near2,
                                         f2& pa2, f2& pw2, f2& ax2, f2& ay2, f2& az2, float& idtn) {
@@ -1345,7 +1347,7 @@ __device__ __forceinline__ void pc_pair(const float4* __restrict__ w, const floa
   f2 bv = mul2(s2, av);
   f2 cv = mul2(bv, s2);  // c / 3
   f2 uv = mul2(cv, s2);  // d / 15
-  if (fminf(q0, q1) <= near2) {
+  if (NEAR && fminf(q0, q1) <= near2) {
     float a_[2], b_[2], c_[2], u_[2], r_[2] = {q0, q1};
     up2(av, a_[0], a_[1]);
     up2(bv, b_[0], b_[1]);
@@ -1443,15 +1445,14 @@ __global__ void __launch_bounds__(kThreads, MINB) list_kernel_tp2(const ListArgs
         tsoft = l.w;
       }
       const float tsmax = warp_max(active ? tsoft : 0.f);
-      /* particles: the targets' bounding box, against which each block's
-       * sources are tested for the softening bound */
-      float3 blo = make_float3(0.f, 0.f, 0.f), bhi = blo;
-      if constexpr (!CELL) {
-        blo = make_float3(warp_min(active ? tx : 3.4e38f), warp_min(active ? ty : 3.4e38f),
-                          warp_min(active ? tz : 3.4e38f));
-        bhi = make_float3(warp_max(active ? tx : -3.4e38f), warp_max(active ? ty : -3.4e38f),
-                          warp_max(active ? tz : -3.4e38f));
-      }
+      /* the targets' bounding box, against which each block's sources are
+       * tested for the softening bound */
+      const float3 blo = make_float3(warp_min(active ? tx : 3.4e38f),
+                                     warp_min(active ? ty : 3.4e38f),
+                                     warp_min(active ? tz : 3.4e38f));
+      const float3 bhi = make_float3(warp_max(active ? tx : -3.4e38f),
+                                     warp_max(active ? ty : -3.4e38f),
+                                     warp_max(active ? tz : -3.4e38f));
       const float tms = CELL ? -tmass : tmass;  // pc_pair takes the target mass negated
       const f2 tx2 = pk2(tx, tx), ty2 = pk2(ty, ty), tz2 = pk2(tz, tz), tm2 = pk2(tms, tms);
 
@@ -1484,11 +1485,11 @@ __global__ void __launch_bounds__(kThreads, MINB) list_kernel_tp2(const ListArgs
         ssoft[warp][buf][lane] = ls;
         const float ss = warp_max(ls) + tsmax;
         const float near2 = ss * ss;
-        /* particles: no source of the block within the softening bound of
-         * the targets' box (then no pair of the block is softened; the
-         * margin covers the rounding of the box distance) */
-        bool far_block = false;
-        if constexpr (!CELL) {
+        /* no source of the block within the softening bound of the targets'
+         * box (then no pair of the block is softened; the margin covers the
+         * rounding of the box distance) */
+        bool far_block;
+        {
           const float bx = fmaxf(fmaxf(blo.x - rec[0].x, rec[0].x - bhi.x), 0.f);
           const float by = fmaxf(fmaxf(blo.y - rec[0].y, rec[0].y - bhi.y), 0.f);
           const float bz = fmaxf(fmaxf(blo.z - rec[0].z, rec[0].z - bhi.z), 0.f);
@@ -1503,10 +1504,13 @@ __global__ void __launch_bounds__(kThreads, MINB) list_kernel_tp2(const ListArgs
         f2 ax2 = 0ull, ay2 = 0ull, az2 = 0ull, pot2 = 0ull;  // +0.0f in both halves
         f2 pw2 = 0ull;
         unsigned nmask = 0;  // particles: sources left for the softened pass
-        /* one staged cell pair on this lane's target */
-        auto body = [&](int p) {
-          pc_pair(st + p * PW, &ssoft[warp][buf][2 * p], tx2, ty2, tz2, tm2, tsoft, near2, pot2,
-                  pw2, ax2, ay2, az2, idt2);
+        using Far = std::integral_constant<bool, false>;
+        using Mark = std::integral_constant<bool, true>;
+        /* one staged cell pair on this lane's target, with or without the
+         * softening test */
+        auto body = [&](int p, auto near) {
+          pc_pair<decltype(near)::value>(st + p * PW, &ssoft[warp][buf][2 * p], tx2, ty2, tz2,
+                                         tm2, tsoft, near2, pot2, pw2, ax2, ay2, az2, idt2);
         };
         /* a staged particle pair without branches: with MARK, halves within
          * the softening bound get a = b = 0 (selects) and their bit in nmask,
@@ -1538,15 +1542,21 @@ __global__ void __launch_bounds__(kThreads, MINB) list_kernel_tp2(const ListArgs
           up2(fma2(tm2, bv, bm), d0, d1);
           idt2 = fmax3(idt2, d0, d1);
         };
-        using Far = std::integral_constant<bool, false>;
-        using Mark = std::integral_constant<bool, true>;
         if constexpr (CELL) {
-          if (G == 1) {
+          if (far_block) {
+            if (G == 1) {
 #pragma unroll 4
-            for (int p = 0; p < 16; ++p) body(p);
+              for (int p = 0; p < 16; ++p) body(p, Far{});
+            } else if (active) {
+#pragma unroll 2
+              for (int p = g; p < 16; p += G) body(p, Far{});
+            }
+          } else if (G == 1) {
+#pragma unroll 4
+            for (int p = 0; p < 16; ++p) body(p, Mark{});
           } else if (active) {
 #pragma unroll 2
-            for (int p = g; p < 16; p += G) body(p);
+            for (int p = g; p < 16; p += G) body(p, Mark{});
           }
         } else if (far_block) {
           if (G == 1) {
