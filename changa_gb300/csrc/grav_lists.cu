@@ -2309,7 +2309,7 @@ cudaError_t launch_kernel(K kernel, int* occ_cache, int kid, const ListArgs& a, 
 }
 
 /* current variant per list kernel id (FP32 forms) */
-int g_variant[6] = {8, 9, 0, 0, 8, 9};
+int g_variant[6] = {8, 10, 0, 0, 8, 10};
 
 /* cuTensorMapEncodeTiled, resolved through the runtime (the library
  * loads on machines without a driver). */

@@ -80,7 +80,7 @@ int changa_gb300_kernel_time(int kernel, double *total_ms, long long *launches);
  * 0-4 source-parallel (resident blocks per SM x list chunks per reduction),
  * 5-7 target-parallel (2/3/4 blocks per SM), 8-10 target-parallel with
  * paired .f32x2 arithmetic (2/3/4 blocks per SM; defaults 8 for cell lists,
- * 9 for particle lists), 11-12 paired with the FP32-mixed cell records
+ * 10 for particle lists), 11-12 paired with the FP32-mixed cell records
  * staged by TMA tile::gather4 copies (2/1 blocks per SM; the other lists
  * run the paired kernel).  The autotuner (changa_gb300/autotune.py) times
  * them on a workload and selects one per kernel. */
