@@ -176,8 +176,10 @@ int changa_gravity_step(int form, const double *moments, long long n_moments,
  * stream while the list kernels run on `stream` over the chunks already
  * landed.  Results ACCUMULATE into vars (host, n_parts x 5); with
  * form | CHANGA_STEP_OVERWRITE they replace it instead (vars is not read,
- * so a fresh evaluation needs no zeroed host buffer).  Returns after the
- * work has finished, so vars is ready on return. */
+ * so a fresh evaluation needs no zeroed host buffer).  When vars is pinned
+ * and the last list's chunks write disjoint particle ranges, each range is
+ * read back on a second copy stream as soon as its kernel is done.
+ * Returns after the work has finished, so vars is ready on return. */
 #define CHANGA_STEP_OVERWRITE 0x100
 
 /* List bytes per upload chunk of changa_gravity_step_host (default 512 MiB,
