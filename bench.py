@@ -177,6 +177,26 @@ def cpu_sample(lists, target, seed=12345):
     return np.array(cid, np.int32), np.array(pid, np.int32), tot
 
 
+def ewald_terms_per_particle(parts, root, ew, sample=4096):
+    """Mean number of real-space Ewald terms one particle evaluates (the
+    replicas inside the cut or the hole, Ewald.cpp BucketEwald's test), over
+    a seeded sample of the particles."""
+    import numpy as np
+    rng = np.random.Generator(np.random.PCG64(20261205))
+    idx = rng.choice(parts.shape[0], size=min(sample, parts.shape[0]), replace=False)
+    d = parts[idx, 2:5] - np.asarray(root[3:6], dtype=np.float64)
+    ne = max(int(np.ceil(ew.fEwCut)), ew.n_reps)
+    r = np.arange(-ne, ne + 1)
+    g = np.stack(np.meshgrid(r, r, r, indexing="ij"), -1).reshape(-1, 3).astype(np.float64)
+    hole = (np.abs(g) <= ew.n_reps).all(1)
+    cut2 = (ew.fEwCut * ew.L) ** 2
+    terms = 0
+    for chunk in np.array_split(d, 16):
+        x = chunk[:, None, :] + g[None, :, :] * ew.L
+        terms += int((((x * x).sum(-1) <= cut2) | hole[None, :]).sum())
+    return terms / len(idx)
+
+
 def run_cpu(lists, ewald, target, kind_pref="auto", reps=1):
     """Times the CPU oracle on a bounded sample; returns dict."""
     import numpy as np
@@ -686,6 +706,21 @@ def main_ours(args):
                    "fma_pipe_active_ncu_pct": tr.get("list_mixed_part_fma_pipe_pct")}
     kshare = {k: {"ms_per_step": v[0] / max(1, args.steps), "launches": v[1]}
               for k, v in ktimes.items() if v[1]}
+    # Ewald on its own: particle evaluations/s and the reference's per-particle
+    # work score (Ewald.cpp:153-159, 259-264: 333 per real-space term, 58 per
+    # h-vector; it weighs erfc and exp far above one FLOP, so it is no
+    # roofline figure)
+    ewald_info = None
+    ms_ew, n_ew = ktimes.get("ewald_mixed", (0.0, 0))
+    if ew is not None and n_ew:
+        t_ew = ms_ew / n_ew / 1e3
+        terms = ewald_terms_per_particle(lists.parts, lists.root, ew)
+        nh = int(ew.params(lists.root).nEwhLoop)
+        fl = 333.0 * terms + 58.0 * nh
+        ewald_info = {"particles_per_launch": int(lists.n), "avg_launch_ms": 1e3 * t_ew,
+                      "particle_evals_per_s": lists.n / t_ew,
+                      "real_space_terms_per_particle": terms, "h_vectors": nh,
+                      "reference_score_per_particle": fl}
 
     adj = None
     if rank == 0 and args.adjoint:
@@ -708,7 +743,7 @@ def main_ours(args):
                                  ((lists.cells.list.nbytes + lists.plist.list.nbytes) / 1e9),
                               host_walk_s=t_walk, gpu_walk_s=walk_gpu and walk_gpu.get("walk_s"),
                               device_pipeline=device_pipeline, hexadecapole=hexa,
-                              fp64_form=fp64, kernels=kshare,
+                              fp64_form=fp64, kernels=kshare, ewald=ewald_info,
                               batched_graph=batched, sequential_plain=seq,
                               autotune=tuning,
                               parallelism="replicas x%d" % world),
