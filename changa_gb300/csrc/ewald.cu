@@ -29,6 +29,7 @@
  *                     turn from the integer h before the hardware sin/cos.
  */
 #include "chg_internal.h"
+#include "f32x2.cuh"
 
 namespace chg {
 namespace {
@@ -523,53 +524,154 @@ __global__ void __launch_bounds__(kMixWarps * 32) ewald_mix_kernel(
   const float a2 = P.alpha2, twoa2 = 2.f * a2, foura4 = twoa2 * twoa2, ka = P.ka;
   const float M = P.M, Q2 = P.Q2;
   float fp = P.k1M, fx = 0.f, fy = 0.f, fz = 0.f;
-  for (int q = 0; q < count; ++q) {
-    const int pk = repl[warp][q];
-    const int ix = (pk & 15) - 8, iy = ((pk >> 4) & 15) - 8, iz = ((pk >> 8) & 15) - 8;
-    const bool hole = (pk >> 12) & 1;
-    const float x = dx + ix * L, y = dy + iy * L, z = dz + iz * L;
-    const float r2 = x * x + y * y + z * z;
-    if (r2 > P.cut2 && !hole) continue;
-    const float s = a2 * r2;
-    float g0, g1, g2, g3, g4 = 0.f, g5 = 0.f;
-    if (hole && s < 1.0f) {
-      g0 = -ka * hole_series<0>(s);
-      g1 = -twoa2 * ka * hole_series<1>(s);
-      g2 = -foura4 * ka * hole_series<2>(s);
-      g3 = -foura4 * twoa2 * ka * hole_series<3>(s);
-      if constexpr (HEX) {
-        g4 = -foura4 * foura4 * ka * hole_series<4>(s);
-        g5 = -foura4 * foura4 * twoa2 * ka * hole_series<5>(s);
+  if constexpr (HEX) {
+    for (int q = 0; q < count; ++q) {
+      const int pk = repl[warp][q];
+      const int ix = (pk & 15) - 8, iy = ((pk >> 4) & 15) - 8, iz = ((pk >> 8) & 15) - 8;
+      const bool hole = (pk >> 12) & 1;
+      const float x = dx + ix * L, y = dy + iy * L, z = dz + iz * L;
+      const float r2 = x * x + y * y + z * z;
+      if (r2 > P.cut2 && !hole) continue;
+      const float s = a2 * r2;
+      float g0, g1, g2, g3, g4 = 0.f, g5 = 0.f;
+      if (hole && s < 1.0f) {
+        g0 = -ka * hole_series<0>(s);
+        g1 = -twoa2 * ka * hole_series<1>(s);
+        g2 = -foura4 * ka * hole_series<2>(s);
+        g3 = -foura4 * twoa2 * ka * hole_series<3>(s);
+        if constexpr (HEX) {
+          g4 = -foura4 * foura4 * ka * hole_series<4>(s);
+          g5 = -foura4 * foura4 * twoa2 * ka * hole_series<5>(s);
+        }
+      } else {
+        const float dir = rsqrtf(r2);
+        const float dir2 = dir * dir;
+        const float ar = sqrtf(s);
+        const float e = __expf(-s);
+        const float a = ka * dir2 * e;
+        const float ec = erfc_nr(ar, s);
+        g0 = (hole ? ec - 1.0f : ec) * dir;
+        g1 = fmaf(g0, dir2, a);
+        g2 = fmaf(3.f * g1, dir2, twoa2 * a);
+        g3 = fmaf(5.f * g2, dir2, foura4 * a);
+        if constexpr (HEX) {
+          g4 = fmaf(7.f * g3, dir2, foura4 * twoa2 * a);
+          g5 = fmaf(9.f * g4, dir2, foura4 * foura4 * a);
+        }
       }
-    } else {
-      const float dir = rsqrtf(r2);
-      const float dir2 = dir * dir;
-      const float ar = sqrtf(s);
-      const float e = __expf(-s);
-      const float a = ka * dir2 * e;
-      const float ec = erfc_nr(ar, s);
-      g0 = (hole ? ec - 1.0f : ec) * dir;
-      g1 = fmaf(g0, dir2, a);
-      g2 = fmaf(3.f * g1, dir2, twoa2 * a);
-      g3 = fmaf(5.f * g2, dir2, foura4 * a);
       if constexpr (HEX) {
-        g4 = fmaf(7.f * g3, dir2, foura4 * twoa2 * a);
-        g5 = fmaf(9.f * g4, dir2, foura4 * foura4 * a);
+        hex_ewald_term<float>(P.hex, x, y, z, g0, g1, g2, g3, g4, g5, fp, fx, fy, fz);
+        continue;
       }
+      const float Q2mirx = P.xx * x + P.xy * y + P.xz * z;
+      const float Q2miry = P.xy * x + P.yy * y + P.yz * z;
+      const float Q2mirz = P.xz * x + P.yz * y + P.zz * z;
+      const float Q2mir = 0.5f * (Q2mirx * x + Q2miry * y + Q2mirz * z);
+      const float Qta = g1 * M - g2 * Q2 + g3 * Q2mir;
+      fp -= g0 * M - g1 * Q2 + g2 * Q2mir;
+      fx += g2 * Q2mirx - x * Qta;
+      fy += g2 * Q2miry - y * Qta;
+      fz += g2 * Q2mirz - z * Qta;
     }
-    if constexpr (HEX) {
-      hex_ewald_term<float>(P.hex, x, y, z, g0, g1, g2, g3, g4, g5, fp, fx, fy, fz);
-      continue;
+  } else {
+    /* two culled replicas per step as packed .f32x2 pairs; a replica past
+     * the cut (outside the hole), or the padding of an odd count, is
+     * evaluated and multiplied by 0 (its terms are finite) */
+    const f2 dx2 = pk2(dx, dx), dy2 = pk2(dy, dy), dz2 = pk2(dz, dz), L2 = pk2(L, L);
+    const f2 a2p = pk2(a2, a2), kap = pk2(ka, ka), twoa2p = pk2(twoa2, twoa2),
+             foura4p = pk2(foura4, foura4), Mp = pk2(M, M), Q2p = pk2(Q2, Q2);
+    const f2 xx = pk2(P.xx, P.xx), xy = pk2(P.xy, P.xy), xz = pk2(P.xz, P.xz),
+             yy = pk2(P.yy, P.yy), yz = pk2(P.yz, P.yz), zz = pk2(P.zz, P.zz);
+    f2 fp2 = 0ull, fx2 = 0ull, fy2 = 0ull, fz2 = 0ull;
+    for (int q = 0; q < count; q += 2) {
+      const bool two = q + 1 < count;
+      const int pk0 = repl[warp][q], pk1 = two ? repl[warp][q + 1] : pk0;
+      const bool hole0 = (pk0 >> 12) & 1, hole1 = (pk1 >> 12) & 1;
+      const f2 x = fma2(pk2((float)((pk0 & 15) - 8), (float)((pk1 & 15) - 8)), L2, dx2);
+      const f2 y = fma2(pk2((float)(((pk0 >> 4) & 15) - 8), (float)(((pk1 >> 4) & 15) - 8)), L2, dy2);
+      const f2 z = fma2(pk2((float)(((pk0 >> 8) & 15) - 8), (float)(((pk1 >> 8) & 15) - 8)), L2, dz2);
+      const f2 r2 = fma2(x, x, fma2(y, y, mul2(z, z)));
+      float r20, r21;
+      up2(r2, r20, r21);
+      const bool k0 = hole0 || r20 <= P.cut2, k1 = two && (hole1 || r21 <= P.cut2);
+      if (!(k0 || k1)) continue;
+      const f2 s2 = mul2(a2p, r2);
+      float s0, s1;
+      up2(s2, s0, s1);
+      /* the erfc form (Numerical Recipes erfcc, as erfc_nr) on both halves */
+      const f2 dir = pk2(rsqrtf(r20), rsqrtf(r21));
+      const f2 dir2 = mul2(dir, dir);
+      const float ar0 = sqrtf(s0), ar1 = sqrtf(s1);
+      const f2 e = pk2(__expf(-s0), __expf(-s1));
+      const f2 av = mul2(kap, mul2(dir2, e));
+      const f2 t = pk2(__fdividef(1.0f, fmaf(0.5f, ar0, 1.0f)), __fdividef(1.0f, fmaf(0.5f, ar1, 1.0f)));
+      f2 pp = pk2(0.17087277f, 0.17087277f);
+      pp = fma2(pp, t, pk2(-0.82215223f, -0.82215223f));
+      pp = fma2(pp, t, pk2(1.48851587f, 1.48851587f));
+      pp = fma2(pp, t, pk2(-1.13520398f, -1.13520398f));
+      pp = fma2(pp, t, pk2(0.27886807f, 0.27886807f));
+      pp = fma2(pp, t, pk2(-0.18628806f, -0.18628806f));
+      pp = fma2(pp, t, pk2(0.09678418f, 0.09678418f));
+      pp = fma2(pp, t, pk2(0.37409196f, 0.37409196f));
+      pp = fma2(pp, t, pk2(1.00002368f, 1.00002368f));
+      pp = fma2(pp, t, pk2(-1.26551223f, -1.26551223f));
+      float p0, p1;
+      up2(sub2(pp, s2), p0, p1);
+      const f2 ec = mul2(t, pk2(__expf(p0), __expf(p1)));
+      f2 g0 = mul2(sub2(ec, pk2(hole0 ? 1.f : 0.f, hole1 ? 1.f : 0.f)), dir);
+      f2 g1 = fma2(g0, dir2, av);
+      f2 g2 = fma2(mul2(pk2(3.f, 3.f), g1), dir2, mul2(twoa2p, av));
+      f2 g3 = fma2(mul2(pk2(5.f, 5.f), g2), dir2, mul2(foura4p, av));
+      /* hole terms with alpha^2 r^2 < 1: the convergent series instead */
+      const bool ser0 = hole0 && s0 < 1.0f, ser1 = hole1 && s1 < 1.0f;
+      if (ser0 || ser1) {
+        float a0_, a1_, b0_, b1_, c0_, c1_, d0_, d1_;
+        up2(g0, a0_, a1_);
+        up2(g1, b0_, b1_);
+        up2(g2, c0_, c1_);
+        up2(g3, d0_, d1_);
+        if (ser0) {
+          a0_ = -ka * hole_series<0>(s0);
+          b0_ = -twoa2 * ka * hole_series<1>(s0);
+          c0_ = -foura4 * ka * hole_series<2>(s0);
+          d0_ = -foura4 * twoa2 * ka * hole_series<3>(s0);
+        }
+        if (ser1) {
+          a1_ = -ka * hole_series<0>(s1);
+          b1_ = -twoa2 * ka * hole_series<1>(s1);
+          c1_ = -foura4 * ka * hole_series<2>(s1);
+          d1_ = -foura4 * twoa2 * ka * hole_series<3>(s1);
+        }
+        g0 = pk2(a0_, a1_);
+        g1 = pk2(b0_, b1_);
+        g2 = pk2(c0_, c1_);
+        g3 = pk2(d0_, d1_);
+      }
+      const f2 keep = pk2(k0 ? 1.f : 0.f, k1 ? 1.f : 0.f);
+      g0 = mul2(g0, keep);
+      g1 = mul2(g1, keep);
+      g2 = mul2(g2, keep);
+      g3 = mul2(g3, keep);
+      const f2 Q2mirx = fma2(xx, x, fma2(xy, y, mul2(xz, z)));
+      const f2 Q2miry = fma2(xy, x, fma2(yy, y, mul2(yz, z)));
+      const f2 Q2mirz = fma2(xz, x, fma2(yz, y, mul2(zz, z)));
+      const f2 Q2mir =
+          mul2(pk2(0.5f, 0.5f), fma2(Q2mirx, x, fma2(Q2miry, y, mul2(Q2mirz, z))));
+      const f2 Qta = fma2(g3, Q2mir, sub2(mul2(g1, Mp), mul2(g2, Q2p)));
+      fp2 = sub2(fp2, fma2(g2, Q2mir, sub2(mul2(g0, Mp), mul2(g1, Q2p))));
+      fx2 = fma2(g2, Q2mirx, sub2(fx2, mul2(x, Qta)));
+      fy2 = fma2(g2, Q2miry, sub2(fy2, mul2(y, Qta)));
+      fz2 = fma2(g2, Q2mirz, sub2(fz2, mul2(z, Qta)));
     }
-    const float Q2mirx = P.xx * x + P.xy * y + P.xz * z;
-    const float Q2miry = P.xy * x + P.yy * y + P.yz * z;
-    const float Q2mirz = P.xz * x + P.yz * y + P.zz * z;
-    const float Q2mir = 0.5f * (Q2mirx * x + Q2miry * y + Q2mirz * z);
-    const float Qta = g1 * M - g2 * Q2 + g3 * Q2mir;
-    fp -= g0 * M - g1 * Q2 + g2 * Q2mir;
-    fx += g2 * Q2mirx - x * Qta;
-    fy += g2 * Q2miry - y * Qta;
-    fz += g2 * Q2mirz - z * Qta;
+    float u0, u1;
+    up2(fp2, u0, u1);
+    fp += u0 + u1;
+    up2(fx2, u0, u1);
+    fx += u0 + u1;
+    up2(fy2, u0, u1);
+    fy += u0 + u1;
+    up2(fz2, u0, u1);
+    fz += u0 + u1;
   }
   /* k-space: phase = 2 pi (h . d) / L, reduced to one turn */
   const float invL = 1.0f / L;

@@ -36,6 +36,7 @@
 #include <utility>
 
 #include "chg_internal.h"
+#include "f32x2.cuh"
 
 namespace chg {
 namespace {
@@ -1247,36 +1248,7 @@ __global__ void __launch_bounds__(kThreads, MINB) list_kernel_tp(const ListArgs 
 /* compiler overlaps consecutive pairs.                                */
 /* ------------------------------------------------------------------ */
 
-typedef unsigned long long f2;
-
-__device__ __forceinline__ f2 pk2(float a, float b) {
-  f2 r;
-  asm("mov.b64 %0, {%1, %2};" : "=l"(r) : "f"(a), "f"(b));
-  return r;
-}
-__device__ __forceinline__ void up2(f2 v, float& a, float& b) {
-  asm("mov.b64 {%0, %1}, %2;" : "=f"(a), "=f"(b) : "l"(v));
-}
-__device__ __forceinline__ f2 add2(f2 a, f2 b) {
-  f2 r;
-  asm("add.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(a), "l"(b));
-  return r;
-}
-__device__ __forceinline__ f2 sub2(f2 a, f2 b) {
-  f2 r;
-  asm("sub.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(a), "l"(b));
-  return r;
-}
-__device__ __forceinline__ f2 mul2(f2 a, f2 b) {
-  f2 r;
-  asm("mul.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(a), "l"(b));
-  return r;
-}
-__device__ __forceinline__ f2 fma2(f2 a, f2 b, f2 c) {
-  f2 r;
-  asm("fma.rn.f32x2 %0, %1, %2, %3;" : "=l"(r) : "l"(a), "l"(b), "l"(c));
-  return r;
-}
+/* f2, pk2/up2 and the packed add2/sub2/mul2/fma2: f32x2.cuh */
 
 /* float index of field f of pair half h inside a pair block */
 __device__ __forceinline__ int pair_slot(int f, int h) { return 4 * (f >> 1) + 2 * (f & 1) + h; }
