@@ -232,6 +232,8 @@ CUDA_SIGNATURES = {
                          C.POINTER(ChangaWalkLists), _VP]),
     "changa_walk_lists_free": (None, [C.POINTER(ChangaWalkLists)]),
     "changa_walk_set_pool_factor": (None, [_D]),
+    "changa_walk_set_test_small_stack": (None, [C.c_int]),
+    "changa_walk_stack_reruns": (C.c_longlong, []),
     "changa_gravity_step_hexa": (_I, [_I, _VP, _LL, _VP, _LL, C.POINTER(ChangaListRequest),
                                       C.POINTER(ChangaListRequest),
                                       C.POINTER(ChangaListRequest), _D,

@@ -46,7 +46,8 @@ namespace chg {
 namespace {
 
 constexpr int kWalkWarps = 4;      // warps (buckets) per block
-constexpr int kWarpStack = 1024;   // stack entries per warp
+constexpr int kWarpStack = 512;    // stack entries per warp (the deepest seen: 211)
+constexpr int kWarpStackLarge = 1024;  // the re-run after a warp exhausted kWarpStack
 constexpr int kChunk = 256;        // entries per pool chunk of the append pass
 constexpr int kMaxChunks = 128;    // chunks per bucket and list in the append pass
 enum { kCount = 0, kFill = 1, kAppend = 2 };
@@ -291,10 +292,10 @@ __device__ __forceinline__ void append_at(const WalkArgs& a, int k, const int* t
   if (c >= 0) a.pool[k][(size_t)c * kChunk + (q - r * kChunk)] = e;
 }
 
-template <int MODE>
+template <int MODE, int STACK>
 __global__ void __launch_bounds__(kWalkWarps * 32) walk_kernel(const WalkArgs a) {
   constexpr bool FILL = MODE == kFill;
-  __shared__ int2 stk[kWalkWarps][kWarpStack];
+  __shared__ int2 stk[kWalkWarps][STACK];
   __shared__ int chain[kWalkWarps][64];
   __shared__ int ctab[MODE == kAppend ? kWalkWarps : 1][3][MODE == kAppend ? kMaxChunks : 1];
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -379,7 +380,7 @@ __global__ void __launch_bounds__(kWalkWarps * 32) walk_kernel(const WalkArgs a)
     const int npush = kind == 3 ? (c0 >= 0) + (c1 >= 0) : (kind == 4 ? 1 : 0);
     int tpush;
     int pos = sp + warp_excl_scan(npush, tpush);
-    if (sp + tpush > kWarpStack) {  // uniform: every lane sees tpush
+    if (sp + tpush > STACK) {  // uniform: every lane sees tpush
       if (lane == 0) atomicExch(a.error, 2);
       break;
     }
@@ -590,13 +591,40 @@ static int walk_setup(const ChangaTreeView* t, const ChangaWalkParams* p, WalkAr
   return 0;
 }
 
+/* Testing only: the first traversal with a 64-entry stack, so that the
+ * re-run with the large stack is taken. */
+static std::atomic<int> g_test_small_stack{0};
+static std::atomic<long long> g_stack_reruns{0};  // launches re-run with the large stack
+
+template <int STACK>
+static void walk_launch_mode(const WalkArgs& a, int mode, int grid, cudaStream_t s) {
+  if (mode == kFill) walk_kernel<kFill, STACK><<<grid, kWalkWarps * 32, 0, s>>>(a);
+  else if (mode == kAppend) walk_kernel<kAppend, STACK><<<grid, kWalkWarps * 32, 0, s>>>(a);
+  else walk_kernel<kCount, STACK><<<grid, kWalkWarps * 32, 0, s>>>(a);
+  count_launch();
+}
+
+/* One traversal.  The per-warp stack of kWarpStack entries keeps the
+ * blocks' shared memory small enough for register-bound residency; a warp
+ * that would exhaust it sets error 2 and stops, and the whole launch then
+ * runs once more with kWarpStackLarge entries (every output of a launch is
+ * rewritten by the re-run: per-bucket counts and entries, and in append
+ * mode the pools, whose counters are reset first). */
 static void walk_run(const WalkArgs& a, int mode, cudaStream_t s) {
   const long long warps = ((long long)a.n_buckets + a.bucket_stride - 1) / a.bucket_stride;
   const int grid = (int)((warps + kWalkWarps - 1) / kWalkWarps);
-  if (mode == kFill) walk_kernel<kFill><<<grid, kWalkWarps * 32, 0, s>>>(a);
-  else if (mode == kAppend) walk_kernel<kAppend><<<grid, kWalkWarps * 32, 0, s>>>(a);
-  else walk_kernel<kCount><<<grid, kWalkWarps * 32, 0, s>>>(a);
-  count_launch();
+  if (g_test_small_stack.load()) walk_launch_mode<64>(a, mode, grid, s);
+  else walk_launch_mode<kWarpStack>(a, mode, grid, s);
+  int h = 0;
+  if (cudaMemcpyAsync(&h, a.error, sizeof(int), cudaMemcpyDeviceToHost, s) != cudaSuccess ||
+      cudaStreamSynchronize(s) != cudaSuccess || h != 2)
+    return;  // launch errors surface at the caller's next check
+  if (cudaMemsetAsync(a.error, 0, sizeof(int), s) != cudaSuccess) return;
+  if (mode == kAppend && a.pool_next &&
+      cudaMemsetAsync(a.pool_next, 0, 64, s) != cudaSuccess)  // pool counters, overflow flag
+    return;
+  walk_launch_mode<kWarpStackLarge>(a, mode, grid, s);
+  g_stack_reruns.fetch_add(1);
 }
 
 static int walk_error(int h_err) {
@@ -658,6 +686,10 @@ extern "C" int changa_walk_fill(const ChangaTreeView* tree, const ChangaWalkPara
 static std::atomic<double> g_pool_factor{1.2};
 
 extern "C" void changa_walk_set_pool_factor(double f) { g_pool_factor.store(f > 0 ? f : 0.0); }
+
+extern "C" void changa_walk_set_test_small_stack(int on) { g_test_small_stack.store(on ? 1 : 0); }
+
+extern "C" long long changa_walk_stack_reruns(void) { return g_stack_reruns.load(); }
 
 static void release_lists(ChangaWalkLists* out) {
   for (int k = 0; k < 3; ++k) {

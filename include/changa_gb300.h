@@ -329,6 +329,12 @@ void changa_walk_lists_free(ChangaWalkLists *out);
  * entries (default 1.2; 0 leaves one chunk per bucket and list, so lists
  * longer than one chunk end in the fill pass). */
 void changa_walk_set_pool_factor(double factor);
+/* Testing only: with on != 0, each traversal first runs with a 64-entry
+ * stack per warp, so that the re-run with the large stack (taken when a
+ * warp exhausts its stack) is exercised. */
+void changa_walk_set_test_small_stack(int on);
+/* Traversal launches re-run with the large stack so far (in this process). */
+long long changa_walk_stack_reruns(void);
 
 /* Tree build on the device (no reference counterpart; restates the host
  * build, TreePiece.cpp:141-165 box and keys, GenericTreeNode.h:473-599

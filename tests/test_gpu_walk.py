@@ -94,6 +94,34 @@ def test_walk_single_traversal_path(cuda_ok):
     assert same_entries(L.cells, one[0], nb) and same_entries(L.plist, one[1], nb)
 
 
+def test_walk_stack_rerun(cuda_ok):
+    """A warp that exhausts its traversal stack makes the launch run once
+    more with the large stack: with the first traversal forced onto a
+    64-entry stack, the single traversal (append, periodic lattice) and the
+    count + fill passes (Plummer) give the host walk's entries."""
+    from changa_gb300 import _native as N
+    lib = N.cuda_lib()
+    p = ics.plummer(65536, ics.rng_for(6), soft=0.01)
+    Lp = tree.build_lists(p["pos"], p["mass"], p["soft"], n_bucket=2, theta=0.7)
+    g = ics.lattice_grf(16, ics.rng_for(7))
+    Lg = tree.build_lists(g["pos"], g["mass"], g["soft"], n_bucket=8, theta=0.7, period=1.0)
+    ref_p = gpu_walk(Lp)
+    ref_g = gpu_walk(Lg, method="two_pass")
+    before = lib.changa_walk_stack_reruns()
+    lib.changa_walk_set_test_small_stack(1)
+    try:
+        one = gpu_walk(Lp)
+        two = gpu_walk(Lg, method="two_pass")
+    finally:
+        lib.changa_walk_set_test_small_stack(0)
+    assert lib.changa_walk_stack_reruns() > before
+    for k in range(2):
+        assert _identical(one[k], ref_p[k]) and _identical(two[k], ref_g[k])
+    nbp, nbg = len(Lp.bucket_starts), len(Lg.bucket_starts)
+    assert same_entries(Lp.cells, one[0], nbp) and same_entries(Lp.plist, one[1], nbp)
+    assert same_entries(Lg.cells, two[0], nbg) and same_entries(Lg.plist, two[1], nbg)
+
+
 def test_device_lists_outlive_their_call(cuda_ok):
     """Tree arrays and lists come back as torch views of library memory;
     each view keeps its owner alive.  Five trees built one after another
