@@ -1428,6 +1428,9 @@ __global__ void __launch_bounds__(kThreads, MINB) list_kernel_tp2(const ListArgs
       const float tms = CELL ? -tmass : tmass;  // pc_pair takes the target mass negated
       const f2 tx2 = pk2(tx, tx), ty2 = pk2(ty, ty), tz2 = pk2(tz, tz), tm2 = pk2(tms, tms);
 
+      /* running sums (Kahan pairs in the mixed form) and dtGrav's running
+       * maximum, kept negated (a running minimum) for cells as pc_pair
+       * keeps it */
       float sx = 0.f, sy = 0.f, sz = 0.f, sp = 0.f, idt2 = 0.f;
       float cx = 0.f, cy = 0.f, cz = 0.f, cp = 0.f;
 
