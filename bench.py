@@ -197,6 +197,48 @@ def ewald_terms_per_particle(parts, root, ew, sample=4096):
     return terms / len(idx)
 
 
+def measure_dropin(lists, ew, interactions, steps):
+    """End to end through the reference-facing boundary (HostCUDA.h /
+    EwaldCUDA.h) with pinned FP32 ABI host buffers, as ChaNGa calls it:
+    DataManagerTransferLocalTree, the cell and particle list transfers,
+    EwaldHost and TransferParticleVarsBack, synchronised per step (wall
+    clock, after one untimed step).  A failure is reported, not raised."""
+    import time
+    from changa_gb300 import _native as N
+    from changa_gb300 import gravity
+    lib = N.cuda_lib()
+    lib.changa_gb300_set_error_mode(N.CHANGA_ERRORS_RECORD)  # an error is reported, not abort()
+    inp = None
+
+    def step():
+        gravity.dropin_step(inp)
+        code = lib.changa_gb300_last_error()
+        if code:
+            raise RuntimeError("drop-in step: error %d" % code)
+    try:
+        lib.changa_gb300_last_error()  # clear
+        inp = gravity.DropInInputs(lists, ew)
+        step()
+        tt = []
+        for _ in range(max(1, steps)):
+            t1 = time.perf_counter()
+            step()
+            tt.append(time.perf_counter() - t1)
+        t = sum(tt) / len(tt)
+        return {"value": interactions / t, "unit": "interactions/s", "ms_per_step": 1e3 * t,
+                "h2d_bytes_per_step": int(inp.h2d_bytes), "d2h_bytes_per_step": int(inp.d2h_bytes),
+                "form": "FP32 (the reference's arithmetic on its ABI structs)",
+                "api": "DataManagerTransferLocalTree, TreePieceCellListDataTransferLocal, "
+                       "TreePiecePartListDataTransferLocal, EwaldHost, TransferParticleVarsBack; "
+                       "one request per list"}
+    except Exception as e:  # noqa: BLE001 - reported in the JSON line
+        return {"error": "%s: %s" % (type(e).__name__, e)}
+    finally:
+        if inp is not None:
+            inp.free()
+        lib.changa_gb300_set_error_mode(N.CHANGA_ERRORS_ABORT)
+
+
 def run_cpu(lists, ewald, target, kind_pref="auto", reps=1):
     """Times the CPU oracle on a bounded sample; returns dict."""
     import numpy as np
@@ -670,6 +712,10 @@ def main_ours(args):
         for a in list(pin.values()) + [out]:
             a.free()
 
+    dropin = None
+    if args.e2e_steps > 0 and getattr(lists, "order", 2) == 2 and not batched_workload(wl):
+        dropin = measure_dropin(lists, ew, I, args.e2e_steps)
+
     # roofline of the dominant kernel (FP32-mixed cell lists) and the P-P kernel.
     # The bound is the FP32 FMA pipe (no tensor-core or HBM bound applies:
     # DRAM traffic is under 5% of peak); traffic comes from the committed ncu
@@ -744,6 +790,7 @@ def main_ours(args):
                               host_walk_s=t_walk, gpu_walk_s=walk_gpu and walk_gpu.get("walk_s"),
                               device_pipeline=device_pipeline, hexadecapole=hexa,
                               fp64_form=fp64, kernels=kshare, ewald=ewald_info,
+                              dropin_e2e=dropin,
                               batched_graph=batched, sequential_plain=seq,
                               autotune=tuning,
                               parallelism="replicas x%d" % world),
