@@ -199,6 +199,8 @@ CUDA_SIGNATURES = {
     "changa_gb300_get_list_variant": (_I, [_I]),
     "changa_gb300_set_hex_variant": (_I, [_I]),
     "changa_gb300_get_hex_variant": (_I, []),
+    "changa_gb300_device_status": (_I, []),
+    "changa_gb300_set_test_wait_limit": (None, [_I]),
     "changa_gb300_kernel_time": (_I, [_I, C.POINTER(C.c_double), C.POINTER(C.c_longlong)]),
     "changa_cell_forces_fp64": (_I, [_VP, _LL, _VP, _LL, C.POINTER(ChangaListRequest), _D, _VP, _VP]),
     "changa_part_forces_fp64": (_I, [_VP, _LL, _VP, _LL, C.POINTER(ChangaListRequest), _D, _VP, _VP]),

@@ -52,6 +52,13 @@ int set_list_variant(int kernel, int variant);
 int get_list_variant(int kernel);
 int set_hex_variant(int v);
 int get_hex_variant();
+/* poll limit of the TMA variants' mbarrier waits (negative: the default) */
+void set_tma_wait_polls(int polls);
+/* TMA-variant launches since load */
+unsigned long long tma_launches();
+/* Synchronises the current device, then returns (in bits) and clears the
+ * library's device status word (bit 0: a TMA wait ran out). */
+cudaError_t read_device_status(unsigned* bits);
 cudaError_t launch_pack_cells(const double* moments, long long n, float4* out, cudaStream_t s);
 cudaError_t launch_pack_parts(const double* parts, long long n, float4* out, cudaStream_t s);
 cudaError_t launch_zero_vars_f32(VariablePartData* v, long long n, cudaStream_t s);

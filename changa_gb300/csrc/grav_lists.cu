@@ -32,6 +32,8 @@
  *         are folded into Kahan-compensated per-particle totals.
  */
 #include <cuda.h>
+
+#include <atomic>
 #include <type_traits>
 #include <utility>
 
@@ -1655,15 +1657,22 @@ __global__ void __launch_bounds__(kThreads, MINB) list_kernel_tp2(const ListArgs
 /* arithmetic is list_kernel_tp2's (pc_pair).                           */
 /* ------------------------------------------------------------------ */
 
-__device__ int g_tma_timeouts = 0;  // mbarrier waits that gave up (results then invalid)
+/* Device status word of this library (one per device): kStatusTmaWait is
+ * set when a TMA-staged list kernel gave up waiting for its copies, so its
+ * forces are incomplete.  read_device_status() returns and clears it. */
+__device__ unsigned int g_device_status = 0;
+constexpr unsigned kStatusTmaWait = 1u;
+/* polls of the wait that drains a copy still in flight after a timeout: it
+ * must outlast any copy, so it never takes the test limit */
+constexpr int kDrainPolls = 1 << 26;
 
 __device__ __forceinline__ unsigned smem_u32(const void* p) {
   return (unsigned)__cvta_generic_to_shared(p);
 }
 
-/* Waits for phase `parity` of the mbarrier, at most 2^22 polls. */
-__device__ __forceinline__ bool mbar_wait(unsigned bar, unsigned parity) {
-  for (int it = 0; it < (1 << 22); ++it) {
+/* Waits for phase `parity` of the mbarrier, at most `polls` polls. */
+__device__ __forceinline__ bool mbar_wait(unsigned bar, unsigned parity, int polls) {
+  for (int it = 0; it < polls; ++it) {
     unsigned done;
     asm volatile(
         "{ .reg .pred p; mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2; "
@@ -1699,7 +1708,8 @@ __device__ __forceinline__ void tma_issue_block(const CUtensorMap* tmap, unsigne
 
 template <int MINB>
 __global__ void __launch_bounds__(kThreads, MINB) list_kernel_tma(const ListArgs a,
-                                                                  const __grid_constant__ CUtensorMap tmap) {
+                                                                  const __grid_constant__ CUtensorMap tmap,
+                                                                  const int wait_polls) {
   constexpr int PW = 6;  // float4 words per staged pair
   __shared__ __align__(1024) float4 raw[kWarps][32 * kCellPackF4];
   __shared__ __align__(16) float4 stage[kWarps][16 * PW];
@@ -1769,9 +1779,12 @@ __global__ void __launch_bounds__(kThreads, MINB) list_kernel_tma(const ListArgs
       }
       for (int e0 = e_begin; e0 < e_end; e0 += 32) {
         const int ne = min(32, e_end - e0);
-        if (!mbar_wait(bar, phase)) {
-          if (lane == 0) atomicAdd(&g_tma_timeouts, 1);
-          mbar_wait(bar, phase);  // once more (bounded) for the copy in flight
+        if (!mbar_wait(bar, phase, wait_polls)) {
+          if (lane == 0) atomicOr(&g_device_status, kStatusTmaWait);
+          /* the block's copy is still in flight into this warp's raw buffer:
+           * wait for it (long, bounded) before the warp stops and the CTA can
+           * end */
+          mbar_wait(bar, phase, kDrainPolls);
           ok = false;
           break;
         }
@@ -2260,19 +2273,20 @@ __global__ void cells_as_parts_kernel(const double* __restrict__ m, int stride, 
  * (the fastest on the measured workloads), the others on request or by the
  * autotuner. */
 template <typename K>
-int blocks_per_sm(K kernel, int* cache) {
-  if (!*cache) {
-    int nb = 0;
+int blocks_per_sm(K kernel, std::atomic<int>* cache) {
+  int nb = cache->load(std::memory_order_relaxed);
+  if (!nb) {
     if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, kernel, kThreads, 0) != cudaSuccess ||
         nb < 1)
       nb = 1;
-    *cache = nb;
+    cache->store(nb, std::memory_order_relaxed);
   }
-  return *cache;
+  return nb;
 }
 
 template <typename K>
-cudaError_t launch_kernel(K kernel, int* occ_cache, int kid, const ListArgs& a, cudaStream_t s) {
+cudaError_t launch_kernel(K kernel, std::atomic<int>* occ_cache, int kid, const ListArgs& a,
+                          cudaStream_t s) {
   if (a.n_buckets <= 0) return cudaSuccess;
   long long want = ((long long)a.n_buckets + kWarps - 1) / kWarps;
   long long cap = (long long)sm_count() * blocks_per_sm(kernel, occ_cache);
@@ -2283,8 +2297,16 @@ cudaError_t launch_kernel(K kernel, int* occ_cache, int kid, const ListArgs& a, 
   return cudaGetLastError();
 }
 
-/* current variant per list kernel id (FP32 forms) */
-int g_variant[6] = {8, 10, 0, 0, 8, 10};
+/* current variant per list kernel id (FP32 forms); several host threads
+ * may launch while another sets a variant, so each launch loads its id's
+ * variant once, atomically */
+std::atomic<int> g_variant[6] = {{8}, {10}, {0}, {0}, {8}, {10}};
+/* poll limit of the TMA variants' mbarrier waits (a test hook lowers it) */
+constexpr int kDefaultWaitPolls = 1 << 22;
+std::atomic<int> g_tma_wait_polls{kDefaultWaitPolls};
+/* TMA-variant launches since load: an entry that synchronises compares it
+ * before and after to know whether to read the device status word */
+std::atomic<unsigned long long> g_tma_launches{0};
 
 /* cuTensorMapEncodeTiled, resolved through the runtime (the library
  * loads on machines without a driver). */
@@ -2325,20 +2347,21 @@ static bool make_cell_tmap(const void* base, long long rows, CUtensorMap* tm) {
 
 template <int MINB>
 cudaError_t launch_tma(const ListArgs& a, const CUtensorMap& tm, cudaStream_t s) {
-  static int occ = 0;
+  static std::atomic<int> occ{0};
   if (a.n_buckets <= 0) return cudaSuccess;
   long long want = ((long long)a.n_buckets + kWarps - 1) / kWarps;
   long long cap = (long long)sm_count() * blocks_per_sm(list_kernel_tma<MINB>, &occ);
   int grid = (int)(want < cap ? want : cap);
   TimingScope ts(list_kernel_id(kMix, true), s);
-  list_kernel_tma<MINB><<<grid, kThreads, 0, s>>>(a, tm);
+  g_tma_launches.fetch_add(1);
+  list_kernel_tma<MINB><<<grid, kThreads, 0, s>>>(a, tm, g_tma_wait_polls.load());
   count_launch();
   return cudaGetLastError();
 }
 
 template <int FORM, bool CELL, int V>
 cudaError_t launch_variant(const ListArgs& a, cudaStream_t s) {
-  static int occ = 0;
+  static std::atomic<int> occ{0};
   constexpr Variant var = kVariants[V];
   if constexpr (var.tp == 3) {
     if constexpr (FORM == kMix && CELL) {
@@ -2378,13 +2401,13 @@ constexpr bool kHexDropIn = false;
 template <int FORM, bool CELL>
 cudaError_t launch_t(const ListArgs& a, cudaStream_t s) {
   if constexpr (FORM == kF64) {
-    static int occ = 0;
+    static std::atomic<int> occ{0};
     return launch_kernel(list_kernel<FORM, CELL>, &occ, list_kernel_id(FORM, CELL), a, s);
   } else if constexpr (kHexDropIn && FORM == kF32 && CELL) {
-    static int occ = 0;
+    static std::atomic<int> occ{0};
     return launch_kernel(list_kernel_hex2<kF32, 2>, &occ, list_kernel_id(kF32, true), a, s);
   } else {
-    return launch_src<FORM, CELL>(g_variant[list_kernel_id(FORM, CELL)], a, s,
+    return launch_src<FORM, CELL>(g_variant[list_kernel_id(FORM, CELL)].load(), a, s,
                                   std::make_integer_sequence<int, kNumVariants>{});
   }
 }
@@ -2397,13 +2420,31 @@ int set_list_variant(int kernel, int variant) {
   if (kernel < 0 || kernel >= 6 || kernel == kKidListF64Cell || kernel == kKidListF64Part)
     return -1;
   if (variant < 0 || variant >= kNumVariants) return -1;
-  g_variant[kernel] = variant;
+  g_variant[kernel].store(variant);
   return 0;
 }
 
 int get_list_variant(int kernel) {
   if (kernel < 0 || kernel >= 6) return -1;
-  return g_variant[kernel];
+  return g_variant[kernel].load();
+}
+
+void set_tma_wait_polls(int polls) { g_tma_wait_polls.store(polls >= 0 ? polls : kDefaultWaitPolls); }
+
+unsigned long long tma_launches() { return g_tma_launches.load(); }
+
+cudaError_t read_device_status(unsigned* bits) {
+  *bits = 0;
+  cudaError_t e = cudaDeviceSynchronize();
+  if (e != cudaSuccess) return e;
+  unsigned v = 0;
+  e = cudaMemcpyFromSymbol(&v, g_device_status, sizeof v);
+  if (e == cudaSuccess && v) {
+    const unsigned z = 0;
+    e = cudaMemcpyToSymbol(g_device_status, &z, sizeof z);
+  }
+  *bits = v;
+  return e;
 }
 
 cudaError_t launch_list(int form, bool cell, const ListArgs& a, cudaStream_t s) {
@@ -2433,24 +2474,25 @@ cudaError_t launch_pack_cells(const double* moments, long long n, float4* out, c
 /* hexadecapole FP32-mixed cell kernel: 0 synchronous staging
  * (list_kernel<kMix, true, true>), 1/2 paired (list_kernel_hex2, 1/2
  * resident blocks per SM) */
-int g_hex_variant = 2;
+std::atomic<int> g_hex_variant{2};
 
 cudaError_t launch_list_hex(int form, const ListArgs& a, cudaStream_t s) {
   if (form == kF64) {
-    static int occ = 0;
+    static std::atomic<int> occ{0};
     return launch_kernel(list_kernel<kF64, true, true>, &occ, list_kernel_id(kF64, true), a, s);
   }
   if (form == kMix) {
     const int kid = list_kernel_id(kMix, true);
-    if (g_hex_variant == 1) {
-      static int occ = 0;
+    const int hv = g_hex_variant.load();
+    if (hv == 1) {
+      static std::atomic<int> occ{0};
       return launch_kernel(list_kernel_hex2<kMix, 1>, &occ, kid, a, s);
     }
-    if (g_hex_variant == 2) {
-      static int occ = 0;
+    if (hv == 2) {
+      static std::atomic<int> occ{0};
       return launch_kernel(list_kernel_hex2<kMix, 2>, &occ, kid, a, s);
     }
-    static int occ = 0;
+    static std::atomic<int> occ{0};
     return launch_kernel(list_kernel<kMix, true, true>, &occ, kid, a, s);
   }
   return cudaErrorInvalidValue;
@@ -2458,11 +2500,11 @@ cudaError_t launch_list_hex(int form, const ListArgs& a, cudaStream_t s) {
 
 int set_hex_variant(int v) {
   if (v < 0 || v > 2) return -1;
-  g_hex_variant = v;
+  g_hex_variant.store(v);
   return 0;
 }
 
-int get_hex_variant() { return g_hex_variant; }
+int get_hex_variant() { return g_hex_variant.load(); }
 
 cudaError_t launch_pack_cells_hex(const double* moments, long long n, float4* out, cudaStream_t s) {
   if (n <= 0) return cudaSuccess;

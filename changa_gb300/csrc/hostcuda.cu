@@ -599,6 +599,7 @@ const char* changa_gb300_error_string(int code) {
     case CHANGA_E_INVALID_ARG: return "invalid argument";
     case CHANGA_E_INVALID_LIST: return "interaction list index or marker out of range";
     case CHANGA_E_TOO_LARGE: return "size beyond a fixed limit";
+    case CHANGA_E_DEVICE_WAIT: return "a kernel's bounded wait ran out (results incomplete)";
   }
   return cudaGetErrorString((cudaError_t)code);
 }
@@ -618,6 +619,14 @@ int changa_gb300_set_hex_variant(int variant) {
   return set_hex_variant(variant) ? CHANGA_E_INVALID_ARG : 0;
 }
 int changa_gb300_get_hex_variant(void) { return get_hex_variant(); }
+int changa_gb300_device_status(void) {
+  unsigned bits = 0;
+  cudaError_t e = read_device_status(&bits);
+  if (e != cudaSuccess) return record_error((int)e, "device_status", __FILE__, __LINE__);
+  if (bits) return record_error(CHANGA_E_DEVICE_WAIT, "device status", __FILE__, __LINE__);
+  return 0;
+}
+void changa_gb300_set_test_wait_limit(int polls) { set_tma_wait_polls(polls); }
 
 int changa_gb300_kernel_time(int kernel, double* total_ms, long long* launches) {
   if (kernel < 0 || kernel >= kKidCount || !total_ms || !launches) return CHANGA_E_INVALID_ARG;
@@ -973,6 +982,7 @@ int changa_gravity_step_host(int form, const double* moments, long long n_moment
   if (ewald && ewald->nEwhLoop > CHANGA_MAX_EWH)
     return record_error(CHANGA_E_TOO_LARGE, "gravity_step_host: nEwhLoop", __FILE__, __LINE__);
   prepare_pool();
+  const unsigned long long tma_before = tma_launches();
   const int f = form == CHANGA_FORM_FP64 ? kF64 : kMix;
   cudaStream_t c = copy_stream();
   if (!c) return record_error(cudaErrorUnknown, "gravity_step_host: copy stream", __FILE__, __LINE__);
@@ -1158,6 +1168,7 @@ int changa_gravity_step_host(int form, const double* moments, long long n_moment
   if (e == cudaSuccess) e = ef;
   if (e == cudaSuccess) e = es;
   if (e != cudaSuccess) return record_error((int)e, "gravity_step_host", __FILE__, __LINE__);
+  if (tma_launches() != tma_before) return changa_gb300_device_status();
   return 0;
 }
 

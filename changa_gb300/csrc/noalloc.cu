@@ -16,7 +16,9 @@
  * code cannot use the array's name as a device address, so the first call
  * on each device (made with that device current) looks the address up once
  * with cudaGetSymbolAddress and caches it.  Make that first call before any
- * stream capture begins.
+ * stream capture begins.  The cache is keyed by the context's id, which the
+ * driver never reuses within a process: after cudaDeviceReset the next call
+ * finds a new context and looks the address up again in it.
  *
  * All calls share the one array and it keeps the previous call's contents:
  * the work-queue counter is cleared on the call's stream before the kernel
@@ -24,6 +26,8 @@
  * whose work overlaps on the GPU (different streams without ordering) race
  * on the array and give wrong results; serialise them.
  */
+#include <cuda.h>
+
 #include <mutex>
 
 #include "chg_internal.h"
@@ -38,7 +42,42 @@ constexpr size_t kNoAllocScratchBytes = kQueueBytes + (16u << 20);
 __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocScratchBytes];
 
 std::mutex g_noalloc_mu;
-void* g_noalloc_ptr[64] = {nullptr};
+struct ScratchAddr {
+  void* ptr = nullptr;
+  unsigned long long ctx_id = 0;
+};
+ScratchAddr g_noalloc_addr[64];
+
+/* The current context's process-unique id (cuCtxGetCurrent + cuCtxGetId,
+ * resolved through the runtime so the library needs no -lcuda).  Returns
+ * false when the driver does not provide them. */
+typedef CUresult (*CtxGetCurrentFn)(CUcontext*);
+typedef CUresult (*CtxGetIdFn)(CUcontext, unsigned long long*);
+bool current_context_id(unsigned long long* id) {
+  static CtxGetCurrentFn get_current = nullptr;
+  static CtxGetIdFn get_id = nullptr;
+  static std::once_flag once;
+  std::call_once(once, [] {
+    void* f = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &f, 12000, cudaEnableDefault, &q) ==
+            cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      get_current = (CtxGetCurrentFn)f;
+    else
+      cudaGetLastError();
+    f = nullptr;
+    if (cudaGetDriverEntryPointByVersion("cuCtxGetId", &f, 12000, cudaEnableDefault, &q) ==
+            cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      get_id = (CtxGetIdFn)f;
+    else
+      cudaGetLastError();
+  });
+  CUcontext ctx = nullptr;
+  if (!get_current || !get_id || get_current(&ctx) != CUDA_SUCCESS || !ctx) return false;
+  return get_id(ctx, id) == CUDA_SUCCESS;
+}
 
 size_t round256(size_t x) { return (x + 255) & ~(size_t)255; }
 
@@ -55,9 +94,15 @@ extern "C" int changa_cell_forces_mixed_noalloc(const double* moments, long long
       (req->n_entries > 0 && !req->list))
     return record_error(CHANGA_E_INVALID_ARG, "cell_forces_mixed_noalloc: arguments", __FILE__,
                         __LINE__);
-  const size_t mom_bytes = round256((size_t)n_moments * kCellPackF4 * sizeof(float4));
-  const size_t tgt_bytes = round256((size_t)n_targets * kPartPackF4 * sizeof(float4));
-  if (mom_bytes + tgt_bytes > kNoAllocScratchBytes - kQueueBytes)
+  /* the counts are compared before any product is formed, so a huge count
+   * cannot wrap around into a small size */
+  constexpr size_t kRoom = kNoAllocScratchBytes - kQueueBytes;
+  constexpr size_t kMomRec = kCellPackF4 * sizeof(float4), kTgtRec = kPartPackF4 * sizeof(float4);
+  bool fits = (unsigned long long)n_moments <= kRoom / kMomRec &&
+              (unsigned long long)n_targets <= kRoom / kTgtRec;
+  const size_t mom_bytes = fits ? round256((size_t)n_moments * kMomRec) : 0;
+  const size_t tgt_bytes = fits ? round256((size_t)n_targets * kTgtRec) : 0;
+  if (!fits || mom_bytes + tgt_bytes > kRoom)
     return record_error(CHANGA_E_TOO_LARGE,
                         "cell_forces_mixed_noalloc: 64 B x moments + 32 B x targets exceeds the "
                         "16 MiB fixed scratch",
@@ -69,15 +114,19 @@ extern "C" int changa_cell_forces_mixed_noalloc(const double* moments, long long
   if (dev < 0 || dev >= 64)
     return record_error(CHANGA_E_INVALID_ARG, "cell_forces_mixed_noalloc: device id", __FILE__,
                         __LINE__);
+  unsigned long long ctx_id = 0;
+  const bool have_id = current_context_id(&ctx_id);
   void* base = nullptr;
   {
     std::lock_guard<std::mutex> lk(g_noalloc_mu);
-    if (!g_noalloc_ptr[dev]) {
+    ScratchAddr& c = g_noalloc_addr[dev];
+    if (!c.ptr || !have_id || c.ctx_id != ctx_id) {
       void* p = nullptr;
       CHG_CUDA(cudaGetSymbolAddress(&p, g_noalloc_scratch));
-      g_noalloc_ptr[dev] = p;
+      c.ptr = p;
+      c.ctx_id = have_id ? ctx_id : 0;
     }
-    base = g_noalloc_ptr[dev];
+    base = c.ptr;
   }
   char* scratch = static_cast<char*>(base);
   unsigned int* queue = reinterpret_cast<unsigned int*>(scratch);

@@ -331,6 +331,10 @@ __global__ void __launch_bounds__(kWalkWarps * 32) walk_kernel(const WalkArgs a)
   }
   /* the root of every replica on the check list */
   const int nr = a.n_replicas, side = 2 * nr + 1, nrep = side * side * side;
+  if (nrep > STACK) {  // uniform; the host re-runs the launch with the larger stack
+    if (lane == 0) atomicExch(a.error, 2);
+    return;
+  }
   for (int r = lane; r < nrep; r += 32) {
     const int x = r / (side * side) - nr, y = (r / side) % side - nr, z = r % side - nr;
     stk[warp][r] = make_int2(0, (x + 3) | ((y + 3) << 3) | ((z + 3) << 6));

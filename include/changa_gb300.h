@@ -36,6 +36,7 @@ extern "C" {
 #define CHANGA_E_INVALID_ARG 1001   /* bad pointer / size / count */
 #define CHANGA_E_INVALID_LIST 1002  /* list index or marker out of range */
 #define CHANGA_E_TOO_LARGE 1003     /* size beyond a fixed limit */
+#define CHANGA_E_DEVICE_WAIT 1004   /* a kernel's bounded wait ran out; its results are incomplete */
 
 #define CHANGA_ERRORS_ABORT 0   /* print and abort() (reference behaviour) */
 #define CHANGA_ERRORS_RECORD 1  /* record; read with changa_gb300_last_error */
@@ -92,6 +93,20 @@ int changa_gb300_get_list_variant(int kernel);
 int changa_gb300_set_hex_variant(int variant);
 int changa_gb300_get_hex_variant(void);
 
+/* The TMA-staged variants (11-12) wait for their copies with an iteration
+ * limit.  A wait that runs out marks the device's status word and ends that
+ * warp's work, so some buckets' forces are incomplete.  This call waits for
+ * the current device, then reads and clears the word: it returns 0, or
+ * CHANGA_E_DEVICE_WAIT (recorded like any other error) when a wait ran out
+ * since the last read.  changa_gravity_step_host reads the word itself when
+ * it launched a TMA variant.  Kernels that finish while this call reads
+ * are seen by the next call. */
+int changa_gb300_device_status(void);
+/* Test hook: the poll limit of those waits (a negative value restores the
+ * default, 2^22).  0 makes every wait run out at once, on purpose; the copy
+ * in flight is still waited for (with a long limit) before the warp stops. */
+void changa_gb300_set_test_wait_limit(int polls);
+
 /* ---- device-resident list requests for the extension forms ---- */
 
 typedef struct ChangaListRequest {
@@ -134,7 +149,9 @@ int changa_part_forces_mixed(const double *sources, long long n_sources,
  * 64 B x n_moments + 32 B x n_targets must fit in 16 MiB (each rounded up to
  * 256 B), else CHANGA_E_TOO_LARGE and nothing is enqueued.  The first call
  * on a device looks up the array's device address: make it before any
- * stream capture.  Calls share the array: two calls that overlap on the GPU
+ * stream capture.  The address is cached per device and context id, so the
+ * first call after a cudaDeviceReset looks it up again (make that call
+ * before any capture too).  Calls share the array: two calls that overlap on the GPU
  * race; order them on one stream.  Inputs and outputs as for
  * changa_cell_forces_mixed (device pointers). */
 int changa_cell_forces_mixed_noalloc(const double *moments, long long n_moments,

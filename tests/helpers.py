@@ -41,3 +41,14 @@ def force_rms_err(a, ref):
 def pot_rms_err(a, ref):
     """|dpot| / rms(pot); the periodic potential's zero point is arbitrary."""
     return np.abs(a[:, 3] - ref[:, 3]) / np.sqrt((ref[:, 3] ** 2).mean())
+
+
+def reference_root():
+    """The reference checkout for tests that read its data files:
+    CHANGA_REFERENCE, else a checkout named "reference" beside this
+    repository; None when neither exists (those tests then skip)."""
+    root = os.environ.get("CHANGA_REFERENCE")
+    if not root:
+        here = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+        root = os.path.join(os.path.dirname(here), "reference")
+    return root if os.path.isdir(root) else None

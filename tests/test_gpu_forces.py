@@ -446,3 +446,41 @@ def test_dropin_concurrent_streams(plummer, lattice):
     assert not errors, errors
     for i in range(len(cases)):
         assert np.array_equal(out[i], serial[i]), i
+
+
+def test_tma_wait_timeout_reports_error(plummer):
+    """The TMA-staged cell variant waits for its copies with an iteration
+    limit.  With the limit at 0 polls every wait runs out at once: each warp
+    still drains its copy in flight (long limit) and stops, the kernel
+    returns, and the device status reads CHANGA_E_DEVICE_WAIT once (then it
+    is cleared).  The GPU stays usable: the next evaluation with the default
+    limit matches the oracle and leaves the status clear.  The same holds
+    through changa_gravity_step_host, which reads the status itself."""
+    L, ref, _ = plummer
+    lib = N.cuda_lib()
+    k = N.KERNEL_IDS["list_mixed_cell"]
+    saved = lib.changa_gb300_get_list_variant(k)
+    assert lib.changa_gb300_device_status() == 0
+    lib.changa_gb300_last_error()
+    try:
+        assert lib.changa_gb300_set_list_variant(k, 11) == 0
+        lib.changa_gb300_set_test_wait_limit(0)
+        ds = gravity.DeviceSystem(L)
+        ds.step("mixed")
+        assert lib.changa_gb300_device_status() == 1004
+        assert lib.changa_gb300_last_error() == 1004
+        assert lib.changa_gb300_device_status() == 0
+        # through the host-array entry, which checks the word after its sync
+        with pytest.raises(RuntimeError, match="1004"):
+            gravity.gravity_step_host(L, "mixed")
+        assert lib.changa_gb300_last_error() == 1004
+        assert lib.changa_gb300_device_status() == 0
+        lib.changa_gb300_set_test_wait_limit(-1)
+        v = gravity.DeviceSystem(L).step("mixed").cpu().numpy()
+        assert lib.changa_gb300_device_status() == 0
+        e = force_rel_err(v, ref)
+        assert np.median(e) < MIX_MEDIAN_TOL and np.percentile(e, 99) < MIX_P99_TOL
+    finally:
+        lib.changa_gb300_set_test_wait_limit(-1)
+        lib.changa_gb300_set_list_variant(k, saved)
+        lib.changa_gb300_last_error()

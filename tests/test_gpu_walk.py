@@ -105,21 +105,34 @@ def test_walk_stack_rerun(cuda_ok):
     Lp = tree.build_lists(p["pos"], p["mass"], p["soft"], n_bucket=2, theta=0.7)
     g = ics.lattice_grf(16, ics.rng_for(7))
     Lg = tree.build_lists(g["pos"], g["mass"], g["soft"], n_bucket=8, theta=0.7, period=1.0)
+    # two replica shells: 125 replica roots start on the stack, more than the
+    # 64-entry first stack holds, so every warp hands over to the re-run
+    h = ics.lattice_grf(8, ics.rng_for(8))
+    Lh = tree.build_lists(h["pos"], h["mass"], h["soft"], n_bucket=8, theta=0.7, period=1.0,
+                          n_replicas=2)
     ref_p = gpu_walk(Lp)
     ref_g = gpu_walk(Lg, method="two_pass")
+    ref_h = [gpu_walk(Lh, method=m) for m in ("two_pass", "single")]
     before = lib.changa_walk_stack_reruns()
     lib.changa_walk_set_test_small_stack(1)
     try:
         one = gpu_walk(Lp)
         two = gpu_walk(Lg, method="two_pass")
+        before_h = lib.changa_walk_stack_reruns()
+        three = [gpu_walk(Lh, method=m) for m in ("two_pass", "single")]
+        assert lib.changa_walk_stack_reruns() >= before_h + 2
     finally:
         lib.changa_walk_set_test_small_stack(0)
     assert lib.changa_walk_stack_reruns() > before
     for k in range(2):
         assert _identical(one[k], ref_p[k]) and _identical(two[k], ref_g[k])
-    nbp, nbg = len(Lp.bucket_starts), len(Lg.bucket_starts)
+        for t3, r3 in zip(three, ref_h):
+            assert _identical(t3[k], r3[k])
+    nbp, nbg, nbh = len(Lp.bucket_starts), len(Lg.bucket_starts), len(Lh.bucket_starts)
     assert same_entries(Lp.cells, one[0], nbp) and same_entries(Lp.plist, one[1], nbp)
     assert same_entries(Lg.cells, two[0], nbg) and same_entries(Lg.plist, two[1], nbg)
+    for t3 in three:
+        assert same_entries(Lh.cells, t3[0], nbh) and same_entries(Lh.plist, t3[1], nbh)
 
 
 def test_device_lists_outlive_their_call(cuda_ok):

@@ -11,8 +11,10 @@ import numpy as np
 import pytest
 
 from changa_gb300 import tipsy
+from helpers import reference_root
 
-KING = "/root/reference/teststep/king_soft.bin"
+_REF = reference_root()
+KING = os.path.join(_REF, "teststep", "king_soft.bin") if _REF else ""
 
 
 def test_roundtrip(tmp_path):
@@ -28,7 +30,8 @@ def test_roundtrip(tmp_path):
     np.testing.assert_allclose(d["soft"], np.float32(0.01))
 
 
-@pytest.mark.skipif(not os.path.exists(KING), reason="reference test data not present")
+@pytest.mark.skipif(not KING or not os.path.exists(KING),
+                    reason="reference test data not present (set CHANGA_REFERENCE)")
 def test_king_model_energies(built):
     import oracle
     from changa_gb300 import tree

@@ -6,7 +6,8 @@ thread that must not wait on cudaMalloc/cudaFree synchronising the device).
 
 Checked through the C-ABI against the allocating entry point,
 changa_cell_forces_mixed, on two calls in a row (the second call finds the
-first one's contents in the shared array and must not depend on them).
+first one's contents in the shared array and must not depend on them), and
+against the CPU oracle's nodeBucketForce on the same cell lists.
 This file sorts last so that a run stopping at its first failure has
 already run every other test."""
 import ctypes as C
@@ -14,12 +15,15 @@ import ctypes as C
 import numpy as np
 import pytest
 
+import oracle
 from changa_gb300 import _native as N
 from changa_gb300 import gravity, ics, tree
 
 pytestmark = pytest.mark.gpu
 
 TOL = 1e-6  # the FP64-form bar; both entries run the same kernels
+# FP32-mixed arithmetic against the FP64 oracle (relative force error)
+ORACLE_MEDIAN, ORACLE_MAX = 1e-6, 1e-4
 
 
 def _call(fn, ds, vars):
@@ -46,11 +50,14 @@ def test_noalloc_matches_allocating_entry(cuda_ok):
     ds = gravity.DeviceSystem(L)
     vars = torch.zeros((L.n, 5), dtype=torch.float64, device="cuda")
     ref = _call(lib.changa_cell_forces_mixed, ds, vars)
+    orc = oracle.cell_forces(L.moments, L.parts, L.cells, fperiod=L.period)
     for _ in range(2):
         out = _call(lib.changa_cell_forces_mixed_noalloc, ds, vars)
         assert _rel(out, ref).max() < TOL
         np.testing.assert_allclose(out[:, 3], ref[:, 3], rtol=TOL)
         np.testing.assert_allclose(out[:, 4], ref[:, 4], rtol=TOL)
+        e = _rel(out, orc)
+        assert np.median(e) < ORACLE_MEDIAN and e.max() < ORACLE_MAX, (np.median(e), e.max())
 
 
 def test_noalloc_rejects_oversize(cuda_ok):
@@ -67,6 +74,11 @@ def test_noalloc_rejects_oversize(cuda_ok):
         rc = lib.changa_cell_forces_mixed_noalloc(8, 300000, 8, 1, C.byref(req), 0.0, 8, None)
         assert rc == 1003
         assert lib.changa_gb300_last_error() == 1003
+        # counts whose byte sizes would wrap around 64 bits are refused too
+        for nm, nt in ((1 << 58, 1), (1, 1 << 59), (1 << 62, 1 << 62)):
+            rc = lib.changa_cell_forces_mixed_noalloc(8, nm, 8, nt, C.byref(req), 0.0, 8, None)
+            assert rc == 1003, (nm, nt, rc)
+            assert lib.changa_gb300_last_error() == 1003
         assert lib.changa_gb300_kernel_launches() == before
     finally:
         lib.changa_gb300_set_error_mode(N.CHANGA_ERRORS_ABORT)
