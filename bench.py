@@ -69,6 +69,8 @@ def parse():
                     help="skip the direct-sum error of the sampled particles")
     ap.add_argument("--no-hexadecapole", dest="hexadecapole", action="store_false",
                     help="skip the hexadecapole-build measurement on the same particles")
+    ap.add_argument("--no-batched", dest="batched", action="store_false",
+                    help="skip the clusters512 batching-form measurement")
     ap.add_argument("--variants", default=None,
                     help="CELL,PART list-kernel shape variants to use instead of the autotuner")
     return ap.parse_args()
@@ -239,8 +241,11 @@ def measure_dropin(lists, ew, interactions, steps):
         lib.changa_gb300_set_error_mode(N.CHANGA_ERRORS_ABORT)
 
 
-def run_cpu(lists, ewald, target, kind_pref="auto", reps=1):
-    """Times the CPU oracle on a bounded sample; returns dict."""
+def run_cpu(lists, ewald, target, kind_pref="auto", reps=1, want_vars=False):
+    """Times the CPU oracle on a bounded sample; returns dict (and, with
+    want_vars, the oracle's vars and the rows whose result is complete: the
+    particles of the sampled buckets, which received their whole cell list,
+    particle list and Ewald term)."""
     import numpy as np
 
     import oracle
@@ -262,18 +267,92 @@ def run_cpu(lists, ewald, target, kind_pref="auto", reps=1):
                            bucket_ids=cid, kind=kind, nthreads=cores)
         oracle.part_forces(lists.parts, lists.parts, lists.plist, fperiod=lists.period, vars=v,
                            bucket_ids=pid, kind=kind, nthreads=cores)
+        ve = None
         if ewald is not None and len(rows):
-            oracle.ewald_forces(lists.parts, lists.root, ewald.L, ewald.n_reps, ewald.fEwCut,
-                                ewald.dEwhCut, idx=rows, kind=kind, nthreads=cores)
+            ve = oracle.ewald_forces(lists.parts, lists.root, ewald.L, ewald.n_reps, ewald.fEwCut,
+                                     ewald.dEwhCut, idx=rows, kind=kind, nthreads=cores)
         times.append(time.perf_counter() - t0)
+        if ve is not None:  # the Ewald rows (idx order) onto the sampled particles
+            v[rows, :4] += ve[:, :4]
     dt = min(times)
-    return {"value": tot / dt, "unit": "interactions/s", "cores": cores,
-            "kind": "reference" if kind == "ref" else "port",
-            "sample": "%d random buckets of the workload (%.3g interactions, cell+particle lists"
-                      "%s), FP64, OpenMP over buckets, best of %d" %
-                      (len(set(cid.tolist()) | set(pid.tolist())), tot,
-                       " + Ewald on their %d particles" % len(rows) if ewald else "", reps),
-            "seconds": dt}
+    out = {"value": tot / dt, "unit": "interactions/s", "cores": cores,
+           "kind": "reference" if kind == "ref" else "port",
+           "sample": "%d random buckets of the workload (%.3g interactions, cell+particle lists"
+                     "%s), FP64, OpenMP over buckets, best of %d" %
+                     (len(set(cid.tolist()) | set(pid.tolist())), tot,
+                      " + Ewald on their %d particles" % len(rows) if ewald else "", reps),
+           "seconds": dt}
+    if want_vars:
+        return out, v, rows
+    return out
+
+
+def rel_err(a, ref):
+    """Per-particle relative force error |a - ref| / |ref|."""
+    import numpy as np
+    return np.linalg.norm(a[:, :3] - ref[:, :3], axis=1) / np.linalg.norm(ref[:, :3], axis=1)
+
+
+def stats(e):
+    import numpy as np
+    return {"median": float(np.median(e)), "p99": float(np.percentile(e, 99)),
+            "max": float(np.max(e))}
+
+
+def parity_block(lists, v_oracle, rows, v64, v_mixed, kind):
+    """The GPU forms against the CPU oracle (ChaNGa's gravity.h/Ewald.cpp or
+    its C restatement) per particle, on the particles whose sampled buckets
+    the oracle evaluated completely (same lists, same inputs)."""
+    import numpy as np
+    ref = v_oracle[rows]
+    out = {"oracle": kind, "particles": int(len(rows)),
+           "fp64_vs_oracle": stats(rel_err(v64[rows], ref)),
+           "mixed_vs_oracle": stats(rel_err(v_mixed[rows], ref))}
+    pot = lambda v: np.abs(v[rows, 3] - ref[:, 3]) / np.abs(ref[:, 3])
+    out["fp64_pot_vs_oracle_max"] = float(pot(v64).max())
+    out["mixed_pot_vs_oracle_median"] = float(np.median(pot(v_mixed)))
+    out["fp64_vs_oracle_max"] = out["fp64_vs_oracle"]["max"]
+    out["bar"] = "FP64 form: 1e-6 relative per particle"
+    return out
+
+
+def accuracy_block(lists, samp, v_mixed, v64, dsum):
+    """Force error against the FP64 direct sum on the sampled particles:
+    relative per particle, normalised by the sample's rms force, and the
+    relative error binned by |a| and by local density (the particle's
+    bucket: targets / box volume), to show where the tail sits."""
+    import numpy as np
+    a_ref = np.linalg.norm(dsum[:, :3], axis=1)
+    rms = float(np.sqrt(np.mean(a_ref ** 2)))
+    out = {"particles": int(len(samp)), "rms_force": rms}
+    for name, v in (("mixed", v_mixed), ("fp64", v64)):
+        e = rel_err(v[samp], dsum)
+        out[name + "_rel"] = stats(e)
+        out[name + "_over_rms"] = stats(np.linalg.norm(v[samp, :3] - dsum[:, :3], axis=1) / rms)
+    e = rel_err(v_mixed[samp], dsum)
+    # |a| quartiles
+    q = np.quantile(a_ref, [0.25, 0.5, 0.75])
+    bins = np.digitize(a_ref, q)
+    out["mixed_rel_by_force_quartile"] = [
+        {"force_range": [float(a_ref[bins == k].min()), float(a_ref[bins == k].max())],
+         "median": float(np.median(e[bins == k])), "p99": float(np.percentile(e[bins == k], 99))}
+        for k in range(4)]
+    # local density: the particle's bucket (targets / bounding-box volume)
+    bstart = lists.bucket_starts.astype(np.int64)
+    b = np.searchsorted(bstart, samp, side="right") - 1
+    bb = lists.bucket_bbox[b]
+    ext = np.maximum(bb[:, 3:6] - bb[:, 0:3], 1e-9)
+    dens = lists.bucket_sizes[b] / np.prod(ext, axis=1)
+    qd = np.quantile(dens, [0.25, 0.5, 0.75])
+    bd = np.digitize(dens, qd)
+    out["mixed_rel_by_density_quartile"] = [
+        {"median": float(np.median(e[bd == k])), "p99": float(np.percentile(e[bd == k], 99))}
+        for k in range(4)]
+    worst = e >= np.percentile(e, 99)
+    out["worst_1pct"] = {"median_force_over_rms": float(np.median(a_ref[worst]) / rms),
+                         "share_below_tenth_median_force":
+                             float(np.mean(a_ref[worst] < 0.1 * np.median(a_ref)))}
+    return out
 
 
 def fp32_peak_tflops():
@@ -330,7 +409,9 @@ def main_reference(args):
            "n_gpus": world, "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms,
            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
            "data": "synthetic (seeded %s)" % wl.name,
-           "config": dict(wl.describe(), sample_interactions=vals[0]["sample"], wall_s=wall),
+           "config": dict(wl.describe(), l2="inputs larger than L2 and a 256 MB flush write "
+                                            "between timed steps"),
+           "workload_detail": {"sample": vals[0]["sample"], "wall_s": wall},
            "cpu_baseline": cb,
            "e2e": {"value": value, "unit": "interactions/s", "h2d_bytes_per_step": 0,
                    "d2h_bytes_per_step": 0}}
@@ -506,6 +587,153 @@ def batched_workload(wl):
     return hasattr(wl, "systems")
 
 
+def measure_batched(steps=5, seq_reps=2):
+    """The batching form on clusters512 (512 independent Plummer clusters,
+    N log-uniform in [1024, 65536]): one CUDA-graph replay of the
+    concatenated requests (one persistent launch per list kind, its work
+    queue balancing every cluster's buckets) against the 512 clusters
+    evaluated one after another as plain evaluations.  Same timing rules as
+    the headline: warm-up, a 256 MB flush between steps, CUDA events on the
+    stream.  The two results must agree (same lists, same kernels)."""
+    import numpy as np
+    import torch
+    from changa_gb300 import autotune, gravity, tree
+    from changa_gb300.workloads import WORKLOADS
+    wl = WORKLOADS["clusters512"]
+    t0 = time.perf_counter()
+    systems = wl.systems()
+    L = tree.concat_systems(systems)
+    host_s = time.perf_counter() - t0
+    I = L.interactions
+    stream = torch.cuda.current_stream()
+    flush = torch.empty(256 * 2 ** 20 // 4, dtype=torch.float32, device="cuda")
+    ds = gravity.DeviceSystem(L, device="cuda")
+    tuning = autotune.tune(ds, "mixed")
+    graph = gravity.GravityGraph(ds, "mixed")
+    for _ in range(3):
+        graph.launch()
+    torch.cuda.synchronize()
+    evs = []
+    for _ in range(steps):
+        flush.fill_(1.0)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        graph.launch()
+        e1.record(stream)
+        evs.append((e0, e1))
+    torch.cuda.synchronize()
+    ms = sum(a.elapsed_time(b) for a, b in evs) / steps
+    v_graph = ds.vars.cpu().numpy()
+    graph.close()
+    del ds
+    singles = [gravity.DeviceSystem(s, device="cuda") for s in systems]
+    for x in singles:
+        x.step("mixed")
+    torch.cuda.synchronize()
+    ms_seq = []
+    for _ in range(seq_reps):
+        flush.fill_(1.0)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for x in singles:
+            x.step("mixed")
+        e1.record(stream)
+        torch.cuda.synchronize()
+        ms_seq.append(e0.elapsed_time(e1))
+    v_seq = np.concatenate([x.vars.cpu().numpy() for x in singles], axis=0)
+    del singles
+    torch.cuda.empty_cache()
+    ms_s = sum(ms_seq) / len(ms_seq)
+    e = rel_err(v_graph, v_seq)
+    return {"workload": "clusters512", "clusters": len(systems), "n": int(L.n),
+            "n_range": [int(min(x.n for x in systems)), int(max(x.n for x in systems))],
+            "interactions": int(I), "form": "FP32-mixed",
+            "graph_ms_per_step": ms, "graph_interactions_per_s": I / (ms / 1e3),
+            "sequential_ms_per_step": ms_s, "sequential_interactions_per_s": I / (ms_s / 1e3),
+            "graph_over_sequential": ms_s / ms,
+            "graph_vs_sequential_max_rel_force_diff": float(e.max()),
+            "autotune": {k: v.get("variant") for k, v in tuning.items() if isinstance(v, dict)},
+            "host_tree_walk_s": host_s}
+
+
+def timed_steps(step, steps, stream, flush):
+    """CUDA-event time of each of `steps` calls of step(), a flush write
+    before each."""
+    import torch
+    evs = []
+    for _ in range(steps):
+        flush.fill_(1.0)
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        step()
+        e1.record(stream)
+        evs.append((e0, e1))
+    torch.cuda.synchronize()
+    return [a.elapsed_time(b) for a, b in evs]
+
+
+def measure_e2e(lists, ew, stream, steps, world):
+    """End to end through changa_gravity_step_host with pinned host buffers:
+    the upload of every input and the read-back of the result are inside
+    the timed region (wall clock per step, after one untimed step)."""
+    import ctypes as C
+
+    import numpy as np
+    from changa_gb300 import _native as N
+    from changa_gb300 import gravity
+    lib = N.cuda_lib()
+    pin = {k: gravity.PinnedArray(a) for k, a in (
+        ("moments", lists.moments), ("parts", lists.parts),
+        ("cl", lists.cells.list), ("cm", lists.cells.markers), ("cs", lists.cells.starts),
+        ("cz", lists.cells.sizes), ("pl", lists.plist.list), ("pm", lists.plist.markers),
+        ("ps", lists.plist.starts), ("pz", lists.plist.sizes))}
+    out = gravity.PinnedArray(np.zeros((lists.n, 5)))
+
+    def req(l, m, s, z, r):
+        q = N.ChangaListRequest()
+        q.list, q.markers, q.starts, q.sizes = pin[l].ptr, pin[m].ptr, pin[s].ptr, pin[z].ptr
+        q.n_buckets, q.n_entries = r.n_buckets, r.n_entries
+        return q
+    cq = req("cl", "cm", "cs", "cz", lists.cells)
+    pq = req("pl", "pm", "ps", "pz", lists.plist)
+    ep = ew.params(lists.root) if ew else None
+    sh = stream.cuda_stream
+
+    def one():
+        # overwrite: the result replaces out (no host zeroing, no vars upload)
+        rc = lib.changa_gravity_step_host(N.CHANGA_FORM_MIXED | N.CHANGA_STEP_OVERWRITE,
+                                          pin["moments"].ptr,
+                                          lists.moments.shape[0], pin["parts"].ptr, lists.n,
+                                          C.byref(cq), C.byref(pq), float(lists.period),
+                                          C.byref(ep) if ep else None, out.ptr, sh)
+        N.check(rc, "changa_gravity_step_host")
+    try:
+        one()
+        tt = []
+        for _ in range(steps):
+            t1 = time.perf_counter()
+            one()
+            tt.append(time.perf_counter() - t1)
+        result = out.array.copy() if hasattr(out, "array") else None
+    finally:
+        for a in list(pin.values()) + [out]:
+            a.free()
+    t_e2e = max_over_ranks(world, sum(tt) / len(tt))
+    h2d = (lists.moments.nbytes + lists.parts.nbytes + lists.cells.list.nbytes +
+           lists.cells.markers.nbytes + lists.cells.starts.nbytes + lists.cells.sizes.nbytes +
+           lists.plist.list.nbytes + lists.plist.markers.nbytes + lists.plist.starts.nbytes +
+           lists.plist.sizes.nbytes)
+    I = lists.interactions
+    return {"value": sum_over_ranks(world, float(I)) / t_e2e, "unit": "interactions/s",
+            "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(lists.parts.nbytes),
+            "ms_per_step": 1e3 * t_e2e,
+            "api": "changa_gravity_step_host (include/changa_gb300.h), pinned host "
+                   "buffers, CHANGA_STEP_OVERWRITE; lists uploaded in 512 MiB chunks (halving "
+                   "toward the end) on a copy stream overlapping the list kernels; each "
+                   "chunk's particles read back on a second copy stream once final"}, result
+
+
 def main_ours(args):
     import numpy as np
     import torch
@@ -519,26 +747,28 @@ def main_ours(args):
     world, rank, local = dist_setup(args)
     lib = N.cuda_lib()
     wl = WORKLOADS[args.workload]
-    pts = None if batched_workload(wl) else wl.particles()
+    batched = batched_workload(wl)
+    pts = None if batched else wl.particles()
     t0 = time.perf_counter()
-    lists = wl.lists(particles=pts)
+    lists = wl.lists(particles=pts) if not batched else wl.lists()
     t_walk = time.perf_counter() - t0
     ew = wl.ewald_config()
     I = lists.interactions
     walk_gpu = None
     device_pipeline = None
-    if not batched_workload(wl):
-        # the same lists built on the GPU (changa_walk_count/fill), timed
+    if not batched:
+        # the same lists built on the GPU (changa_walk), timed
         from changa_gb300.walk import gpu_walk
         gpu_walk(lists)
         walk_gpu = {}
         gpu_walk(lists, timings=walk_gpu)
         device_pipeline = measure_device_pipeline(wl, pts, I)
+        device_pipeline["walk_on_host_lists_s"] = walk_gpu.get("walk_s")
+        device_pipeline["host_tree_walk_serialise_s"] = t_walk
     I_c, I_p = lists.cells.interactions(), lists.plist.interactions()
     ds = gravity.DeviceSystem(lists, device="cuda", ewald=ew)
     stream = torch.cuda.current_stream()
     flush = torch.empty(256 * 2 ** 20 // 4, dtype=torch.float32, device="cuda")  # > L2
-    batched = hasattr(wl, "systems")
     from changa_gb300 import autotune
     if args.variants:
         # fixed shapes (profiling runs): no autotuner launches
@@ -567,154 +797,68 @@ def main_ours(args):
     for k in N.KERNEL_IDS:
         N.kernel_time(k)
     launches0 = lib.changa_gb300_kernel_launches()
-    evs = []
-    t_wall = time.perf_counter()
-    for _ in range(args.steps):
-        flush.fill_(1.0)
-        e0 = torch.cuda.Event(enable_timing=True)
-        e1 = torch.cuda.Event(enable_timing=True)
-        e0.record(stream)
-        step()
-        e1.record(stream)
-        evs.append((e0, e1))
-    torch.cuda.synchronize()
-    t_wall = time.perf_counter() - t_wall
+    ms_steps = timed_steps(step, args.steps, stream, flush)
     barrier(world)
     torch.cuda.synchronize()
     launches = lib.changa_gb300_kernel_launches() - launches0
     ktimes = {k: N.kernel_time(k) for k in N.KERNEL_IDS}
     lib.changa_gb300_set_timing(0)
     clk = clocks.stop()
-    ms_steps = [a.elapsed_time(b) for a, b in evs]
     ms = sum(ms_steps) / len(ms_steps)
     ms_max = max_over_ranks(world, ms)
     value = sum_over_ranks(world, float(I)) / (ms_max / 1e3)
     v_mixed = ds.vars.cpu().numpy().copy()
-
-    # batching form: the same systems as sequential plain evaluations
-    seq = None
-    if batched:
+    if graph is not None:
         graph.close()
-        singles = [gravity.DeviceSystem(s, device="cuda") for s in wl.systems()]
-        for s in singles:
-            s.step("mixed")
-        torch.cuda.synchronize()
-        e0 = torch.cuda.Event(enable_timing=True)
-        e1 = torch.cuda.Event(enable_timing=True)
-        e0.record(stream)
-        for s in singles:
-            s.step("mixed")
-        e1.record(stream)
-        torch.cuda.synchronize()
-        ms_seq = e0.elapsed_time(e1)
-        seq = {"systems": len(singles), "ms_per_step": ms_seq,
-               "interactions_per_s": I / (ms_seq / 1e3),
-               "graph_batch_over_sequential": (I / (ms / 1e3)) / (I / (ms_seq / 1e3))}
-        del singles
-        for k in N.KERNEL_IDS:
-            N.kernel_time(k)
 
     # FP64 form on the same lists (the precision yardstick and the 3x target)
-    fp64 = None
+    fp64, acc, v64, samp, dsum = None, None, None, None, None
     if args.fp64_steps > 0:
         ds.step("fp64")
         torch.cuda.synchronize()
-        e0 = torch.cuda.Event(enable_timing=True)
-        e1 = torch.cuda.Event(enable_timing=True)
-        e0.record(stream)
-        for _ in range(args.fp64_steps):
-            ds.step("fp64")
-        e1.record(stream)
-        torch.cuda.synchronize()
-        ms64 = e0.elapsed_time(e1) / args.fp64_steps
+        ms64 = sum(timed_steps(lambda: ds.step("fp64"), args.fp64_steps, stream, flush)) / \
+            args.fp64_steps
         v64 = ds.vars.cpu().numpy()
         rng = np.random.default_rng(7)
-        samp = rng.choice(lists.n, min(16384, lists.n), replace=False)
-
-        def rel(a, ref):
-            e = np.linalg.norm(a[:, :3] - ref[:, :3], axis=1) / np.linalg.norm(ref[:, :3], axis=1)
-            return float(np.median(e)), float(np.percentile(e, 99))
-        err = rel(v_mixed[samp], v64[samp])
+        samp = np.sort(rng.choice(lists.n, min(16384, lists.n), replace=False))
+        e = rel_err(v_mixed[samp], v64[samp])
         fp64 = {"ms_per_step": ms64, "interactions_per_s": I / (ms64 / 1e3),
-                "mixed_over_fp64": (I / (ms / 1e3)) / (I / (ms64 / 1e3)),
-                "median_rel_force_err_vs_fp64": err[0],
-                "p99_rel_force_err_vs_fp64": err[1],
-                "sampled_particles": int(len(samp))}
-        if args.direct:
+                "mixed_ms_per_step": ms, "mixed_interactions_per_s": I / (ms / 1e3),
+                "mixed_over_fp64": ms64 / ms,
+                "mixed_vs_fp64": stats(e), "sampled_particles": int(len(samp))}
+        if args.direct and not batched:
             # the same sample against the direct sum (Ewald-summed when periodic)
             t0 = time.perf_counter()
             dsum = gravity.direct_forces(ds.parts, samp, period=float(lists.period))
-            em, e64 = rel(v_mixed[samp], dsum), rel(v64[samp], dsum)
-            fp64.update({"median_rel_force_err_mixed_vs_direct": em[0],
-                         "p99_rel_force_err_mixed_vs_direct": em[1],
-                         "median_rel_force_err_fp64_vs_direct": e64[0],
-                         "p99_rel_force_err_fp64_vs_direct": e64[1],
-                         "direct_sum": "changa_direct_forces, FP64-accumulated%s, %.1f s" % (
-                             " Ewald sum" if lists.period else "", time.perf_counter() - t0)})
+            acc = accuracy_block(lists, samp, v_mixed, v64, dsum)
+            acc["direct_sum"] = "changa_direct_forces, FP64-accumulated%s, %.1f s" % (
+                " Ewald sum" if lists.period else "", time.perf_counter() - t0)
         for k in N.KERNEL_IDS:
             N.kernel_time(k)
+    del ds
+    torch.cuda.empty_cache()
 
     # ChaNGa's default build (hexadecapole) on the same particles
     hexa = None
     if args.hexadecapole and pts is not None:
-        samp_h = samp if fp64 is not None else None
-        dsum_h = dsum if (fp64 is not None and args.direct) else None
-        hexa = measure_hexadecapole(wl, pts, samp_h, dsum_h)
+        hexa = measure_hexadecapole(wl, pts, samp, dsum)
+        if acc is not None and "median_rel_force_err_vs_direct" in hexa:
+            acc["hexadecapole_rel"] = {"median": hexa["median_rel_force_err_vs_direct"],
+                                       "p99": hexa["p99_rel_force_err_vs_direct"]}
     pts = None
 
     # end to end through the public C-ABI with pinned host buffers
     e2e = None
     if args.e2e_steps > 0:
-        import ctypes as C
-        pin = {k: gravity.PinnedArray(a) for k, a in (
-            ("moments", lists.moments), ("parts", lists.parts),
-            ("cl", lists.cells.list), ("cm", lists.cells.markers), ("cs", lists.cells.starts),
-            ("cz", lists.cells.sizes), ("pl", lists.plist.list), ("pm", lists.plist.markers),
-            ("ps", lists.plist.starts), ("pz", lists.plist.sizes))}
-        out = gravity.PinnedArray(np.zeros((lists.n, 5)))
-
-        def req(l, m, s, z, r):
-            q = N.ChangaListRequest()
-            q.list, q.markers, q.starts, q.sizes = pin[l].ptr, pin[m].ptr, pin[s].ptr, pin[z].ptr
-            q.n_buckets, q.n_entries = r.n_buckets, r.n_entries
-            return q
-        cq = req("cl", "cm", "cs", "cz", lists.cells)
-        pq = req("pl", "pm", "ps", "pz", lists.plist)
-        ep = ew.params(lists.root) if ew else None
-        sh = stream.cuda_stream
-
-        def one():
-            # overwrite: the result replaces out (no host zeroing, no vars upload)
-            rc = lib.changa_gravity_step_host(N.CHANGA_FORM_MIXED | N.CHANGA_STEP_OVERWRITE,
-                                              pin["moments"].ptr,
-                                              lists.moments.shape[0], pin["parts"].ptr, lists.n,
-                                              C.byref(cq), C.byref(pq), float(lists.period),
-                                              C.byref(ep) if ep else None, out.ptr, sh)
-            N.check(rc, "changa_gravity_step_host")
-        one()
-        tt = []
-        for _ in range(args.e2e_steps):
-            t1 = time.perf_counter()
-            one()
-            tt.append(time.perf_counter() - t1)
-        t_e2e = max_over_ranks(world, sum(tt) / len(tt))
-        h2d = (lists.moments.nbytes + lists.parts.nbytes + lists.cells.list.nbytes +
-               lists.cells.markers.nbytes + lists.cells.starts.nbytes + lists.cells.sizes.nbytes +
-               lists.plist.list.nbytes + lists.plist.markers.nbytes + lists.plist.starts.nbytes +
-               lists.plist.sizes.nbytes)
-        e2e = {"value": sum_over_ranks(world, float(I)) / t_e2e, "unit": "interactions/s",
-               "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(lists.parts.nbytes),
-               "ms_per_step": 1e3 * t_e2e,
-               "api": "changa_gravity_step_host (include/changa_gb300.h), pinned host "
-                      "buffers, CHANGA_STEP_OVERWRITE; lists uploaded in 512 MiB chunks (halving "
-                      "toward the end) on a copy stream overlapping the list kernels; each "
-                      "chunk's particles read back on a second copy stream once final"}
-        for a in list(pin.values()) + [out]:
-            a.free()
+        e2e, r = measure_e2e(lists, ew, stream, args.e2e_steps, world)
+        if r is not None:  # the same evaluation as the device-resident step
+            e2e["max_rel_force_diff_vs_device_step"] = float(rel_err(r, v_mixed).max())
 
     dropin = None
-    if args.e2e_steps > 0 and getattr(lists, "order", 2) == 2 and not batched_workload(wl):
+    if args.e2e_steps > 0 and getattr(lists, "order", 2) == 2 and not batched:
         dropin = measure_dropin(lists, ew, I, args.e2e_steps)
+        if e2e is not None and "ms_per_step" in dropin:
+            dropin["over_e2e_ms"] = dropin["ms_per_step"] / e2e["ms_per_step"]
 
     # roofline of the dominant kernel (FP32-mixed cell lists) and the P-P kernel.
     # The bound is the FP32 FMA pipe (no tensor-core or HBM bound applies:
@@ -768,34 +912,47 @@ def main_ours(args):
                       "real_space_terms_per_particle": terms, "h_vectors": nh,
                       "reference_score_per_particle": fl}
 
+    # the CPU oracle on a bounded sample: the reported baseline, and the
+    # per-particle parity of both GPU forms on the particles it evaluated
+    cpu, parity = None, None
+    if rank == 0 and world == 1 and not args.no_cpu:
+        cpu, v_orc, rows = run_cpu(lists, ew, args.cpu_sample, want_vars=True)
+        if v64 is not None:
+            parity = parity_block(lists, v_orc, rows, v64, v_mixed, cpu["kind"])
+        del v_orc
+    list_bytes = int(lists.cells.list.nbytes + lists.plist.list.nbytes)
+    del lists, v64
+    torch.cuda.empty_cache()
+
+    bat = None
+    if rank == 0 and args.batched and not batched:
+        try:
+            bat = measure_batched()
+        except Exception as ex:  # noqa: BLE001 - reported in the JSON line
+            bat = {"error": "%s: %s" % (type(ex).__name__, ex)}
+
     adj = None
     if rank == 0 and args.adjoint:
         adj = measure_adjoint(args.adjoint_leapfrog, tune=not args.variants)
 
-    cpu = None
-    if rank == 0 and world == 1 and not args.no_cpu:
-        cpu = run_cpu(lists, ew, args.cpu_sample)
-
     if rank == 0:
-        out = {"metric": metric_for(args.workload), "value": value, "unit": "interactions/s", "n_gpus": world,
-               "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_max,
+        cfg = dict(wl.describe(), l2="inputs larger than L2 and a 256 MB flush write between "
+                                     "timed steps")
+        out = {"metric": metric_for(args.workload), "value": value, "unit": "interactions/s",
+               "n_gpus": world, "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_max,
                "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
                "data": "synthetic (seeded %s; no dataset)" % wl.name,
-               "config": dict(wl.describe(), form="FP32-mixed", interactions=I,
-                              cell_interactions=I_c, particle_interactions=I_p,
-                              list_bytes=int(lists.cells.list.nbytes + lists.plist.list.nbytes),
-                              l2="inputs larger than L2 (%.2f GB of lists) and a 256 MB flush "
-                                 "write between timed steps" %
-                                 ((lists.cells.list.nbytes + lists.plist.list.nbytes) / 1e9),
-                              host_walk_s=t_walk, gpu_walk_s=walk_gpu and walk_gpu.get("walk_s"),
-                              device_pipeline=device_pipeline, hexadecapole=hexa,
-                              fp64_form=fp64, kernels=kshare, ewald=ewald_info,
-                              dropin_e2e=dropin,
-                              batched_graph=batched, sequential_plain=seq,
-                              autotune=tuning,
-                              parallelism="replicas x%d" % world),
+               "config": cfg,
+               "workload_detail": {"form": "FP32-mixed", "interactions": I,
+                                   "cell_interactions": I_c, "particle_interactions": I_p,
+                                   "list_bytes": list_bytes, "host_walk_s": t_walk,
+                                   "autotune": tuning, "kernels": kshare,
+                                   "parallelism": "replicas x%d" % world},
                "roofline": roof, "roofline_pp": roof_pp, "cpu_baseline": cpu, "e2e": e2e,
-               "gpu_launches": int(launches), "clocks": clk, "adjoint": adj}
+               "gpu_launches": int(launches), "clocks": clk,
+               "fp64_form": fp64, "parity": parity, "accuracy": acc, "hexadecapole": hexa,
+               "dropin_e2e": dropin, "batched": bat, "ewald": ewald_info,
+               "device_pipeline": device_pipeline, "adjoint": adj}
         print(json.dumps(out), flush=True)
     if world > 1:
         import torch.distributed as dist

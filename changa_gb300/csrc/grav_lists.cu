@@ -672,11 +672,13 @@ struct Variant {
   int minb, group;
   int tp;  // 0 source-parallel, 1 target-parallel (list_kernel_tp), 2 paired (list_kernel_tp2),
            // 3 paired with TMA-staged cell records (list_kernel_tma; FP32-mixed cell lists,
-           //   list_kernel_tp2 for the others)
+           //   list_kernel_tp2 for the others), 4 register-blocked paired (list_kernel_rb,
+           //   group = the most targets per lane)
 };
 constexpr Variant kVariants[] = {{2, 16, 0}, {3, 16, 0}, {4, 16, 0}, {3, 32, 0}, {2, 32, 0},
                                  {2, 0, 1},  {3, 0, 1},  {4, 0, 1},  {2, 0, 2},  {3, 0, 2},
-                                 {4, 0, 2},  {2, 0, 3},  {1, 0, 3}};
+                                 {4, 0, 2},  {2, 0, 3},  {1, 0, 3},  {2, 3, 4},  {2, 2, 4},
+                                 {3, 2, 4},  {1, 3, 4}};
 constexpr int kNumVariants = sizeof(kVariants) / sizeof(kVariants[0]);
 
 /* Source-parallel list kernel of the FP32 forms.  Per warp and bucket: the
@@ -1301,14 +1303,23 @@ __device__ __forceinline__ void stage_cell_half(float* pb, int h, float4 p, floa
  * keeps the minimum of -(m_t b + M b) (dtGrav's maximum, negated).  sft
  * holds the pair's two softenings.  NEAR = false leaves out the softening
  * test (for blocks whose cells all lie beyond the softening bound). */
+/* A staged cell pair's six words, read from shared memory once and used
+ * for every target of a lane (pc_pair_w). */
+struct CellPair {
+  float4 w0, w1, w2, w3, w4, w5;
+};
+__device__ __forceinline__ CellPair load_cell_pair(const float4* __restrict__ w) {
+  return CellPair{w[0], w[1], w[2], w[3], w[4], w[5]};
+}
+
 template <bool NEAR = true>
-__device__ __forceinline__ void pc_pair(const float4* __restrict__ w, const float* __restrict__ sft,
-                                        f2 tx2, f2 ty2, f2 tz2, f2 tmn2, float tsoft, float near2,
-                                        f2& pa2, f2& pw2, f2& ax2, f2& ay2, f2& az2, float& idtn) {
-  const float4 w0 = w[0], w1 = w[1];
+__device__ __forceinline__ void pc_pair_w(const CellPair& cp, const float* __restrict__ sft,
+                                          f2 tx2, f2 ty2, f2 tz2, f2 tmn2, float tsoft,
+                                          float near2, f2& pa2, f2& pw2, f2& ax2, f2& ay2, f2& az2,
+                                          float& idtn) {
+  const float4 w0 = cp.w0, w1 = cp.w1;
   const f2 px = pk2(w0.x, w0.y), py = pk2(w0.z, w0.w), pz = pk2(w1.x, w1.y), mn = pk2(w1.z, w1.w);
-  const float4 w2 = w[2], w3 = w[3], w4 = w[4],
-               w5 = w[5];
+  const float4 w2 = cp.w2, w3 = cp.w3, w4 = cp.w4, w5 = cp.w5;
   const f2 sxx = pk2(w2.x, w2.y), sxy = pk2(w2.z, w2.w), sxz = pk2(w3.x, w3.y),
            syy = pk2(w3.z, w3.w), syz = pk2(w4.x, w4.y), szz = pk2(w4.z, w4.w),
            tr = pk2(w5.x, w5.y), tr3 = pk2(w5.z, w5.w);
@@ -1361,6 +1372,14 @@ __device__ __forceinline__ void pc_pair(const float4* __restrict__ w, const floa
   float d0, d1;
   up2(fma2(tmn2, bv, bmn), d0, d1);
   idtn = fmin3(idtn, d0, d1);
+}
+
+template <bool NEAR = true>
+__device__ __forceinline__ void pc_pair(const float4* __restrict__ w, const float* __restrict__ sft,
+                                        f2 tx2, f2 ty2, f2 tz2, f2 tmn2, float tsoft, float near2,
+                                        f2& pa2, f2& pw2, f2& ax2, f2& ay2, f2& az2, float& idtn) {
+  pc_pair_w<NEAR>(load_cell_pair(w), sft, tx2, ty2, tz2, tmn2, tsoft, near2, pa2, pw2, ax2, ay2,
+                  az2, idtn);
 }
 
 
@@ -1643,6 +1662,366 @@ __global__ void __launch_bounds__(kThreads, MINB) list_kernel_tp2(const ListArgs
         }
       }
       __syncwarp();
+    }
+  }
+}
+
+/* ------------------------------------------------------------------ */
+/* Register-blocked paired kernel: list_kernel_tp2's staging and pair   */
+/* arithmetic with R targets per lane.  A chunk of nt targets is split  */
+/* into c = ceil(nt / R) slots of R targets each (slot s holds targets  */
+/* s, s + c, ...), and G = 32 / c groups of c lanes take the staged     */
+/* pairs g, g + G, ...  With one target per lane, 32 - G nt lanes sit   */
+/* idle (nt = 20: 12 of 32); R is chosen per chunk to minimise the pair */
+/* steps per 32-entry block, R ceil(16 / G) (nt = 20: R = 2, 30 lanes;  */
+/* nt = 24: R = 3, all 32), and each staged pair read from shared       */
+/* memory serves all R targets of a lane.  The last block of a list     */
+/* runs only its own pairs.                                             */
+/* ------------------------------------------------------------------ */
+
+/* targets per lane for a chunk of nt <= 32 targets, at most RMAX */
+template <int RMAX>
+__device__ __forceinline__ int rb_targets_per_lane(int nt) {
+  int best = 1, cost = 1 << 30;
+#pragma unroll
+  for (int r = 1; r <= RMAX; ++r) {
+    const int c = (nt + r - 1) / r, G = 32 / c;
+    const int k = r * ((16 + G - 1) / G);
+    if (k < cost) {
+      cost = k;
+      best = r;
+    }
+  }
+  return best;
+}
+
+/* One target of a lane: packed position and mass (negated for cells, as
+ * pc_pair takes it), softening, and whether it is a target of the chunk
+ * (a lane's spare slots compute on target 0's data and are discarded). */
+struct RbTarget {
+  f2 x2, y2, z2, m2;
+  float soft;
+  bool valid;
+};
+
+/* running per-target sums: Kahan pairs in the mixed form, and dtGrav's
+ * running maximum (kept negated, a running minimum, for cells) */
+struct RbSums {
+  float sx, sy, sz, sp, cx, cy, cz, cp, idt;
+};
+
+template <int FORM, bool CELL, int R>
+__device__ __forceinline__ void rb_chunk(const ListArgs& a, const int lane, const int e_begin,
+                                         const int e_end, const long long tb, const int nt,
+                                         const float3 chi, const float3 clo,
+                                         float4 (&stage)[2][16 * (CELL ? 6 : 2)],
+                                         float (&ssoft)[2][32], double (&red)[5][32]) {
+  constexpr int PW = CELL ? 6 : 2;  // float4 words per staged pair
+  const int c = (nt + R - 1) / R;
+  const int G = 32 / c;
+  const int g = lane / c, s = lane - g * c;
+  const bool active = g < G;
+
+  RbTarget T[R];
+  float tsm = 0.f;
+  float3 blo = make_float3(3.4e38f, 3.4e38f, 3.4e38f), bhi = make_float3(-3.4e38f, -3.4e38f, -3.4e38f);
+#pragma unroll
+  for (int k = 0; k < R; ++k) {
+    const int t = s + k * c;
+    T[k].valid = active && t < nt;
+    const long long ti = tb + (T[k].valid ? t : 0);
+    float tx, ty, tz, tmass, tsoft;
+    if constexpr (FORM == kF32) {
+      const CompactPartData* p = static_cast<const CompactPartData*>(a.tgt) + ti;
+      tmass = __ldg(&p->mass);
+      tsoft = __ldg(&p->soft);
+      tx = __ldg(&p->position.x);
+      ty = __ldg(&p->position.y);
+      tz = __ldg(&p->position.z);
+    } else {
+      const float4* p = static_cast<const float4*>(a.tgt) + kPartPackF4 * ti;
+      const float4 h = __ldg(p), l = __ldg(p + 1);
+      tx = (h.x - chi.x) + (l.x - clo.x);
+      ty = (h.y - chi.y) + (l.y - clo.y);
+      tz = (h.z - chi.z) + (l.z - clo.z);
+      tmass = h.w;
+      tsoft = l.w;
+    }
+    if (T[k].valid) {
+      tsm = fmaxf(tsm, tsoft);
+      blo = make_float3(fminf(blo.x, tx), fminf(blo.y, ty), fminf(blo.z, tz));
+      bhi = make_float3(fmaxf(bhi.x, tx), fmaxf(bhi.y, ty), fmaxf(bhi.z, tz));
+    }
+    const float tms = CELL ? -tmass : tmass;
+    T[k].x2 = pk2(tx, tx);
+    T[k].y2 = pk2(ty, ty);
+    T[k].z2 = pk2(tz, tz);
+    T[k].m2 = pk2(tms, tms);
+    T[k].soft = tsoft;
+  }
+  const float tsmax = warp_max(tsm);
+  blo = make_float3(warp_min(blo.x), warp_min(blo.y), warp_min(blo.z));
+  bhi = make_float3(warp_max(bhi.x), warp_max(bhi.y), warp_max(bhi.z));
+
+  RbSums S[R];
+#pragma unroll
+  for (int k = 0; k < R; ++k) S[k] = RbSums{0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+
+  /* records one block ahead, their list entries two blocks ahead */
+  RawRec<FORM, CELL> raw;
+  int2 ent = load_entry(a, e_begin + lane, e_end);
+  gather_raw_entry<FORM, CELL>(a, ent, raw);
+  ent = load_entry(a, e_begin + 32 + lane, e_end);
+  int buf = 0;
+  for (int e0 = e_begin; e0 < e_end; e0 += 32, buf ^= 1) {
+    const int ne = min(32, e_end - e0);
+    const int np = (ne + 1) >> 1;  // staged pairs of this block
+    float4 rec[3];
+    const float ls = finish_raw<FORM, CELL>(a, raw, lane < ne, chi, clo, rec);
+    {
+      /* this lane's record into its half of pair lane/2 */
+      float* pb = reinterpret_cast<float*>(stage[buf] + (lane >> 1) * PW);
+      const int h = lane & 1;
+      if constexpr (CELL) {
+        stage_cell_half(pb, h, rec[0], rec[1], rec[2]);
+      } else {
+        pb[pair_slot(0, h)] = rec[0].x;
+        pb[pair_slot(1, h)] = rec[0].y;
+        pb[pair_slot(2, h)] = rec[0].z;
+        pb[pair_slot(3, h)] = rec[0].w;
+      }
+    }
+    ssoft[buf][lane] = ls;
+    const float ss = warp_max(ls) + tsmax;
+    const float near2 = ss * ss;
+    /* no source of the block within the softening bound of the targets' box */
+    bool far_block;
+    {
+      const float bx = fmaxf(fmaxf(blo.x - rec[0].x, rec[0].x - bhi.x), 0.f);
+      const float by = fmaxf(fmaxf(blo.y - rec[0].y, rec[0].y - bhi.y), 0.f);
+      const float bz = fmaxf(fmaxf(blo.z - rec[0].z, rec[0].z - bhi.z), 0.f);
+      far_block = __all_sync(kFull, fmaf(bx, bx, fmaf(by, by, bz * bz)) > near2 * 1.0001f);
+    }
+    __syncwarp();
+    if (e0 + 32 < e_end) {
+      gather_raw_entry<FORM, CELL>(a, ent, raw);
+      ent = load_entry(a, e0 + 64 + lane, e_end);
+    }
+    const float4* st = stage[buf];
+    const float* sf = ssoft[buf];
+    f2 ax[R], ay[R], az[R], pt[R], pw[R];
+    unsigned nm[R];
+#pragma unroll
+    for (int k = 0; k < R; ++k) {
+      ax[k] = ay[k] = az[k] = pt[k] = pw[k] = 0ull;  // +0.0f in both halves
+      nm[k] = 0u;
+    }
+    /* staged pair p on every target of the lane, with or without the
+     * softening test (cells) or the marking of softened pairs (particles) */
+    auto step = [&](int p, auto near) {
+      constexpr bool NEAR = decltype(near)::value;
+      if constexpr (CELL) {
+        const CellPair cpw = load_cell_pair(st + p * PW);
+#pragma unroll
+        for (int k = 0; k < R; ++k)
+          pc_pair_w<NEAR>(cpw, sf + 2 * p, T[k].x2, T[k].y2, T[k].z2, T[k].m2, T[k].soft, near2,
+                          pt[k], pw[k], ax[k], ay[k], az[k], S[k].idt);
+      } else {
+        const float4 w0 = st[p * PW], w1 = st[p * PW + 1];
+        const f2 sx2 = pk2(w0.x, w0.y), sy2 = pk2(w0.z, w0.w), sz2 = pk2(w1.x, w1.y);
+        const f2 pm = pk2(w1.z, w1.w);
+#pragma unroll
+        for (int k = 0; k < R; ++k) {
+          /* gravity.h:276-301: r = source - target */
+          const f2 rx = sub2(sx2, T[k].x2), ry = sub2(sy2, T[k].y2), rz = sub2(sz2, T[k].z2);
+          const f2 rsq = fma2(rx, rx, fma2(ry, ry, mul2(rz, rz)));
+          float q0, q1;
+          up2(rsq, q0, q1);
+          float a0 = rsqrt_ftz(q0), a1 = rsqrt_ftz(q1);
+          if constexpr (NEAR) {
+            const bool n0 = q0 <= near2, n1 = q1 <= near2;
+            nm[k] |= ((n0 ? 1u : 0u) | (n1 ? 2u : 0u)) << (2 * p);
+            a0 = n0 ? 0.f : a0;
+            a1 = n1 ? 0.f : a1;
+          }
+          const f2 av = pk2(a0, a1);
+          const f2 bv = mul2(mul2(av, av), av);
+          const f2 bm = mul2(bv, pm);
+          pt[k] = fma2(pm, av, pt[k]);  // opposite sign, negated at the fold
+          ax[k] = fma2(rx, bm, ax[k]);
+          ay[k] = fma2(ry, bm, ay[k]);
+          az[k] = fma2(rz, bm, az[k]);
+          float d0, d1;
+          up2(fma2(T[k].m2, bv, bm), d0, d1);
+          S[k].idt = fmax3(S[k].idt, d0, d1);
+        }
+      }
+    };
+    using Far = std::integral_constant<bool, false>;
+    using Near = std::integral_constant<bool, true>;
+    if (G == 1) {
+      if (far_block) {
+#pragma unroll 2
+        for (int p = 0; p < np; ++p) step(p, Far{});
+      } else {
+#pragma unroll 2
+        for (int p = 0; p < np; ++p) step(p, Near{});
+      }
+    } else if (active) {
+      if (far_block) {
+        for (int p = g; p < np; p += G) step(p, Far{});
+      } else {
+        for (int p = g; p < np; p += G) step(p, Near{});
+      }
+    }
+#pragma unroll
+    for (int k = 0; k < R; ++k) {
+      /* the marked sources (within the softening bound of the block), each
+       * lane its own: gravity.h:276-301 with the spline inside 2h, zero at
+       * r = 0 */
+      float ex = 0.f, ey = 0.f, ez = 0.f, ep = 0.f;
+      if constexpr (!CELL) {
+        float tx, ty, tz, tm, d_;
+        up2(T[k].x2, tx, d_);
+        up2(T[k].y2, ty, d_);
+        up2(T[k].z2, tz, d_);
+        up2(T[k].m2, tm, d_);
+        unsigned m = T[k].valid ? nm[k] : 0u;
+        while (m) {
+          const int jb = __ffs(m) - 1;
+          m &= m - 1u;
+          const float* pb = reinterpret_cast<const float*>(st + (jb >> 1) * PW);
+          const int h = jb & 1;
+          const float dx = pb[pair_slot(0, h)] - tx, dy = pb[pair_slot(1, h)] - ty,
+                      dz = pb[pair_slot(2, h)] - tz, sm = pb[pair_slot(3, h)];
+          const float q = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
+          float av = 0.f, bv = 0.f;
+          if (q != 0.f) {
+            av = rsqrt_ftz(q);
+            bv = (av * av) * av;
+            const float twoh = sf[jb] + T[k].soft;
+            const float r1 = q * av;
+            if (r1 < twoh) spline_near(r1, av, twoh, av, bv);
+          }
+          const float bm = bv * sm;
+          ep = fmaf(sm, av, ep);
+          ex = fmaf(dx, bm, ex);
+          ey = fmaf(dy, bm, ey);
+          ez = fmaf(dz, bm, ez);
+          S[k].idt = fmaxf(S[k].idt, fmaf(tm, bv, bm));
+        }
+      }
+      float x0, x1, y0, y1, z0, z1, p0, p1;
+      up2(ax[k], x0, x1);
+      up2(ay[k], y0, y1);
+      up2(az[k], z0, z1);
+      up2(pt[k], p0, p1);
+      float pb_;  // this block's potential
+      if constexpr (CELL) {
+        float w0_, w1_;
+        up2(pw[k], w0_, w1_);
+        pb_ = (p0 + p1) - 0.5f * (w0_ + w1_);
+      } else {
+        pb_ = -((p0 + p1) + ep);
+      }
+      if constexpr (FORM == kMix) {
+        kahan_add(S[k].sx, S[k].cx, (x0 + x1) + ex);
+        kahan_add(S[k].sy, S[k].cy, (y0 + y1) + ey);
+        kahan_add(S[k].sz, S[k].cz, (z0 + z1) + ez);
+        kahan_add(S[k].sp, S[k].cp, pb_);
+      } else {
+        S[k].sx += (x0 + x1) + ex;
+        S[k].sy += (y0 + y1) + ey;
+        S[k].sz += (z0 + z1) + ez;
+        S[k].sp += pb_;
+      }
+    }
+  }
+
+  /* per target slot k: the G groups' partial sums of each target */
+#pragma unroll
+  for (int k = 0; k < R; ++k) {
+    if (T[k].valid) {
+      red[0][lane] = (double)S[k].sx - (double)S[k].cx;
+      red[1][lane] = (double)S[k].sy - (double)S[k].cy;
+      red[2][lane] = (double)S[k].sz - (double)S[k].cz;
+      red[3][lane] = (double)S[k].sp - (double)S[k].cp;
+      red[4][lane] = CELL ? -(double)S[k].idt : (double)S[k].idt;
+    }
+    __syncwarp();
+    const int t = lane + k * c;
+    if (lane < c && t < nt) {
+      double rx = 0, ry = 0, rz = 0, rp = 0, ri = 0;
+      for (int gg = 0; gg < G; ++gg) {
+        const int l = gg * c + lane;
+        rx += red[0][l];
+        ry += red[1][l];
+        rz += red[2][l];
+        rp += red[3][l];
+        ri = fmax(ri, red[4][l]);
+      }
+      const long long to = tb + t;
+      if constexpr (FORM == kF32) {
+        VariablePartData* v = static_cast<VariablePartData*>(a.vars) + to;
+        v->a.x += (float)rx;
+        v->a.y += (float)ry;
+        v->a.z += (float)rz;
+        v->potential += (float)rp;
+        v->dtGrav = fmaxf((float)ri, v->dtGrav);
+      } else {
+        double* v = static_cast<double*>(a.vars) + 5 * to;
+        v[0] += rx;
+        v[1] += ry;
+        v[2] += rz;
+        v[3] += rp;
+        v[4] = fmax(ri, v[4]);
+      }
+    }
+    __syncwarp();
+  }
+}
+
+template <int FORM, bool CELL, int MINB, int RMAX>
+__global__ void __launch_bounds__(kThreads, MINB) list_kernel_rb(const ListArgs a) {
+  static_assert(FORM != kF64, "FP32 arithmetic forms only");
+  static_assert(RMAX >= 1 && RMAX <= 3, "1 to 3 targets per lane");
+  constexpr int PW = CELL ? 6 : 2;
+  __shared__ __align__(16) float4 stage[kWarps][2][16 * PW];
+  __shared__ float ssoft[kWarps][2][32];
+  __shared__ double red[kWarps][5][32];
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+
+  for (;;) {
+    int b = 0;
+    if (lane == 0) b = (int)atomicAdd(a.queue, 1u);
+    b = __shfl_sync(kFull, b, 0);
+    if (b >= a.n_buckets) break;
+    const int e_begin = max(__ldg(a.markers + b), 0);
+    const int e_end = (int)min((long long)__ldg(a.markers + b + 1), a.n_entries);  // memory safety
+    const long long tbase = __ldg(a.starts + b);
+    const int n = __ldg(a.sizes + b);
+    if (n <= 0 || tbase < 0 || tbase + n > a.n_tgt) continue;  // memory safety
+
+    float3 chi = make_float3(0.f, 0.f, 0.f), clo = chi;
+    if constexpr (FORM == kMix) {
+      const float4* tp = static_cast<const float4*>(a.tgt) + kPartPackF4 * tbase;
+      const float4 h = __ldg(tp), l = __ldg(tp + 1);
+      chi = make_float3(h.x, h.y, h.z);
+      clo = make_float3(l.x, l.y, l.z);
+    }
+    for (int t0 = 0; t0 < n; t0 += 32) {
+      const int nt = min(32, n - t0);
+      const int r = rb_targets_per_lane<RMAX>(nt);
+      if (RMAX >= 3 && r == 3) {
+        rb_chunk<FORM, CELL, (RMAX >= 3 ? 3 : 1)>(a, lane, e_begin, e_end, tbase + t0, nt, chi,
+                                                  clo, stage[warp], ssoft[warp], red[warp]);
+      } else if (RMAX >= 2 && r == 2) {
+        rb_chunk<FORM, CELL, (RMAX >= 2 ? 2 : 1)>(a, lane, e_begin, e_end, tbase + t0, nt, chi,
+                                                  clo, stage[warp], ssoft[warp], red[warp]);
+      } else {
+        rb_chunk<FORM, CELL, 1>(a, lane, e_begin, e_end, tbase + t0, nt, chi, clo, stage[warp],
+                                ssoft[warp], red[warp]);
+      }
     }
   }
 }
@@ -2370,7 +2749,10 @@ cudaError_t launch_variant(const ListArgs& a, cudaStream_t s) {
     }
     return launch_kernel(list_kernel_tp2<FORM, CELL, var.minb>, &occ, list_kernel_id(FORM, CELL),
                          a, s);
-  } else if constexpr (var.tp == 2)
+  } else if constexpr (var.tp == 4)
+    return launch_kernel(list_kernel_rb<FORM, CELL, var.minb, var.group>, &occ,
+                         list_kernel_id(FORM, CELL), a, s);
+  else if constexpr (var.tp == 2)
     return launch_kernel(list_kernel_tp2<FORM, CELL, var.minb>, &occ, list_kernel_id(FORM, CELL),
                          a, s);
   else if constexpr (var.tp == 1)

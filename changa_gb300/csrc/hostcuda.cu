@@ -151,6 +151,47 @@ static void signal(cudaStream_t s, void* cb) {
 
 static size_t align256(size_t x) { return (x + 255) & ~(size_t)255; }
 
+static std::atomic<size_t> g_host_chunk_bytes{size_t(512) << 20};
+
+/* The copy streams of the host-array entries on each device (created
+ * once): which 0 carries the uploads, which 1 the read-backs, so the two
+ * directions of the host link run at once. */
+static cudaStream_t copy_stream(int which = 0) {
+  static cudaStream_t st[64][2] = {{nullptr}};
+  static std::mutex mu;
+  int dev = 0;
+  cudaGetDevice(&dev);
+  if (dev < 0 || dev >= 64) dev = 0;
+  std::lock_guard<std::mutex> lk(mu);
+  cudaStream_t& x = st[dev][which & 1];
+  if (!x && cudaStreamCreateWithFlags(&x, cudaStreamNonBlocking) != cudaSuccess) x = nullptr;
+  return x;
+}
+
+/* Bucket ranges [b0, b1) of a request, about `per` list entries each; with
+ * shrink, the last 2 per entries go in halving chunks (down to per / 16),
+ * so little arithmetic is left once the final entries have landed. */
+static void list_chunks(const ChangaListRequest* r, long long per, bool shrink,
+                        std::vector<std::pair<int, int>>& out) {
+  const long long total = r->markers[r->n_buckets];
+  const long long floor_ = std::max<long long>(1, per / 16);
+  int b0 = 0;
+  while (b0 < r->n_buckets) {
+    const long long left = total - r->markers[b0];
+    long long want_n = per;
+    if (shrink && left <= 2 * per) want_n = std::max(floor_, left / 2);
+    const int* lo = r->markers + b0 + 1;
+    const int* hi = r->markers + r->n_buckets + 1;
+    const long long want = (long long)r->markers[b0] + want_n;
+    const int* it = std::upper_bound(lo, hi, (int)std::min<long long>(want, INT_MAX));
+    int b1 = (int)(it - r->markers) - 1;
+    if (b1 <= b0) b1 = b0 + 1;
+    if (b1 > r->n_buckets) b1 = r->n_buckets;
+    out.push_back({b0, b1});
+    b0 = b1;
+  }
+}
+
 /* Device copy of one request (list, markers, starts, sizes, queue). */
 struct ReqDev {
   char* block = nullptr;
@@ -164,7 +205,7 @@ struct ReqDev {
 
 static int upload_request(const void* h_list, long long n_entries, const int* h_markers,
                           const int* h_starts, const int* h_sizes, int n_buckets, cudaStream_t s,
-                          ReqDev& d) {
+                          ReqDev& d, bool copy_list = true) {
   prepare_pool();
   size_t lb = align256((size_t)(n_entries > 0 ? n_entries : 0) * sizeof(ILCell));
   size_t mb = align256((size_t)(n_buckets + 1) * sizeof(int));
@@ -177,7 +218,7 @@ static int upload_request(const void* h_list, long long n_entries, const int* h_
   d.starts = (int*)(d.block + lb + mb);
   d.sizes = (int*)(d.block + lb + mb + sb);
   d.queue = (unsigned int*)(d.block + lb + mb + 2 * sb);
-  if (n_entries > 0)
+  if (copy_list && n_entries > 0)
     CHG_CUDA(cudaMemcpyAsync(d.list, h_list, (size_t)n_entries * sizeof(ILCell),
                              cudaMemcpyHostToDevice, s));
   CHG_CUDA(cudaMemcpyAsync(d.markers, h_markers, (size_t)(n_buckets + 1) * sizeof(int),
@@ -195,6 +236,80 @@ static int upload_request(const void* h_list, long long n_entries, const int* h_
 static int release_request(ReqDev& d) {
   if (d.block) CHG_CUDA(cudaFreeAsync(d.block, d.stream));
   d.block = nullptr;
+  return 0;
+}
+
+/* A large drop-in request, pipelined: the markers, starts and sizes go
+ * first on the request's stream; the list follows in chunks of about `per`
+ * entries (the last ones halving) on the library's copy stream, and the
+ * list kernel runs over each chunk's bucket range on the request's stream
+ * as soon as that chunk has landed, so the upload overlaps the arithmetic.
+ * Every kernel waits for its chunk's copy, so the request's stream (and the
+ * completion signalled on it) finishes after every read of the caller's
+ * host arrays, which the caller may free in its callback. */
+static int run_request_chunked(CudaRequest* r, bool cell, const void* sources, long long n_src,
+                               long long n_tgt, int nb, long long per, cudaStream_t c) {
+  cudaStream_t s = r->stream;
+  ReqDev d;
+  int rc = upload_request(r->list, r->numInteractions, r->bucketMarkers, r->bucketStarts,
+                          r->bucketSizes, nb, s, d, /*copy_list=*/false);
+  if (rc) return rc;
+  ChangaListRequest h;  // the host arrays, for the chunk boundaries
+  h.list = (const ILCell*)r->list;
+  h.markers = r->bucketMarkers;
+  h.starts = r->bucketStarts;
+  h.sizes = r->bucketSizes;
+  h.n_buckets = nb;
+  h.n_entries = r->numInteractions;
+  std::vector<std::pair<int, int>> chunks;
+  list_chunks(&h, per, true, chunks);
+  /* events are released by the runtime once complete; a wait enqueued
+   * before the destroy still sees the recorded work */
+  auto mark = [](cudaStream_t on, cudaEvent_t* ev) -> cudaError_t {
+    cudaError_t x = cudaEventCreateWithFlags(ev, cudaEventDisableTiming);
+    if (x != cudaSuccess) return x;
+    return cudaEventRecord(*ev, on);
+  };
+  cudaEvent_t ready = nullptr;
+  cudaError_t e = mark(s, &ready);  // the block is allocated on s
+  if (e == cudaSuccess) e = cudaStreamWaitEvent(c, ready, 0);
+  if (ready) cudaEventDestroy(ready);
+  const ILCell* hl = (const ILCell*)r->list;
+  for (size_t i = 0; i < chunks.size() && e == cudaSuccess; ++i) {
+    const int b0 = chunks[i].first, b1 = chunks[i].second;
+    const long long e0 = std::max(0, h.markers[b0]);
+    const long long e1 = std::min<long long>(h.markers[b1], r->numInteractions);
+    cudaEvent_t landed = nullptr;
+    if (e1 > e0)
+      e = cudaMemcpyAsync(d.list + e0, hl + e0, (size_t)(e1 - e0) * sizeof(ILCell),
+                          cudaMemcpyHostToDevice, c);
+    if (e == cudaSuccess) e = mark(c, &landed);
+    if (e == cudaSuccess) e = cudaStreamWaitEvent(s, landed, 0);
+    if (landed) cudaEventDestroy(landed);
+    if (e != cudaSuccess) break;
+    if (i > 0) e = cudaMemsetAsync(d.queue, 0, sizeof(unsigned int), s);
+    if (e != cudaSuccess) break;
+    ListArgs a;
+    a.src = sources;
+    a.n_src = n_src;
+    a.tgt = r->d_localParts;
+    a.n_tgt = n_tgt;
+    a.vars = r->d_localVars;
+    a.list = d.list;
+    a.n_entries = e1 > e0 ? e1 : e0;  // entries past this chunk have not landed yet
+    a.markers = d.markers + b0;
+    a.starts = d.starts + b0;
+    a.sizes = d.sizes + b0;
+    a.n_buckets = b1 - b0;
+    a.fperiod_f = r->fperiod;
+    a.fperiod_d = r->fperiod;
+    a.queue = d.queue;
+    e = launch_list(kF32, cell, a, s);
+  }
+  rc = release_request(d);
+  if (e != cudaSuccess) return record_error((int)e, "chunked request", __FILE__, __LINE__);
+  if (rc) return rc;
+  signal(s, r->cb);
   return 0;
 }
 
@@ -219,6 +334,12 @@ static int run_request(CudaRequest* r, bool cell, const void* sources, long long
     int rc = changa_validate_request((const ILCell*)r->list, r->numInteractions, r->bucketMarkers,
                                      r->bucketStarts, r->bucketSizes, nb, n_src, n_tgt);
     if (rc) return record_error(rc, "request validation", __FILE__, __LINE__);
+  }
+  /* a list of more than two chunks streams in chunk by chunk */
+  const long long per = (long long)(g_host_chunk_bytes.load() / sizeof(ILCell));
+  if (r->numInteractions > 2 * per) {
+    cudaStream_t c = copy_stream();
+    if (c) return run_request_chunked(r, cell, sources, n_src, n_tgt, nb, per, c);
   }
   ReqDev d;
   int rc = upload_request(r->list, r->numInteractions, r->bucketMarkers, r->bucketStarts,
@@ -886,49 +1007,8 @@ int changa_gravity_step_hexa(int form, const double* moments, long long n_moment
   return 0;
 }
 
-static std::atomic<size_t> g_host_chunk_bytes{size_t(512) << 20};
-
 void changa_gb300_set_host_chunk_bytes(size_t bytes) {
   g_host_chunk_bytes.store(bytes < 4096 ? 4096 : bytes);
-}
-
-/* The copy streams of the host entry on each device (created once):
- * which 0 carries the uploads, which 1 the read-backs, so the two
- * directions of the host link run at once. */
-static cudaStream_t copy_stream(int which = 0) {
-  static cudaStream_t st[64][2] = {{nullptr}};
-  static std::mutex mu;
-  int dev = 0;
-  cudaGetDevice(&dev);
-  if (dev < 0 || dev >= 64) dev = 0;
-  std::lock_guard<std::mutex> lk(mu);
-  cudaStream_t& x = st[dev][which & 1];
-  if (!x && cudaStreamCreateWithFlags(&x, cudaStreamNonBlocking) != cudaSuccess) x = nullptr;
-  return x;
-}
-
-/* Bucket ranges [b0, b1) of a request, about `per` list entries each; with
- * shrink, the last 2 per entries go in halving chunks (down to per / 16),
- * so little arithmetic is left once the final entries have landed. */
-static void list_chunks(const ChangaListRequest* r, long long per, bool shrink,
-                        std::vector<std::pair<int, int>>& out) {
-  const long long total = r->markers[r->n_buckets];
-  const long long floor_ = std::max<long long>(1, per / 16);
-  int b0 = 0;
-  while (b0 < r->n_buckets) {
-    const long long left = total - r->markers[b0];
-    long long want_n = per;
-    if (shrink && left <= 2 * per) want_n = std::max(floor_, left / 2);
-    const int* lo = r->markers + b0 + 1;
-    const int* hi = r->markers + r->n_buckets + 1;
-    const long long want = (long long)r->markers[b0] + want_n;
-    const int* it = std::upper_bound(lo, hi, (int)std::min<long long>(want, INT_MAX));
-    int b1 = (int)(it - r->markers) - 1;
-    if (b1 <= b0) b1 = b0 + 1;
-    if (b1 > r->n_buckets) b1 = r->n_buckets;
-    out.push_back({b0, b1});
-    b0 = b1;
-  }
 }
 
 /* Page-locked (or registered) host memory: a read-back into it returns at

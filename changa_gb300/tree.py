@@ -188,24 +188,25 @@ def concat_systems(systems):
     m_off = np.cumsum([0] + [s.moments.shape[0] for s in systems])
 
     def cat(reqs, idx_off):
-        lists, markers, starts, sizes, ids = [], [np.zeros(1, np.int64)], [], [], []
-        base = 0
-        for k, r in enumerate(reqs):
-            l = r.list.copy()
-            l[:, 0] += idx_off[k]
-            lists.append(l)
-            markers.append(r.markers[1:].astype(np.int64) + base)
-            base += r.n_entries
-            starts.append(r.starts.astype(np.int64) + p_off[k])
-            sizes.append(r.sizes)
-            ids.append(r.bucket_ids)
-        mk = np.concatenate(markers)
-        if mk[-1] >= 2 ** 31:
+        ne = np.cumsum([0] + [r.n_entries for r in reqs])
+        nb = np.cumsum([0] + [r.n_buckets for r in reqs])
+        if ne[-1] >= 2 ** 31:
             raise ValueError("batched list exceeds int32 markers")
-        return ListRequest(np.concatenate(lists, axis=0).astype(np.int32), mk.astype(np.int32),
-                           np.concatenate(starts).astype(np.int32),
-                           np.concatenate(sizes).astype(np.int32),
-                           np.concatenate(ids).astype(np.int32))
+        lst = np.empty((int(ne[-1]), 2), np.int32)
+        mk = np.empty(int(nb[-1]) + 1, np.int32)
+        starts = np.empty(int(nb[-1]), np.int32)
+        sizes = np.empty(int(nb[-1]), np.int32)
+        ids = np.empty(int(nb[-1]), np.int32)
+        mk[0] = 0
+        for k, r in enumerate(reqs):
+            e0, e1, b0, b1 = ne[k], ne[k + 1], nb[k], nb[k + 1]
+            np.add(r.list[:, 0], np.int32(idx_off[k]), out=lst[e0:e1, 0])
+            lst[e0:e1, 1] = r.list[:, 1]
+            mk[b0 + 1:b1 + 1] = r.markers[1:] + np.int32(e0)
+            starts[b0:b1] = r.starts + np.int32(p_off[k])
+            sizes[b0:b1] = r.sizes
+            ids[b0:b1] = r.bucket_ids
+        return ListRequest(lst, mk, starts, sizes, ids)
 
     cells = cat([s.cells for s in systems], m_off)
     plist = cat([s.plist for s in systems], p_off)

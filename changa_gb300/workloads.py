@@ -77,13 +77,23 @@ class ClusterBatch:
     period: float = 0.0
     ewald: tuple | None = None
 
+    def clusters(self):
+        return ics.plummer_clusters(self.n_clusters, ics.rng_for(self.index), self.nmin, self.nmax)
+
     def systems(self, nthreads=0):
-        rng = ics.rng_for(self.index)
-        out = []
-        for p in ics.plummer_clusters(self.n_clusters, rng, self.nmin, self.nmax):
-            out.append(tree.build_lists(p["pos"], p["mass"], p["soft"], n_bucket=self.n_bucket,
-                                        theta=self.theta, nthreads=nthreads))
-        return out
+        """Each cluster's host tree, walk and lists.  The clusters are small,
+        so they are built concurrently, one host thread each (the tree
+        library's calls release the interpreter lock)."""
+        import os
+        from concurrent.futures import ThreadPoolExecutor
+        cl = self.clusters()
+        workers = nthreads if nthreads > 0 else (os.cpu_count() or 1)
+
+        def one(p):
+            return tree.build_lists(p["pos"], p["mass"], p["soft"], n_bucket=self.n_bucket,
+                                    theta=self.theta, nthreads=1)
+        with ThreadPoolExecutor(max_workers=workers) as ex:
+            return list(ex.map(one, cl))
 
     def lists(self, nthreads=0):
         return tree.concat_systems(self.systems(nthreads))

@@ -83,8 +83,11 @@ int changa_gb300_kernel_time(int kernel, double *total_ms, long long *launches);
  * paired .f32x2 arithmetic (2/3/4 blocks per SM; defaults 8 for cell lists,
  * 10 for particle lists), 11-12 paired with the FP32-mixed cell records
  * staged by TMA tile::gather4 copies (2/1 blocks per SM; the other lists
- * run the paired kernel).  The autotuner (changa_gb300/autotune.py) times
- * them on a workload and selects one per kernel. */
+ * run the paired kernel), 13-16 paired with 1-3 targets per lane chosen
+ * per bucket (blocks per SM / most targets per lane: 2/3, 2/2, 3/2, 1/3),
+ * which keeps the lanes of buckets of 17-31 targets busy.  The autotuner
+ * (changa_gb300/autotune.py) times them on a workload and selects one per
+ * kernel. */
 int changa_gb300_list_variant_count(void);
 int changa_gb300_set_list_variant(int kernel, int variant);
 int changa_gb300_get_list_variant(int kernel);
@@ -199,8 +202,10 @@ int changa_gravity_step(int form, const double *moments, long long n_moments,
  * Returns after the work has finished, so vars is ready on return. */
 #define CHANGA_STEP_OVERWRITE 0x100
 
-/* List bytes per upload chunk of changa_gravity_step_host (default 512 MiB,
- * at least 4 KiB). */
+/* List bytes per upload chunk of changa_gravity_step_host and of the
+ * drop-in list transfers (default 512 MiB, at least 4 KiB).  A drop-in
+ * request whose list exceeds two chunks uploads it chunk by chunk on the
+ * library's copy stream, each chunk's buckets evaluated as it lands. */
 void changa_gb300_set_host_chunk_bytes(size_t bytes);
 int changa_gravity_step_host(int form, const double *moments, long long n_moments,
                              const double *parts, long long n_parts,

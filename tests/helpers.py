@@ -52,3 +52,29 @@ def reference_root():
         here = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
         root = os.path.join(os.path.dirname(here), "reference")
     return root if os.path.isdir(root) else None
+
+
+def sampled_oracle(L, ew, bucket_ids, kind="port"):
+    """The oracle on a subset of buckets: nodeBucketForce over their cell
+    lists, partBucketForce over their particle lists and (ew given)
+    BucketEwald on their particles.  Returns (vars N x 5, rows): rows are
+    the particles of those buckets, whose results are complete."""
+    import oracle
+    b = np.asarray(bucket_ids)
+    c_of = {int(x): i for i, x in enumerate(L.cells.bucket_ids)}
+    p_of = {int(x): i for i, x in enumerate(L.plist.bucket_ids)}
+    cid = np.array([c_of[int(x)] for x in b if int(x) in c_of], np.int32)
+    pid = np.array([p_of[int(x)] for x in b if int(x) in p_of], np.int32)
+    v = np.zeros((L.n, 5))
+    oracle.cell_forces(L.moments, L.parts, L.cells, fperiod=L.period, vars=v, bucket_ids=cid,
+                       kind=kind)
+    oracle.part_forces(L.parts, L.parts, L.plist, fperiod=L.period, vars=v, bucket_ids=pid,
+                       kind=kind)
+    rows = np.concatenate([np.arange(L.bucket_starts[x], L.bucket_starts[x] + L.bucket_sizes[x])
+                           for x in b]).astype(np.int32)
+    rows.sort()
+    if ew is not None:
+        ve = oracle.ewald_forces(L.parts, L.root, ew.L, ew.n_reps, ew.fEwCut, ew.dEwhCut, idx=rows,
+                                 kind=kind)
+        v[rows, :4] += ve[:, :4]
+    return v, rows

@@ -53,3 +53,29 @@ def test_ewald_terms_per_particle():
                     hole = max(abs(ix), abs(iy), abs(iz)) <= 1
                     total += hole or x @ x <= 2.6 ** 2
     assert abs(got - total / n) < 1e-12
+
+
+def test_oracle_sample_rows_are_complete(built):
+    """bench.py's CPU baseline evaluates a sample of buckets; the rows it
+    reports for the parity check hold the whole evaluation (cell list,
+    particle list and Ewald term) of their particles: equal to the oracle run
+    over every bucket."""
+    sys.path.insert(0, ROOT)
+    import bench
+    import oracle
+    from changa_gb300 import gravity, ics, tree
+    p = ics.lattice_grf(10, ics.rng_for(1))
+    L = tree.build_lists(p["pos"], p["mass"], p["soft"], n_bucket=16, theta=0.7, period=1.0)
+    ew = gravity.EwaldConfig(1.0, 1, 2.6, 2.8)
+    full = oracle.cell_forces(L.moments, L.parts, L.cells, fperiod=1.0)
+    full = oracle.part_forces(L.parts, L.parts, L.plist, fperiod=1.0, vars=full)
+    full = oracle.ewald_forces(L.parts, L.root, 1.0, 1, 2.6, 2.8, vars=full)
+    _, v, rows = bench.run_cpu(L, ew, L.interactions / 3, kind_pref="port", want_vars=True)
+    assert 0 < len(rows) < L.n
+    np.testing.assert_allclose(v[rows, :4], full[rows, :4], rtol=1e-12, atol=1e-14)
+    np.testing.assert_array_equal(v[rows, 4], full[rows, 4])
+    par = bench.parity_block(L, v, rows, full, full * (1 + 1e-7), "port")
+    assert par["fp64_vs_oracle_max"] < 1e-12
+    assert abs(par["mixed_vs_oracle"]["median"] - 1e-7) < 1e-9
+    acc = bench.accuracy_block(L, rows[:200], full, full, full[rows[:200]])
+    assert acc["mixed_rel"]["max"] == 0.0 and len(acc["mixed_rel_by_force_quartile"]) == 4

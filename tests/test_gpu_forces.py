@@ -484,3 +484,29 @@ def test_tma_wait_timeout_reports_error(plummer):
         lib.changa_gb300_set_test_wait_limit(-1)
         lib.changa_gb300_set_list_variant(k, saved)
         lib.changa_gb300_last_error()
+
+
+def test_dropin_chunked_upload(plummer, lattice):
+    """A drop-in request whose list is longer than two upload chunks streams
+    its list in chunks on the copy stream, each chunk's buckets launched as
+    the chunk lands.  Every bucket is still evaluated by one warp with the
+    same arithmetic, so the result equals the single-upload result bit for
+    bit (cell and particle lists, with Ewald on the lattice); with the
+    completion hook counting, each request still signals once."""
+    lib = N.cuda_lib()
+    for L, ew in ((plummer[0], None), (lattice[0], lattice[1])):
+        inp = gravity.DropInInputs(L, ew)
+        try:
+            whole = gravity.dropin_step(inp).copy()
+            n_entries = min(L.cells.n_entries, L.plist.n_entries)
+            # chunks of ~1/5 of the shorter list: both requests take the chunked path
+            chunk = max(4096, n_entries * 8 // 5)
+            lib.changa_gb300_set_host_chunk_bytes(chunk)
+            try:
+                chunked = gravity.dropin_step(inp).copy()
+            finally:
+                lib.changa_gb300_set_host_chunk_bytes(512 << 20)
+        finally:
+            inp.free()
+        assert n_entries * 8 > 2 * chunk
+        np.testing.assert_array_equal(chunked, whole)

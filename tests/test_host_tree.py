@@ -50,3 +50,35 @@ def test_range_moments_match_host(small_tree):
         ref = t.moments[i, 1:]
         scale = np.array([1, M, 1, 1, 1] + [max(q.trace(), 1e-300)] * 6)
         np.testing.assert_allclose(got / scale, ref / scale, rtol=0, atol=1e-12)
+
+
+def test_concat_systems_shifts_indices():
+    """The batched request of several systems: each system's buckets keep
+    their entries, with source indices shifted by the system's first moment
+    (cells) or particle (particles) and targets by its first particle."""
+    from changa_gb300 import ics, tree
+    rng = ics.rng_for(9)
+    systems = []
+    for n in (300, 1000, 77):
+        p = ics.plummer(n, rng, soft=0.02)
+        systems.append(tree.build_lists(p["pos"], p["mass"], p["soft"], n_bucket=8, theta=0.6))
+    B = tree.concat_systems(systems)
+    assert B.n == sum(s.n for s in systems)
+    assert B.interactions == sum(s.interactions for s in systems)
+    p_off = np.cumsum([0] + [s.n for s in systems])
+    m_off = np.cumsum([0] + [s.moments.shape[0] for s in systems])
+    for kind, off in (("cells", m_off), ("plist", p_off)):
+        R = getattr(B, kind)
+        b0 = 0
+        for k, s in enumerate(systems):
+            r = getattr(s, kind)
+            for j in range(r.n_buckets):
+                lo, hi = R.markers[b0 + j], R.markers[b0 + j + 1]
+                got = R.list[lo:hi]
+                want = r.list[r.markers[j]:r.markers[j + 1]]
+                np.testing.assert_array_equal(got[:, 0], want[:, 0] + off[k])
+                np.testing.assert_array_equal(got[:, 1], want[:, 1])
+                assert R.starts[b0 + j] == r.starts[j] + p_off[k]
+                assert R.sizes[b0 + j] == r.sizes[j]
+            b0 += r.n_buckets
+        assert b0 == R.n_buckets
