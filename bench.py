@@ -281,7 +281,9 @@ def run_cpu(lists, ewald, target, kind_pref="auto", reps=1, want_vars=False):
                      "%s), FP64, OpenMP over buckets, best of %d" %
                      (len(set(cid.tolist()) | set(pid.tolist())), tot,
                       " + Ewald on their %d particles" % len(rows) if ewald else "", reps),
-           "seconds": dt}
+           "seconds": dt,
+           "note": "scalar FP64 restatement of gravity.h/Ewald.cpp (the reference's CMK_SSE "
+                   "vector path needs its absent SSE-Double.h), one OpenMP thread per core"}
     if want_vars:
         return out, v, rows
     return out
@@ -356,20 +358,27 @@ def accuracy_block(lists, samp, v_mixed, v64, dsum):
 
 
 def fp32_peak_tflops():
-    """FP32 FMA peak: SMs x 128 lanes x 2 FLOP x max SM clock."""
+    """FP32 FMA peak, measured on this GPU (changa_gb300_fp32_fma_peak: every
+    SM running independent fma.rn.f32 chains, best of 5), with the derived
+    figure SMs x 128 lanes x 2 FLOP x max SM clock beside it."""
+    import ctypes as C
+
     import torch
+    from changa_gb300 import _native as N
     sms = torch.cuda.get_device_properties(0).multi_processor_count
-    mhz, src = None, None
+    mhz = None
     p = os.path.join(ROOT, "MEASURED_PEAKS.json")
     if os.path.exists(p):
         with open(p) as f:
-            mp = json.load(f)
-        mhz = mp.get("sm_max_mhz")
-        src = "%d SMs x 128 FP32 lanes x 2 x sm_max_mhz %.0f (MEASURED_PEAKS.json)" % (sms, mhz)
-    if mhz is None:
-        mhz = 2070.0
-        src = "%d SMs x 128 FP32 lanes x 2 x 2070 MHz (nominal max clock)" % sms
-    return sms * 128 * 2 * mhz * 1e6 / 1e12, src
+            mhz = json.load(f).get("sm_max_mhz")
+    derived = sms * 128 * 2 * (mhz or 2070.0) * 1e6 / 1e12
+    got = C.c_double(0.0)
+    rc = N.cuda_lib().changa_gb300_fp32_fma_peak(C.byref(got))
+    if rc == 0 and got.value > 0:
+        return got.value, ("measured: changa_gb300_fp32_fma_peak, %d SMs x 8 blocks x 256 threads "
+                           "of independent fma.rn.f32 chains, best of 5 (derived %d x 128 x 2 x "
+                           "%.0f MHz = %.1f TFLOP/s)" % (sms, sms, mhz or 2070.0, derived))
+    return derived, "derived: %d SMs x 128 FP32 lanes x 2 x %.0f MHz" % (sms, mhz or 2070.0)
 
 
 def traffic_from_profiles():
@@ -526,7 +535,7 @@ def measure_device_pipeline(wl, pts, interactions, reps=3):
     return best
 
 
-def measure_hexadecapole(wl, pts, samp=None, dsum=None, steps=5):
+def measure_hexadecapole(wl, pts, samp=None, dsum=None, steps=5, fp64_steps=1):
     """ChaNGa's default build on the same particles: the hexadecapole lists
     (host tree and walk, order 4) evaluated in the FP32-mixed form with the
     hexadecapole Ewald term; same timing rules as the headline (warm-up, a
@@ -578,6 +587,24 @@ def measure_hexadecapole(wl, pts, samp=None, dsum=None, steps=5):
         e = np.linalg.norm(v[:, :3] - dsum[:, :3], axis=1) / np.linalg.norm(dsum[:, :3], axis=1)
         out.update({"median_rel_force_err_vs_direct": float(np.median(e)),
                     "p99_rel_force_err_vs_direct": float(np.percentile(e, 99))})
+    if fp64_steps > 0:
+        # the FP64 form of the same build (its denominator), one warm step timed
+        ds.step("fp64")
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        flush.fill_(1.0)
+        e0.record(stream)
+        for _ in range(fp64_steps):
+            ds.step("fp64")
+        e1.record(stream)
+        torch.cuda.synchronize()
+        ms64 = e0.elapsed_time(e1) / fp64_steps
+        out.update({"fp64_ms_per_step": ms64, "fp64_interactions_per_s": I / (ms64 / 1e3),
+                    "mixed_over_fp64": ms64 / ms})
+        if samp is not None and dsum is not None:
+            v = ds.vars.cpu().numpy()[samp]
+            e = np.linalg.norm(v[:, :3] - dsum[:, :3], axis=1) / np.linalg.norm(dsum[:, :3], axis=1)
+            out["fp64_median_rel_force_err_vs_direct"] = float(np.median(e))
     del ds, L
     torch.cuda.empty_cache()
     return out

@@ -191,6 +191,7 @@ CUDA_SIGNATURES = {
     "changa_gb300_set_validate": (None, [_I]),
     "changa_validate_request": (_I, [_VP, _LL, _VP, _VP, _VP, _I, _LL, _LL]),
     "changa_gb300_version": (_I, []),
+    "changa_gb300_fp32_fma_peak": (_I, [C.POINTER(C.c_double)]),
     "changa_gb300_kernel_launches": (C.c_ulonglong, []),
     "changa_gb300_set_timing": (None, [_I]),
     "changa_gb300_set_host_chunk_bytes": (None, [_SZ]),

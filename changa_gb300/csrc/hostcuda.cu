@@ -371,6 +371,24 @@ static int run_request(CudaRequest* r, bool cell, const void* sources, long long
 static std::mutex g_basic_mu;
 static std::unordered_map<void*, cudaStream_t> g_basic_streams;
 
+/* FP32 FMA throughput probe: every thread runs 8 independent dependent
+ * chains of scalar fma.rn.f32 (the multiplier and addend keep the values
+ * bounded); 2 FLOP per FMA.  The result is written so nothing is dropped. */
+__global__ void fma_probe_kernel(float* out, int iters) {
+  float x[8];
+#pragma unroll
+  for (int k = 0; k < 8; ++k) x[k] = 1e-3f * (float)(threadIdx.x + k);
+  const float m = 0.999f, c = 1e-3f;
+  for (int i = 0; i < iters; ++i) {
+#pragma unroll
+    for (int k = 0; k < 8; ++k) x[k] = fmaf(x[k], m, c);
+  }
+  float s = 0.f;
+#pragma unroll
+  for (int k = 0; k < 8; ++k) s += x[k];
+  out[blockIdx.x * blockDim.x + threadIdx.x] = s;
+}
+
 }  // namespace chg
 
 using namespace chg;
@@ -727,6 +745,36 @@ const char* changa_gb300_error_string(int code) {
 void changa_gb300_set_completion_hook(changa_completion_hook hook) { g_hook.store(hook); }
 void changa_gb300_set_validate(int on) { g_validate.store(on); }
 int changa_gb300_version(void) { return 100; }
+
+/* Measures the device's FP32 FMA peak: a grid of 8 blocks of 256 threads
+ * per SM running fma_probe_kernel, timed with events (best of 5 after a
+ * warm-up), in TFLOP/s. */
+int changa_gb300_fp32_fma_peak(double* tflops) {
+  if (!tflops) return record_error(CHANGA_E_INVALID_ARG, "fp32_fma_peak", __FILE__, __LINE__);
+  const int threads = 256, blocks = sm_count() * 8, iters = 1 << 14;
+  float* out = nullptr;
+  cudaEvent_t e0 = nullptr, e1 = nullptr;
+  CHG_CUDA(cudaMalloc(&out, (size_t)blocks * threads * sizeof(float)));
+  cudaError_t e = cudaEventCreate(&e0);
+  if (e == cudaSuccess) e = cudaEventCreate(&e1);
+  float best = 0.f;
+  for (int rep = 0; rep < 6 && e == cudaSuccess; ++rep) {
+    cudaEventRecord(e0, 0);
+    fma_probe_kernel<<<blocks, threads>>>(out, iters);
+    cudaEventRecord(e1, 0);
+    e = cudaEventSynchronize(e1);
+    float ms = 0.f;
+    if (e == cudaSuccess) e = cudaEventElapsedTime(&ms, e0, e1);
+    if (e == cudaSuccess && rep > 0 && (best == 0.f || ms < best)) best = ms;
+  }
+  if (e0) cudaEventDestroy(e0);
+  if (e1) cudaEventDestroy(e1);
+  cudaFree(out);
+  if (e != cudaSuccess) return record_error((int)e, "fp32_fma_peak", __FILE__, __LINE__);
+  const double flop = 2.0 * 8.0 * (double)iters * (double)blocks * threads;
+  *tflops = flop / (best * 1e-3) / 1e12;
+  return 0;
+}
 unsigned long long changa_gb300_kernel_launches(void) { return g_launches.load(); }
 
 void changa_gb300_set_timing(int on) { g_timing.store(on); }

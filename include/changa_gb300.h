@@ -64,6 +64,12 @@ int changa_validate_request(const ILCell *list, long long n_entries, const int *
 
 int changa_gb300_version(void);
 
+/* Measures the current device's FP32 FMA throughput (TFLOP/s, 2 FLOP per
+ * fma.rn.f32, every SM busy): the roofline denominator of the list kernels,
+ * whose bound is the FP32 FMA pipe.  Synchronous; allocates a small
+ * buffer. */
+int changa_gb300_fp32_fma_peak(double *tflops);
+
 /* Number of kernels this library has launched since load (all forms). */
 unsigned long long changa_gb300_kernel_launches(void);
 
