@@ -58,7 +58,7 @@ def parse():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default="nfw8m")
     ap.add_argument("--fp64-steps", type=int, default=2)
-    ap.add_argument("--e2e-steps", type=int, default=3)
+    ap.add_argument("--e2e-steps", type=int, default=5)
     ap.add_argument("--cpu-sample", type=float, default=1.5e10,
                     help="interactions in the bounded CPU sample")
     ap.add_argument("--no-cpu", action="store_true")
@@ -226,8 +226,18 @@ def measure_dropin(lists, ew, interactions, steps):
             t1 = time.perf_counter()
             step()
             tt.append(time.perf_counter() - t1)
-        t = sum(tt) / len(tt)
+        t = sorted(tt)[len(tt) // 2]  # median step
+        # where the time goes: the drop-in kernels of one more step, by events
+        lib.changa_gb300_set_timing(1)
+        for k in N.KERNEL_IDS:
+            N.kernel_time(k)
+        t1 = time.perf_counter()
+        step()
+        t_one = time.perf_counter() - t1
+        kt = {k: N.kernel_time(k)[0] for k in ("list_f32_cell", "list_f32_part", "ewald_f32")}
+        lib.changa_gb300_set_timing(0)
         return {"value": interactions / t, "unit": "interactions/s", "ms_per_step": 1e3 * t,
+                "kernel_ms_one_step": kt, "timed_step_ms": 1e3 * t_one,
                 "h2d_bytes_per_step": int(inp.h2d_bytes), "d2h_bytes_per_step": int(inp.d2h_bytes),
                 "form": "FP32 (the reference's arithmetic on its ABI structs)",
                 "api": "DataManagerTransferLocalTree, TreePieceCellListDataTransferLocal, "
@@ -700,22 +710,29 @@ def timed_steps(step, steps, stream, flush):
     return [a.elapsed_time(b) for a, b in evs]
 
 
-def measure_e2e(lists, ew, stream, steps, world):
+def measure_e2e(lists, ew, stream, steps, world, runs=None):
     """End to end through changa_gravity_step_host with pinned host buffers:
     the upload of every input and the read-back of the result are inside
-    the timed region (wall clock per step, after one untimed step)."""
+    the timed region (wall clock per step, after one untimed step).  With
+    runs (a tree.PartRuns of the particle lists) the call is
+    changa_gravity_step_host_runs and the particle lists travel as runs."""
     import ctypes as C
 
     import numpy as np
     from changa_gb300 import _native as N
     from changa_gb300 import gravity
     lib = N.cuda_lib()
-    pin = {k: gravity.PinnedArray(a) for k, a in (
-        ("moments", lists.moments), ("parts", lists.parts),
-        ("cl", lists.cells.list), ("cm", lists.cells.markers), ("cs", lists.cells.starts),
-        ("cz", lists.cells.sizes), ("pl", lists.plist.list), ("pm", lists.plist.markers),
-        ("ps", lists.plist.starts), ("pz", lists.plist.sizes))}
+    arrays = [("moments", lists.moments), ("parts", lists.parts),
+              ("cl", lists.cells.list), ("cm", lists.cells.markers), ("cs", lists.cells.starts),
+              ("cz", lists.cells.sizes), ("pm", lists.plist.markers), ("ps", lists.plist.starts),
+              ("pz", lists.plist.sizes)]
+    if runs is None:
+        arrays.append(("pl", lists.plist.list))
+    else:
+        arrays += [("pr", runs.runs), ("prm", runs.run_markers)]
+    pin = {k: gravity.PinnedArray(a) for k, a in arrays}
     out = gravity.PinnedArray(np.zeros((lists.n, 5)))
+    h2d = sum(int(a.nbytes) for _, a in arrays)
 
     def req(l, m, s, z, r):
         q = N.ChangaListRequest()
@@ -723,18 +740,23 @@ def measure_e2e(lists, ew, stream, steps, world):
         q.n_buckets, q.n_entries = r.n_buckets, r.n_entries
         return q
     cq = req("cl", "cm", "cs", "cz", lists.cells)
-    pq = req("pl", "pm", "ps", "pz", lists.plist)
+    if runs is None:
+        pq = req("pl", "pm", "ps", "pz", lists.plist)
+    else:
+        pq = N.ChangaPartRuns()
+        pq.runs, pq.run_markers = pin["pr"].ptr, pin["prm"].ptr
+        pq.markers, pq.starts, pq.sizes = pin["pm"].ptr, pin["ps"].ptr, pin["pz"].ptr
+        pq.n_buckets, pq.n_runs = runs.n_buckets, runs.n_runs
     ep = ew.params(lists.root) if ew else None
     sh = stream.cuda_stream
+    fn = lib.changa_gravity_step_host if runs is None else lib.changa_gravity_step_host_runs
 
     def one():
         # overwrite: the result replaces out (no host zeroing, no vars upload)
-        rc = lib.changa_gravity_step_host(N.CHANGA_FORM_MIXED | N.CHANGA_STEP_OVERWRITE,
-                                          pin["moments"].ptr,
-                                          lists.moments.shape[0], pin["parts"].ptr, lists.n,
-                                          C.byref(cq), C.byref(pq), float(lists.period),
-                                          C.byref(ep) if ep else None, out.ptr, sh)
-        N.check(rc, "changa_gravity_step_host")
+        rc = fn(N.CHANGA_FORM_MIXED | N.CHANGA_STEP_OVERWRITE, pin["moments"].ptr,
+                lists.moments.shape[0], pin["parts"].ptr, lists.n, C.byref(cq), C.byref(pq),
+                float(lists.period), C.byref(ep) if ep else None, out.ptr, sh)
+        N.check(rc, fn.__name__)
     try:
         one()
         tt = []
@@ -742,23 +764,27 @@ def measure_e2e(lists, ew, stream, steps, world):
             t1 = time.perf_counter()
             one()
             tt.append(time.perf_counter() - t1)
-        result = out.array.copy() if hasattr(out, "array") else None
+        result = out.array.copy()
     finally:
         for a in list(pin.values()) + [out]:
             a.free()
-    t_e2e = max_over_ranks(world, sum(tt) / len(tt))
-    h2d = (lists.moments.nbytes + lists.parts.nbytes + lists.cells.list.nbytes +
-           lists.cells.markers.nbytes + lists.cells.starts.nbytes + lists.cells.sizes.nbytes +
-           lists.plist.list.nbytes + lists.plist.markers.nbytes + lists.plist.starts.nbytes +
-           lists.plist.sizes.nbytes)
+    t_e2e = max_over_ranks(world, sorted(tt)[len(tt) // 2])  # median step
     I = lists.interactions
+    api = ("changa_gravity_step_host (include/changa_gb300.h), pinned host buffers, "
+           "CHANGA_STEP_OVERWRITE; lists uploaded in 512 MiB chunks (halving toward the end) on a "
+           "copy stream overlapping the list kernels; each chunk's particles read back on a "
+           "second copy stream once final")
+    if runs is not None:
+        api = ("changa_gravity_step_host_runs (include/changa_gb300.h): as "
+               "changa_gravity_step_host, with the particle lists as runs (ILPart, 12 B per run of "
+               "consecutive source particles, %d runs for %d entries) expanded on the device "
+               "chunk by chunk" % (runs.n_runs, lists.plist.n_entries))
     return {"value": sum_over_ranks(world, float(I)) / t_e2e, "unit": "interactions/s",
             "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(lists.parts.nbytes),
-            "ms_per_step": 1e3 * t_e2e,
-            "api": "changa_gravity_step_host (include/changa_gb300.h), pinned host "
-                   "buffers, CHANGA_STEP_OVERWRITE; lists uploaded in 512 MiB chunks (halving "
-                   "toward the end) on a copy stream overlapping the list kernels; each "
-                   "chunk's particles read back on a second copy stream once final"}, result
+            "ms_per_step": 1e3 * t_e2e, "ms_steps": [round(1e3 * x, 3) for x in tt],
+            "timing": "wall clock per call (each call returns with the results in host "
+                      "memory), median of the steps after one untimed call",
+            "api": api}, result
 
 
 def main_ours(args):
@@ -874,18 +900,27 @@ def main_ours(args):
                                        "p99": hexa["p99_rel_force_err_vs_direct"]}
     pts = None
 
-    # end to end through the public C-ABI with pinned host buffers
+    # end to end through the public C-ABI with pinned host buffers: the
+    # particle lists as runs (the headline), and as flat lists
     e2e = None
     if args.e2e_steps > 0:
-        e2e, r = measure_e2e(lists, ew, stream, args.e2e_steps, world)
-        if r is not None:  # the same evaluation as the device-resident step
-            e2e["max_rel_force_diff_vs_device_step"] = float(rel_err(r, v_mixed).max())
+        from changa_gb300 import tree as T
+        runs = T.part_runs(lists.plist)
+        e2e, r = measure_e2e(lists, ew, stream, args.e2e_steps, world, runs=runs)
+        e2e["max_rel_force_diff_vs_device_step"] = float(rel_err(r, v_mixed).max())
+        del runs
+        flat, r = measure_e2e(lists, ew, stream, args.e2e_steps, world)
+        e2e["flat_lists"] = {"value": flat["value"], "ms_per_step": flat["ms_per_step"],
+                             "h2d_bytes_per_step": flat["h2d_bytes_per_step"],
+                             "max_rel_force_diff_vs_device_step":
+                                 float(rel_err(r, v_mixed).max()),
+                             "api": flat["api"]}
 
     dropin = None
     if args.e2e_steps > 0 and getattr(lists, "order", 2) == 2 and not batched:
         dropin = measure_dropin(lists, ew, I, args.e2e_steps)
         if e2e is not None and "ms_per_step" in dropin:
-            dropin["over_e2e_ms"] = dropin["ms_per_step"] / e2e["ms_per_step"]
+            dropin["over_e2e_flat_ms"] = dropin["ms_per_step"] / e2e["flat_lists"]["ms_per_step"]
 
     # roofline of the dominant kernel (FP32-mixed cell lists) and the P-P kernel.
     # The bound is the FP32 FMA pipe (no tensor-core or HBM bound applies:

@@ -107,6 +107,12 @@ class ChangaListRequest(C.Structure):
                 ("sizes", C.c_void_p), ("n_buckets", C.c_int), ("n_entries", C.c_longlong)]
 
 
+class ChangaPartRuns(C.Structure):
+    _fields_ = [("runs", C.c_void_p), ("run_markers", C.c_void_p), ("markers", C.c_void_p),
+                ("starts", C.c_void_p), ("sizes", C.c_void_p), ("n_buckets", C.c_int),
+                ("n_runs", C.c_longlong)]
+
+
 class ChangaTreeView(C.Structure):
     _fields_ = [("geom", C.c_void_p), ("bbox", C.c_void_p), ("info", C.c_void_p),
                 ("parent", C.c_void_p), ("n_nodes", C.c_longlong), ("bucket_node", C.c_void_p),
@@ -215,6 +221,9 @@ CUDA_SIGNATURES = {
     "changa_gravity_step_host": (_I, [_I, _VP, _LL, _VP, _LL, C.POINTER(ChangaListRequest),
                                       C.POINTER(ChangaListRequest), _D,
                                       C.POINTER(ChangaEwaldParams), _VP, _VP]),
+    "changa_gravity_step_host_runs": (_I, [_I, _VP, _LL, _VP, _LL, C.POINTER(ChangaListRequest),
+                                           C.POINTER(ChangaPartRuns), _D,
+                                           C.POINTER(ChangaEwaldParams), _VP, _VP]),
     "changa_gravity_graph_create": (_VP, [_I, _VP, _LL, _VP, _LL, C.POINTER(ChangaListRequest),
                                          C.POINTER(ChangaListRequest), _D,
                                          C.POINTER(ChangaEwaldParams), _VP, _I]),
@@ -236,6 +245,7 @@ CUDA_SIGNATURES = {
     "changa_walk_lists_free": (None, [C.POINTER(ChangaWalkLists)]),
     "changa_walk_set_pool_factor": (None, [_D]),
     "changa_walk_set_test_small_stack": (None, [C.c_int]),
+    "changa_walk_set_groups": (None, [C.c_int, C.c_int]),
     "changa_walk_stack_reruns": (C.c_longlong, []),
     "changa_gravity_step_hexa": (_I, [_I, _VP, _LL, _VP, _LL, C.POINTER(ChangaListRequest),
                                       C.POINTER(ChangaListRequest),

@@ -251,9 +251,14 @@ static int run_request_chunked(CudaRequest* r, bool cell, const void* sources, l
                                long long n_tgt, int nb, long long per, cudaStream_t c) {
   cudaStream_t s = r->stream;
   ReqDev d;
+  /* the block is allocated and its small arrays uploaded on the copy
+   * stream, so this request's upload does not wait for the work already on
+   * the request's stream (a previous request's kernels); each kernel waits
+   * for its chunk's copy, which follows the allocation on the copy stream */
   int rc = upload_request(r->list, r->numInteractions, r->bucketMarkers, r->bucketStarts,
-                          r->bucketSizes, nb, s, d, /*copy_list=*/false);
+                          r->bucketSizes, nb, c, d, /*copy_list=*/false);
   if (rc) return rc;
+  d.stream = s;  // released on the request's stream, after its kernels
   ChangaListRequest h;  // the host arrays, for the chunk boundaries
   h.list = (const ILCell*)r->list;
   h.markers = r->bucketMarkers;
@@ -270,10 +275,7 @@ static int run_request_chunked(CudaRequest* r, bool cell, const void* sources, l
     if (x != cudaSuccess) return x;
     return cudaEventRecord(*ev, on);
   };
-  cudaEvent_t ready = nullptr;
-  cudaError_t e = mark(s, &ready);  // the block is allocated on s
-  if (e == cudaSuccess) e = cudaStreamWaitEvent(c, ready, 0);
-  if (ready) cudaEventDestroy(ready);
+  cudaError_t e = cudaSuccess;
   const ILCell* hl = (const ILCell*)r->list;
   for (size_t i = 0; i < chunks.size() && e == cudaSuccess; ++i) {
     const int b0 = chunks[i].first, b1 = chunks[i].second;
@@ -846,6 +848,90 @@ static int check_req(const ChangaListRequest* r) {
   return 0;
 }
 
+/* Host particle runs: pointers present, run markers rising from 0 to at
+ * most n_runs and flat markers rising from 0 (the copies and chunk bounds
+ * read the host arrays through them). */
+static int check_runs(const ChangaPartRuns* r) {
+  if (!r || r->n_buckets < 0 || r->n_runs < 0) return CHANGA_E_INVALID_ARG;
+  if (r->n_buckets == 0) return 0;
+  if (!r->run_markers || !r->markers || !r->starts || !r->sizes || (r->n_runs > 0 && !r->runs))
+    return CHANGA_E_INVALID_ARG;
+  if (r->run_markers[0] != 0 || r->markers[0] != 0) return CHANGA_E_INVALID_ARG;
+  for (int b = 0; b < r->n_buckets; ++b)
+    if (r->run_markers[b + 1] < r->run_markers[b] || r->markers[b + 1] < r->markers[b])
+      return CHANGA_E_INVALID_ARG;
+  if (r->run_markers[r->n_buckets] > r->n_runs) return CHANGA_E_INVALID_ARG;
+  return 0;
+}
+
+/* Particle runs into flat entries: bucket b (of nb; the marker pointers
+ * start at the chunk's first bucket) owns runs [rm[b], rm[b+1]) and flat
+ * entries [fm[b], fm[b+1]); run {index, off, num} becomes num entries
+ * {index + k, off}, k = 0 .. num-1.  One warp per bucket: the lanes take 32
+ * runs, an exclusive scan places them, and each write of 32 entries finds
+ * its run by a binary search over the lanes' inclusive ends.  Runs past
+ * n_runs are not read; writes outside the bucket's flat range or past
+ * n_flat are dropped. */
+__global__ void expand_runs_kernel(const ILPart* __restrict__ runs, long long n_runs,
+                                   const int* __restrict__ rm, const int* __restrict__ fm, int nb,
+                                   ILCell* __restrict__ flat, long long n_flat) {
+  const int lane = threadIdx.x & 31;
+  const unsigned full = 0xffffffffu;
+  const long long warps = (long long)gridDim.x * (blockDim.x >> 5);
+  for (long long b = (long long)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); b < nb;
+       b += warps) {
+    const long long r0 = rm[b] > 0 ? rm[b] : 0;
+    const long long r1 = (long long)rm[b + 1] < n_runs ? (long long)rm[b + 1] : n_runs;
+    long long pos = fm[b];
+    const long long end = (long long)fm[b + 1] < n_flat ? (long long)fm[b + 1] : n_flat;
+    for (long long rb = r0; rb < r1; rb += 32) {
+      const long long r = rb + lane;
+      ILPart run = {0, 0, 0};
+      if (r < r1) run = runs[r];
+      const int num = run.num > 0 ? (run.num < (1 << 25) ? run.num : (1 << 25)) : 0;
+      int incl = num;
+#pragma unroll
+      for (int o = 1; o < 32; o <<= 1) {
+        const int y = __shfl_up_sync(full, incl, o);
+        if (lane >= o) incl += y;
+      }
+      const int total = __shfl_sync(full, incl, 31);
+      const int excl = incl - num;
+      for (int j0 = 0; j0 < total; j0 += 32) {
+        const int j = j0 + lane;
+        int owner = 0;
+#pragma unroll
+        for (int bit = 16; bit > 0; bit >>= 1)
+          if (__shfl_sync(full, incl, owner + bit - 1) <= j) owner += bit;
+        const int o_excl = __shfl_sync(full, excl, owner);
+        const int o_index = __shfl_sync(full, run.index, owner);
+        const int o_off = __shfl_sync(full, run.off, owner);
+        const long long q = pos + j;
+        if (j < total && q >= 0 && q < end) {
+          ILCell c;
+          c.index = o_index + (j - o_excl);
+          c.offsetID = o_off;
+          flat[q] = c;
+        }
+      }
+      pos += total;
+    }
+  }
+}
+
+static cudaError_t launch_expand_runs(const ILPart* runs, long long n_runs, const int* rm,
+                                      const int* fm, int nb, ILCell* flat, long long n_flat,
+                                      cudaStream_t s) {
+  if (nb <= 0) return cudaSuccess;
+  long long blocks = ((long long)nb + 7) / 8;
+  const long long cap = (long long)sm_count() * 16;
+  if (blocks > cap) blocks = cap;
+  TimingScope ts(kKidPack, s);
+  expand_runs_kernel<<<(int)blocks, 256, 0, s>>>(runs, n_runs, rm, fm, nb, flat, n_flat);
+  count_launch();
+  return cudaGetLastError();
+}
+
 /* One list evaluation over device-resident inputs (FP64 or mixed form). */
 static int run_fp(int form, bool cell, const void* src, long long n_src, const void* tgt,
                   long long n_tgt, const ChangaListRequest* req, double fperiod, double* vars,
@@ -1095,18 +1181,31 @@ static std::pair<long long, long long> target_range(const ChangaListRequest* r, 
  * second copy stream as soon as its kernel is done (every other
  * contribution to those particles is ordered before it), so the read-back
  * overlaps the remaining uploads. */
-int changa_gravity_step_host(int form, const double* moments, long long n_moments,
-                             const double* parts, long long n_parts, const ChangaListRequest* cells,
-                             const ChangaListRequest* plist, double fperiod,
-                             const ChangaEwaldParams* ewald, double* vars, cudaStream_t s) {
+static int step_host_impl(int form, const double* moments, long long n_moments,
+                          const double* parts, long long n_parts, const ChangaListRequest* cells,
+                          const ChangaListRequest* plist, const ChangaPartRuns* pruns,
+                          double fperiod, const ChangaEwaldParams* ewald, double* vars,
+                          cudaStream_t s) {
   const bool overwrite = (form & CHANGA_STEP_OVERWRITE) != 0;
   form &= ~CHANGA_STEP_OVERWRITE;
   if (form != CHANGA_FORM_FP64 && form != CHANGA_FORM_MIXED)
     return record_error(CHANGA_E_INVALID_ARG, "gravity_step_host: form", __FILE__, __LINE__);
   if (!moments || !parts || !vars || n_moments < 0 || n_parts < 0)
     return record_error(CHANGA_E_INVALID_ARG, "gravity_step_host: arrays", __FILE__, __LINE__);
-  if ((cells && check_req(cells)) || (plist && check_req(plist)))
+  if ((cells && check_req(cells)) || (plist && check_req(plist)) || (pruns && check_runs(pruns)))
     return record_error(CHANGA_E_INVALID_ARG, "gravity_step_host: requests", __FILE__, __LINE__);
+  /* particle lists as runs: a host view of the flat request they expand to
+   * (markers, starts and sizes; the flat entries exist only on the device) */
+  ChangaListRequest pview;
+  if (pruns) {
+    pview.list = nullptr;
+    pview.markers = pruns->markers;
+    pview.starts = pruns->starts;
+    pview.sizes = pruns->sizes;
+    pview.n_buckets = pruns->n_buckets;
+    pview.n_entries = pruns->n_buckets > 0 ? pruns->markers[pruns->n_buckets] : 0;
+    plist = &pview;
+  }
   if (ewald && ewald->nEwhLoop > CHANGA_MAX_EWH)
     return record_error(CHANGA_E_TOO_LARGE, "gravity_step_host: nEwhLoop", __FILE__, __LINE__);
   prepare_pool();
@@ -1125,10 +1224,18 @@ int changa_gravity_step_host(int form, const double* moments, long long n_moment
   for (int k = 0; k < 2; ++k)
     if (reqs[k] && reqs[k]->n_buckets > 0) last = k;
   std::vector<std::pair<int, int>> chunks[2];
+  ChangaListRequest rview;  // the runs' own CSR, for chunking the run uploads
   for (int k = 0; k < 2; ++k) {
     const ChangaListRequest* r = reqs[k];
     if (!r || r->n_buckets == 0) continue;
-    list_chunks(r, (long long)(kChunkBytes / sizeof(ILCell)), k == last, chunks[k]);
+    if (k == 1 && pruns) {
+      rview = pview;
+      rview.markers = pruns->run_markers;
+      rview.n_entries = pruns->n_runs;
+      list_chunks(&rview, (long long)(kChunkBytes / sizeof(ILPart)), k == last, chunks[k]);
+    } else {
+      list_chunks(r, (long long)(kChunkBytes / sizeof(ILCell)), k == last, chunks[k]);
+    }
   }
 
   /* one device block: FP64 inputs, packed inputs, requests, queue counters */
@@ -1150,6 +1257,13 @@ int changa_gravity_step_host(int form, const double* moments, long long n_moment
       off[k][j] = total;
       total += align256(sz[k][j]);
     }
+  }
+  size_t roff = 0, rmoff = 0;  // runs and their markers (pruns only)
+  if (pruns) {
+    roff = total;
+    total += align256((size_t)pruns->n_runs * sizeof(ILPart));
+    rmoff = total;
+    total += align256((size_t)(pruns->n_buckets + 1) * sizeof(int));
   }
   const size_t qoff = total;
   total += 256;
@@ -1191,6 +1305,9 @@ int changa_gravity_step_host(int form, const double* moments, long long n_moment
       for (int j = 1; j < 4 && e == cudaSuccess; ++j)
         e = cudaMemcpyAsync(block + off[k][j], src[j - 1], sz[k][j], cudaMemcpyHostToDevice, c);
     }
+    if (e == cudaSuccess && pruns && pruns->n_buckets > 0)
+      e = cudaMemcpyAsync(block + rmoff, pruns->run_markers,
+                          (size_t)(pruns->n_buckets + 1) * sizeof(int), cudaMemcpyHostToDevice, c);
     if (e != cudaSuccess) break;
     cudaEvent_t small = event(c);
     /* the lists, chunk by chunk */
@@ -1198,6 +1315,17 @@ int changa_gravity_step_host(int form, const double* moments, long long n_moment
     for (int k = 0; k < 2 && e == cudaSuccess; ++k) {
       const ChangaListRequest* r = reqs[k];
       for (auto& ch : chunks[k]) {
+        if (k == 1 && pruns) {
+          const size_t r0 = (size_t)pruns->run_markers[ch.first];
+          const size_t r1 = (size_t)pruns->run_markers[ch.second];
+          if (r1 > r0 &&
+              (e = cudaMemcpyAsync(block + roff + r0 * sizeof(ILPart), pruns->runs + r0,
+                                   (r1 - r0) * sizeof(ILPart), cudaMemcpyHostToDevice, c)) !=
+                  cudaSuccess)
+            break;
+          landed[k].push_back(event(c));
+          continue;
+        }
         const size_t e0 = (size_t)r->markers[ch.first], e1 = (size_t)r->markers[ch.second];
         if (e1 > e0 &&
             (e = cudaMemcpyAsync(block + off[k][0] + e0 * sizeof(ILCell), r->list + e0,
@@ -1265,6 +1393,13 @@ int changa_gravity_step_host(int form, const double* moments, long long n_moment
       for (size_t i = 0; i < chunks[k].size() && !rc && e == cudaSuccess; ++i) {
         if (!landed[k][i] || (e = cudaStreamWaitEvent(s, landed[k][i], 0)) != cudaSuccess) break;
         const int b0 = chunks[k][i].first, b1 = chunks[k][i].second;
+        if (k == 1 && pruns &&
+            (e = launch_expand_runs((const ILPart*)(block + roff), pruns->n_runs,
+                                    (const int*)(block + rmoff) + b0,
+                                    (const int*)(block + off[k][1]) + b0, b1 - b0,
+                                    (ILCell*)(block + off[k][0]), plist->n_entries, s)) !=
+                cudaSuccess)
+          break;
         ChangaListRequest sub;
         sub.list = (const ILCell*)(block + off[k][0]);
         sub.markers = (const int*)(block + off[k][1]) + b0;
@@ -1298,6 +1433,26 @@ int changa_gravity_step_host(int form, const double* moments, long long n_moment
   if (e != cudaSuccess) return record_error((int)e, "gravity_step_host", __FILE__, __LINE__);
   if (tma_launches() != tma_before) return changa_gb300_device_status();
   return 0;
+}
+
+
+int changa_gravity_step_host(int form, const double* moments, long long n_moments,
+                             const double* parts, long long n_parts, const ChangaListRequest* cells,
+                             const ChangaListRequest* plist, double fperiod,
+                             const ChangaEwaldParams* ewald, double* vars, cudaStream_t s) {
+  return step_host_impl(form, moments, n_moments, parts, n_parts, cells, plist, nullptr, fperiod,
+                        ewald, vars, s);
+}
+
+int changa_gravity_step_host_runs(int form, const double* moments, long long n_moments,
+                                  const double* parts, long long n_parts,
+                                  const ChangaListRequest* cells, const ChangaPartRuns* pruns,
+                                  double fperiod, const ChangaEwaldParams* ewald, double* vars,
+                                  cudaStream_t s) {
+  if (!pruns)
+    return record_error(CHANGA_E_INVALID_ARG, "gravity_step_host_runs: runs", __FILE__, __LINE__);
+  return step_host_impl(form, moments, n_moments, parts, n_parts, cells, nullptr, pruns, fperiod,
+                        ewald, vars, s);
 }
 
 int changa_ewald_forces(int form, const double* parts, long long n_parts, const int* idx,

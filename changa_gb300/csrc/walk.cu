@@ -89,6 +89,22 @@ struct WalkArgs {
   const struct WalkNode* nodes;
   const float4* boxf;   // 2 n_nodes: {lesser.xyz, 0}, {greater.xyz, 0}
   float period32;
+  /* two-phase walk.  Groups: nodes whose subtree holds few buckets (each
+   * bucket in exactly one group, the group node on its chain).  Phase 1
+   * walks a group node's chain once for all its buckets: its units are the
+   * groups (group_node), the counts/offsets/lists above are the group's
+   * prefix lists (entries accepted against the shared local nodes) and
+   * entries still undecided at the group node go to the frontier.  Phase 2
+   * walks each bucket from its group's frontier, after copying the group's
+   * prefix lists into its own. */
+  const int* group_node;     // n_groups
+  int n_groups;
+  const int* bucket_group;   // n_buckets: group of each bucket
+  int* n_front;              // phase 1 count pass: frontier entries per group
+  const long long* off_front;  // phase 1 fill pass: frontier offsets; phase 2: CSR over groups
+  int2* front;               // phase 1 fill pass output, phase 2 input: {node, replica code}
+  const long long* pre_off[2];  // phase 2: CSR over groups of the prefix cells / particles
+  const int2* pre[2];
 };
 
 /* What the traversal reads of a source node, in one 32-byte record (two
@@ -292,7 +308,10 @@ __device__ __forceinline__ void append_at(const WalkArgs& a, int k, const int* t
   if (c >= 0) a.pool[k][(size_t)c * kChunk + (q - r * kChunk)] = e;
 }
 
-template <int MODE, int STACK>
+/* PHASE 0: the whole walk of each bucket; 1: the shared walk of each group
+ * down to its group node (prefix lists and frontier); 2: each bucket from
+ * its group's frontier, after its group's prefix lists (quadrupole walk). */
+template <int MODE, int STACK, int PHASE>
 __global__ void __launch_bounds__(kWalkWarps * 32) walk_kernel(const WalkArgs a) {
   constexpr bool FILL = MODE == kFill;
   __shared__ int2 stk[kWalkWarps][STACK];
@@ -301,12 +320,15 @@ __global__ void __launch_bounds__(kWalkWarps * 32) walk_kernel(const WalkArgs a)
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const unsigned full = 0xffffffffu;
   const long long bl = ((long long)blockIdx.x * kWalkWarps + warp) * a.bucket_stride;
-  if (bl >= a.n_buckets) return;  // the whole warp
-  const int b = (int)bl;
-  const int bn = a.bucket_node[b];
+  if (bl >= (PHASE == 1 ? (long long)a.n_groups : (long long)a.n_buckets)) return;  // whole warp
+  const int b = (int)bl;  // the unit: a bucket, or a group in phase 1
+  const int bn = PHASE == 1 ? a.group_node[b] : a.bucket_node[b];
   if (bn < 0 || bn >= a.n_nodes) return;
-  /* local nodes from the root down to this bucket */
-  int depth = 0;
+  const int gid = PHASE == 2 ? a.bucket_group[b] : 0;
+  const int gnode = PHASE == 2 ? a.group_node[gid] : -1;
+  /* local nodes from the root down to this unit (and, phase 2, the level
+   * of the bucket's group node on that chain) */
+  int depth = 0, gdepth = -1;
   if (lane == 0) {
     int n = 0;
     for (int x = bn; x >= 0 && x < a.n_nodes && n < 65; x = a.parent[x]) ++n;
@@ -314,48 +336,95 @@ __global__ void __launch_bounds__(kWalkWarps * 32) walk_kernel(const WalkArgs a)
       depth = -1;
     } else {
       int k = n - 1;
-      for (int x = bn; k >= 0; x = a.parent[x]) chain[warp][k--] = x;
+      for (int x = bn; k >= 0; x = a.parent[x]) {
+        if (x == gnode) gdepth = k;
+        chain[warp][k--] = x;
+      }
       depth = chain[warp][0] == 0 ? n - 1 : -1;
     }
   }
   depth = __shfl_sync(full, depth, 0);
-  if (depth < 0) {
+  gdepth = __shfl_sync(full, gdepth, 0);
+  if (depth < 0 || (PHASE == 2 && gdepth < 0)) {
     if (lane == 0) atomicExch(a.error, 1);
     return;
   }
-  long long oc = 0, op = 0, os = 0;
+  /* a group node with children is not a bucket: entries undecided at its
+   * level go to the frontier instead of being opened */
+  const bool unit_bucket = PHASE != 1 || (a.info[4 * (size_t)bn] < 0 && a.info[4 * (size_t)bn + 1] < 0);
+  long long oc = 0, op = 0, os = 0, of = 0;
   if (FILL) {
     oc = a.off_cells[b];
     op = a.off_parts[b];
     os = a.off_soft ? a.off_soft[b] : 0;
+    if (PHASE == 1) of = a.off_front[b];
   }
-  /* the root of every replica on the check list */
-  const int nr = a.n_replicas, side = 2 * nr + 1, nrep = side * side * side;
-  if (nrep > STACK) {  // uniform; the host re-runs the launch with the larger stack
-    if (lane == 0) atomicExch(a.error, 2);
-    return;
+  int sp = 0;
+  long long fpos = 0, fend = 0;  // phase 2: the group's frontier, fed when the stack is empty
+  if (PHASE == 2) {
+    fpos = a.off_front[gid];
+    fend = a.off_front[gid + 1];
+  } else {
+    /* the root of every replica on the check list */
+    const int nr = a.n_replicas, side = 2 * nr + 1, nrep = side * side * side;
+    if (nrep > STACK) {  // uniform; the host re-runs the launch with the larger stack
+      if (lane == 0) atomicExch(a.error, 2);
+      return;
+    }
+    for (int r = lane; r < nrep; r += 32) {
+      const int x = r / (side * side) - nr, y = (r / side) % side - nr, z = r % side - nr;
+      stk[warp][r] = make_int2(0, (x + 3) | ((y + 3) << 3) | ((z + 3) << 6));
+    }
+    sp = nrep;
   }
-  for (int r = lane; r < nrep; r += 32) {
-    const int x = r / (side * side) - nr, y = (r / side) % side - nr, z = r % side - nr;
-    stk[warp][r] = make_int2(0, (x + 3) | ((y + 3) << 3) | ((z + 3) << 6));
-  }
-  int sp = nrep;
-  long long nc = 0, np = 0, ns = 0;
+  long long nc = 0, np = 0, ns = 0, nf = 0;
   int na[3] = {0, 0, 0};  // append pass: chunks taken per list
+  if (PHASE == 2) {
+    /* the group's prefix lists (entries accepted against the local nodes
+     * the group walk covered, the same for every bucket of the group) */
+#pragma unroll
+    for (int k = 0; k < 2; ++k) {
+      const long long p0 = a.pre_off[k][gid], cnt = a.pre_off[k][gid + 1] - p0;
+      long long& n_k = k == 0 ? nc : np;
+      if (MODE != kCount) {
+        for (long long j0 = 0; j0 < cnt; j0 += 32) {
+          const int tot = (int)(cnt - j0 < 32 ? cnt - j0 : 32);
+          if (MODE == kAppend) ensure_chunks(a, k, b, ctab[warp][k], na[k], n_k + j0, tot);
+          if (lane < tot) {
+            const int2 e = a.pre[k][p0 + j0 + lane];
+            if (FILL) (k == 0 ? a.cells[oc + n_k + j0 + lane] : a.parts[op + n_k + j0 + lane]) = e;
+            if (MODE == kAppend) append_at(a, k, ctab[warp][k], n_k + j0 + lane, e);
+          }
+        }
+      }
+      n_k += cnt;
+    }
+  }
   __syncwarp();
-  while (sp > 0) {
-    const int n = sp < 32 ? sp : 32;
-    const int top = sp - n;
+  while (sp > 0 || fpos < fend) {
+    int n;
     int2 e = make_int2(-1, 0);
-    if (lane < n) e = stk[warp][top + lane];
-    sp = top;
+    if (sp > 0) {
+      n = sp < 32 ? sp : 32;
+      const int top = sp - n;
+      if (lane < n) e = stk[warp][top + lane];
+      sp = top;
+    } else {  // phase 2: the next frontier entries, tested one level below the group node
+      n = (int)(fend - fpos < 32 ? fend - fpos : 32);
+      if (lane < n) {
+        const int2 f = a.front[fpos + lane];
+        e = make_int2(f.x, ((gdepth + 1) << 16) | (f.y & 0xffff));
+      }
+      fpos += n;
+    }
     __syncwarp();  // popped before anything is pushed over them
-    /* kind: 0 cell, 1 softened cell, 2 particles, 3 open, 4 defer, -1 none */
+    /* kind: 0 cell, 1 softened cell, 2 particles, 3 open, 4 defer, 5 frontier
+     * (phase 1: undecided at the group node), -1 none */
     int kind = -1, c0 = -1, c1 = -1, pfirst = 0, pcount = 0;
     const int g = e.x, level = e.y >> 16, code = e.y & 0xffff;
-    if (g >= 0 && g < a.n_nodes) {  // memory safety
+    if (g >= 0 && g < a.n_nodes && level <= depth) {  // memory safety
       const int local = chain[warp][level];
-      const bool local_bucket = level == depth;
+      const bool local_bucket = level == depth && unit_bucket;
       const WalkNode nd = a.nodes[g];
       const int open = open_criterion_screened(a, nd, g, local, local_bucket, code);
       if (open == 0) {
@@ -377,7 +446,7 @@ __global__ void __launch_bounds__(kWalkWarps * 32) walk_kernel(const WalkArgs a)
         c0 = nd.link.x;
         c1 = nd.link.y;
       } else {
-        kind = 4;
+        kind = level == depth ? 5 : 4;  // 5 only in phase 1 (level == depth is a bucket otherwise)
       }
     }
     /* pushes, in lane order; within a lane child 1 below child 0 */
@@ -436,6 +505,11 @@ __global__ void __launch_bounds__(kWalkWarps * 32) walk_kernel(const WalkArgs a)
         }
       }
     }
+    if (PHASE == 1) {
+      const unsigned mf = __ballot_sync(full, kind == 5);
+      if (FILL && kind == 5) a.front[of + nf + __popc(mf & below)] = make_int2(g, code);
+      nf += __popc(mf);
+    }
     nc += __popc(mc);
     ns += __popc(ms);
     np += tpart;
@@ -446,6 +520,7 @@ __global__ void __launch_bounds__(kWalkWarps * 32) walk_kernel(const WalkArgs a)
     a.n_cells[i] = (int)nc;
     a.n_parts[i] = (int)np;
     if (a.n_soft) a.n_soft[i] = (int)ns;
+    if (PHASE == 1) a.n_front[i] = (int)nf;
   }
 }
 
@@ -547,6 +622,75 @@ __global__ void scan_apply_kernel(const int* __restrict__ in, int n, const long 
   }
 }
 
+/* ---- groups for the two-phase walk ---- */
+
+/* First particle of each bucket (buckets are numbered in particle order,
+ * so the array rises). */
+__global__ void bucket_first_kernel(const int* __restrict__ bucket_node, const int* __restrict__ info,
+                                    long long n_nodes, int nb, int* __restrict__ bfirst) {
+  for (long long b = blockIdx.x * (long long)blockDim.x + threadIdx.x; b < nb;
+       b += (long long)gridDim.x * blockDim.x) {
+    const int x = bucket_node[b];
+    bfirst[b] = (x >= 0 && x < n_nodes) ? info[4 * (size_t)x + 2] : 0;
+  }
+}
+
+/* Buckets whose first particle lies in [lo, hi): the buckets of the node
+ * covering those particles. */
+__device__ __forceinline__ int buckets_in(const int* bfirst, int nb, int lo, int hi) {
+  int a0 = 0, a1 = nb;  // first index with bfirst >= lo
+  while (a0 < a1) {
+    const int m = (a0 + a1) >> 1;
+    if (bfirst[m] < lo) a0 = m + 1; else a1 = m;
+  }
+  int b0 = a0, b1 = nb;  // first index with bfirst >= hi
+  while (b0 < b1) {
+    const int m = (b0 + b1) >> 1;
+    if (bfirst[m] < hi) b0 = m + 1; else b1 = m;
+  }
+  return b0 - a0;
+}
+
+/* Each bucket's group node: its highest ancestor whose subtree holds at
+ * most gmax buckets (the bucket itself when its parent's holds more). */
+__global__ void bucket_group_node_kernel(const int* __restrict__ bucket_node,
+                                         const int* __restrict__ parent, const int* __restrict__ info,
+                                         const int* __restrict__ bfirst, long long n_nodes, int nb,
+                                         int gmax, int* __restrict__ gn) {
+  for (long long b = blockIdx.x * (long long)blockDim.x + threadIdx.x; b < nb;
+       b += (long long)gridDim.x * blockDim.x) {
+    int x = bucket_node[b];
+    for (int up = 0; up < 64 && x >= 0 && x < n_nodes; ++up) {
+      const int q = parent[x];
+      if (q < 0 || q >= n_nodes) break;
+      const int lo = info[4 * (size_t)q + 2], cnt = info[4 * (size_t)q + 3];
+      if (buckets_in(bfirst, nb, lo, lo + cnt) > gmax) break;
+      x = q;
+    }
+    gn[b] = x;
+  }
+}
+
+/* 1 where a run of buckets with the same group node starts. */
+__global__ void group_flag_kernel(const int* __restrict__ gn, int nb, int* __restrict__ flag) {
+  for (long long b = blockIdx.x * (long long)blockDim.x + threadIdx.x; b < nb;
+       b += (long long)gridDim.x * blockDim.x)
+    flag[b] = (b == 0 || gn[b] != gn[b - 1]) ? 1 : 0;
+}
+
+/* Group id of every bucket and the node of every group, from the
+ * exclusive scan of the flags. */
+__global__ void group_ids_kernel(const int* __restrict__ gn, const int* __restrict__ flag,
+                                 const long long* __restrict__ excl, int nb,
+                                 int* __restrict__ bucket_group, int* __restrict__ group_node) {
+  for (long long b = blockIdx.x * (long long)blockDim.x + threadIdx.x; b < nb;
+       b += (long long)gridDim.x * blockDim.x) {
+    const int gid = (int)(flag[b] ? excl[b] : excl[b] - 1);
+    bucket_group[b] = gid;
+    if (flag[b]) group_node[gid] = gn[b];
+  }
+}
+
 }  // namespace
 }  // namespace chg
 
@@ -600,12 +744,20 @@ static int walk_setup(const ChangaTreeView* t, const ChangaWalkParams* p, WalkAr
 static std::atomic<int> g_test_small_stack{0};
 static std::atomic<long long> g_stack_reruns{0};  // launches re-run with the large stack
 
-template <int STACK>
-static void walk_launch_mode(const WalkArgs& a, int mode, int grid, cudaStream_t s) {
-  if (mode == kFill) walk_kernel<kFill, STACK><<<grid, kWalkWarps * 32, 0, s>>>(a);
-  else if (mode == kAppend) walk_kernel<kAppend, STACK><<<grid, kWalkWarps * 32, 0, s>>>(a);
-  else walk_kernel<kCount, STACK><<<grid, kWalkWarps * 32, 0, s>>>(a);
+template <int STACK, int PHASE>
+static void walk_launch_phase(const WalkArgs& a, int mode, int grid, cudaStream_t s) {
+  if (mode == kFill) walk_kernel<kFill, STACK, PHASE><<<grid, kWalkWarps * 32, 0, s>>>(a);
+  else if (mode == kAppend && PHASE != 1)
+    walk_kernel<(PHASE != 1 ? kAppend : kCount), STACK, PHASE><<<grid, kWalkWarps * 32, 0, s>>>(a);
+  else walk_kernel<kCount, STACK, PHASE><<<grid, kWalkWarps * 32, 0, s>>>(a);
   count_launch();
+}
+
+template <int STACK>
+static void walk_launch_mode(const WalkArgs& a, int mode, int phase, int grid, cudaStream_t s) {
+  if (phase == 1) walk_launch_phase<STACK, 1>(a, mode, grid, s);
+  else if (phase == 2) walk_launch_phase<STACK, 2>(a, mode, grid, s);
+  else walk_launch_phase<STACK, 0>(a, mode, grid, s);
 }
 
 /* One traversal.  The per-warp stack of kWarpStack entries keeps the
@@ -614,11 +766,13 @@ static void walk_launch_mode(const WalkArgs& a, int mode, int grid, cudaStream_t
  * runs once more with kWarpStackLarge entries (every output of a launch is
  * rewritten by the re-run: per-bucket counts and entries, and in append
  * mode the pools, whose counters are reset first). */
-static void walk_run(const WalkArgs& a, int mode, cudaStream_t s) {
-  const long long warps = ((long long)a.n_buckets + a.bucket_stride - 1) / a.bucket_stride;
+static void walk_run(const WalkArgs& a, int mode, cudaStream_t s, int phase = 0) {
+  const long long units = phase == 1 ? a.n_groups : a.n_buckets;
+  const long long warps = (units + a.bucket_stride - 1) / a.bucket_stride;
   const int grid = (int)((warps + kWalkWarps - 1) / kWalkWarps);
-  if (g_test_small_stack.load()) walk_launch_mode<64>(a, mode, grid, s);
-  else walk_launch_mode<kWarpStack>(a, mode, grid, s);
+  if (grid <= 0) return;
+  if (g_test_small_stack.load()) walk_launch_mode<64>(a, mode, phase, grid, s);
+  else walk_launch_mode<kWarpStack>(a, mode, phase, grid, s);
   int h = 0;
   if (cudaMemcpyAsync(&h, a.error, sizeof(int), cudaMemcpyDeviceToHost, s) != cudaSuccess ||
       cudaStreamSynchronize(s) != cudaSuccess || h != 2)
@@ -627,7 +781,7 @@ static void walk_run(const WalkArgs& a, int mode, cudaStream_t s) {
   if (mode == kAppend && a.pool_next &&
       cudaMemsetAsync(a.pool_next, 0, 64, s) != cudaSuccess)  // pool counters, overflow flag
     return;
-  walk_launch_mode<kWarpStackLarge>(a, mode, grid, s);
+  walk_launch_mode<kWarpStackLarge>(a, mode, phase, grid, s);
   g_stack_reruns.fetch_add(1);
 }
 
@@ -693,6 +847,16 @@ extern "C" void changa_walk_set_pool_factor(double f) { g_pool_factor.store(f > 
 
 extern "C" void changa_walk_set_test_small_stack(int on) { g_test_small_stack.store(on ? 1 : 0); }
 
+/* Two-phase walk: groups of at most g_group_max buckets, for quadrupole
+ * walks of at least g_group_min buckets (0 turns it off). */
+static std::atomic<int> g_group_max{32};
+static std::atomic<int> g_group_min{4096};
+
+extern "C" void changa_walk_set_groups(int max_buckets, int min_tree_buckets) {
+  g_group_max.store(max_buckets > 0 ? max_buckets : 0);
+  g_group_min.store(min_tree_buckets > 0 ? min_tree_buckets : 0);
+}
+
 extern "C" long long changa_walk_stack_reruns(void) { return g_stack_reruns.load(); }
 
 static void release_lists(ChangaWalkLists* out) {
@@ -749,6 +913,95 @@ extern "C" int changa_walk(const ChangaTreeView* t, const ChangaWalkParams* p,
   if (!cnt || !ts || !off || !ctr)
     return finish(record_error(cudaErrorMemoryAllocation, "walk: memory", __FILE__, __LINE__));
   int h_err = 0;
+  /* Quadrupole walks of many buckets run in two phases.  Phase 1 walks each
+   * group's node once: its chain down to the group node is shared by all
+   * the group's buckets, so the entries accepted on it (the group's prefix
+   * lists) and those still undecided at the group node (its frontier) are
+   * the same for each of them.  Phase 2 walks each bucket from its group's
+   * frontier, its lists starting with the group's prefix. */
+  int phase = 0;
+  const int gmax = g_group_max.load();
+  if (p->order == 2 && gmax > 0 && g_group_min.load() > 0 && nb >= g_group_min.load()) {
+    int* bfirst = (int*)alloc((size_t)nb * sizeof(int));
+    int* gn = (int*)alloc((size_t)nb * sizeof(int));
+    int* flag = (int*)alloc((size_t)nb * sizeof(int));
+    long long* gex = (long long*)alloc((size_t)(nb + 1) * sizeof(long long));
+    int* gex32 = (int*)alloc((size_t)(nb + 1) * sizeof(int));
+    int* bucket_group = (int*)alloc((size_t)nb * sizeof(int));
+    int* group_node = (int*)alloc((size_t)nb * sizeof(int));
+    if (!bfirst || !gn || !flag || !gex || !gex32 || !bucket_group || !group_node)
+      return finish(record_error(cudaErrorMemoryAllocation, "walk: memory", __FILE__, __LINE__));
+    const long long gb = ((long long)nb + 255) / 256, cap = (long long)sm_count() * 8;
+    const int grid = (int)(gb < cap ? gb : cap);
+    bucket_first_kernel<<<grid, 256, 0, s>>>(t->bucket_node, t->info, t->n_nodes, nb, bfirst);
+    bucket_group_node_kernel<<<grid, 256, 0, s>>>(t->bucket_node, t->parent, t->info, bfirst,
+                                                  t->n_nodes, nb, gmax, gn);
+    group_flag_kernel<<<grid, 256, 0, s>>>(gn, nb, flag);
+    scan_tile_sums_kernel<<<tiles, kScanThreads, 0, s>>>(flag, nb, ts);
+    scan_tiles_kernel<<<1, kScanThreads, 0, s>>>(ts, tiles);
+    scan_apply_kernel<<<tiles, kScanThreads, 0, s>>>(flag, nb, ts, gex, gex32);
+    group_ids_kernel<<<grid, 256, 0, s>>>(gn, flag, gex, nb, bucket_group, group_node);
+    count_launch(7);
+    long long ng_ll = 0;
+    if (cudaMemcpyAsync(&ng_ll, gex + nb, sizeof(long long), cudaMemcpyDeviceToHost, s) !=
+            cudaSuccess ||
+        cudaStreamSynchronize(s) != cudaSuccess || ng_ll <= 0 || ng_ll > nb)
+      return finish(record_error((int)cudaGetLastError(), "walk: groups", __FILE__, __LINE__));
+    const int ng = (int)ng_ll;
+    int* gcnt = (int*)alloc((size_t)3 * ng * sizeof(int));
+    long long* goff = (long long*)alloc((size_t)3 * (ng + 1) * sizeof(long long));
+    int* goff32 = (int*)alloc((size_t)3 * (ng + 1) * sizeof(int));
+    if (!gcnt || !goff || !goff32)
+      return finish(record_error(cudaErrorMemoryAllocation, "walk: memory", __FILE__, __LINE__));
+    a.group_node = group_node;
+    a.n_groups = ng;
+    a.bucket_group = bucket_group;
+    a.n_cells = gcnt;
+    a.n_parts = gcnt + ng;
+    a.n_soft = nullptr;
+    a.n_front = gcnt + 2 * (size_t)ng;
+    walk_run(a, kCount, s, 1);
+    const int gtiles = (ng + kScanTile - 1) / kScanTile;
+    for (int k = 0; k < 3; ++k) {
+      scan_tile_sums_kernel<<<gtiles, kScanThreads, 0, s>>>(gcnt + (size_t)k * ng, ng, ts);
+      scan_tiles_kernel<<<1, kScanThreads, 0, s>>>(ts, gtiles);
+      scan_apply_kernel<<<gtiles, kScanThreads, 0, s>>>(gcnt + (size_t)k * ng, ng, ts,
+                                                        goff + (size_t)k * (ng + 1),
+                                                        goff32 + (size_t)k * (ng + 1));
+      count_launch(3);
+    }
+    long long gtot[3] = {0, 0, 0};
+    for (int k = 0; k < 3; ++k)
+      cudaMemcpyAsync(&gtot[k], goff + (size_t)k * (ng + 1) + ng, sizeof(long long),
+                      cudaMemcpyDeviceToHost, s);
+    cudaMemcpyAsync(&h_err, a.error, sizeof(int), cudaMemcpyDeviceToHost, s);
+    if (cudaStreamSynchronize(s) != cudaSuccess)
+      return finish(record_error((int)cudaGetLastError(), "walk: group count", __FILE__, __LINE__));
+    if (h_err) return finish(walk_error(h_err));
+    int2* pre_cells = (int2*)alloc((size_t)(gtot[0] > 0 ? gtot[0] : 1) * sizeof(int2));
+    int2* pre_parts = (int2*)alloc((size_t)(gtot[1] > 0 ? gtot[1] : 1) * sizeof(int2));
+    int2* front = (int2*)alloc((size_t)(gtot[2] > 0 ? gtot[2] : 1) * sizeof(int2));
+    if (!pre_cells || !pre_parts || !front)
+      return finish(record_error(cudaErrorMemoryAllocation, "walk: memory", __FILE__, __LINE__));
+    a.off_cells = goff;
+    a.off_parts = goff + (ng + 1);
+    a.off_soft = nullptr;
+    a.off_front = goff + 2 * (size_t)(ng + 1);
+    a.cells = pre_cells;
+    a.parts = pre_parts;
+    a.soft = nullptr;
+    a.front = front;
+    walk_run(a, kFill, s, 1);
+    /* phase 2 reads the group outputs */
+    a.pre_off[0] = goff;
+    a.pre_off[1] = goff + (ng + 1);
+    a.pre[0] = pre_cells;
+    a.pre[1] = pre_parts;
+    a.off_cells = a.off_parts = a.off_soft = nullptr;
+    a.cells = a.parts = a.soft = nullptr;
+    a.n_front = nullptr;
+    phase = 2;
+  }
   /* Large trees: one traversal appends the entries into pools of chunks
    * sized from a sampled count (every 16th bucket); small trees (where the
    * sample's fixed costs dominate) count, then fill. */
@@ -763,7 +1016,7 @@ extern "C" int changa_walk(const ChangaTreeView* t, const ChangaWalkParams* p,
     a.n_parts = samp + nsamp;
     a.n_soft = nl == 3 ? samp + 2 * nsamp : nullptr;
     a.bucket_stride = stride;
-    walk_run(a, kCount, s);
+    walk_run(a, kCount, s, phase);
     a.bucket_stride = 1;
     std::vector<int> hs((size_t)nl * nsamp);
     if (cudaMemcpyAsync(hs.data(), samp, hs.size() * sizeof(int), cudaMemcpyDeviceToHost, s) !=
@@ -787,7 +1040,7 @@ extern "C" int changa_walk(const ChangaTreeView* t, const ChangaWalkParams* p,
       a.n_cells = cnt;
       a.n_parts = cnt + nb;
       a.n_soft = nl == 3 ? cnt + 2 * (size_t)nb : nullptr;
-      walk_run(a, kAppend, s);
+      walk_run(a, kAppend, s, phase);
       appended = true;
     } else {
       cudaGetLastError();  // a pool that did not fit: count and fill instead
@@ -797,7 +1050,7 @@ extern "C" int changa_walk(const ChangaTreeView* t, const ChangaWalkParams* p,
     a.n_cells = cnt;
     a.n_parts = cnt + nb;
     a.n_soft = nl == 3 ? cnt + 2 * (size_t)nb : nullptr;
-    walk_run(a, kCount, s);
+    walk_run(a, kCount, s, phase);
   }
   /* offsets (and the int32 markers) of every list */
   for (int k = 0; k < nl; ++k) {
@@ -848,7 +1101,7 @@ extern "C" int changa_walk(const ChangaTreeView* t, const ChangaWalkParams* p,
     a.cells = (int2*)out->list[0];
     a.parts = (int2*)out->list[1];
     a.soft = nl == 3 ? (int2*)out->list[2] : nullptr;
-    walk_run(a, kFill, s);
+    walk_run(a, kFill, s, phase);
     cudaMemcpyAsync(&h_err, a.error, sizeof(int), cudaMemcpyDeviceToHost, s);
   }
   out->passes = appended ? (overflow ? 3 : 1) : 2;

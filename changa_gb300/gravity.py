@@ -153,16 +153,41 @@ def _host_req(req):
     return r
 
 
+def host_runs(pr):
+    """ChangaPartRuns over a tree.PartRuns (host numpy arrays, kept alive by
+    the caller)."""
+    r = N.ChangaPartRuns()
+    r.runs = pr.runs.ctypes.data
+    r.run_markers = pr.run_markers.ctypes.data
+    r.markers = pr.markers.ctypes.data
+    r.starts = pr.starts.ctypes.data
+    r.sizes = pr.sizes.ctypes.data
+    r.n_buckets = pr.n_buckets
+    r.n_runs = pr.n_runs
+    return r
+
+
 def gravity_step_host(lists, form="mixed", ewald: EwaldConfig | None = None, stream=None,
-                      vars=None, overwrite=False):
+                      vars=None, overwrite=False, runs=None):
     """One force evaluation from host arrays; returns vars (N x 5 FP64).
-    Results accumulate into vars unless overwrite (then vars is not read)."""
+    Results accumulate into vars unless overwrite (then vars is not read).
+    With runs (a tree.PartRuns of lists.plist) the particle lists travel as
+    runs (changa_gravity_step_host_runs)."""
     lib = N.cuda_lib()
     if vars is None:
         vars = np.empty((lists.n, 5)) if overwrite else np.zeros((lists.n, 5))
-    cr, pr = _host_req(lists.cells), _host_req(lists.plist)
+    cr = _host_req(lists.cells)
     ep = ewald.params(lists.root) if ewald else None
     f = FORMS[form] | (N.CHANGA_STEP_OVERWRITE if overwrite else 0)
+    if runs is not None:
+        rr = host_runs(runs)
+        rc = lib.changa_gravity_step_host_runs(f, _p(lists.moments), lists.moments.shape[0],
+                                               _p(lists.parts), lists.n, C.byref(cr), C.byref(rr),
+                                               float(lists.period), C.byref(ep) if ep else None,
+                                               _p(vars), stream)
+        N.check(rc, "changa_gravity_step_host_runs")
+        return vars
+    pr = _host_req(lists.plist)
     rc = lib.changa_gravity_step_host(f, _p(lists.moments), lists.moments.shape[0],
                                       _p(lists.parts), lists.n, C.byref(cr), C.byref(pr),
                                       float(lists.period), C.byref(ep) if ep else None, _p(vars),

@@ -178,6 +178,61 @@ def build_lists(pos, mass, soft, n_bucket=16, theta=0.7, period=0.0, n_replicas=
                      order=order, softcells=softcells)
 
 
+@dataclass
+class PartRuns:
+    """A particle request as runs of consecutive source particles: runs (R x
+    3 int32: first particle, offsetID, num; the reference's ILPart) with
+    their per-bucket CSR run_markers, next to the flat request's markers,
+    starts and sizes."""
+    runs: np.ndarray
+    run_markers: np.ndarray
+    markers: np.ndarray
+    starts: np.ndarray
+    sizes: np.ndarray
+
+    @property
+    def n_buckets(self):
+        return int(len(self.starts))
+
+    @property
+    def n_runs(self):
+        return int(self.runs.shape[0])
+
+
+def part_runs(req: ListRequest) -> PartRuns:
+    """Runs of a flat particle request: a run ends where the next entry is
+    not the next particle with the same replica code, or at a bucket's end.
+    Expanding the runs gives back req.list exactly (expand_runs)."""
+    lst = req.list
+    n = lst.shape[0]
+    idx, off = lst[:, 0], lst[:, 1]
+    brk = np.ones(n, dtype=bool)
+    if n > 1:
+        np.not_equal(idx[1:], idx[:-1] + 1, out=brk[1:])
+        brk[1:] |= off[1:] != off[:-1]
+    mk = req.markers.astype(np.int64)
+    brk[mk[:-1][mk[:-1] < n]] = True
+    first = np.flatnonzero(brk)
+    num = np.diff(np.append(first, n))
+    runs = np.empty((len(first), 3), dtype=np.int32)
+    runs[:, 0] = idx[first]
+    runs[:, 1] = off[first]
+    runs[:, 2] = num
+    run_markers = np.searchsorted(first, mk).astype(np.int32)
+    return PartRuns(runs, run_markers, req.markers, req.starts, req.sizes)
+
+
+def expand_runs(pr: PartRuns) -> np.ndarray:
+    """The flat (L x 2) entries of a PartRuns (numpy; the check of part_runs)."""
+    num = pr.runs[:, 2].astype(np.int64)
+    rep = np.repeat(np.arange(len(num)), num)
+    first = np.repeat(np.cumsum(num) - num, num)
+    out = np.empty((int(num.sum()), 2), dtype=np.int32)
+    out[:, 0] = pr.runs[rep, 0] + (np.arange(len(rep)) - first)
+    out[:, 1] = pr.runs[rep, 1]
+    return out
+
+
 def concat_systems(systems):
     """Concatenates independent systems into one TreeLists with one pair of
     requests (list indices and bucket starts shifted), for one batched

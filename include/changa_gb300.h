@@ -208,6 +208,33 @@ int changa_gravity_step(int form, const double *moments, long long n_moments,
  * Returns after the work has finished, so vars is ready on return. */
 #define CHANGA_STEP_OVERWRITE 0x100
 
+/* Particle lists as runs of consecutive source particles, one ILPart
+ * {first source particle, offsetID, num} per run: the form ChaNGa's walk
+ * produces (a source bucket is one run) before the reference flattens it to
+ * one ILCell per particle.  All host arrays.  Bucket b owns runs
+ * [run_markers[b], run_markers[b+1]) and, once expanded, the flat entries
+ * [markers[b], markers[b+1]) (so markers[b+1] - markers[b] is the sum of its
+ * runs' num); starts and sizes as in ChangaListRequest. */
+typedef struct ChangaPartRuns {
+  const ILPart *runs;
+  const int *run_markers;  /* n_buckets + 1 */
+  const int *markers;      /* n_buckets + 1 */
+  const int *starts;
+  const int *sizes;
+  int n_buckets;
+  long long n_runs;
+} ChangaPartRuns;
+
+/* changa_gravity_step_host with the particle lists as runs: each chunk of
+ * runs is uploaded (12 bytes per run instead of 8 per source particle),
+ * expanded into flat entries on the device and evaluated as it lands.  The
+ * same results as the flat lists. */
+int changa_gravity_step_host_runs(int form, const double *moments, long long n_moments,
+                                  const double *parts, long long n_parts,
+                                  const ChangaListRequest *cells, const ChangaPartRuns *pruns,
+                                  double fperiod, const ChangaEwaldParams *ewald, double *vars,
+                                  cudaStream_t stream);
+
 /* List bytes per upload chunk of changa_gravity_step_host and of the
  * drop-in list transfers (default 512 MiB, at least 4 KiB).  A drop-in
  * request whose list exceeds two chunks uploads it chunk by chunk on the
@@ -363,6 +390,13 @@ void changa_walk_set_pool_factor(double factor);
 void changa_walk_set_test_small_stack(int on);
 /* Traversal launches re-run with the large stack so far (in this process). */
 long long changa_walk_stack_reruns(void);
+/* changa_walk of a quadrupole tree with at least min_tree_buckets buckets
+ * walks in two phases: first once per group of at most max_buckets buckets
+ * (the highest node whose subtree holds no more), down to the group node,
+ * which the group's buckets share; then each bucket from the entries still
+ * undecided there.  The lists hold the same entries as the one-phase walk.
+ * Defaults 32 and 4096; 0 for either walks every bucket from the root. */
+void changa_walk_set_groups(int max_buckets, int min_tree_buckets);
 
 /* Tree build on the device (no reference counterpart; restates the host
  * build, TreePiece.cpp:141-165 box and keys, GenericTreeNode.h:473-599

@@ -510,3 +510,26 @@ def test_dropin_chunked_upload(plummer, lattice):
             inp.free()
         assert n_entries * 8 > 2 * chunk
         np.testing.assert_array_equal(chunked, whole)
+
+
+def test_host_entry_particle_runs(plummer, lattice):
+    """changa_gravity_step_host_runs: the particle lists travel as runs
+    (ILPart, 12 bytes per run), are expanded on the device chunk by chunk
+    and evaluated as they land.  The expanded lists are the flat lists, and
+    each bucket is evaluated by one warp in the same order, so the result
+    equals the flat-list entry's bit for bit: both forms, with Ewald on the
+    lattice, with one chunk and with chunks of a few hundred runs."""
+    from changa_gb300 import tree as T
+    lib = N.cuda_lib()
+    for L, ew in ((plummer[0], None), (lattice[0], lattice[1])):
+        pr = T.part_runs(L.plist)
+        for form in ("fp64", "mixed"):
+            flat = gravity.gravity_step_host(L, form, ewald=ew)
+            runs = gravity.gravity_step_host(L, form, ewald=ew, runs=pr)
+            np.testing.assert_array_equal(runs, flat)
+        lib.changa_gb300_set_host_chunk_bytes(4096)  # 341 runs per chunk
+        try:
+            small = gravity.gravity_step_host(L, "mixed", ewald=ew, runs=pr)
+        finally:
+            lib.changa_gb300_set_host_chunk_bytes(512 << 20)
+        np.testing.assert_array_equal(small, gravity.gravity_step_host(L, "mixed", ewald=ew))

@@ -89,9 +89,44 @@ def test_walk_single_traversal_path(cuda_ok):
     finally:
         lib.changa_walk_set_pool_factor(1.2)
     assert tm3["passes"] == 3
+    # this tree takes the two-phase walk: count + fill (one phase) holds the
+    # same entries per bucket in another order; the fill-pass fallback writes
+    # the append pass's arrays
     for k in range(2):
-        assert _identical(one[k], two[k]) and _identical(short[k], two[k])
+        assert _identical(short[k], one[k])
     assert same_entries(L.cells, one[0], nb) and same_entries(L.plist, one[1], nb)
+    assert same_entries(L.cells, two[0], nb) and same_entries(L.plist, two[1], nb)
+
+
+@pytest.mark.parametrize("gmax", [1, 2, 8, 32, 256])
+def test_walk_two_phase(cuda_ok, gmax):
+    """The two-phase walk (each group of at most gmax buckets walked once
+    down to its group node, then each bucket from the group's frontier, its
+    lists starting with the group's prefix lists) gives every bucket the
+    host walk's entries: open and periodic trees (one and two replica
+    shells), small and large buckets, single traversal and count + fill,
+    and the forces of the one-phase lists."""
+    from changa_gb300 import _native as N
+    lib = N.cuda_lib()
+    p = ics.plummer(65536, ics.rng_for(6), soft=0.01)
+    g = ics.lattice_grf(16, ics.rng_for(7))
+    cases = [tree.build_lists(p["pos"], p["mass"], p["soft"], n_bucket=4, theta=0.7),
+             tree.build_lists(p["pos"], p["mass"], p["soft"], n_bucket=32, theta=0.5),
+             tree.build_lists(g["pos"], g["mass"], g["soft"], n_bucket=8, theta=0.7, period=1.0),
+             tree.build_lists(g["pos"], g["mass"], g["soft"], n_bucket=8, theta=0.7, period=1.0,
+                              n_replicas=2)]
+    lib.changa_walk_set_groups(gmax, 1)
+    try:
+        for L in cases:
+            nb = len(L.bucket_starts)
+            for method in ("single", "two_pass"):
+                cells, plist, _ = gpu_walk(L, method=method)
+                assert same_entries(L.cells, cells, nb) and same_entries(L.plist, plist, nb)
+            host = gravity.DeviceSystem(L).step("fp64").cpu().numpy()
+            dev = gravity.DeviceSystem(L, device_reqs=[cells, plist]).step("fp64").cpu().numpy()
+            assert force_rel_err(dev, host).max() < 1e-12
+    finally:
+        lib.changa_walk_set_groups(32, 4096)
 
 
 def test_walk_stack_rerun(cuda_ok):

@@ -82,3 +82,22 @@ def test_concat_systems_shifts_indices():
                 assert R.sizes[b0 + j] == r.sizes[j]
             b0 += r.n_buckets
         assert b0 == R.n_buckets
+
+
+def test_part_runs_round_trip():
+    """Particle lists as runs (the reference's ILPart form): expanding the
+    runs gives the flat list back entry for entry, every run stays inside its
+    bucket, and runs are far fewer than entries."""
+    from changa_gb300 import ics, tree
+    p = ics.plummer(8000, ics.rng_for(3), soft=0.02)
+    g = ics.lattice_grf(12, ics.rng_for(4))
+    for q, period in ((p, 0.0), (g, 1.0)):
+        L = tree.build_lists(q["pos"], q["mass"], q["soft"], n_bucket=16, theta=0.7,
+                             period=period)
+        pr = tree.part_runs(L.plist)
+        np.testing.assert_array_equal(tree.expand_runs(pr), L.plist.list)
+        rm = pr.run_markers.astype(np.int64)
+        assert rm[0] == 0 and rm[-1] == pr.n_runs and np.all(np.diff(rm) >= 0)
+        per_bucket = np.add.reduceat(pr.runs[:, 2].astype(np.int64), rm[:-1]) * (np.diff(rm) > 0)
+        np.testing.assert_array_equal(per_bucket, np.diff(L.plist.markers.astype(np.int64)))
+        assert pr.n_runs * 4 < L.plist.n_entries
