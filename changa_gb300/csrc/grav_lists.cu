@@ -673,14 +673,12 @@ struct Variant {
   int tp;  // 0 source-parallel, 1 target-parallel (list_kernel_tp), 2 paired (list_kernel_tp2),
            // 3 paired with TMA-staged cell records (list_kernel_tma; FP32-mixed cell lists,
            //   list_kernel_tp2 for the others), 4 register-blocked paired (list_kernel_rb,
-           //   group = the most targets per lane), 5 register-blocked paired staged in rounds
-           //   (list_kernel_rb2, group = 16 x most targets per lane + most blocks per round)
+           //   group = the most targets per lane)
 };
 constexpr Variant kVariants[] = {{2, 16, 0}, {3, 16, 0}, {4, 16, 0}, {3, 32, 0}, {2, 32, 0},
                                  {2, 0, 1},  {3, 0, 1},  {4, 0, 1},  {2, 0, 2},  {3, 0, 2},
                                  {4, 0, 2},  {2, 0, 3},  {1, 0, 3},  {2, 3, 4},  {2, 2, 4},
-                                 {3, 2, 4},  {1, 3, 4},  {2, 3 * 16 + 4, 5}, {2, 2 * 16 + 3, 5},
-                                 {2, 3 * 16 + 6, 5}, {1, 3 * 16 + 3, 5}};
+                                 {3, 2, 4},  {1, 3, 4}};
 constexpr int kNumVariants = sizeof(kVariants) / sizeof(kVariants[0]);
 
 /* Source-parallel list kernel of the FP32 forms.  Per warp and bucket: the
@@ -2031,407 +2029,6 @@ __global__ void __launch_bounds__(kThreads, MINB) list_kernel_rb(const ListArgs 
 }
 
 /* ------------------------------------------------------------------ */
-/* Register-blocked paired kernel staged in rounds: R targets per lane  */
-/* (as list_kernel_rb), and per round gb blocks of 32 entries staged at */
-/* once, so a group of lanes takes a whole block of 16 pairs and each   */
-/* lane still runs 16 pair steps per round whatever R is.  The records  */
-/* of the next round travel to shared memory by cp.async while the      */
-/* current round computes, so the gather latency hides behind a round's */
-/* arithmetic and no record waits in registers.  Shape per chunk of nt  */
-/* targets: c = ceil(nt / R) slots of R targets, G = 32 / c groups, gb  */
-/* = min(G, GMAX) blocks per round and gp = G / gb groups per block     */
-/* (taking the pairs p, p + gp, ...).                                   */
-/* ------------------------------------------------------------------ */
-
-struct RbShape {
-  int r, c, gb, gp;
-};
-
-/* The shape with the most useful pair steps per lane step, nt gb /
- * (R ceil(16 / gp)); ties keep the smaller R. */
-template <int RMAX, int GMAX>
-__device__ __forceinline__ RbShape rb2_shape(int nt) {
-  RbShape best{1, nt, 1, 1};
-  int bn = -1, bd = 1;  // best value as the fraction bn / bd
-#pragma unroll
-  for (int r = 1; r <= RMAX; ++r) {
-    const int c = (nt + r - 1) / r, G = 32 / c;
-    const int gb = G < GMAX ? G : GMAX, gp = G / gb;
-    const int n = nt * gb, d = r * ((16 + gp - 1) / gp);
-    if (n * bd > bn * d) {
-      bn = n;
-      bd = d;
-      best = RbShape{r, c, gb, gp};
-    }
-  }
-  return best;
-}
-
-/* Per-warp shared memory of list_kernel_rb2 (bytes). */
-template <int FORM, bool CELL, int GMAX>
-struct Rb2Smem {
-  using RW = RawWords<FORM, CELL>;
-  static constexpr int kW = RW::kWords;
-  static constexpr int kPW = CELL ? 6 : 2;
-  static constexpr size_t kRaw4 = RW::kWide ? (size_t)GMAX * kW * 32 * sizeof(float4) : 0;
-  static constexpr size_t kRaw1 = RW::kWide ? 0 : (size_t)GMAX * kW * 32 * sizeof(float);
-  static constexpr size_t kStage = (size_t)GMAX * 16 * kPW * sizeof(float4);
-  static constexpr size_t kRed = 5 * 32 * sizeof(double);
-  static constexpr size_t kSoft = (size_t)GMAX * 32 * sizeof(float);
-  static constexpr size_t kCodes = (size_t)GMAX * 32 * sizeof(int);
-  static constexpr size_t kWarpBytes = kRaw4 + kRaw1 + kStage + kRed + kSoft + kCodes;
-};
-
-template <int FORM, bool CELL, int R, int GMAX>
-__device__ __forceinline__ void rb2_chunk(const ListArgs& a, const int lane, const int e_begin,
-                                          const int e_end, const long long tb, const int nt,
-                                          const RbShape sh, const float3 chi, const float3 clo,
-                                          char* wsm) {
-  using SM = Rb2Smem<FORM, CELL, GMAX>;
-  constexpr int kW = SM::kW, PW = SM::kPW;
-  /* this warp's shared memory: records of the round, staged pairs, partial
-   * sums, softenings and replica codes */
-  float4* rb4 = reinterpret_cast<float4*>(wsm);
-  float* rb1 = reinterpret_cast<float*>(wsm + SM::kRaw4);
-  float4* stage = reinterpret_cast<float4*>(wsm + SM::kRaw4 + SM::kRaw1);
-  double(*red)[32] = reinterpret_cast<double(*)[32]>(wsm + SM::kRaw4 + SM::kRaw1 + SM::kStage);
-  float* ssoft = reinterpret_cast<float*>(wsm + SM::kRaw4 + SM::kRaw1 + SM::kStage + SM::kRed);
-  int* codes =
-      reinterpret_cast<int*>(wsm + SM::kRaw4 + SM::kRaw1 + SM::kStage + SM::kRed + SM::kSoft);
-
-  const int c = sh.c, gb = sh.gb, gp = sh.gp;
-  const int G = gb * gp;
-  const int g = lane / c, s = lane - g * c;
-  const bool active = g < G;
-  const int jb = g % gb, po = g / gb;  // this group's block and first pair
-
-  RbTarget T[R];
-  float tsm = 0.f;
-  float3 blo = make_float3(3.4e38f, 3.4e38f, 3.4e38f), bhi = make_float3(-3.4e38f, -3.4e38f, -3.4e38f);
-#pragma unroll
-  for (int k = 0; k < R; ++k) {
-    const int t = s + k * c;
-    T[k].valid = active && t < nt;
-    const long long ti = tb + (T[k].valid ? t : 0);
-    float tx, ty, tz, tmass, tsoft;
-    if constexpr (FORM == kF32) {
-      const CompactPartData* p = static_cast<const CompactPartData*>(a.tgt) + ti;
-      tmass = __ldg(&p->mass);
-      tsoft = __ldg(&p->soft);
-      tx = __ldg(&p->position.x);
-      ty = __ldg(&p->position.y);
-      tz = __ldg(&p->position.z);
-    } else {
-      const float4* p = static_cast<const float4*>(a.tgt) + kPartPackF4 * ti;
-      const float4 h = __ldg(p), l = __ldg(p + 1);
-      tx = (h.x - chi.x) + (l.x - clo.x);
-      ty = (h.y - chi.y) + (l.y - clo.y);
-      tz = (h.z - chi.z) + (l.z - clo.z);
-      tmass = h.w;
-      tsoft = l.w;
-    }
-    if (T[k].valid) {
-      tsm = fmaxf(tsm, tsoft);
-      blo = make_float3(fminf(blo.x, tx), fminf(blo.y, ty), fminf(blo.z, tz));
-      bhi = make_float3(fmaxf(bhi.x, tx), fmaxf(bhi.y, ty), fmaxf(bhi.z, tz));
-    }
-    const float tms = CELL ? -tmass : tmass;
-    T[k].x2 = pk2(tx, tx);
-    T[k].y2 = pk2(ty, ty);
-    T[k].z2 = pk2(tz, tz);
-    T[k].m2 = pk2(tms, tms);
-    T[k].soft = tsoft;
-  }
-  const float tsmax = warp_max(tsm);
-  blo = make_float3(warp_min(blo.x), warp_min(blo.y), warp_min(blo.z));
-  bhi = make_float3(warp_max(bhi.x), warp_max(bhi.y), warp_max(bhi.z));
-
-  RbSums S[R];
-#pragma unroll
-  for (int k = 0; k < R; ++k) S[k] = RbSums{0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
-
-  const int W = 32 * gb;  // entries per round
-  /* the copies of the round starting at entry r0 (entries past the list
-   * are marked by code -1 and not fetched) */
-  auto issue = [&](int r0) {
-#pragma unroll
-    for (int j = 0; j < GMAX; ++j) {
-      if (j < gb) {
-        const int e = r0 + 32 * j + lane;
-        int code = -1;
-        if (e < e_end) {
-          const int2 ent = __ldg(a.list + e);
-          long long idx = ent.x;
-          if ((unsigned long long)idx >= (unsigned long long)a.n_src) idx = 0;  // memory safety
-          code = (ent.y >> 22) & 0x1ff;
-          fetch_source<FORM, CELL>(a, idx, rb4 + j * kW * 32, rb1 + j * kW * 32, lane);
-        }
-        codes[j * 32 + lane] = code;
-      }
-    }
-    cp_commit();
-  };
-  issue(e_begin);
-  for (int e0 = e_begin; e0 < e_end; e0 += W) {
-    cp_wait<0>();
-    __syncwarp();
-    /* each lane's record of every block of the round into its half of
-     * pair lane / 2 of that block */
-    bool far_all = true;
-    float near2 = 0.f;  // this group's block
-#pragma unroll
-    for (int j = 0; j < GMAX; ++j) {
-      if (j < gb) {
-        const int code = codes[j * 32 + lane];
-        const bool valid = code >= 0;
-        SrcRec r;
-        if (valid) {
-          r = finish_source<FORM, CELL>(a, rb4 + j * kW * 32, rb1 + j * kW * 32, lane, code, chi,
-                                        clo);
-        } else {
-          r.x = r.y = r.z = 1e30f;
-          r.m = r.soft = 0.f;
-          r.tr = r.xx = r.xy = r.xz = r.yy = r.yz = r.zz = 0.f;
-        }
-        float* pb = reinterpret_cast<float*>(stage + j * 16 * PW + (lane >> 1) * PW);
-        const int h = lane & 1;
-        if constexpr (CELL) {
-          stage_cell_half(pb, h, make_float4(r.x, r.y, r.z, r.m),
-                          make_float4(r.xx, r.xy, r.xz, r.yy), make_float4(r.yz, r.zz, r.tr, r.soft));
-        } else {
-          pb[pair_slot(0, h)] = r.x;
-          pb[pair_slot(1, h)] = r.y;
-          pb[pair_slot(2, h)] = r.z;
-          pb[pair_slot(3, h)] = r.m;
-        }
-        ssoft[j * 32 + lane] = r.soft;
-        const float ss = warp_max(r.soft) + tsmax;
-        if (j == jb) near2 = ss * ss;
-        const float bx = fmaxf(fmaxf(blo.x - r.x, r.x - bhi.x), 0.f);
-        const float by = fmaxf(fmaxf(blo.y - r.y, r.y - bhi.y), 0.f);
-        const float bz = fmaxf(fmaxf(blo.z - r.z, r.z - bhi.z), 0.f);
-        far_all = __all_sync(kFull, fmaf(bx, bx, fmaf(by, by, bz * bz)) > ss * ss * 1.0001f) && far_all;
-      }
-    }
-    __syncwarp();
-    if (e0 + W < e_end) issue(e0 + W);  // the raw slots are free again
-    const int nej = max(0, min(32, e_end - (e0 + 32 * jb)));
-    const int np = (nej + 1) >> 1;  // this group's pairs
-    const float4* st = stage + jb * 16 * PW;
-    const float* sf = ssoft + jb * 32;
-    f2 ax[R], ay[R], az[R], pt[R], pw[R];
-    unsigned nm[R];
-#pragma unroll
-    for (int k = 0; k < R; ++k) {
-      ax[k] = ay[k] = az[k] = pt[k] = pw[k] = 0ull;
-      nm[k] = 0u;
-    }
-    auto step = [&](int p, auto near) {
-      constexpr bool NEAR = decltype(near)::value;
-      if constexpr (CELL) {
-        const CellPair cpw = load_cell_pair(st + p * PW);
-#pragma unroll
-        for (int k = 0; k < R; ++k)
-          pc_pair_w<NEAR>(cpw, sf + 2 * p, T[k].x2, T[k].y2, T[k].z2, T[k].m2, T[k].soft, near2,
-                          pt[k], pw[k], ax[k], ay[k], az[k], S[k].idt);
-      } else {
-        const float4 w0 = st[p * PW], w1 = st[p * PW + 1];
-        const f2 sx2 = pk2(w0.x, w0.y), sy2 = pk2(w0.z, w0.w), sz2 = pk2(w1.x, w1.y);
-        const f2 pm = pk2(w1.z, w1.w);
-#pragma unroll
-        for (int k = 0; k < R; ++k) {
-          /* gravity.h:276-301: r = source - target */
-          const f2 rx = sub2(sx2, T[k].x2), ry = sub2(sy2, T[k].y2), rz = sub2(sz2, T[k].z2);
-          const f2 rsq = fma2(rx, rx, fma2(ry, ry, mul2(rz, rz)));
-          float q0, q1;
-          up2(rsq, q0, q1);
-          float a0 = rsqrt_ftz(q0), a1 = rsqrt_ftz(q1);
-          if constexpr (NEAR) {
-            const bool n0 = q0 <= near2, n1 = q1 <= near2;
-            nm[k] |= ((n0 ? 1u : 0u) | (n1 ? 2u : 0u)) << (2 * p);
-            a0 = n0 ? 0.f : a0;
-            a1 = n1 ? 0.f : a1;
-          }
-          const f2 av = pk2(a0, a1);
-          const f2 bv = mul2(mul2(av, av), av);
-          const f2 bm = mul2(bv, pm);
-          pt[k] = fma2(pm, av, pt[k]);  // opposite sign, negated at the fold
-          ax[k] = fma2(rx, bm, ax[k]);
-          ay[k] = fma2(ry, bm, ay[k]);
-          az[k] = fma2(rz, bm, az[k]);
-          float d0, d1;
-          up2(fma2(T[k].m2, bv, bm), d0, d1);
-          S[k].idt = fmax3(S[k].idt, d0, d1);
-        }
-      }
-    };
-    using Far = std::integral_constant<bool, false>;
-    using Near = std::integral_constant<bool, true>;
-    /* one loop shape, unrolled only for one target per lane: the R targets
-     * give the independent work, and a larger body would crowd the
-     * instruction cache */
-    if (active) {
-      if (far_all) {
-#pragma unroll(R == 1 ? 2 : 1)
-        for (int p = po; p < np; p += gp) step(p, Far{});
-      } else {
-#pragma unroll(R == 1 ? 2 : 1)
-        for (int p = po; p < np; p += gp) step(p, Near{});
-      }
-    }
-#pragma unroll
-    for (int k = 0; k < R; ++k) {
-      float ex = 0.f, ey = 0.f, ez = 0.f, ep = 0.f;
-      if constexpr (!CELL) {
-        /* the marked sources (within the softening bound of the block),
-         * each lane its own: gravity.h:276-301 with the spline inside 2h,
-         * zero at r = 0 */
-        float tx, ty, tz, tm, d_;
-        up2(T[k].x2, tx, d_);
-        up2(T[k].y2, ty, d_);
-        up2(T[k].z2, tz, d_);
-        up2(T[k].m2, tm, d_);
-        unsigned m = T[k].valid ? nm[k] : 0u;
-        while (m) {
-          const int b_ = __ffs(m) - 1;
-          m &= m - 1u;
-          const float* pb = reinterpret_cast<const float*>(st + (b_ >> 1) * PW);
-          const int h = b_ & 1;
-          const float dx = pb[pair_slot(0, h)] - tx, dy = pb[pair_slot(1, h)] - ty,
-                      dz = pb[pair_slot(2, h)] - tz, sm = pb[pair_slot(3, h)];
-          const float q = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
-          float av = 0.f, bv = 0.f;
-          if (q != 0.f) {
-            av = rsqrt_ftz(q);
-            bv = (av * av) * av;
-            const float twoh = sf[b_] + T[k].soft;
-            const float r1 = q * av;
-            if (r1 < twoh) spline_near(r1, av, twoh, av, bv);
-          }
-          const float bm = bv * sm;
-          ep = fmaf(sm, av, ep);
-          ex = fmaf(dx, bm, ex);
-          ey = fmaf(dy, bm, ey);
-          ez = fmaf(dz, bm, ez);
-          S[k].idt = fmaxf(S[k].idt, fmaf(tm, bv, bm));
-        }
-      }
-      float x0, x1, y0, y1, z0, z1, p0, p1;
-      up2(ax[k], x0, x1);
-      up2(ay[k], y0, y1);
-      up2(az[k], z0, z1);
-      up2(pt[k], p0, p1);
-      float pb_;  // this round's potential
-      if constexpr (CELL) {
-        float w0_, w1_;
-        up2(pw[k], w0_, w1_);
-        pb_ = (p0 + p1) - 0.5f * (w0_ + w1_);
-      } else {
-        pb_ = -((p0 + p1) + ep);
-      }
-      if constexpr (FORM == kMix) {
-        kahan_add(S[k].sx, S[k].cx, (x0 + x1) + ex);
-        kahan_add(S[k].sy, S[k].cy, (y0 + y1) + ey);
-        kahan_add(S[k].sz, S[k].cz, (z0 + z1) + ez);
-        kahan_add(S[k].sp, S[k].cp, pb_);
-      } else {
-        S[k].sx += (x0 + x1) + ex;
-        S[k].sy += (y0 + y1) + ey;
-        S[k].sz += (z0 + z1) + ez;
-        S[k].sp += pb_;
-      }
-    }
-    __syncwarp();  // the stage is rewritten by the next round
-  }
-
-  /* per target slot k: the G groups' partial sums of each target */
-#pragma unroll
-  for (int k = 0; k < R; ++k) {
-    if (T[k].valid) {
-      red[0][lane] = (double)S[k].sx - (double)S[k].cx;
-      red[1][lane] = (double)S[k].sy - (double)S[k].cy;
-      red[2][lane] = (double)S[k].sz - (double)S[k].cz;
-      red[3][lane] = (double)S[k].sp - (double)S[k].cp;
-      red[4][lane] = CELL ? -(double)S[k].idt : (double)S[k].idt;
-    }
-    __syncwarp();
-    const int t = lane + k * c;
-    if (lane < c && t < nt) {
-      double rx = 0, ry = 0, rz = 0, rp = 0, ri = 0;
-      for (int gg = 0; gg < G; ++gg) {
-        const int l = gg * c + lane;
-        rx += red[0][l];
-        ry += red[1][l];
-        rz += red[2][l];
-        rp += red[3][l];
-        ri = fmax(ri, red[4][l]);
-      }
-      const long long to = tb + t;
-      if constexpr (FORM == kF32) {
-        VariablePartData* v = static_cast<VariablePartData*>(a.vars) + to;
-        v->a.x += (float)rx;
-        v->a.y += (float)ry;
-        v->a.z += (float)rz;
-        v->potential += (float)rp;
-        v->dtGrav = fmaxf((float)ri, v->dtGrav);
-      } else {
-        double* v = static_cast<double*>(a.vars) + 5 * to;
-        v[0] += rx;
-        v[1] += ry;
-        v[2] += rz;
-        v[3] += rp;
-        v[4] = fmax(ri, v[4]);
-      }
-    }
-    __syncwarp();
-  }
-}
-
-/* Shared memory is dynamic (kWarps x Rb2Smem::kWarpBytes, above the static
- * 48 KB per block). */
-template <int FORM, bool CELL, int MINB, int RMAX, int GMAX>
-__global__ void __launch_bounds__(kThreads, MINB) list_kernel_rb2(const ListArgs a) {
-  static_assert(FORM != kF64, "FP32 arithmetic forms only");
-  static_assert(RMAX >= 1 && RMAX <= 3 && GMAX >= 1 && GMAX <= 8, "shape bounds");
-  using SM = Rb2Smem<FORM, CELL, GMAX>;
-  extern __shared__ __align__(16) char rb2_smem[];
-  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  char* wsm = rb2_smem + (size_t)warp * SM::kWarpBytes;
-
-  for (;;) {
-    int b = 0;
-    if (lane == 0) b = (int)atomicAdd(a.queue, 1u);
-    b = __shfl_sync(kFull, b, 0);
-    if (b >= a.n_buckets) break;
-    const int e_begin = max(__ldg(a.markers + b), 0);
-    const int e_end = (int)min((long long)__ldg(a.markers + b + 1), a.n_entries);  // memory safety
-    const long long tbase = __ldg(a.starts + b);
-    const int n = __ldg(a.sizes + b);
-    if (n <= 0 || tbase < 0 || tbase + n > a.n_tgt) continue;  // memory safety
-
-    float3 chi = make_float3(0.f, 0.f, 0.f), clo = chi;
-    if constexpr (FORM == kMix) {
-      const float4* tp = static_cast<const float4*>(a.tgt) + kPartPackF4 * tbase;
-      const float4 h = __ldg(tp), l = __ldg(tp + 1);
-      chi = make_float3(h.x, h.y, h.z);
-      clo = make_float3(l.x, l.y, l.z);
-    }
-    for (int t0 = 0; t0 < n; t0 += 32) {
-      const int nt = min(32, n - t0);
-      const RbShape sh = rb2_shape<RMAX, GMAX>(nt);
-      if (RMAX >= 3 && sh.r == 3)
-        rb2_chunk<FORM, CELL, (RMAX >= 3 ? 3 : 1), GMAX>(a, lane, e_begin, e_end, tbase + t0, nt,
-                                                         sh, chi, clo, wsm);
-      else if (RMAX >= 2 && sh.r == 2)
-        rb2_chunk<FORM, CELL, (RMAX >= 2 ? 2 : 1), GMAX>(a, lane, e_begin, e_end, tbase + t0, nt,
-                                                         sh, chi, clo, wsm);
-      else
-        rb2_chunk<FORM, CELL, 1, GMAX>(a, lane, e_begin, e_end, tbase + t0, nt, sh, chi, clo, wsm);
-    }
-  }
-}
-
-/* ------------------------------------------------------------------ */
 /* Paired cell kernel with TMA staging (FP32-mixed form): the packed    */
 /* cell records (64 bytes, one row of a 2-D tensor map) of each         */
 /* 32-entry block arrive in shared memory by eight tile::gather4 bulk   */
@@ -3143,40 +2740,6 @@ cudaError_t launch_tma(const ListArgs& a, const CUtensorMap& tm, cudaStream_t s)
   return cudaGetLastError();
 }
 
-/* list_kernel_rb2 with its dynamic shared memory (the attribute is set
- * once per device). */
-template <int FORM, bool CELL, int MINB, int RMAX, int GMAX>
-cudaError_t launch_rb2(const ListArgs& a, cudaStream_t s) {
-  static std::atomic<int> occ{0};
-  static std::atomic<unsigned long long> attr_devs{0};
-  if (a.n_buckets <= 0) return cudaSuccess;
-  constexpr size_t smem = (size_t)kWarps * Rb2Smem<FORM, CELL, GMAX>::kWarpBytes;
-  auto kernel = list_kernel_rb2<FORM, CELL, MINB, RMAX, GMAX>;
-  int dev = 0;
-  if (cudaGetDevice(&dev) != cudaSuccess) return cudaGetLastError();
-  const unsigned long long bit = 1ull << (dev & 63);
-  if (!(attr_devs.load() & bit)) {
-    const cudaError_t e =
-        cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    if (e != cudaSuccess) return e;
-    attr_devs.fetch_or(bit);
-  }
-  int nb = occ.load(std::memory_order_relaxed);
-  if (!nb) {
-    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, kernel, kThreads, smem) != cudaSuccess ||
-        nb < 1)
-      nb = 1;
-    occ.store(nb, std::memory_order_relaxed);
-  }
-  const long long want = ((long long)a.n_buckets + kWarps - 1) / kWarps;
-  const long long cap = (long long)sm_count() * nb;
-  const int grid = (int)(want < cap ? want : cap);
-  TimingScope ts(list_kernel_id(FORM, CELL), s);
-  kernel<<<grid, kThreads, smem, s>>>(a);
-  count_launch();
-  return cudaGetLastError();
-}
-
 template <int FORM, bool CELL, int V>
 cudaError_t launch_variant(const ListArgs& a, cudaStream_t s) {
   static std::atomic<int> occ{0};
@@ -3188,9 +2751,7 @@ cudaError_t launch_variant(const ListArgs& a, cudaStream_t s) {
     }
     return launch_kernel(list_kernel_tp2<FORM, CELL, var.minb>, &occ, list_kernel_id(FORM, CELL),
                          a, s);
-  } else if constexpr (var.tp == 5)
-    return launch_rb2<FORM, CELL, var.minb, var.group / 16, var.group % 16>(a, s);
-  else if constexpr (var.tp == 4)
+  } else if constexpr (var.tp == 4)
     return launch_kernel(list_kernel_rb<FORM, CELL, var.minb, var.group>, &occ,
                          list_kernel_id(FORM, CELL), a, s);
   else if constexpr (var.tp == 2)

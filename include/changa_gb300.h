@@ -91,10 +91,7 @@ int changa_gb300_kernel_time(int kernel, double *total_ms, long long *launches);
  * staged by TMA tile::gather4 copies (2/1 blocks per SM; the other lists
  * run the paired kernel), 13-16 paired with 1-3 targets per lane chosen
  * per bucket (blocks per SM / most targets per lane: 2/3, 2/2, 3/2, 1/3),
- * which keeps the lanes of buckets of 17-31 targets busy, 17-20 the same
- * with several 32-entry blocks staged per round and the next round's
- * records fetched by cp.async (blocks per SM / most targets per lane / most
- * blocks per round: 2/3/4, 2/2/3, 2/3/6, 1/3/3).  The autotuner
+ * which keeps the lanes of buckets of 17-31 targets busy.  The autotuner
  * (changa_gb300/autotune.py) times them on a workload and selects one per
  * kernel. */
 int changa_gb300_list_variant_count(void);
