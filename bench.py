@@ -562,6 +562,15 @@ def measure_hexadecapole(wl, pts, samp=None, dsum=None, steps=5, fp64_steps=1):
                          theta=wl.theta, period=wl.period, n_replicas=1 if wl.period else 0,
                          order=4)
     host_s = time.perf_counter() - t0
+    # the same tree's lists walked on the GPU (two phases; the entries
+    # counted against the host walk's)
+    from changa_gb300.walk import gpu_walk
+    gpu_walk(L)
+    wt = {}
+    dc, dp, dsoft = gpu_walk(L, timings=wt)
+    walk_match = (dc.interactions() + dp.interactions() + dsoft.interactions() ==
+                  L.cells.interactions() + L.plist.interactions() + L.softcells.interactions())
+    del dc, dp, dsoft
     ds = gravity.DeviceSystem(L, device="cuda", ewald=wl.ewald_config())
     stream = torch.cuda.current_stream()
     flush = torch.empty(256 * 2 ** 20 // 4, dtype=torch.float32, device="cuda")
@@ -591,7 +600,8 @@ def measure_hexadecapole(wl, pts, samp=None, dsum=None, steps=5, fp64_steps=1):
            "softened_cell_interactions": Is, "ms_per_step": ms,
            "interactions_per_s": I / (ms / 1e3), "kernel_ms": kt,
            "cell_tflops_counted": Ic * 196 / (kt["list_mixed_cell"] / 1e3) / 1e12,
-           "host_tree_walk_s": host_s}
+           "host_tree_walk_s": host_s, "gpu_walk_s": wt.get("walk_s"),
+           "gpu_walk_interactions_match": bool(walk_match)}
     if samp is not None and dsum is not None:
         v = ds.vars.cpu().numpy()[samp]
         e = np.linalg.norm(v[:, :3] - dsum[:, :3], axis=1) / np.linalg.norm(dsum[:, :3], axis=1)

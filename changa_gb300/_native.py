@@ -231,6 +231,7 @@ CUDA_SIGNATURES = {
     "changa_gravity_vjp_mixed": (_I, [_VP, _LL, _VP, _LL, C.POINTER(ChangaListRequest),
                                       C.POINTER(ChangaListRequest), _D, _VP, _VP, _VP, _VP, _VP]),
     "changa_gravity_graph_destroy": (None, [_VP]),
+    "changa_ewald_vjp": (_I, [_VP, _LL, C.POINTER(ChangaEwaldParams), _VP, _VP, _VP]),
     "changa_tree_moments": (_I, [_VP, _LL, _VP, _VP, _LL, _VP, _VP]),
     "changa_direct_forces": (_I, [_VP, _LL, _VP, _LL, _D, _D, _VP, _VP]),
     "changa_tree_build": (_VP, [_VP, _VP, _VP, _LL, _I, _VP]),

@@ -6,7 +6,8 @@ same tree, walk and interaction lists:
 * ``TreeStep``  -- one tree (topology + lists) built at one set of positions
   and held on the device.  ``accel`` runs the list forces
   (changa_gravity_step), ``vjp`` the hand-written adjoint kernels
-  (changa_gravity_vjp_mixed: dL/dx and dL/dm from lambda = dL/da), and
+  (changa_gravity_vjp_mixed: dL/dx and dL/dm from lambda = dL/da; for a
+  periodic system changa_ewald_vjp adds the Ewald term's part), and
   ``load`` moves the particles while keeping the topology (the device moment
   up-pass changa_tree_moments refreshes the moments), which is the function
   the adjoint differentiates: lists and topology fixed, moments exact.
@@ -46,10 +47,16 @@ class TreeStep:
     per-bucket entries."""
 
     def __init__(self, x, mass, soft, theta=0.7, n_bucket=16, device="cuda", nthreads=0,
-                 builder="host"):
+                 builder="host", period=0.0, ewald=None):
+        """period, ewald: a periodic system (host builder): the walk covers
+        one replica shell and ewald (gravity.EwaldConfig) adds the Ewald
+        term, whose root parameters follow every load."""
         import torch
         self.torch = torch
+        self.period = float(period)
         if builder == "device":
+            if period:
+                raise ValueError("the device builder walks isolated systems")
             self._init_device(x, mass, soft, theta, n_bucket, device)
             return
         if builder != "host":
@@ -57,10 +64,11 @@ class TreeStep:
         x_h = x.detach().cpu().numpy() if hasattr(x, "detach") else np.asarray(x)
         m_h = mass.detach().cpu().numpy() if hasattr(mass, "detach") else np.asarray(mass)
         s_h = soft.detach().cpu().numpy() if hasattr(soft, "detach") else np.asarray(soft)
-        lists = build_lists(x_h, m_h, s_h, n_bucket=n_bucket, theta=theta, nthreads=nthreads)
+        lists = build_lists(x_h, m_h, s_h, n_bucket=n_bucket, theta=theta, nthreads=nthreads,
+                            period=self.period, n_replicas=1 if self.period else 0)
         self.lists = lists
         self.n = lists.n
-        self.ds = DeviceSystem(lists, device=device)
+        self.ds = DeviceSystem(lists, device=device, ewald=ewald if self.period else None)
         t = lambda a: torch.from_numpy(np.ascontiguousarray(a)).to(device)
         self.perm = t(lists.perm)
         self.parent = t(lists.meta["parent"])
@@ -103,6 +111,9 @@ class TreeStep:
                                               self.count.data_ptr(), mo.shape[0], mo.data_ptr(),
                                               self._stream(stream))
         N.check(rc, "changa_tree_moments")
+        if self.ds.ewald_params is not None:
+            # the Ewald term expands about the refreshed root
+            self.ds.ewald_params = self.ds.ewald.params(mo[0].cpu().numpy())
 
     def accel(self, form="mixed", stream=None):
         """Accelerations (caller order, N x 3 FP64) from the current arrays."""
@@ -120,9 +131,15 @@ class TreeStep:
         grad = torch.zeros((self.n, 4), dtype=torch.float64, device=lam.device)
         rc = N.cuda_lib().changa_gravity_vjp_mixed(
             ds.moments.data_ptr(), ds.moments.shape[0], ds.parts.data_ptr(), self.n,
-            C.byref(ds.reqs[0]["c"]), C.byref(ds.reqs[1]["c"]), 0.0, self.parent.data_ptr(),
-            self.leaf.data_ptr(), lam_g.data_ptr(), grad.data_ptr(), self._stream(stream))
+            C.byref(ds.reqs[0]["c"]), C.byref(ds.reqs[1]["c"]), self.period,
+            self.parent.data_ptr(), self.leaf.data_ptr(), lam_g.data_ptr(), grad.data_ptr(),
+            self._stream(stream))
         N.check(rc, "changa_gravity_vjp_mixed")
+        if ds.ewald_params is not None:
+            rc = N.cuda_lib().changa_ewald_vjp(ds.parts.data_ptr(), self.n,
+                                               C.byref(ds.ewald_params), lam_g.data_ptr(),
+                                               grad.data_ptr(), self._stream(stream))
+            N.check(rc, "changa_ewald_vjp")
         gx = torch.empty((self.n, 3), dtype=torch.float64, device=lam.device)
         gm = torch.empty(self.n, dtype=torch.float64, device=lam.device)
         gx[self.perm] = grad[:, :3]

@@ -80,6 +80,12 @@ cudaError_t launch_ewald_fp(int form, const double* parts, long long n_parts, co
                             long long n_idx, const ChangaEwaldParams& p, double* vars,
                             cudaStream_t s, bool hex = false);
 
+/* adjoint of the Ewald term (quadrupole root expansion, FP64): adds the
+ * vector-Jacobian product of lam . a_ewald to grad (n x 4 {dL/dx, dL/dm});
+ * acc: 10 doubles of device scratch */
+cudaError_t launch_ewald_vjp(const double* parts, long long n_parts, const ChangaEwaldParams& p,
+                             const double* lam, double* grad, double* acc, cudaStream_t s);
+
 /* runtime helpers (hostcuda.cu) */
 int sm_count();
 void count_launch(unsigned n = 1);

@@ -28,6 +28,8 @@
  *                     the hardware exp2; the k-space phase is reduced to one
  *                     turn from the integer h before the hardware sin/cos.
  */
+#include <cmath>
+
 #include "chg_internal.h"
 #include "f32x2.cuh"
 
@@ -784,6 +786,242 @@ cudaError_t launch_ewald_fp(int form, const double* parts, long long n_parts, co
   TimingScope ts(kKidEwaldMix, s);
   if (hex) ewald_mix_kernel<true><<<blocks, threads, 0, s>>>(parts, n_parts, idx, n_idx, vars, P);
   else ewald_mix_kernel<false><<<blocks, threads, 0, s>>>(parts, n_parts, idx, n_idx, vars, P);
+  count_launch();
+  return cudaGetLastError();
+}
+
+namespace {
+
+/* ---- adjoint of the Ewald term (quadrupole build, FP64) ----
+ *
+ * The forward term of one replica at r (particle - root centre + replica
+ * shift) is a = g2 q - r S with q = Q r, S = g1 M - g2 Q2 + g3 w, Q2 = tr Q
+ * / 2, w = r.q / 2 (Ewald.cpp:137-240), and the Fourier part adds
+ * h' C_h sin(h'.d) with C_h = -g0(h) M - g2(h) h.Q.h / 2 (Ewald.cpp:285-383).
+ * With D_n = -(1/r) dg_n/dr (= g_{n+1} on the erfc branch; on the series
+ * branch below fInner2 the derivative of its truncated polynomial), the
+ * vector-Jacobian product of lam . a is
+ *   d/dr:  g2 Q lam - S lam - D2 (lam.q) r - g3 (lam.r) q
+ *          + (lam.r)(D1 M - D2 Q2 + D3 w) r,
+ *   d/dM:  -g1 (lam.r),
+ *   d/dQ_kl (both entries of a symmetric pair):
+ *          g2 lam_k r_l + g2 (lam.r) delta_kl / 2 - g3 (lam.r) r_k r_l / 2,
+ * and the Fourier part gives (lam.h') C cos(h'.d) h' to d/dr and
+ * (lam.h') sin(h'.d) dC/d(M, Q) to the root moments.  The root's centre
+ * enters through r = x - cm, so d/dcm is minus the sum of every particle's
+ * d/dr.  ewald_vjp_kernel adds each particle's d/dr to its gradient and
+ * sums the root-moment gradients; ewald_vjp_chain_kernel carries those to
+ * every particle through M = sum m, cm = sum m x / M, Q = sum m (x-cm)(x-cm). */
+
+struct EwaldVjpArgs {
+  double mom[12];
+  double L, fEwCut2, fInner2, alpha, alpha2, ka;
+  int nReps, nEwReps, nEwhLoop;
+  double ewt[CHANGA_MAX_EWH][4];  // h' (2 pi / L h) and C_h
+  double hg[CHANGA_MAX_EWH][4];   // integer h and -g2(h) / 2 (dC/dQ_kl = -g2 h_k h_l / 2)
+  double g0h[CHANGA_MAX_EWH];     // -g0(h) = dC/dM
+};
+
+/* acc: 10 sums {dL/dcm (3), dL/dM, dL/dQ xx xy xz yy yz zz (stored, symmetric)} */
+__global__ void __launch_bounds__(128) ewald_vjp_kernel(const double* __restrict__ parts,
+                                                        long long n_parts,
+                                                        const double* __restrict__ lam,
+                                                        double* __restrict__ grad,
+                                                        double* __restrict__ acc,
+                                                        const __grid_constant__ EwaldVjpArgs P) {
+  __shared__ double red[10][4];
+  const long long j = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  double sums[10] = {0, 0, 0, 0, 0, 0, 0, 0, 0, 0};
+  if (j < n_parts) {
+    const double* p = parts + 5 * j;
+    const double lx = lam[3 * j], ly = lam[3 * j + 1], lz = lam[3 * j + 2];
+    const double dxd = p[2] - P.mom[3], dyd = p[3] - P.mom[4], dzd = p[4] - P.mom[5];
+    const double M = P.mom[2];
+    const double xx = P.mom[6], xy = P.mom[7], xz = P.mom[8], yy = P.mom[9], yz = P.mom[10],
+                 zz = P.mom[11];
+    const double Q2 = 0.5 * (xx + yy + zz);
+    const double qlx = xx * lx + xy * ly + xz * lz, qly = xy * lx + yy * ly + yz * lz,
+                 qlz = xz * lx + yz * ly + zz * lz;  // Q lam
+    double gx = 0, gy = 0, gz = 0, gM = 0, gxx = 0, gxy = 0, gxz = 0, gyy = 0, gyz = 0, gzz = 0;
+    const int nE = P.nEwReps, nR = P.nReps;
+    for (int ix = -nE; ix <= nE; ++ix) {
+      const bool hx = (ix >= -nR && ix <= nR);
+      const double x = dxd + ix * P.L;
+      for (int iy = -nE; iy <= nE; ++iy) {
+        const bool hxy = hx && (iy >= -nR && iy <= nR);
+        const double y = dyd + iy * P.L;
+        for (int iz = -nE; iz <= nE; ++iz) {
+          const bool hole = hxy && (iz >= -nR && iz <= nR);
+          const double z = dzd + iz * P.L;
+          const double r2 = x * x + y * y + z * z;
+          if (r2 > P.fEwCut2 && !hole) continue;
+          double g1, g2, g3, D1, D2, D3;
+          if (r2 < P.fInner2) {
+            /* the forward's series: g_n = A_n (u / (2n+3) - 1 / (2n+1)),
+             * u = alpha^2 r^2, A_{n+1} = 2 alpha^2 A_n */
+            const double u = r2 * P.alpha2, a2 = 2 * P.alpha2;
+            const double A1 = P.ka * a2, A2 = A1 * a2, A3 = A2 * a2;
+            g1 = A1 * ((1.0 / 5.0) * u - (1.0 / 3.0));
+            g2 = A2 * ((1.0 / 7.0) * u - (1.0 / 5.0));
+            g3 = A3 * ((1.0 / 9.0) * u - (1.0 / 7.0));
+            D1 = -A1 * a2 * (1.0 / 5.0);
+            D2 = -A2 * a2 * (1.0 / 7.0);
+            D3 = -A3 * a2 * (1.0 / 9.0);
+          } else {
+            const double dir = rsqrt(r2);
+            const double dir2 = dir * dir;
+            double a = exp(-r2 * P.alpha2);
+            a *= P.ka * dir2;
+            const double ar = P.alpha * (r2 * dir);
+            double g0 = hole ? -erf(ar) : erfc(ar);
+            g0 *= dir;
+            g1 = g0 * dir2 + a;
+            double alphan = 2 * P.alpha2;
+            g2 = 3 * g1 * dir2 + alphan * a;
+            alphan *= 2 * P.alpha2;
+            g3 = 5 * g2 * dir2 + alphan * a;
+            alphan *= 2 * P.alpha2;
+            const double g4 = 7 * g3 * dir2 + alphan * a;
+            D1 = g2;
+            D2 = g3;
+            D3 = g4;
+          }
+          const double qx = xx * x + xy * y + xz * z, qy = xy * x + yy * y + yz * z,
+                       qz = xz * x + yz * y + zz * z;
+          const double w = 0.5 * (qx * x + qy * y + qz * z);
+          const double S = g1 * M - g2 * Q2 + g3 * w;
+          const double lr = lx * x + ly * y + lz * z, lq = lx * qx + ly * qy + lz * qz;
+          const double T = lr * (D1 * M - D2 * Q2 + D3 * w) - D2 * lq;
+          gx += g2 * qlx - S * lx - g3 * lr * qx + T * x;
+          gy += g2 * qly - S * ly - g3 * lr * qy + T * y;
+          gz += g2 * qlz - S * lz - g3 * lr * qz + T * z;
+          gM -= g1 * lr;
+          const double hd = 0.5 * g2 * lr, h3 = 0.5 * g3 * lr;
+          gxx += g2 * lx * x + hd - h3 * x * x;
+          gyy += g2 * ly * y + hd - h3 * y * y;
+          gzz += g2 * lz * z + hd - h3 * z * z;
+          gxy += g2 * (lx * y + ly * x) - g3 * lr * x * y;
+          gxz += g2 * (lx * z + lz * x) - g3 * lr * x * z;
+          gyz += g2 * (ly * z + lz * y) - g3 * lr * y * z;
+        }
+      }
+    }
+    for (int i = 0; i < P.nEwhLoop; ++i) {
+      const double* e = P.ewt[i];
+      const double hdotx = e[0] * dxd + e[1] * dyd + e[2] * dzd;
+      double s, c;
+      sincos(hdotx, &s, &c);
+      const double lh = lx * e[0] + ly * e[1] + lz * e[2];
+      const double t = lh * e[3] * c;
+      gx += t * e[0];
+      gy += t * e[1];
+      gz += t * e[2];
+      const double ls = lh * s;
+      gM += ls * P.g0h[i];
+      const double* h = P.hg[i];
+      const double f = ls * h[3];
+      gxx += f * h[0] * h[0];
+      gyy += f * h[1] * h[1];
+      gzz += f * h[2] * h[2];
+      gxy += 2 * f * h[0] * h[1];
+      gxz += 2 * f * h[0] * h[2];
+      gyz += 2 * f * h[1] * h[2];
+    }
+    double* g = grad + 4 * j;
+    g[0] += gx;
+    g[1] += gy;
+    g[2] += gz;
+    const double v[10] = {-gx, -gy, -gz, gM, gxx, gxy, gxz, gyy, gyz, gzz};
+#pragma unroll
+    for (int k = 0; k < 10; ++k) sums[k] = v[k];
+  }
+  /* the block's sums, one FP64 atomic per value and block */
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+#pragma unroll
+  for (int k = 0; k < 10; ++k) {
+    double v = sums[k];
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    if (lane == 0) red[k][warp] = v;
+  }
+  __syncthreads();
+  if (threadIdx.x < 10) {
+    const double v = red[threadIdx.x][0] + red[threadIdx.x][1] + red[threadIdx.x][2] +
+                     red[threadIdx.x][3];
+    atomicAdd(acc + threadIdx.x, v);
+  }
+}
+
+/* The root-moment gradients acc to every particle: M = sum m, cm = sum m x
+ * / M, Q = sum m (x - cm)(x - cm) (the cm dependence of Q vanishes, as
+ * sum m (x - cm) = 0).  With G the symmetric matrix of dL/dQ (diagonal
+ * entries, halves of the off-diagonal ones) and e = x - cm:
+ *   dL/dx += m / M dL/dcm + 2 m G e,   dL/dm += dL/dM + dL/dcm . e / M + e.G e. */
+__global__ void ewald_vjp_chain_kernel(const double* __restrict__ parts, long long n_parts,
+                                       const double* __restrict__ acc, double M, double cmx,
+                                       double cmy, double cmz, double* __restrict__ grad) {
+  for (long long j = blockIdx.x * (long long)blockDim.x + threadIdx.x; j < n_parts;
+       j += (long long)gridDim.x * blockDim.x) {
+    const double* p = parts + 5 * j;
+    const double m = p[0], ex = p[2] - cmx, ey = p[3] - cmy, ez = p[4] - cmz;
+    const double gcx = acc[0], gcy = acc[1], gcz = acc[2], gM = acc[3];
+    const double Gxx = acc[4], Gxy = 0.5 * acc[5], Gxz = 0.5 * acc[6], Gyy = acc[7],
+                 Gyz = 0.5 * acc[8], Gzz = acc[9];
+    const double Gex = Gxx * ex + Gxy * ey + Gxz * ez, Gey = Gxy * ex + Gyy * ey + Gyz * ez,
+                 Gez = Gxz * ex + Gyz * ey + Gzz * ez;
+    double* g = grad + 4 * j;
+    const double mM = M != 0 ? m / M : 0.0, iM = M != 0 ? 1.0 / M : 0.0;
+    g[0] += mM * gcx + 2 * m * Gex;
+    g[1] += mM * gcy + 2 * m * Gey;
+    g[2] += mM * gcz + 2 * m * Gez;
+    g[3] += gM + (gcx * ex + gcy * ey + gcz * ez) * iM + (ex * Gex + ey * Gey + ez * Gez);
+  }
+}
+
+}  // namespace
+
+cudaError_t launch_ewald_vjp(const double* parts, long long n_parts, const ChangaEwaldParams& p,
+                             const double* lam, double* grad, double* acc, cudaStream_t s) {
+  if (n_parts <= 0) return cudaSuccess;
+  if (p.nEwhLoop < 0 || p.nEwhLoop > CHANGA_MAX_EWH || (p.nEwhLoop > 0 && !p.ewt) || !(p.L > 0))
+    return cudaErrorInvalidValue;
+  const double L = p.L;
+  EwaldVjpArgs P;
+  for (int i = 0; i < 12; ++i) P.mom[i] = p.root[i];
+  P.L = L;
+  P.alpha = 2.0 / L;
+  P.alpha2 = P.alpha * P.alpha;
+  P.ka = 2.0 * P.alpha / sqrt(M_PI);
+  P.fEwCut2 = p.fEwCut * p.fEwCut * L * L;
+  P.fInner2 = 1.2e-3 * L * L;  // the FP64 forward's series radius
+  P.nReps = p.nReps;
+  const int nE0 = (int)ceil(p.fEwCut);
+  P.nEwReps = nE0 > p.nReps ? nE0 : p.nReps;
+  P.nEwhLoop = p.nEwhLoop;
+  const double k4 = M_PI * M_PI / (P.alpha2 * L * L);
+  for (int i = 0; i < p.nEwhLoop; ++i) {
+    const double* e = p.ewt + 5 * i;
+    for (int k = 0; k < 4; ++k) P.ewt[i][k] = e[k];
+    /* the integer h and the gammas of the table's row (changa_ewald_table) */
+    double h[3], h2 = 0;
+    for (int k = 0; k < 3; ++k) {
+      h[k] = std::round(e[k] * L / (2 * M_PI));
+      h2 += h[k] * h[k];
+    }
+    const double g0 = h2 > 0 ? std::exp(-k4 * h2) / (M_PI * h2 * L) : 0.0;
+    const double g2 = -(2 * M_PI / L) * (2 * M_PI / L) * g0;
+    for (int k = 0; k < 3; ++k) P.hg[i][k] = h[k];
+    P.hg[i][3] = -0.5 * g2;
+    P.g0h[i] = -g0;
+  }
+  const int blocks = (int)((n_parts + 127) / 128);
+  cudaError_t e = cudaMemsetAsync(acc, 0, 10 * sizeof(double), s);
+  if (e != cudaSuccess) return e;
+  ewald_vjp_kernel<<<blocks, 128, 0, s>>>(parts, n_parts, lam, grad, acc, P);
+  count_launch();
+  if ((e = cudaGetLastError()) != cudaSuccess) return e;
+  const int cb = blocks < sm_count() * 8 ? blocks : sm_count() * 8;
+  ewald_vjp_chain_kernel<<<cb, 128, 0, s>>>(parts, n_parts, acc, p.root[2], p.root[3], p.root[4],
+                                            p.root[5], grad);
   count_launch();
   return cudaGetLastError();
 }

@@ -1455,6 +1455,23 @@ int changa_gravity_step_host_runs(int form, const double* moments, long long n_m
                         ewald, vars, s);
 }
 
+int changa_ewald_vjp(const double* parts, long long n_parts, const ChangaEwaldParams* p,
+                     const double* lam, double* grad, cudaStream_t stream) {
+  if (!p || !parts || !lam || !grad || n_parts < 0)
+    return record_error(CHANGA_E_INVALID_ARG, "ewald_vjp: arguments", __FILE__, __LINE__);
+  if (p->nEwhLoop > CHANGA_MAX_EWH)
+    return record_error(CHANGA_E_TOO_LARGE, "ewald_vjp: nEwhLoop", __FILE__, __LINE__);
+  if (n_parts == 0) return 0;
+  prepare_pool();
+  double* acc = nullptr;
+  CHG_CUDA(cudaMallocAsync((void**)&acc, 16 * sizeof(double), stream));
+  const cudaError_t e = launch_ewald_vjp(parts, n_parts, *p, lam, grad, acc, stream);
+  const cudaError_t ef = cudaFreeAsync(acc, stream);
+  if (e != cudaSuccess) return record_error((int)e, "ewald_vjp", __FILE__, __LINE__);
+  if (ef != cudaSuccess) return record_error((int)ef, "ewald_vjp: free", __FILE__, __LINE__);
+  return 0;
+}
+
 int changa_ewald_forces(int form, const double* parts, long long n_parts, const int* idx,
                         long long n_idx, const ChangaEwaldParams* p, double* vars,
                         cudaStream_t stream) {

@@ -310,7 +310,7 @@ __device__ __forceinline__ void append_at(const WalkArgs& a, int k, const int* t
 
 /* PHASE 0: the whole walk of each bucket; 1: the shared walk of each group
  * down to its group node (prefix lists and frontier); 2: each bucket from
- * its group's frontier, after its group's prefix lists (quadrupole walk). */
+ * its group's frontier, after its group's prefix lists. */
 template <int MODE, int STACK, int PHASE>
 __global__ void __launch_bounds__(kWalkWarps * 32) walk_kernel(const WalkArgs a) {
   constexpr bool FILL = MODE == kFill;
@@ -382,8 +382,50 @@ __global__ void __launch_bounds__(kWalkWarps * 32) walk_kernel(const WalkArgs a)
   if (PHASE == 2) {
     /* the group's prefix lists (entries accepted against the local nodes
      * the group walk covered, the same for every bucket of the group) */
+    if (a.order == 4) {
+      /* hexadecapole: the group's accepted cells split here into cells and
+       * softened cells, by openSoftening against this bucket, as the
+       * one-phase walk splits them when it accepts them */
+      const unsigned below = (1u << lane) - 1u;
+      const long long p0 = a.pre_off[0][gid], cnt = a.pre_off[0][gid + 1] - p0;
+      for (long long j0 = 0; j0 < cnt; j0 += 32) {
+        const int tot = (int)(cnt - j0 < 32 ? cnt - j0 : 32);
+        int2 e = make_int2(-1, 0);
+        bool soft = false;
+        if (lane < tot) {
+          e = a.pre[0][p0 + j0 + lane];
+          if (e.x >= 0 && e.x < a.n_nodes) {
+            double o[3];
+            decode((e.y >> 22) & 0x1ff, a.period, o);
+            const double* gg = a.geom + 6 * (size_t)e.x;
+            const double cc[3] = {gg[0] + o[0], gg[1] + o[1], gg[2] + o[2]};
+            soft = open_softening(a, e.x, bn, cc);
+          }
+        }
+        const unsigned mc = __ballot_sync(full, lane < tot && !soft);
+        const unsigned ms = __ballot_sync(full, lane < tot && soft);
+        if (MODE == kAppend) {
+          if (mc) ensure_chunks(a, 0, b, ctab[warp][0], na[0], nc, __popc(mc));
+          if (ms) ensure_chunks(a, 2, b, ctab[warp][2], na[2], ns, __popc(ms));
+        }
+        if (MODE != kCount && lane < tot) {
+          if (!soft) {
+            const long long q = nc + __popc(mc & below);
+            if (FILL) a.cells[oc + q] = e;
+            if (MODE == kAppend) append_at(a, 0, ctab[warp][0], q, e);
+          } else {
+            const long long q = ns + __popc(ms & below);
+            if (FILL) a.soft[os + q] = e;
+            if (MODE == kAppend) append_at(a, 2, ctab[warp][2], q, e);
+          }
+        }
+        nc += __popc(mc);
+        ns += __popc(ms);
+      }
+    }
 #pragma unroll
     for (int k = 0; k < 2; ++k) {
+      if (k == 0 && a.order == 4) continue;  // split above
       const long long p0 = a.pre_off[k][gid], cnt = a.pre_off[k][gid + 1] - p0;
       long long& n_k = k == 0 ? nc : np;
       if (MODE != kCount) {
@@ -429,7 +471,7 @@ __global__ void __launch_bounds__(kWalkWarps * 32) walk_kernel(const WalkArgs a)
       const int open = open_criterion_screened(a, nd, g, local, local_bucket, code);
       if (open == 0) {
         bool softened = false;
-        if (a.order == 4) {
+        if (a.order == 4 && PHASE != 1) {  // phase 2 splits the group's cells per bucket
           double o[3];
           decode(code, a.period, o);
           const double* gg = a.geom + 6 * (size_t)g;
@@ -913,7 +955,7 @@ extern "C" int changa_walk(const ChangaTreeView* t, const ChangaWalkParams* p,
   if (!cnt || !ts || !off || !ctr)
     return finish(record_error(cudaErrorMemoryAllocation, "walk: memory", __FILE__, __LINE__));
   int h_err = 0;
-  /* Quadrupole walks of many buckets run in two phases.  Phase 1 walks each
+  /* Walks of many buckets run in two phases.  Phase 1 walks each
    * group's node once: its chain down to the group node is shared by all
    * the group's buckets, so the entries accepted on it (the group's prefix
    * lists) and those still undecided at the group node (its frontier) are
@@ -921,7 +963,7 @@ extern "C" int changa_walk(const ChangaTreeView* t, const ChangaWalkParams* p,
    * frontier, its lists starting with the group's prefix. */
   int phase = 0;
   const int gmax = g_group_max.load();
-  if (p->order == 2 && gmax > 0 && g_group_min.load() > 0 && nb >= g_group_min.load()) {
+  if (gmax > 0 && g_group_min.load() > 0 && nb >= g_group_min.load()) {
     int* bfirst = (int*)alloc((size_t)nb * sizeof(int));
     int* gn = (int*)alloc((size_t)nb * sizeof(int));
     int* flag = (int*)alloc((size_t)nb * sizeof(int));

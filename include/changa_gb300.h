@@ -288,13 +288,27 @@ int changa_gravity_step_hexa(int form, const double *moments, long long n_moment
  * dL/dx and dL/dm into grad (n_parts x 4 {dx, dy, dz, dm}) through the same
  * lists, the tidal tensor of every interaction and the moment construction
  * (tree topology held fixed).  parent: BFS parent of every moment (-1 at
- * the root); leaf: moment index of each particle's bucket.  Isolated
- * systems (the Ewald term has no adjoint here). */
+ * the root); leaf: moment index of each particle's bucket.  fperiod: the
+ * period of the lists' replica offsets (0 for isolated systems); the
+ * Ewald term's part is changa_ewald_vjp. */
 int changa_gravity_vjp_mixed(const double *moments, long long n_moments, const double *parts,
                              long long n_parts, const ChangaListRequest *cells,
                              const ChangaListRequest *plist, double fperiod, const int *parent,
                              const int *leaf, const double *lam, double *grad,
                              cudaStream_t stream);
+
+/* Adjoint of the Ewald term of the quadrupole build (FP64; no reference
+ * counterpart): given lam = dL/da (n_parts x 3, the particles' order in
+ * parts), ACCUMULATES into grad (n_parts x 4 {dx, dy, dz, dm}) the
+ * derivative of sum lam . a_ewald, both through each particle's own position
+ * (the tidal tensor of the real-space replica terms and of the Fourier
+ * sum) and through the root moments (mass, centre of mass, quadrupole) that
+ * every particle shapes.  p: the parameters the forward evaluation used
+ * (root moments and h-table of changa_ewald_table).  Together with
+ * changa_gravity_vjp_mixed at fperiod it gives the adjoint of a periodic
+ * evaluation. */
+int changa_ewald_vjp(const double *parts, long long n_parts, const ChangaEwaldParams *p,
+                     const double *lam, double *grad, cudaStream_t stream);
 
 /* Moment up-pass on the device over a fixed topology (no reference
  * counterpart; the reference builds moments on the host,
@@ -390,8 +404,8 @@ void changa_walk_set_pool_factor(double factor);
 void changa_walk_set_test_small_stack(int on);
 /* Traversal launches re-run with the large stack so far (in this process). */
 long long changa_walk_stack_reruns(void);
-/* changa_walk of a quadrupole tree with at least min_tree_buckets buckets
- * walks in two phases: first once per group of at most max_buckets buckets
+/* changa_walk of a tree with at least min_tree_buckets buckets walks in
+ * two phases: first once per group of at most max_buckets buckets
  * (the highest node whose subtree holds no more), down to the group node,
  * which the group's buckets share; then each bucket from the entries still
  * undecided there.  The lists hold the same entries as the one-phase walk.

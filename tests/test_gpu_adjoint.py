@@ -290,3 +290,117 @@ def test_leapfrog_gradient_vs_fd_plummer64k(cuda_ok):
         e = np.abs(g - fd) / (np.abs(fd) + 1e-3 * np.abs(fd).max())
         print("plummer64k FD %s: max rel %.3e median %.3e" % (kind, e.max(), np.median(e)))
         assert e.max() < 1e-3, kind
+
+
+def _root(parts):
+    """Root moments (moments layout) of FP64 parts {m, soft, x, y, z}: mass,
+    centre of mass and the raw second moment about it."""
+    m, x = parts[:, 0], parts[:, 2:5]
+    M = m.sum()
+    cm = (m[:, None] * x).sum(0) / M
+    e = x - cm
+    Q = np.einsum("i,ij,ik->jk", m, e, e)
+    return np.array([0.0, 0.0, M, cm[0], cm[1], cm[2], Q[0, 0], Q[0, 1], Q[0, 2], Q[1, 1],
+                     Q[1, 2], Q[2, 2]])
+
+
+def test_ewald_vjp_matches_fd(cuda_ok):
+    """changa_ewald_vjp against central differences of the FP64 Ewald term
+    (changa_ewald_forces) with its root moments and h-table recomputed at
+    every perturbed configuration: the derivative through each particle's
+    own position and through the root's mass, centre and quadrupole, on a
+    clustered periodic set whose particles reach the series branch near the
+    centre of mass and the erf hole."""
+    import ctypes as C
+
+    import torch
+    from changa_gb300 import _native as N
+    from changa_gb300 import gravity, ics
+    lib = N.cuda_lib()
+    p = ics.nfw_halos(512, ics.rng_for(8), soft=1e-3)
+    parts = np.concatenate([p["mass"][:, None], p["soft"][:, None], p["pos"]], axis=1)
+    ew = gravity.EwaldConfig(1.0, 1, 2.6, 2.8)
+    rng = np.random.default_rng(3)
+    lam = rng.normal(size=(len(parts), 3))
+
+    def accel(pp):
+        ep = ew.params(_root(pp))
+        dp = torch.from_numpy(np.ascontiguousarray(pp)).cuda()
+        v = torch.zeros((len(pp), 5), dtype=torch.float64, device="cuda")
+        N.check(lib.changa_ewald_forces(N.CHANGA_FORM_FP64, dp.data_ptr(), len(pp), None, len(pp),
+                                        C.byref(ep), v.data_ptr(),
+                                        torch.cuda.current_stream().cuda_stream), "ewald_forces")
+        return v[:, :3].cpu().numpy()
+
+    def f(pp):
+        return float((accel(pp) * lam).sum())
+
+    ep = ew.params(_root(parts))
+    dp = torch.from_numpy(np.ascontiguousarray(parts)).cuda()
+    dl = torch.from_numpy(np.ascontiguousarray(lam)).cuda()
+    grad = torch.zeros((len(parts), 4), dtype=torch.float64, device="cuda")
+    N.check(lib.changa_ewald_vjp(dp.data_ptr(), len(parts), C.byref(ep), dl.data_ptr(),
+                                 grad.data_ptr(), torch.cuda.current_stream().cuda_stream),
+            "ewald_vjp")
+    g = grad.cpu().numpy()
+    h = 1e-5
+    errs = []
+    for i in rng.choice(len(parts), 24, replace=False):
+        for c in (2, 3, 4, 0):  # x, y, z, then the mass
+            hh = h if c else h * parts[i, 0]
+            pp, pm = parts.copy(), parts.copy()
+            pp[i, c] += hh
+            pm[i, c] -= hh
+            fd = (f(pp) - f(pm)) / (2 * hh)
+            got = g[i, c - 2] if c else g[i, 3]
+            scale = np.abs(g[:, :3]).max() if c else np.abs(g[:, 3]).max()
+            errs.append(abs(fd - got) / (abs(fd) + 1e-4 * scale))
+    print("ewald vjp vs FD: max %.2e, median %.2e" % (max(errs), np.median(errs)))
+    assert max(errs) < 1e-5
+
+
+def test_vjp_periodic_matches_fd(cuda_ok):
+    """A periodic evaluation (cell and particle lists with replica offsets,
+    plus the Ewald term) through one fixed tree: the list adjoint at the
+    period plus changa_ewald_vjp against central differences of the FP64
+    form, with the moments and the Ewald root refreshed at every perturbed
+    configuration."""
+    import torch
+    from changa_gb300 import gravity, ics
+    from changa_gb300.adjoint import TreeStep
+    p = ics.nfw_halos(4096, ics.rng_for(9), soft=1e-3)
+    t_ = lambda a: torch.from_numpy(np.ascontiguousarray(a, dtype=np.float64)).cuda()
+    x, m, s = t_(p["pos"]), t_(p["mass"]), t_(p["soft"])
+    ew = gravity.EwaldConfig(1.0, 1, 2.6, 2.8)
+    t = TreeStep(x, m, s, theta=0.7, period=1.0, ewald=ew)
+    assert t.lists.cells.n_entries > 0 and t.ds.ewald_params is not None
+    lam = torch.randn(x.shape, dtype=torch.float64, device="cuda",
+                      generator=torch.Generator("cuda").manual_seed(4))
+    t.load(x, m, s)
+    gx, gm = t.vjp(lam)
+
+    def f(xx, mm):
+        t.load(xx, mm, s)
+        return (t.accel("fp64") * lam).sum().item()
+
+    # close pairs in the halo cores: the central difference's truncation
+    # error reaches 5e-4 at h = 1e-5 and 4e-6 at h = 1e-6 (isolated or not)
+    rng = np.random.default_rng(6)
+    h = 1e-6
+    errs_x, errs_m = [], []
+    for i in rng.choice(x.shape[0], 12, replace=False):
+        for c in range(3):
+            xp, xm_ = x.clone(), x.clone()
+            xp[i, c] += h
+            xm_[i, c] -= h
+            fd = (f(xp, m) - f(xm_, m)) / (2 * h)
+            errs_x.append(abs(fd - gx[i, c].item()) / (abs(fd) + 1e-3 * gx.abs().max().item()))
+    for i in rng.choice(x.shape[0], 12, replace=False):
+        hm = 1e-4 * m[i].item()
+        mp, mm_ = m.clone(), m.clone()
+        mp[i] += hm
+        mm_[i] -= hm
+        fd = (f(x, mp) - f(x, mm_)) / (2 * hm)
+        errs_m.append(abs(fd - gm[i].item()) / (abs(fd) + 1e-3 * gm.abs().max().item()))
+    print("periodic single-eval FD: x max %.3e, m max %.3e" % (max(errs_x), max(errs_m)))
+    assert max(errs_x) < 3e-5 and max(errs_m) < 3e-5

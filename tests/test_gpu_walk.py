@@ -104,26 +104,33 @@ def test_walk_two_phase(cuda_ok, gmax):
     down to its group node, then each bucket from the group's frontier, its
     lists starting with the group's prefix lists) gives every bucket the
     host walk's entries: open and periodic trees (one and two replica
-    shells), small and large buckets, single traversal and count + fill,
-    and the forces of the one-phase lists."""
+    shells), small and large buckets, the hexadecapole rules with softened
+    cells (split per bucket from the group's cells), single traversal and
+    count + fill, and the forces of the one-phase lists."""
     from changa_gb300 import _native as N
     lib = N.cuda_lib()
     p = ics.plummer(65536, ics.rng_for(6), soft=0.01)
     g = ics.lattice_grf(16, ics.rng_for(7))
+    h = ics.plummer(16384, ics.rng_for(3))
+    h["soft"][:] = 0.3  # hexadecapole rules with many softened cells
     cases = [tree.build_lists(p["pos"], p["mass"], p["soft"], n_bucket=4, theta=0.7),
              tree.build_lists(p["pos"], p["mass"], p["soft"], n_bucket=32, theta=0.5),
              tree.build_lists(g["pos"], g["mass"], g["soft"], n_bucket=8, theta=0.7, period=1.0),
              tree.build_lists(g["pos"], g["mass"], g["soft"], n_bucket=8, theta=0.7, period=1.0,
-                              n_replicas=2)]
+                              n_replicas=2),
+             tree.build_lists(h["pos"], h["mass"], h["soft"], n_bucket=8, theta=0.7, order=4)]
     lib.changa_walk_set_groups(gmax, 1)
     try:
         for L in cases:
             nb = len(L.bucket_starts)
             for method in ("single", "two_pass"):
-                cells, plist, _ = gpu_walk(L, method=method)
+                cells, plist, soft = gpu_walk(L, method=method)
                 assert same_entries(L.cells, cells, nb) and same_entries(L.plist, plist, nb)
+                if L.order == 4:
+                    assert L.softcells.n_entries > 0 and same_entries(L.softcells, soft, nb)
+            reqs = [cells, plist] + ([soft] if L.order == 4 else [])
             host = gravity.DeviceSystem(L).step("fp64").cpu().numpy()
-            dev = gravity.DeviceSystem(L, device_reqs=[cells, plist]).step("fp64").cpu().numpy()
+            dev = gravity.DeviceSystem(L, device_reqs=reqs).step("fp64").cpu().numpy()
             assert force_rel_err(dev, host).max() < 1e-12
     finally:
         lib.changa_walk_set_groups(32, 4096)
