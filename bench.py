@@ -514,19 +514,26 @@ def measure_adjoint(leapfrog=True, reps=20, tune=True):
     return out
 
 
-def measure_device_pipeline(wl, pts, interactions, reps=3):
+def measure_device_pipeline(wl, pts, interactions, ew=None, reps=3):
     """Positions already on the device to device-resident lists: the tree
-    built on the GPU (changa_tree_build) and walked there
-    (changa_walk_count/fill); best of `reps` after one untimed run.  The
-    interaction count must equal the host lists'."""
+    built on the GPU (changa_tree_build) and walked there (changa_walk);
+    best of `reps` after one untimed run.  The interaction count must equal
+    the host lists'.  Then the fused route on the last tree
+    (changa_walk_forces: walk and FP32-mixed forces in one pass, no lists,
+    with the Ewald term), best of `reps`, against the list route's forces
+    on the same tree (walk + changa_gravity_step)."""
     import numpy as np
     import torch
+    from changa_gb300 import gravity
     from changa_gb300.gputree import DeviceTree
-    from changa_gb300.walk import gpu_walk
+    from changa_gb300.walk import gpu_walk, walk_forces
     t = lambda a: torch.from_numpy(np.ascontiguousarray(a, dtype=np.float64)).cuda()
     pos, m, s = t(pts["pos"]), t(pts["mass"]), t(pts["soft"])
     best = None
+    tree = None
     for rep in range(reps + 1):
+        if tree is not None:
+            tree.close()
         torch.cuda.synchronize()
         t0 = time.perf_counter()
         tree = DeviceTree(pos, m, s, n_bucket=wl.n_bucket, theta=wl.theta, period=wl.period)
@@ -536,12 +543,37 @@ def measure_device_pipeline(wl, pts, interactions, reps=3):
         torch.cuda.synchronize()
         t2 = time.perf_counter()
         n_int = cells.interactions() + plist.interactions()
-        tree.close()
-        del cells, plist
         if rep and (best is None or t2 - t0 < best["tree_build_s"] + best["walk_s"]):
             best = {"tree_build_s": t1 - t0, "walk_s": t2 - t1, "n_nodes": tree.n_nodes,
                     "n_buckets": tree.n_buckets}
+        if rep < reps:
+            del cells, plist
     best["interactions_match"] = n_int == interactions
+    ds = gravity.DeviceSystem(tree, device_reqs=[cells, plist], ewald=ew)
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    list_ms = []
+    for _ in range(reps + 1):
+        ev0.record()
+        ref = ds.step("mixed")
+        ev1.record()
+        torch.cuda.synchronize()
+        list_ms.append(ev0.elapsed_time(ev1))
+    best["list_forces_s"] = min(list_ms[1:]) * 1e-3
+    out = torch.empty((tree.n, 5), dtype=torch.float64, device="cuda")
+    fused = []
+    for _ in range(reps + 1):
+        torch.cuda.synchronize()
+        f0 = time.perf_counter()
+        walk_forces(tree, ewald=ds.ewald_params, out=out)
+        torch.cuda.synchronize()
+        fused.append(time.perf_counter() - f0)
+    da = (out[:, :3] - ref[:, :3]).norm(dim=1) / ref[:, :3].norm(dim=1)
+    best["fused"] = {"walk_forces_s": min(fused[1:]),
+                     "vs_walk_plus_list_forces_s": best["walk_s"] + best["list_forces_s"],
+                     "interactions_per_s": interactions / min(fused[1:]),
+                     "max_rel_diff_vs_lists": float(da.max().item()),
+                     "median_rel_diff_vs_lists": float(da.median().item())}
+    tree.close()
     return best
 
 
@@ -825,7 +857,7 @@ def main_ours(args):
         gpu_walk(lists)
         walk_gpu = {}
         gpu_walk(lists, timings=walk_gpu)
-        device_pipeline = measure_device_pipeline(wl, pts, I)
+        device_pipeline = measure_device_pipeline(wl, pts, I, ew=ew)
         device_pipeline["walk_on_host_lists_s"] = walk_gpu.get("walk_s")
         device_pipeline["host_tree_walk_serialise_s"] = t_walk
     I_c, I_p = lists.cells.interactions(), lists.plist.interactions()

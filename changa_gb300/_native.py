@@ -247,6 +247,8 @@ CUDA_SIGNATURES = {
     "changa_walk_set_pool_factor": (None, [_D]),
     "changa_walk_set_test_small_stack": (None, [C.c_int]),
     "changa_walk_set_groups": (None, [C.c_int, C.c_int]),
+    "changa_walk_forces": (_I, [C.POINTER(ChangaTreeView), C.POINTER(ChangaWalkParams), _VP, _VP,
+                                _LL, C.POINTER(ChangaEwaldParams), _VP, _VP]),
     "changa_walk_stack_reruns": (C.c_longlong, []),
     "changa_gravity_step_hexa": (_I, [_I, _VP, _LL, _VP, _LL, C.POINTER(ChangaListRequest),
                                       C.POINTER(ChangaListRequest),

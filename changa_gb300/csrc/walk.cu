@@ -38,9 +38,11 @@
  */
 #include <atomic>
 #include <cstring>
+#include <type_traits>
 #include <vector>
 
 #include "chg_internal.h"
+#include "list_eval.cuh"
 
 namespace chg {
 namespace {
@@ -566,6 +568,368 @@ __global__ void __launch_bounds__(kWalkWarps * 32) walk_kernel(const WalkArgs a)
   }
 }
 
+/* ---- fused walk and evaluation (FP32-mixed form, quadrupole) ----
+ *
+ * Phase 2 of the two-phase walk with the forces evaluated as the entries
+ * are decided, instead of written to lists (the reference's prototype of a
+ * walk that evaluates as it goes is gpuLocalTreeWalk, HostCUDA.cu:724-942).
+ * A warp takes buckets from a work queue.  Per chunk of up to 32 targets it
+ * keeps the paired target-parallel evaluation of the list kernels (lanes
+ * own targets in G = 32 / nt groups; list_kernel_tp2): blocks of 32
+ * entries are gathered, finished relative to the bucket, staged in pairs
+ * and evaluated with pc_pair / pp_pair, and each block's sums are folded
+ * into Kahan-compensated totals.  The blocks come, in this order of
+ * preference, from the group's prefix cells and particles (phase 1's
+ * output, shared by the group's buckets), from the cells the walk has
+ * accepted so far, and from the particles of the source buckets it has
+ * opened (queued as runs); a walk step runs only when no block is ready,
+ * so each step adds at most 32 cells and 32 runs to buffers of 64.  Each of
+ * the two evaluations has one call site in the kernel.  A bucket of more
+ * than 32 targets is walked once per chunk.  The decisions, and so the
+ * interactions, are the list walk's; only the summation order differs. */
+constexpr int kFusedWarps = 4;        // warps per block (2 with the re-run's larger stack)
+constexpr int kFusedWarpsPerSM = 16;  // the register cap: 128 per thread
+
+struct FusedArgs {
+  ListArgs cells;       // src: packed FP32-mixed cells, n_src: nodes; fperiod_f
+  ListArgs parts;       // src: packed FP32-mixed particles, n_src: particles
+  double* vars;         // n_src(parts) x 5 FP64, written per target
+  unsigned int* queue;  // bucket counter, zero at launch
+};
+
+/* One loop per list, not unrolled, with the softening test on every block:
+ * the walk and both evaluations share the SM's instruction cache, which the
+ * list kernels' four unrolled loop copies per list overran (nfw8m: 83.9 ms
+ * this way, 89.5 ms with those copies, 132 ms with one loop unrolled by 2;
+ * a 168-register budget of 12 warps per SM was slower still). */
+template <int STACK, int WARPS>
+__global__ void __launch_bounds__(WARPS * 32, kFusedWarpsPerSM / WARPS)
+    walk_eval_kernel(const WalkArgs a, const FusedArgs f) {
+  __shared__ int2 stk[WARPS][STACK];
+  __shared__ int chain[WARPS][64];
+  __shared__ int2 pcell[WARPS][64];  // accepted cells waiting for a block
+  __shared__ int4 prun[WARPS][64];   // opened source buckets {first, count, code}
+  __shared__ __align__(16) float4 stage[WARPS][16 * 6];
+  __shared__ float ssoft[WARPS][32];
+  __shared__ double red[WARPS][5][32];
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const unsigned below = (1u << lane) - 1u;
+  const float4* pp = static_cast<const float4*>(f.parts.src);
+  using CellT = std::integral_constant<bool, true>;
+  using PartT = std::integral_constant<bool, false>;
+  using Mark = std::integral_constant<bool, true>;
+
+  for (;;) {
+    int b = 0;
+    if (lane == 0) b = (int)atomicAdd(f.queue, 1u);
+    b = __shfl_sync(kFull, b, 0);
+    if (b >= a.n_buckets) return;
+    const int bn = a.bucket_node[b];
+    const int gid = a.bucket_group[b];
+    if (bn < 0 || bn >= a.n_nodes || gid < 0 || gid >= a.n_groups) {  // memory safety
+      if (lane == 0) atomicExch(a.error, 1);
+      continue;
+    }
+    const int gnode = a.group_node[gid];
+    int depth = 0, gdepth = -1;
+    if (lane == 0) {
+      int n = 0;
+      for (int x = bn; x >= 0 && x < a.n_nodes && n < 65; x = a.parent[x]) ++n;
+      if (n > 64) {
+        depth = -1;
+      } else {
+        int k = n - 1;
+        for (int x = bn; k >= 0; x = a.parent[x]) {
+          if (x == gnode) gdepth = k;
+          chain[warp][k--] = x;
+        }
+        depth = chain[warp][0] == 0 ? n - 1 : -1;
+      }
+    }
+    depth = __shfl_sync(kFull, depth, 0);
+    gdepth = __shfl_sync(kFull, gdepth, 0);
+    const long long tbase = a.info[4 * (size_t)bn + 2];
+    const int n = a.info[4 * (size_t)bn + 3];
+    if (depth < 0 || gdepth < 0 || n <= 0 || tbase < 0 || tbase + n > f.parts.n_src) {
+      if (lane == 0) atomicExch(a.error, 1);
+      continue;
+    }
+    /* the bucket's reference point: its first particle's split position */
+    const float4 h0 = __ldg(pp + kPartPackF4 * tbase), l0 = __ldg(pp + kPartPackF4 * tbase + 1);
+    const float3 chi = make_float3(h0.x, h0.y, h0.z), clo = make_float3(l0.x, l0.y, l0.z);
+
+    for (int t0 = 0; t0 < n; t0 += 32) {
+      const int nt = min(32, n - t0);
+      const int G = 32 / nt, grp = lane / nt;
+      const bool active = grp < G;
+      const long long ti = tbase + t0 + (active ? lane - grp * nt : 0);
+      const float4 th = __ldg(pp + kPartPackF4 * ti), tl = __ldg(pp + kPartPackF4 * ti + 1);
+      const float tx = (th.x - chi.x) + (tl.x - clo.x), ty = (th.y - chi.y) + (tl.y - clo.y),
+                  tz = (th.z - chi.z) + (tl.z - clo.z);
+      const float tmass = th.w, tsoft = tl.w;
+      const float tsmax = warp_max(active ? tsoft : 0.f);
+      const float3 blo = make_float3(warp_min(active ? tx : 3.4e38f),
+                                     warp_min(active ? ty : 3.4e38f),
+                                     warp_min(active ? tz : 3.4e38f));
+      const float3 bhi = make_float3(warp_max(active ? tx : -3.4e38f),
+                                     warp_max(active ? ty : -3.4e38f),
+                                     warp_max(active ? tz : -3.4e38f));
+      const f2 tx2 = pk2(tx, tx), ty2 = pk2(ty, ty), tz2 = pk2(tz, tz);
+      const f2 tmc = pk2(-tmass, -tmass), tmp = pk2(tmass, tmass);
+      float sx = 0.f, sy = 0.f, sz = 0.f, sp = 0.f, cx = 0.f, cy = 0.f, cz = 0.f, cp = 0.f;
+      float idc = 0.f;  // cells: the minimum of -(m_t + M) b (pc_pair's form)
+      float idp = 0.f;  // particles: the maximum of (m_t + m) b
+
+      /* One block: this lane's entry ent (valid when v) gathered, finished
+       * and staged, then every staged pair on this lane's target. */
+      auto eval_block = [&](int2 ent, bool v, auto cellc) {
+        constexpr bool CELL = decltype(cellc)::value;
+        constexpr int PW = CELL ? 6 : 2;
+        const ListArgs& la = CELL ? f.cells : f.parts;
+        RawRec<kMix, CELL> raw;
+        gather_raw_entry<kMix, CELL>(la, v ? ent : make_int2(0, 0x49 << 22), raw);
+        float4 rec[3];
+        const float ls = finish_raw<kMix, CELL>(la, raw, v, chi, clo, rec);
+        {
+          float* pb = reinterpret_cast<float*>(stage[warp] + (lane >> 1) * PW);
+          const int h = lane & 1;
+          if constexpr (CELL) {
+            stage_cell_half(pb, h, rec[0], rec[1], rec[2]);
+          } else {
+            pb[pair_slot(0, h)] = rec[0].x;
+            pb[pair_slot(1, h)] = rec[0].y;
+            pb[pair_slot(2, h)] = rec[0].z;
+            pb[pair_slot(3, h)] = rec[0].w;
+          }
+        }
+        ssoft[warp][lane] = ls;
+        const float ss = warp_max(ls) + tsmax;
+        const float near2 = ss * ss;
+        __syncwarp();
+        const float4* st = stage[warp];
+        f2 ax2 = 0ull, ay2 = 0ull, az2 = 0ull, pot2 = 0ull, pw2 = 0ull;
+        unsigned nmask = 0;
+        float ex = 0.f, ey = 0.f, ez = 0.f, ep = 0.f;
+        if constexpr (CELL) {
+          auto body = [&](int p, auto near) {
+            pc_pair<decltype(near)::value>(st + p * PW, &ssoft[warp][2 * p], tx2, ty2, tz2, tmc,
+                                           tsoft, near2, pot2, pw2, ax2, ay2, az2, idc);
+          };
+          if (active) {
+#pragma unroll 1
+            for (int p = grp; p < 16; p += G) body(p, Mark{});
+          }
+        } else {
+          auto body = [&](int p, auto mark) {
+            pp_pair<decltype(mark)::value>(st + p * PW, p, tx2, ty2, tz2, tmp, near2, pot2, ax2,
+                                           ay2, az2, idp, nmask);
+          };
+          if (active) {
+#pragma unroll 1
+            for (int p = grp; p < 16; p += G) body(p, Mark{});
+          }
+          pp_soft_pass(st, ssoft[warp], nmask, tx, ty, tz, tsoft, tmass, ex, ey, ez, ep, idp);
+        }
+        float x0, x1, y0, y1, z0, z1, p0, p1;
+        up2(ax2, x0, x1);
+        up2(ay2, y0, y1);
+        up2(az2, z0, z1);
+        up2(pot2, p0, p1);
+        float pblk;
+        if constexpr (CELL) {
+          float w0_, w1_;
+          up2(pw2, w0_, w1_);
+          pblk = (p0 + p1) - 0.5f * (w0_ + w1_);
+        } else {
+          pblk = -((p0 + p1) + ep);
+        }
+        kahan_add(sx, cx, (x0 + x1) + ex);
+        kahan_add(sy, cy, (y0 + y1) + ey);
+        kahan_add(sz, cz, (z0 + z1) + ez);
+        kahan_add(sp, cp, pblk);
+        __syncwarp();  // the stage is rewritten by the next block
+      };
+
+      long long pc_pos = a.pre_off[0][gid], pc_end = a.pre_off[0][gid + 1];
+      long long pp_pos = a.pre_off[1][gid], pp_end = a.pre_off[1][gid + 1];
+      long long fpos = a.off_front[gid], fend = a.off_front[gid + 1];
+      int sp_ = 0;       // walk stack entries
+      int npc = 0;       // pending cells
+      int nrun = 0;      // pending runs
+      int roff = 0;      // particles of run 0 already evaluated
+      int npart = 0;     // pending particles (over the runs, less roff)
+      __syncwarp();
+      for (;;) {
+        const bool walked = sp_ == 0 && fpos >= fend;
+        int which = -1;  // 0 a cell block, 1 a particle block
+        int2 ent = make_int2(0, 0x49 << 22);
+        bool v = false;
+        if (pc_pos < pc_end) {
+          const int ne = (int)min(32LL, pc_end - pc_pos);
+          v = lane < ne;
+          if (v) ent = a.pre[0][pc_pos + lane];
+          pc_pos += ne;
+          which = 0;
+        } else if (pp_pos < pp_end) {
+          const int ne = (int)min(32LL, pp_end - pp_pos);
+          v = lane < ne;
+          if (v) ent = a.pre[1][pp_pos + lane];
+          pp_pos += ne;
+          which = 1;
+        } else if (npc >= 32 || (walked && npc > 0)) {
+          const int ne = min(32, npc);
+          v = lane < ne;
+          if (v) ent = pcell[warp][lane];
+          const int rest = npc - ne;  // at most 31
+          const int2 keep = lane < rest ? pcell[warp][ne + lane] : make_int2(0, 0);
+          __syncwarp();
+          if (lane < rest) pcell[warp][lane] = keep;
+          npc = rest;
+          which = 0;
+        } else if (npart >= 32 || (walked && npart > 0)) {
+          /* the next min(32, npart) particles of the queued runs: entry j
+           * belongs to the first run whose inclusive end exceeds j */
+          const int ne = min(32, npart);
+          int cnt = 0;
+          int4 run = make_int4(0, 0, 0, 0);
+          if (lane < nrun) {
+            run = prun[warp][lane];
+            cnt = run.y - (lane == 0 ? roff : 0);
+          }
+          int tot;
+          const int excl = warp_excl_scan(cnt, tot);
+          const int incl = excl + cnt;
+          int owner = 0;
+#pragma unroll
+          for (int bit = 16; bit > 0; bit >>= 1)
+            if (__shfl_sync(kFull, incl, owner + bit - 1) <= lane) owner += bit;
+          const int o_excl = __shfl_sync(kFull, excl, owner);
+          const int o_first = __shfl_sync(kFull, run.x, owner);
+          const int o_code = __shfl_sync(kFull, run.z, owner);
+          v = lane < ne;
+          if (v) ent = make_int2(o_first + (owner == 0 ? roff : 0) + (lane - o_excl), o_code << 22);
+          /* runs used up by the block, and how far into the next one */
+          const int done = __popc(__ballot_sync(kFull, lane < nrun && incl <= ne));
+          int used = __shfl_sync(kFull, excl, done & 31);
+          if (done == 32) used = ne;  // 32 runs of one particle each
+          roff = done < nrun ? (done == 0 ? roff : 0) + (ne - used) : 0;
+          const int left = nrun - done;  // at most 64
+          const int4 k0 = lane < left ? prun[warp][done + lane] : make_int4(0, 0, 0, 0);
+          const int4 k1 = lane + 32 < left ? prun[warp][done + lane + 32] : make_int4(0, 0, 0, 0);
+          __syncwarp();
+          if (lane < left) prun[warp][lane] = k0;
+          if (lane + 32 < left) prun[warp][lane + 32] = k1;
+          nrun = left;
+          npart -= ne;
+          which = 1;
+        } else if (walked) {
+          break;
+        }
+        if (which == 0) {
+          eval_block(ent, v, CellT{});
+          continue;
+        }
+        if (which == 1) {
+          eval_block(ent, v, PartT{});
+          continue;
+        }
+        /* one walk step (walk_kernel, phase 2, quadrupole): up to 32 entries
+         * tested; opened children pushed, accepted cells and opened source
+         * buckets queued */
+        int nst;
+        int2 e = make_int2(-1, 0);
+        if (sp_ > 0) {
+          nst = sp_ < 32 ? sp_ : 32;
+          const int top = sp_ - nst;
+          if (lane < nst) e = stk[warp][top + lane];
+          sp_ = top;
+        } else {
+          nst = (int)(fend - fpos < 32 ? fend - fpos : 32);
+          if (lane < nst) {
+            const int2 fr = a.front[fpos + lane];
+            e = make_int2(fr.x, ((gdepth + 1) << 16) | (fr.y & 0xffff));
+          }
+          fpos += nst;
+        }
+        __syncwarp();
+        int kind = -1, c0 = -1, c1 = -1, pfirst = 0, pcount = 0;
+        const int src = e.x, level = e.y >> 16, code = e.y & 0xffff;
+        if (src >= 0 && src < a.n_nodes && level <= depth) {
+          const int local = chain[warp][level];
+          const bool local_bucket = level == depth;
+          const WalkNode nd = a.nodes[src];
+          const int open = open_criterion_screened(a, nd, src, local, local_bucket, code);
+          if (open == 0) {
+            kind = 0;
+          } else if (nd.link.x < 0 && nd.link.y < 0) {
+            kind = 2;
+            pfirst = nd.link.z;
+            pcount = nd.link.w;
+          } else if (open == 1 || local_bucket) {
+            kind = 3;
+            c0 = nd.link.x;
+            c1 = nd.link.y;
+          } else {
+            kind = 4;
+          }
+        }
+        const int npush = kind == 3 ? (c0 >= 0) + (c1 >= 0) : (kind == 4 ? 1 : 0);
+        int tpush;
+        int pos = sp_ + warp_excl_scan(npush, tpush);
+        if (sp_ + tpush > STACK) {  // uniform; the host re-runs the launch with the larger stack
+          if (lane == 0) atomicExch(a.error, 2);
+          return;
+        }
+        if (kind == 3) {
+          if (c1 >= 0) stk[warp][pos++] = make_int2(c1, (level << 16) | code);
+          if (c0 >= 0) stk[warp][pos++] = make_int2(c0, (level << 16) | code);
+        } else if (kind == 4) {
+          stk[warp][pos] = make_int2(src, ((level + 1) << 16) | code);
+        }
+        sp_ += tpush;
+        const unsigned mc = __ballot_sync(kFull, kind == 0);
+        const unsigned mr = __ballot_sync(kFull, kind == 2 && pcount > 0);
+        if (kind == 0) pcell[warp][npc + __popc(mc & below)] = make_int2(src, code << 22);
+        if (kind == 2 && pcount > 0)
+          prun[warp][nrun + __popc(mr & below)] = make_int4(pfirst, pcount, code, 0);
+        int tpart;
+        warp_excl_scan(kind == 2 && pcount > 0 ? pcount : 0, tpart);
+        npc += __popc(mc);
+        nrun += __popc(mr);
+        npart += tpart;
+        __syncwarp();  // pushes and queued entries visible to the next step
+      }
+
+      if (active) {
+        red[warp][0][lane] = (double)sx - (double)cx;
+        red[warp][1][lane] = (double)sy - (double)cy;
+        red[warp][2][lane] = (double)sz - (double)cz;
+        red[warp][3][lane] = (double)sp - (double)cp;
+        red[warp][4][lane] = fmax(-(double)idc, (double)idp);
+      }
+      __syncwarp();
+      if (lane < nt) {
+        double rx = 0, ry = 0, rz = 0, rp = 0, ri = 0;
+        for (int gg = 0; gg < G; ++gg) {
+          const int l = gg * nt + lane;
+          rx += red[warp][0][l];
+          ry += red[warp][1][l];
+          rz += red[warp][2][l];
+          rp += red[warp][3][l];
+          ri = fmax(ri, red[warp][4][l]);
+        }
+        double* out = f.vars + 5 * (tbase + t0 + lane);
+        out[0] = rx;
+        out[1] = ry;
+        out[2] = rz;
+        out[3] = rp;
+        out[4] = ri;
+      }
+      __syncwarp();
+    }
+  }
+}
+
 /* The append pass's chunks into CSR order: entry j of chunk c (rank r of
  * bucket b) goes to off[b] + r kChunk + j when it lies inside b's list. */
 __global__ void gather_chunks_kernel(const int2* __restrict__ pool, const int* __restrict__ cb,
@@ -917,6 +1281,116 @@ extern "C" void changa_walk_lists_free(ChangaWalkLists* out) {
   std::memset(out, 0, sizeof(*out));
 }
 
+/* Stream-ordered scratch blocks of one call, freed together. */
+struct Scratch {
+  cudaStream_t s;
+  std::vector<void*> blocks;
+  void* alloc(size_t bytes) {
+    void* q = nullptr;
+    if (cudaMallocAsync(&q, bytes < 256 ? 256 : bytes, s) != cudaSuccess) return nullptr;
+    blocks.push_back(q);
+    return q;
+  }
+  void release() {
+    for (void* q : blocks) cudaFreeAsync(q, s);
+    blocks.clear();
+  }
+};
+
+/* Groups of at most gmax buckets and phase 1 of the two-phase walk.
+ * Phase 1 walks each group's node once: its chain down to the group node
+ * is shared by all the group's buckets, so the entries accepted on it (the
+ * group's prefix lists) and those still undecided at the group node (its
+ * frontier) are the same for each of them.  Fills a's group fields and the
+ * phase 2 inputs (prefix lists, frontier), in scratch of sc. */
+static int walk_phase1(WalkArgs& a, const ChangaTreeView* t, int gmax, Scratch& sc,
+                       cudaStream_t s) {
+  const int nb = t->n_buckets;
+  const int tiles = (nb + kScanTile - 1) / kScanTile;
+  long long* ts = (long long*)sc.alloc((size_t)tiles * sizeof(long long));
+  if (!ts) return record_error(cudaErrorMemoryAllocation, "walk: memory", __FILE__, __LINE__);
+  int h_err = 0;
+  int* bfirst = (int*)sc.alloc((size_t)nb * sizeof(int));
+  int* gn = (int*)sc.alloc((size_t)nb * sizeof(int));
+  int* flag = (int*)sc.alloc((size_t)nb * sizeof(int));
+  long long* gex = (long long*)sc.alloc((size_t)(nb + 1) * sizeof(long long));
+  int* gex32 = (int*)sc.alloc((size_t)(nb + 1) * sizeof(int));
+  int* bucket_group = (int*)sc.alloc((size_t)nb * sizeof(int));
+  int* group_node = (int*)sc.alloc((size_t)nb * sizeof(int));
+  if (!bfirst || !gn || !flag || !gex || !gex32 || !bucket_group || !group_node)
+    return record_error(cudaErrorMemoryAllocation, "walk: memory", __FILE__, __LINE__);
+  const long long gb = ((long long)nb + 255) / 256, cap = (long long)sm_count() * 8;
+  const int grid = (int)(gb < cap ? gb : cap);
+  bucket_first_kernel<<<grid, 256, 0, s>>>(t->bucket_node, t->info, t->n_nodes, nb, bfirst);
+  bucket_group_node_kernel<<<grid, 256, 0, s>>>(t->bucket_node, t->parent, t->info, bfirst,
+                                                t->n_nodes, nb, gmax, gn);
+  group_flag_kernel<<<grid, 256, 0, s>>>(gn, nb, flag);
+  scan_tile_sums_kernel<<<tiles, kScanThreads, 0, s>>>(flag, nb, ts);
+  scan_tiles_kernel<<<1, kScanThreads, 0, s>>>(ts, tiles);
+  scan_apply_kernel<<<tiles, kScanThreads, 0, s>>>(flag, nb, ts, gex, gex32);
+  group_ids_kernel<<<grid, 256, 0, s>>>(gn, flag, gex, nb, bucket_group, group_node);
+  count_launch(7);
+  long long ng_ll = 0;
+  if (cudaMemcpyAsync(&ng_ll, gex + nb, sizeof(long long), cudaMemcpyDeviceToHost, s) !=
+          cudaSuccess ||
+      cudaStreamSynchronize(s) != cudaSuccess || ng_ll <= 0 || ng_ll > nb)
+    return record_error((int)cudaGetLastError(), "walk: groups", __FILE__, __LINE__);
+  const int ng = (int)ng_ll;
+  int* gcnt = (int*)sc.alloc((size_t)3 * ng * sizeof(int));
+  long long* goff = (long long*)sc.alloc((size_t)3 * (ng + 1) * sizeof(long long));
+  int* goff32 = (int*)sc.alloc((size_t)3 * (ng + 1) * sizeof(int));
+  if (!gcnt || !goff || !goff32)
+    return record_error(cudaErrorMemoryAllocation, "walk: memory", __FILE__, __LINE__);
+  a.group_node = group_node;
+  a.n_groups = ng;
+  a.bucket_group = bucket_group;
+  a.n_cells = gcnt;
+  a.n_parts = gcnt + ng;
+  a.n_soft = nullptr;
+  a.n_front = gcnt + 2 * (size_t)ng;
+  walk_run(a, kCount, s, 1);
+  const int gtiles = (ng + kScanTile - 1) / kScanTile;
+  for (int k = 0; k < 3; ++k) {
+    scan_tile_sums_kernel<<<gtiles, kScanThreads, 0, s>>>(gcnt + (size_t)k * ng, ng, ts);
+    scan_tiles_kernel<<<1, kScanThreads, 0, s>>>(ts, gtiles);
+    scan_apply_kernel<<<gtiles, kScanThreads, 0, s>>>(gcnt + (size_t)k * ng, ng, ts,
+                                                      goff + (size_t)k * (ng + 1),
+                                                      goff32 + (size_t)k * (ng + 1));
+    count_launch(3);
+  }
+  long long gtot[3] = {0, 0, 0};
+  for (int k = 0; k < 3; ++k)
+    cudaMemcpyAsync(&gtot[k], goff + (size_t)k * (ng + 1) + ng, sizeof(long long),
+                    cudaMemcpyDeviceToHost, s);
+  cudaMemcpyAsync(&h_err, a.error, sizeof(int), cudaMemcpyDeviceToHost, s);
+  if (cudaStreamSynchronize(s) != cudaSuccess)
+    return record_error((int)cudaGetLastError(), "walk: group count", __FILE__, __LINE__);
+  if (h_err) return walk_error(h_err);
+  int2* pre_cells = (int2*)sc.alloc((size_t)(gtot[0] > 0 ? gtot[0] : 1) * sizeof(int2));
+  int2* pre_parts = (int2*)sc.alloc((size_t)(gtot[1] > 0 ? gtot[1] : 1) * sizeof(int2));
+  int2* front = (int2*)sc.alloc((size_t)(gtot[2] > 0 ? gtot[2] : 1) * sizeof(int2));
+  if (!pre_cells || !pre_parts || !front)
+    return record_error(cudaErrorMemoryAllocation, "walk: memory", __FILE__, __LINE__);
+  a.off_cells = goff;
+  a.off_parts = goff + (ng + 1);
+  a.off_soft = nullptr;
+  a.off_front = goff + 2 * (size_t)(ng + 1);
+  a.cells = pre_cells;
+  a.parts = pre_parts;
+  a.soft = nullptr;
+  a.front = front;
+  walk_run(a, kFill, s, 1);
+  /* phase 2 reads the group outputs */
+  a.pre_off[0] = goff;
+  a.pre_off[1] = goff + (ng + 1);
+  a.pre[0] = pre_cells;
+  a.pre[1] = pre_parts;
+  a.off_cells = a.off_parts = a.off_soft = nullptr;
+  a.cells = a.parts = a.soft = nullptr;
+  a.n_front = nullptr;
+  return 0;
+}
+
 extern "C" int changa_walk(const ChangaTreeView* t, const ChangaWalkParams* p,
                            ChangaWalkLists* out, cudaStream_t s) {
   if (!out) return record_error(CHANGA_E_INVALID_ARG, "walk: output", __FILE__, __LINE__);
@@ -931,22 +1405,16 @@ extern "C" int changa_walk(const ChangaTreeView* t, const ChangaWalkParams* p,
   WalkArgs a;
   char* block = nullptr;
   if (int rc = walk_setup(t, p, a, &block, s)) return rc;
-  std::vector<void*> scratch{block};
+  Scratch sc{s, {block}};
   auto finish = [&](int rc) {
-    for (void* q : scratch) cudaFreeAsync(q, s);
-    scratch.clear();
+    sc.release();
     if (rc) {
       cudaStreamSynchronize(s);
       release_lists(out);
     }
     return rc;
   };
-  auto alloc = [&](size_t bytes) -> void* {
-    void* q = nullptr;
-    if (cudaMallocAsync(&q, bytes < 256 ? 256 : bytes, s) != cudaSuccess) return nullptr;
-    scratch.push_back(q);
-    return q;
-  };
+  auto alloc = [&](size_t bytes) { return sc.alloc(bytes); };
   int* cnt = (int*)alloc((size_t)3 * nb * sizeof(int));
   const int tiles = (nb + kScanTile - 1) / kScanTile;
   long long* ts = (long long*)alloc((size_t)tiles * sizeof(long long));
@@ -955,93 +1423,13 @@ extern "C" int changa_walk(const ChangaTreeView* t, const ChangaWalkParams* p,
   if (!cnt || !ts || !off || !ctr)
     return finish(record_error(cudaErrorMemoryAllocation, "walk: memory", __FILE__, __LINE__));
   int h_err = 0;
-  /* Walks of many buckets run in two phases.  Phase 1 walks each
-   * group's node once: its chain down to the group node is shared by all
-   * the group's buckets, so the entries accepted on it (the group's prefix
-   * lists) and those still undecided at the group node (its frontier) are
-   * the same for each of them.  Phase 2 walks each bucket from its group's
-   * frontier, its lists starting with the group's prefix. */
+  /* Walks of many buckets run in two phases (walk_phase1); phase 2 walks
+   * each bucket from its group's frontier, its lists starting with the
+   * group's prefix. */
   int phase = 0;
   const int gmax = g_group_max.load();
   if (gmax > 0 && g_group_min.load() > 0 && nb >= g_group_min.load()) {
-    int* bfirst = (int*)alloc((size_t)nb * sizeof(int));
-    int* gn = (int*)alloc((size_t)nb * sizeof(int));
-    int* flag = (int*)alloc((size_t)nb * sizeof(int));
-    long long* gex = (long long*)alloc((size_t)(nb + 1) * sizeof(long long));
-    int* gex32 = (int*)alloc((size_t)(nb + 1) * sizeof(int));
-    int* bucket_group = (int*)alloc((size_t)nb * sizeof(int));
-    int* group_node = (int*)alloc((size_t)nb * sizeof(int));
-    if (!bfirst || !gn || !flag || !gex || !gex32 || !bucket_group || !group_node)
-      return finish(record_error(cudaErrorMemoryAllocation, "walk: memory", __FILE__, __LINE__));
-    const long long gb = ((long long)nb + 255) / 256, cap = (long long)sm_count() * 8;
-    const int grid = (int)(gb < cap ? gb : cap);
-    bucket_first_kernel<<<grid, 256, 0, s>>>(t->bucket_node, t->info, t->n_nodes, nb, bfirst);
-    bucket_group_node_kernel<<<grid, 256, 0, s>>>(t->bucket_node, t->parent, t->info, bfirst,
-                                                  t->n_nodes, nb, gmax, gn);
-    group_flag_kernel<<<grid, 256, 0, s>>>(gn, nb, flag);
-    scan_tile_sums_kernel<<<tiles, kScanThreads, 0, s>>>(flag, nb, ts);
-    scan_tiles_kernel<<<1, kScanThreads, 0, s>>>(ts, tiles);
-    scan_apply_kernel<<<tiles, kScanThreads, 0, s>>>(flag, nb, ts, gex, gex32);
-    group_ids_kernel<<<grid, 256, 0, s>>>(gn, flag, gex, nb, bucket_group, group_node);
-    count_launch(7);
-    long long ng_ll = 0;
-    if (cudaMemcpyAsync(&ng_ll, gex + nb, sizeof(long long), cudaMemcpyDeviceToHost, s) !=
-            cudaSuccess ||
-        cudaStreamSynchronize(s) != cudaSuccess || ng_ll <= 0 || ng_ll > nb)
-      return finish(record_error((int)cudaGetLastError(), "walk: groups", __FILE__, __LINE__));
-    const int ng = (int)ng_ll;
-    int* gcnt = (int*)alloc((size_t)3 * ng * sizeof(int));
-    long long* goff = (long long*)alloc((size_t)3 * (ng + 1) * sizeof(long long));
-    int* goff32 = (int*)alloc((size_t)3 * (ng + 1) * sizeof(int));
-    if (!gcnt || !goff || !goff32)
-      return finish(record_error(cudaErrorMemoryAllocation, "walk: memory", __FILE__, __LINE__));
-    a.group_node = group_node;
-    a.n_groups = ng;
-    a.bucket_group = bucket_group;
-    a.n_cells = gcnt;
-    a.n_parts = gcnt + ng;
-    a.n_soft = nullptr;
-    a.n_front = gcnt + 2 * (size_t)ng;
-    walk_run(a, kCount, s, 1);
-    const int gtiles = (ng + kScanTile - 1) / kScanTile;
-    for (int k = 0; k < 3; ++k) {
-      scan_tile_sums_kernel<<<gtiles, kScanThreads, 0, s>>>(gcnt + (size_t)k * ng, ng, ts);
-      scan_tiles_kernel<<<1, kScanThreads, 0, s>>>(ts, gtiles);
-      scan_apply_kernel<<<gtiles, kScanThreads, 0, s>>>(gcnt + (size_t)k * ng, ng, ts,
-                                                        goff + (size_t)k * (ng + 1),
-                                                        goff32 + (size_t)k * (ng + 1));
-      count_launch(3);
-    }
-    long long gtot[3] = {0, 0, 0};
-    for (int k = 0; k < 3; ++k)
-      cudaMemcpyAsync(&gtot[k], goff + (size_t)k * (ng + 1) + ng, sizeof(long long),
-                      cudaMemcpyDeviceToHost, s);
-    cudaMemcpyAsync(&h_err, a.error, sizeof(int), cudaMemcpyDeviceToHost, s);
-    if (cudaStreamSynchronize(s) != cudaSuccess)
-      return finish(record_error((int)cudaGetLastError(), "walk: group count", __FILE__, __LINE__));
-    if (h_err) return finish(walk_error(h_err));
-    int2* pre_cells = (int2*)alloc((size_t)(gtot[0] > 0 ? gtot[0] : 1) * sizeof(int2));
-    int2* pre_parts = (int2*)alloc((size_t)(gtot[1] > 0 ? gtot[1] : 1) * sizeof(int2));
-    int2* front = (int2*)alloc((size_t)(gtot[2] > 0 ? gtot[2] : 1) * sizeof(int2));
-    if (!pre_cells || !pre_parts || !front)
-      return finish(record_error(cudaErrorMemoryAllocation, "walk: memory", __FILE__, __LINE__));
-    a.off_cells = goff;
-    a.off_parts = goff + (ng + 1);
-    a.off_soft = nullptr;
-    a.off_front = goff + 2 * (size_t)(ng + 1);
-    a.cells = pre_cells;
-    a.parts = pre_parts;
-    a.soft = nullptr;
-    a.front = front;
-    walk_run(a, kFill, s, 1);
-    /* phase 2 reads the group outputs */
-    a.pre_off[0] = goff;
-    a.pre_off[1] = goff + (ng + 1);
-    a.pre[0] = pre_cells;
-    a.pre[1] = pre_parts;
-    a.off_cells = a.off_parts = a.off_soft = nullptr;
-    a.cells = a.parts = a.soft = nullptr;
-    a.n_front = nullptr;
+    if (int rc = walk_phase1(a, t, gmax, sc, s)) return finish(rc);
     phase = 2;
   }
   /* Large trees: one traversal appends the entries into pools of chunks
@@ -1150,5 +1538,92 @@ extern "C" int changa_walk(const ChangaTreeView* t, const ChangaWalkParams* p,
   if (cudaStreamSynchronize(s) != cudaSuccess)
     return finish(record_error((int)cudaGetLastError(), "walk: entries", __FILE__, __LINE__));
   if (h_err) return finish(walk_error(h_err));
+  return finish(0);
+}
+
+/* ---- fused walk and evaluation: the host side ---- */
+
+template <int STACK, int WARPS>
+static cudaError_t launch_walk_eval(const WalkArgs& a, const FusedArgs& f, cudaStream_t s) {
+  int per_sm = 0;
+  cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(
+      &per_sm, walk_eval_kernel<STACK, WARPS>, WARPS * 32, 0);
+  if (e != cudaSuccess) return e;
+  if (per_sm < 1) per_sm = 1;
+  const long long want = ((long long)a.n_buckets + WARPS - 1) / WARPS;
+  const long long cap = (long long)sm_count() * per_sm;
+  walk_eval_kernel<STACK, WARPS><<<(int)(want < cap ? want : cap), WARPS * 32, 0, s>>>(a, f);
+  count_launch();
+  return cudaGetLastError();
+}
+
+extern "C" int changa_walk_forces(const ChangaTreeView* t, const ChangaWalkParams* p,
+                                  const double* moments, const double* parts, long long n_parts,
+                                  const ChangaEwaldParams* ewald, double* vars, cudaStream_t s) {
+  if (!walk_args_ok(t, p) || p->order != 2)
+    return record_error(CHANGA_E_INVALID_ARG, "walk_forces: arguments (quadrupole trees)",
+                        __FILE__, __LINE__);
+  if (!moments || !parts || !vars || n_parts <= 0)
+    return record_error(CHANGA_E_INVALID_ARG, "walk_forces: arrays", __FILE__, __LINE__);
+  if (t->n_buckets == 0) return 0;
+  WalkArgs a;
+  char* block = nullptr;
+  if (int rc = walk_setup(t, p, a, &block, s)) return rc;
+  Scratch sc{s, {block}};
+  auto finish = [&](int rc) {
+    sc.release();
+    if (rc) cudaStreamSynchronize(s);
+    return rc;
+  };
+  const size_t cb = (size_t)t->n_nodes * kCellPackF4 * sizeof(float4);
+  const size_t pb = (size_t)n_parts * kPartPackF4 * sizeof(float4);
+  float4* pc = (float4*)sc.alloc(cb);
+  float4* ppk = (float4*)sc.alloc(pb);
+  unsigned int* queue = (unsigned int*)sc.alloc(256);
+  if (!pc || !ppk || !queue)
+    return finish(record_error(cudaErrorMemoryAllocation, "walk_forces: memory", __FILE__, __LINE__));
+  cudaError_t e;
+  if ((e = launch_pack_cells(moments, t->n_nodes, pc, s)) != cudaSuccess ||
+      (e = launch_pack_parts(parts, n_parts, ppk, s)) != cudaSuccess)
+    return finish(record_error((int)e, "walk_forces: pack", __FILE__, __LINE__));
+  const int gmax = g_group_max.load() > 0 ? g_group_max.load() : 32;
+  if (int rc = walk_phase1(a, t, gmax, sc, s)) return finish(rc);
+  FusedArgs f{};
+  f.cells.src = pc;
+  f.cells.n_src = t->n_nodes;
+  f.cells.fperiod_f = (float)p->period;
+  f.cells.fperiod_d = p->period;
+  f.parts.src = ppk;
+  f.parts.n_src = n_parts;
+  f.parts.fperiod_f = (float)p->period;
+  f.parts.fperiod_d = p->period;
+  f.vars = vars;
+  f.queue = queue;
+  /* a warp that would exhaust its stack stops with error 2; the launch
+   * then runs again with the larger stack and rewrites every target */
+  int h_err = 0;
+  for (int attempt = 0; attempt < 2; ++attempt) {
+    if ((e = cudaMemsetAsync(queue, 0, sizeof(unsigned int), s)) != cudaSuccess ||
+        (e = cudaMemsetAsync(a.error, 0, sizeof(int), s)) != cudaSuccess)
+      return finish(record_error((int)e, "walk_forces: reset", __FILE__, __LINE__));
+    if (attempt == 1) {
+      e = launch_walk_eval<kWarpStackLarge, 2>(a, f, s);
+      g_stack_reruns.fetch_add(1);
+    } else if (g_test_small_stack.load()) {
+      e = launch_walk_eval<32, kFusedWarps>(a, f, s);  // runs out on the first opening steps
+    } else {
+      e = launch_walk_eval<kWarpStack, kFusedWarps>(a, f, s);
+    }
+    if (e != cudaSuccess) return finish(record_error((int)e, "walk_forces: launch", __FILE__, __LINE__));
+    if ((e = cudaMemcpyAsync(&h_err, a.error, sizeof(int), cudaMemcpyDeviceToHost, s)) !=
+            cudaSuccess ||
+        (e = cudaStreamSynchronize(s)) != cudaSuccess)
+      return finish(record_error((int)e, "walk_forces: status", __FILE__, __LINE__));
+    if (h_err != 2) break;
+  }
+  if (h_err) return finish(walk_error(h_err));
+  if (ewald && (e = launch_ewald_fp(kMix, parts, n_parts, nullptr, n_parts, *ewald, vars, s)) !=
+                   cudaSuccess)
+    return finish(record_error((int)e, "walk_forces: ewald", __FILE__, __LINE__));
   return finish(0);
 }

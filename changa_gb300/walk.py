@@ -138,3 +138,34 @@ def same_entries(host_req, dev_req, n_buckets):
         if not np.array_equal(key(d), key(h)):
             return False
     return True
+
+
+def walk_forces(lists, ewald=None, device="cuda", stream=None, out=None):
+    """Forces straight from the tree, with no interaction lists
+    (changa_walk_forces: the two-phase walk's second phase evaluates each
+    block of accepted cells and opened particles as it decides them,
+    FP32-mixed form, quadrupole trees).  lists: a TreeLists or a DeviceTree
+    (its node arrays, moments and particles); ewald: a ChangaEwaldParams for
+    a periodic tree.  Returns the N x 5 FP64 device array {a.xyz, potential,
+    dtGrav} in the tree's particle order (written, then the Ewald term
+    added)."""
+    import torch
+    lib = N.cuda_lib()
+    m = lists.meta
+    t = lambda a: (a.to(device) if isinstance(a, torch.Tensor)
+                   else torch.from_numpy(np.ascontiguousarray(a)).to(device))
+    geom, bbox, info = t(m["node_geom"]), t(m["node_bbox"]), t(m["node_info"])
+    parent, bnode = t(m["parent"]), t(m["bucket_node"])
+    moments, parts = t(lists.moments).contiguous(), t(lists.parts).contiguous()
+    tv = N.ChangaTreeView(geom.data_ptr(), bbox.data_ptr(), info.data_ptr(), parent.data_ptr(),
+                          int(geom.shape[0]), bnode.data_ptr(), int(bnode.shape[0]))
+    wp = N.ChangaWalkParams(float(lists.theta), int(getattr(lists, "order", 2)),
+                            float(lists.period), int(lists.n_replicas))
+    n = int(parts.shape[0])
+    if out is None:
+        out = torch.empty((n, 5), dtype=torch.float64, device=device)
+    s = stream if stream is not None else torch.cuda.current_stream().cuda_stream
+    N.check(lib.changa_walk_forces(C.byref(tv), C.byref(wp), moments.data_ptr(), parts.data_ptr(),
+                                   n, C.byref(ewald) if ewald is not None else None,
+                                   out.data_ptr(), s), "changa_walk_forces")
+    return out

@@ -412,6 +412,24 @@ long long changa_walk_stack_reruns(void);
  * Defaults 32 and 4096; 0 for either walks every bucket from the root. */
 void changa_walk_set_groups(int max_buckets, int min_tree_buckets);
 
+/* Walk and forces in one pass, with no interaction lists (FP32-mixed form,
+ * quadrupole trees).  Phase 1 of the two-phase walk writes each group's
+ * prefix lists and frontier; then a warp per bucket walks from its group's
+ * frontier and evaluates each 32 accepted cells or opened particles as they
+ * are decided, with the list kernels' paired arithmetic (the reference's
+ * prototype of the idea: gpuLocalTreeWalk, HostCUDA.cu:724-942).
+ * moments: n_nodes x 12 FP64 in the tree's node order (the moments the list
+ * entries index), parts: n_parts x 5 {m, soft, x, y, z} in tree order,
+ * vars: n_parts x 5 FP64, WRITTEN (not accumulated) for every particle of a
+ * bucket, then the Ewald term added when ewald is given.  The interactions
+ * are the list walk's; the sums agree with changa_gravity_step on its lists
+ * to FP32 summation order.  On GB300 it is slower than changa_walk plus
+ * changa_gravity_step (nfw8m: 86.6 ms against 37.7 ms), which stays the
+ * fast route.  Returns after the stream has finished. */
+int changa_walk_forces(const ChangaTreeView *tree, const ChangaWalkParams *p,
+                       const double *moments, const double *parts, long long n_parts,
+                       const ChangaEwaldParams *ewald, double *vars, cudaStream_t stream);
+
 /* Tree build on the device (no reference counterpart; restates the host
  * build, TreePiece.cpp:141-165 box and keys, GenericTreeNode.h:473-599
  * split, MultipoleMoments.h:206-352, 460-526 moments and radii): positions
