@@ -95,7 +95,11 @@ def test_walk_forces_device_tree(cuda_ok):
 
 
 def test_walk_forces_rejects_hexadecapole(cuda_ok):
+    from changa_gb300 import _native as N
+    lib = N.cuda_lib()
     p = ics.plummer(2048, ics.rng_for(3))
     L = tree.build_lists(p["pos"], p["mass"], p["soft"], n_bucket=16, theta=0.7, order=4)
+    lib.changa_gb300_last_error()  # clear
     with pytest.raises(RuntimeError, match="1001"):  # CHANGA_E_INVALID_ARG
         walk_forces(L)
+    assert lib.changa_gb300_last_error() == 1001  # read, and so cleared

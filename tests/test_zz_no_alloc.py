@@ -70,6 +70,7 @@ def test_noalloc_rejects_oversize(cuda_ok):
         req.list = req.markers = req.starts = req.sizes = 1  # never read
         req.n_buckets = 1
         req.n_entries = 1
+        lib.changa_gb300_last_error()  # the first error since the last read is kept: clear it
         before = lib.changa_gb300_kernel_launches()
         rc = lib.changa_cell_forces_mixed_noalloc(8, 300000, 8, 1, C.byref(req), 0.0, 8, None)
         assert rc == 1003
