@@ -286,6 +286,11 @@ def dropin_step(inp: DropInInputs, stream=None, cudart=None):
     lib.DataManagerTransferLocalTree(inp.moments.ptr, inp.moments.nbytes, inp.parts.ptr,
                                      inp.parts.nbytes, inp.vars.ptr, inp.vars.nbytes,
                                      C.byref(d_m), C.byref(d_p), C.byref(d_v), stream, inp.n, None)
+    # ChaNGa queues the Ewald launch right after the local tree transfer
+    # (DataManager.cpp:495-510, TreePiece::calculateEwald -> EwaldGPU), so
+    # it runs while the walk produces the lists and they are uploaded
+    if inp.ewald_data is not None:
+        lib.EwaldHost(d_p, d_v, C.byref(inp.ewald_data), stream, None, 0, 1)
     for k, (lst, mk, st, sz, req) in enumerate(inp.reqs):
         if req.n_buckets == 0:
             continue
@@ -306,8 +311,6 @@ def dropin_step(inp: DropInInputs, stream=None, cudart=None):
             lib.TreePieceCellListDataTransferLocal(C.byref(r))
         else:
             lib.TreePiecePartListDataTransferLocal(C.byref(r))
-    if inp.ewald_data is not None:
-        lib.EwaldHost(d_p, d_v, C.byref(inp.ewald_data), stream, None, 0, 1)
     lib.TransferParticleVarsBack(inp.out.ptr, inp.out.nbytes, d_v, stream, None)
     rt.cudaStreamSynchronize(stream)
     for p in (d_m, d_p, d_v):
