@@ -29,6 +29,7 @@
  *                     turn from the integer h before the hardware sin/cos.
  */
 #include <cmath>
+#include <vector>
 
 #include "chg_internal.h"
 #include "f32x2.cuh"
@@ -580,18 +581,24 @@ __global__ void __launch_bounds__(kMixWarps * 32) ewald_mix_kernel(
      * the cut (outside the hole), or the padding of an odd count, is
      * evaluated and multiplied by 0 (its terms are finite) */
     const f2 dx2 = pk2(dx, dx), dy2 = pk2(dy, dy), dz2 = pk2(dz, dz), L2 = pk2(L, L);
+    const float alpha = sqrtf(a2);
+    const f2 alphap = pk2(alpha, alpha);
     const f2 a2p = pk2(a2, a2), kap = pk2(ka, ka), twoa2p = pk2(twoa2, twoa2),
              foura4p = pk2(foura4, foura4), Mp = pk2(M, M), Q2p = pk2(Q2, Q2);
     const f2 xx = pk2(P.xx, P.xx), xy = pk2(P.xy, P.xy), xz = pk2(P.xz, P.xz),
              yy = pk2(P.yy, P.yy), yz = pk2(P.yz, P.yz), zz = pk2(P.zz, P.zz);
     f2 fp2 = 0ull, fx2 = 0ull, fy2 = 0ull, fz2 = 0ull;
+    /* a packed offset nibble k (0..15) as the float k - 8: k placed in the
+     * mantissa of 2^23 (exact), then 2^23 + 8 subtracted (exact) */
+    const f2 bias2 = pk2(8388616.0f, 8388616.0f);
+    auto nib = [](int v, int sh) { return __int_as_float(0x4B000000 | ((v >> sh) & 15)); };
     for (int q = 0; q < count; q += 2) {
       const bool two = q + 1 < count;
       const int pk0 = repl[warp][q], pk1 = two ? repl[warp][q + 1] : pk0;
       const bool hole0 = (pk0 >> 12) & 1, hole1 = (pk1 >> 12) & 1;
-      const f2 x = fma2(pk2((float)((pk0 & 15) - 8), (float)((pk1 & 15) - 8)), L2, dx2);
-      const f2 y = fma2(pk2((float)(((pk0 >> 4) & 15) - 8), (float)(((pk1 >> 4) & 15) - 8)), L2, dy2);
-      const f2 z = fma2(pk2((float)(((pk0 >> 8) & 15) - 8), (float)(((pk1 >> 8) & 15) - 8)), L2, dz2);
+      const f2 x = fma2(sub2(pk2(nib(pk0, 0), nib(pk1, 0)), bias2), L2, dx2);
+      const f2 y = fma2(sub2(pk2(nib(pk0, 4), nib(pk1, 4)), bias2), L2, dy2);
+      const f2 z = fma2(sub2(pk2(nib(pk0, 8), nib(pk1, 8)), bias2), L2, dz2);
       const f2 r2 = fma2(x, x, fma2(y, y, mul2(z, z)));
       float r20, r21;
       up2(r2, r20, r21);
@@ -603,7 +610,9 @@ __global__ void __launch_bounds__(kMixWarps * 32) ewald_mix_kernel(
       /* the erfc form (Numerical Recipes erfcc, as erfc_nr) on both halves */
       const f2 dir = pk2(rsqrtf(r20), rsqrtf(r21));
       const f2 dir2 = mul2(dir, dir);
-      const float ar0 = sqrtf(s0), ar1 = sqrtf(s1);
+      /* alpha r = alpha r^2 / r, from the reciprocal root already taken */
+      float ar0, ar1;
+      up2(mul2(alphap, mul2(r2, dir)), ar0, ar1);
       const f2 e = pk2(__expf(-s0), __expf(-s1));
       const f2 av = mul2(kap, mul2(dir2, e));
       const f2 t = pk2(__fdividef(1.0f, fmaf(0.5f, ar0, 1.0f)), __fdividef(1.0f, fmaf(0.5f, ar1, 1.0f)));
@@ -772,13 +781,38 @@ cudaError_t launch_ewald_fp(int form, const double* parts, long long n_parts, co
   P.twopi_over_L = (float)(2.0 * M_PI / L);
   P.nReps = p.nReps;
   P.nEwReps = nE;
-  P.nEwhLoop = p.nEwhLoop;
-  for (int i = 0; i < p.nEwhLoop; ++i) {
-    const double* e = p.ewt + 5 * i;
+  /* The terms of h and -h are equal: the cosine coefficient is even in h,
+   * the sine coefficient and the phase odd.  The table (EwaldInit's loop
+   * over the cube of h) holds both; one of each pair is kept with its
+   * coefficients doubled (exact in floating point), which halves the
+   * k-space loop.  Entries without an exact mirror are kept as they are. */
+  {
     const double f = L / (2.0 * M_PI);
-    P.h[i] = make_float4((float)rint(e[0] * f), (float)rint(e[1] * f), (float)rint(e[2] * f),
-                         (float)e[3]);
-    P.hs[i] = (float)e[4];
+    const int n = p.nEwhLoop;
+    std::vector<int> hi(3 * (size_t)n);
+    std::vector<char> used((size_t)n, 0);
+    for (int i = 0; i < n; ++i)
+      for (int k = 0; k < 3; ++k) hi[3 * i + k] = (int)rint(p.ewt[5 * i + k] * f);
+    int m = 0;
+    for (int i = 0; i < n; ++i) {
+      if (used[i]) continue;
+      const double* e = p.ewt + 5 * i;
+      double scale = 1.0;
+      for (int j = i + 1; j < n; ++j) {
+        const double* g = p.ewt + 5 * j;
+        if (!used[j] && hi[3 * j] == -hi[3 * i] && hi[3 * j + 1] == -hi[3 * i + 1] &&
+            hi[3 * j + 2] == -hi[3 * i + 2] && g[3] == e[3] && g[4] == -e[4]) {
+          used[j] = 1;
+          scale = 2.0;
+          break;
+        }
+      }
+      P.h[m] = make_float4((float)hi[3 * i], (float)hi[3 * i + 1], (float)hi[3 * i + 2],
+                           (float)(scale * e[3]));
+      P.hs[m] = (float)(scale * e[4]);
+      ++m;
+    }
+    P.nEwhLoop = m;
   }
   if (hex) fill_hex_root(p.momc, P.hex);
   int threads = kMixWarps * 32;
