@@ -1461,6 +1461,14 @@ int changa_ewald_vjp(const double* parts, long long n_parts, const ChangaEwaldPa
     return record_error(CHANGA_E_INVALID_ARG, "ewald_vjp: arguments", __FILE__, __LINE__);
   if (p->nEwhLoop > CHANGA_MAX_EWH)
     return record_error(CHANGA_E_TOO_LARGE, "ewald_vjp: nEwhLoop", __FILE__, __LINE__);
+  /* the quadrupole root expansion: a table without sine terms (a
+   * hexadecapole table has them) about a root with mass */
+  if (!(p->root[2] > 0) || (p->nEwhLoop > 0 && !p->ewt))
+    return record_error(CHANGA_E_INVALID_ARG, "ewald_vjp: root or table", __FILE__, __LINE__);
+  for (int i = 0; i < p->nEwhLoop; ++i)
+    if (p->ewt[5 * i + 4] != 0.0)
+      return record_error(CHANGA_E_INVALID_ARG, "ewald_vjp: sine terms (hexadecapole table)",
+                          __FILE__, __LINE__);
   if (n_parts == 0) return 0;
   prepare_pool();
   double* acc = nullptr;

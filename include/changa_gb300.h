@@ -306,7 +306,8 @@ int changa_gravity_vjp_mixed(const double *moments, long long n_moments, const d
  * every particle shapes.  p: the parameters the forward evaluation used
  * (root moments and h-table of changa_ewald_table).  Together with
  * changa_gravity_vjp_mixed at fperiod it gives the adjoint of a periodic
- * evaluation. */
+ * evaluation.  CHANGA_E_INVALID_ARG for a root without mass or a table
+ * with sine terms (the hexadecapole build's). */
 int changa_ewald_vjp(const double *parts, long long n_parts, const ChangaEwaldParams *p,
                      const double *lam, double *grad, cudaStream_t stream);
 

@@ -210,3 +210,33 @@ def test_host_validator(lib):
     bad_mk = np.array([0, 3, 2], np.int32)
     assert lib.changa_validate_request(p(lst), 3, p(bad_mk), p(st), p(sz), 2, 6, 8) == 1002
     assert lib.changa_validate_request(p(lst), 3, p(mk), p(st), p(sz), 0, 6, 8) == 0  # empty
+
+
+def test_ewald_vjp_rejects_hexadecapole_tables():
+    """The Ewald adjoint is the quadrupole root expansion's: a table with
+    sine terms (the hexadecapole build's) or a massless root is refused
+    before anything runs on the device."""
+    import ctypes as C
+    lib = N.cuda_lib()
+    lib.changa_gb300_set_error_mode(N.CHANGA_ERRORS_RECORD)
+    try:
+        lib.changa_gb300_last_error()
+        ewt = np.zeros((2, 5))
+        ewt[:, 3] = 1.0
+        ewt[1, 4] = 0.5  # a sine term
+        p = N.ChangaEwaldParams()
+        p.root[2] = 1.0
+        p.L = 1.0
+        p.nReps = 1
+        p.fEwCut = 2.6
+        p.nEwhLoop = 2
+        p.ewt = ewt.ctypes.data
+        dummy = C.c_void_p(8)  # never dereferenced
+        assert lib.changa_ewald_vjp(dummy, 4, C.byref(p), dummy, dummy, None) == 1001
+        assert lib.changa_gb300_last_error() == 1001
+        ewt[1, 4] = 0.0
+        p.root[2] = 0.0  # no mass
+        assert lib.changa_ewald_vjp(dummy, 4, C.byref(p), dummy, dummy, None) == 1001
+        assert lib.changa_gb300_last_error() == 1001
+    finally:
+        lib.changa_gb300_set_error_mode(N.CHANGA_ERRORS_ABORT)
