@@ -90,6 +90,7 @@ struct WalkArgs {
   /* per node, one 32-byte record for the traversal (see WalkNode) */
   const struct WalkNode* nodes;
   const float4* boxf;   // 2 n_nodes: {lesser.xyz, 0}, {greater.xyz, 0}
+  const float2* hexf;   // n_nodes: {softening, monopole opening radius^2} (hexadecapole rules)
   float period32;
   /* two-phase walk.  Groups: nodes whose subtree holds few buckets (each
    * bucket in exactly one group, the group node on its chain).  Phase 1
@@ -125,7 +126,8 @@ constexpr float kU = 5.9604645e-08f;  // 2^-24, the FP32 unit roundoff
  * links) and its FP32 box. */
 __global__ void walk_prep_kernel(const double* __restrict__ geom, const double* __restrict__ bbox,
                                  const int* __restrict__ info, long long n_nodes, double theta,
-                                 WalkNode* __restrict__ nodes, float4* __restrict__ boxf) {
+                                 double theta_mono, WalkNode* __restrict__ nodes,
+                                 float4* __restrict__ boxf, float2* __restrict__ hexf) {
   for (long long g = blockIdx.x * (long long)blockDim.x + threadIdx.x; g < n_nodes;
        g += (long long)gridDim.x * blockDim.x) {
     const double* gg = geom + 6 * g;
@@ -138,6 +140,9 @@ __global__ void walk_prep_kernel(const double* __restrict__ geom, const double* 
     const double* b = bbox + 6 * g;
     boxf[2 * g] = make_float4((float)b[0], (float)b[1], (float)b[2], 0.0f);
     boxf[2 * g + 1] = make_float4((float)b[3], (float)b[4], (float)b[5], 0.0f);
+    /* the monopole radius as open_criterion forms it, squared in FP64 */
+    const double rm = kOpenGeom * gg[3] / theta_mono;
+    hexf[g] = make_float2((float)gg[4], (float)(rm * rm));
   }
 }
 
@@ -176,6 +181,71 @@ __device__ bool open_softening(const WalkArgs& a, int g, int local, const double
   const double rr = r + 2.0 * lg[4];
   if (dx * dx + dy * dy + dz * dz <= rr * rr) return true;
   return box_dist2(a.bbox + 6 * (size_t)local, c) <= r * r;
+}
+
+/* v <= t decided from an FP32 value v within ev of the FP64 one and an
+ * FP32 threshold t within et of the FP64 one: 1 certainly, 0 certainly
+ * not, -1 too close (NaN or infinity give -1).  Each side carries two more
+ * unit roundoffs for the rounding of the sums compared here. */
+__device__ __forceinline__ int screen_le_t(float v, float ev, float t, float et) {
+  const float mv = ev + 2.0f * kU * v, mt = et + 2.0f * kU * t;
+  if (v + mv < t - mt) return 1;
+  if (v - mv > t + mt) return 0;
+  return -1;
+}
+
+/* open_softening in FP32 for a source g at c = cm + offset (FP32, with
+ * the per-axis inputs cm and o for the error bound) against node `node`:
+ * 1 certainly true, 0 certainly false, -1 too close to call.  Errors as in
+ * open_criterion_screened: per axis the FP32 inputs and their sums carry at
+ * most delta = 6u (|cm| + |o| + |node's cm or box face|) against the FP64
+ * values; the softening sums 2 s_g + 2 s_node carry at most 3u of their
+ * value, so their square at most 7u (bounded here by 8u). */
+__device__ int open_softening_screened(const WalkArgs& a, float sg, const float* c,
+                                       const float* cm, const float* o, int node) {
+  const float4 nc = a.nodes[node].geo;
+  const float sn = a.hexf[node].x;
+  const float4 lo = a.boxf[2 * (size_t)node], hi = a.boxf[2 * (size_t)node + 1];
+  const float ncm[3] = {nc.x, nc.y, nc.z};
+  const float bl[3] = {lo.x, lo.y, lo.z}, bh[3] = {hi.x, hi.y, hi.z};
+  float v = 0.0f, ev = 0.0f, d2 = 0.0f, e = 0.0f;
+#pragma unroll
+  for (int k = 0; k < 3; ++k) {
+    const float dk = 6.0f * kU * (fabsf(cm[k]) + fabsf(o[k]) + fabsf(ncm[k])) + 1e-30f;
+    const float dx = c[k] - ncm[k];
+    v += dx * dx;
+    ev += 2.0f * fabsf(dx) * dk + 3.0f * dk * dk;
+    const float db = 6.0f * kU * (fabsf(cm[k]) + fabsf(o[k]) + fabsf(bl[k]) + fabsf(bh[k])) + 1e-30f;
+    const float gk = fmaxf(0.0f, fmaxf(bl[k] - c[k], c[k] - bh[k]));
+    d2 += gk * gk;
+    e += 2.0f * gk * db + 3.0f * db * db;
+  }
+  ev += 4.0f * kU * v;
+  e += 4.0f * kU * d2;
+  const float rr = 2.0f * sg + 2.0f * sn, rr2 = rr * rr;
+  const int sph = screen_le_t(v, ev, rr2, 8.0f * kU * rr2);
+  if (sph == 1) return 1;
+  const float r2 = 4.0f * sg * sg;  // (2 s_g)^2
+  const int box = screen_le_t(d2, e, r2, 4.0f * kU * r2);
+  if (box == 1) return 1;
+  return sph == 0 && box == 0 ? 0 : -1;
+}
+
+/* open_softening for source g at replica code `off` against node `node`:
+ * the FP32 screen, then the FP64 test when too close to call. */
+__device__ bool open_softening_fast(const WalkArgs& a, int g, int off, int node) {
+  const float4 gf = a.nodes[g].geo;
+  const float cm[3] = {gf.x, gf.y, gf.z};
+  const float o[3] = {(float)((off & 7) - 3) * a.period32, (float)(((off >> 3) & 7) - 3) * a.period32,
+                      (float)(((off >> 6) & 7) - 3) * a.period32};
+  const float c[3] = {cm[0] + o[0], cm[1] + o[1], cm[2] + o[2]};
+  const int r = open_softening_screened(a, a.hexf[g].x, c, cm, o, node);
+  if (r >= 0) return r == 1;
+  double o64[3];
+  decode(off, a.period, o64);
+  const double* gg = a.geom + 6 * (size_t)g;
+  const double c64[3] = {gg[0] + o64[0], gg[1] + o64[1], gg[2] + o64[2]};
+  return open_softening(a, g, node, c64);
 }
 
 /* openCriterionNode (gravity.h:652-723), quadrupole and hexadecapole
@@ -257,9 +327,15 @@ __device__ int open_criterion_screened(const WalkArgs& a, const WalkNode& nd, in
     return far ? 1 : -1;
   }
   /* outside the opening sphere: accepted, unless the hexadecapole rules
-   * (softening, monopole radius) open it, which stay in FP64 */
+   * open it: a softening sphere that meets the local node, and then the
+   * monopole radius (both screened in FP32, FP64 when too close to call) */
   if (a.order != 4) return 0;
-  return open_criterion(a, g, local, local_bucket, off);
+  const int sof = open_softening_screened(a, a.hexf[g].x, c, cm, o, local);
+  if (sof < 0) return open_criterion(a, g, local, local_bucket, off);
+  if (sof == 0) return 0;
+  const int mono = screen_le(d2, e, a.hexf[g].y);
+  if (mono < 0) return open_criterion(a, g, local, local_bucket, off);
+  return mono;
 }
 
 __device__ __forceinline__ int warp_excl_scan(int v, int& total) {
@@ -396,13 +472,7 @@ __global__ void __launch_bounds__(kWalkWarps * 32) walk_kernel(const WalkArgs a)
         bool soft = false;
         if (lane < tot) {
           e = a.pre[0][p0 + j0 + lane];
-          if (e.x >= 0 && e.x < a.n_nodes) {
-            double o[3];
-            decode((e.y >> 22) & 0x1ff, a.period, o);
-            const double* gg = a.geom + 6 * (size_t)e.x;
-            const double cc[3] = {gg[0] + o[0], gg[1] + o[1], gg[2] + o[2]};
-            soft = open_softening(a, e.x, bn, cc);
-          }
+          if (e.x >= 0 && e.x < a.n_nodes) soft = open_softening_fast(a, e.x, (e.y >> 22) & 0x1ff, bn);
         }
         const unsigned mc = __ballot_sync(full, lane < tot && !soft);
         const unsigned ms = __ballot_sync(full, lane < tot && soft);
@@ -473,13 +543,8 @@ __global__ void __launch_bounds__(kWalkWarps * 32) walk_kernel(const WalkArgs a)
       const int open = open_criterion_screened(a, nd, g, local, local_bucket, code);
       if (open == 0) {
         bool softened = false;
-        if (a.order == 4 && PHASE != 1) {  // phase 2 splits the group's cells per bucket
-          double o[3];
-          decode(code, a.period, o);
-          const double* gg = a.geom + 6 * (size_t)g;
-          const double c[3] = {gg[0] + o[0], gg[1] + o[1], gg[2] + o[2]};
-          softened = open_softening(a, g, bn, c);
-        }
+        if (a.order == 4 && PHASE != 1)  // phase 2 splits the group's cells per bucket
+          softened = open_softening_fast(a, g, code, bn);
         kind = softened ? 1 : 0;
       } else if (nd.link.x < 0 && nd.link.y < 0) {  // a source bucket: its particles
         kind = 2;
@@ -1114,15 +1179,18 @@ static int walk_setup(const ChangaTreeView* t, const ChangaWalkParams* p, WalkAr
                       cudaStream_t s) {
   prepare_pool();
   const size_t nn = (size_t)t->n_nodes;
-  CHG_CUDA(cudaMallocAsync((void**)block, 256 + nn * (sizeof(WalkNode) + 2 * sizeof(float4)), s));
+  CHG_CUDA(cudaMallocAsync((void**)block,
+                           256 + nn * (sizeof(WalkNode) + 2 * sizeof(float4) + sizeof(float2)), s));
   int* err = (int*)*block;
   WalkNode* nodes = (WalkNode*)(*block + 256);
   float4* boxf = (float4*)(nodes + nn);
+  float2* hexf = (float2*)(boxf + 2 * nn);
   CHG_CUDA(cudaMemsetAsync(err, 0, sizeof(int), s));
   long long g = (t->n_nodes + 255) / 256;
   const long long cap = (long long)sm_count() * 8;
-  walk_prep_kernel<<<(int)(g < cap ? g : cap), 256, 0, s>>>(t->geom, t->bbox, t->info, t->n_nodes,
-                                                            p->theta, nodes, boxf);
+  walk_prep_kernel<<<(int)(g < cap ? g : cap), 256, 0, s>>>(
+      t->geom, t->bbox, t->info, t->n_nodes, p->theta,
+      p->theta * p->theta * p->theta * p->theta, nodes, boxf, hexf);
   count_launch();
   a = WalkArgs{};
   a.geom = t->geom;
@@ -1140,6 +1208,7 @@ static int walk_setup(const ChangaTreeView* t, const ChangaWalkParams* p, WalkAr
   a.error = err;
   a.nodes = nodes;
   a.boxf = boxf;
+  a.hexf = hexf;
   a.period32 = (float)p->period;
   a.bucket_stride = 1;
   return 0;
