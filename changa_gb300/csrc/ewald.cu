@@ -527,12 +527,17 @@ __global__ void __launch_bounds__(kMixWarps * 32) ewald_mix_kernel(
   const float a2 = P.alpha2, twoa2 = 2.f * a2, foura4 = twoa2 * twoa2, ka = P.ka;
   const float M = P.M, Q2 = P.Q2;
   float fp = P.k1M, fx = 0.f, fy = 0.f, fz = 0.f;
+  /* a packed offset nibble k (0..15) as the float k - 8: k placed in the
+   * mantissa of 2^23 (exact), then 2^23 + 8 subtracted (exact) */
+  auto nibr = [](int v, int sh) { return __int_as_float(0x4B000000 | ((v >> sh) & 15)); };
+  auto nib = [&](int v, int sh) { return nibr(v, sh) - 8388616.0f; };
   if constexpr (HEX) {
+    const float alpha = sqrtf(a2);
     for (int q = 0; q < count; ++q) {
       const int pk = repl[warp][q];
-      const int ix = (pk & 15) - 8, iy = ((pk >> 4) & 15) - 8, iz = ((pk >> 8) & 15) - 8;
       const bool hole = (pk >> 12) & 1;
-      const float x = dx + ix * L, y = dy + iy * L, z = dz + iz * L;
+      const float x = fmaf(nib(pk, 0), L, dx), y = fmaf(nib(pk, 4), L, dy),
+                  z = fmaf(nib(pk, 8), L, dz);
       const float r2 = x * x + y * y + z * z;
       if (r2 > P.cut2 && !hole) continue;
       const float s = a2 * r2;
@@ -549,7 +554,7 @@ __global__ void __launch_bounds__(kMixWarps * 32) ewald_mix_kernel(
       } else {
         const float dir = rsqrtf(r2);
         const float dir2 = dir * dir;
-        const float ar = sqrtf(s);
+        const float ar = alpha * (r2 * dir);  // alpha r from the reciprocal root
         const float e = __expf(-s);
         const float a = ka * dir2 * e;
         const float ec = erfc_nr(ar, s);
@@ -588,17 +593,14 @@ __global__ void __launch_bounds__(kMixWarps * 32) ewald_mix_kernel(
     const f2 xx = pk2(P.xx, P.xx), xy = pk2(P.xy, P.xy), xz = pk2(P.xz, P.xz),
              yy = pk2(P.yy, P.yy), yz = pk2(P.yz, P.yz), zz = pk2(P.zz, P.zz);
     f2 fp2 = 0ull, fx2 = 0ull, fy2 = 0ull, fz2 = 0ull;
-    /* a packed offset nibble k (0..15) as the float k - 8: k placed in the
-     * mantissa of 2^23 (exact), then 2^23 + 8 subtracted (exact) */
     const f2 bias2 = pk2(8388616.0f, 8388616.0f);
-    auto nib = [](int v, int sh) { return __int_as_float(0x4B000000 | ((v >> sh) & 15)); };
     for (int q = 0; q < count; q += 2) {
       const bool two = q + 1 < count;
       const int pk0 = repl[warp][q], pk1 = two ? repl[warp][q + 1] : pk0;
       const bool hole0 = (pk0 >> 12) & 1, hole1 = (pk1 >> 12) & 1;
-      const f2 x = fma2(sub2(pk2(nib(pk0, 0), nib(pk1, 0)), bias2), L2, dx2);
-      const f2 y = fma2(sub2(pk2(nib(pk0, 4), nib(pk1, 4)), bias2), L2, dy2);
-      const f2 z = fma2(sub2(pk2(nib(pk0, 8), nib(pk1, 8)), bias2), L2, dz2);
+      const f2 x = fma2(sub2(pk2(nibr(pk0, 0), nibr(pk1, 0)), bias2), L2, dx2);
+      const f2 y = fma2(sub2(pk2(nibr(pk0, 4), nibr(pk1, 4)), bias2), L2, dy2);
+      const f2 z = fma2(sub2(pk2(nibr(pk0, 8), nibr(pk1, 8)), bias2), L2, dz2);
       const f2 r2 = fma2(x, x, fma2(y, y, mul2(z, z)));
       float r20, r21;
       up2(r2, r20, r21);

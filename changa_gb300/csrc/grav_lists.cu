@@ -1963,11 +1963,17 @@ __device__ __forceinline__ void gather_hex(const ListArgs& a, int e, int e_end, 
   }
 }
 
-/* The 26 fields of one record into half h of a staged pair: the source
+/* One record into half h of a staged pair (kHexFields fields): the source
  * position with the replica offset (kMix: relative to the bucket's centre,
  * as stage_entry forms it; kF32: offset + cm as the reference forms it,
- * HostCUDA.cu:1094-1099), M, the radius and the 21 moments; entries past
- * the list end become massless cells far away (they add exact zeros). */
+ * HostCUDA.cu:1094-1099), M, then the 21 reduced moments each scaled by its
+ * order's gamma factor at unit distance (second order 3 R^2, third 15 R^3,
+ * fourth 105 R^4, R the radius), so that the pair evaluation multiplies
+ * them by 1/r^3, 1/r^4, 1/r^5 only, and four sums of scaled moments the
+ * traces need (the first negated).  Entries past the list end become massless cells far away
+ * (they add exact zeros). */
+constexpr int kHexFields = 30;  // 15 float4 words per staged pair
+
 template <int FORM>
 __device__ __forceinline__ void stage_hex(const ListArgs& a, const RawHex& r, bool valid,
                                           float3 chi, float3 clo, float* pb, int h) {
@@ -1975,7 +1981,7 @@ __device__ __forceinline__ void stage_hex(const ListArgs& a, const RawHex& r, bo
   const float4 hi = r.w[0], lo = r.w[1];
   const float ox = (float)((r.code & 7) - 3) * fp, oy = (float)(((r.code >> 3) & 7) - 3) * fp,
               oz = (float)(((r.code >> 6) & 7) - 3) * fp;
-  float f[26];
+  float f[kHexFields];
   if constexpr (FORM == kMix) {
     f[0] = ((hi.x - chi.x) + ox) + (lo.x - clo.x);
     f[1] = ((hi.y - chi.y) + oy) + (lo.y - clo.y);
@@ -1986,37 +1992,59 @@ __device__ __forceinline__ void stage_hex(const ListArgs& a, const RawHex& r, bo
     f[2] = oz + hi.z;
   }
   f[3] = hi.w;
+  /* raw words 2..7: the radius, then the 21 moments (two zeros after) */
+  float q[24];
 #pragma unroll
   for (int w = 0; w < 6; ++w) {
     const float4 v = r.w[2 + w];
-    if (4 + 4 * w < 26) f[4 + 4 * w] = v.x;
-    if (5 + 4 * w < 26) f[5 + 4 * w] = v.y;
-    if (6 + 4 * w < 26) f[6 + 4 * w] = v.z;
-    if (7 + 4 * w < 26) f[7 + 4 * w] = v.w;
+    q[4 * w] = v.x;
+    q[4 * w + 1] = v.y;
+    q[4 * w + 2] = v.z;
+    q[4 * w + 3] = v.w;
   }
+  const float R = q[0];
+  const float R2 = R * R;
+  const float s2 = 3.f * R2, s3 = 5.f * s2 * R, s4 = 7.f * s3 * R;
+#pragma unroll
+  for (int k = 0; k < 21; ++k) f[4 + k] = q[1 + k] * (k < 5 ? s2 : (k < 12 ? s3 : s4));
+  f[25] = -(f[4] + f[7]);  // -(Q0 + Q3)
+  f[26] = f[9] + f[10];   // Q5 + Q6
+  f[27] = f[11] + f[12];  // Q7 + Q8
+  f[28] = f[17] + f[18];  // Q13 + Q14
+  f[29] = 0.f;
   if (!valid) {
     f[0] = f[1] = f[2] = 1e30f;
 #pragma unroll
-    for (int k = 3; k < 26; ++k) f[k] = 0.f;
+    for (int k = 3; k < kHexFields; ++k) f[k] = 0.f;
   }
 #pragma unroll
-  for (int k = 0; k < 26; ++k) pb[pair_slot(k, h)] = f[k];
+  for (int k = 0; k < kHexFields; ++k) pb[pair_slot(k, h)] = f[k];
 }
 
 __device__ __forceinline__ f2 lo2(float4 v) { return pk2(v.x, v.y); }
 __device__ __forceinline__ f2 hi2(float4 v) { return pk2(v.z, v.w); }
 
-/* hex_eval on the two cells of staged pair w (13 words) for one target
- * (r = target - cell).  Field k of the pair sits in word k/2, in its low
- * half for even k and its high half for odd k. */
+/* hex_eval (momEvalFmomrcm, moments.c) on the two cells of staged pair w
+ * (15 words, stage_hex's fields) for one target, r = target - cell.  Field
+ * k of the pair sits in word k/2, in its low half for even k and its high
+ * half for odd k.  With x = r/|r| and the staged moments Q' already scaled
+ * by the gamma factor of their order at unit distance, the gammas are
+ * d3 = 1/r^3, d4 = 1/r^4, d5 = 1/r^5:
+ *   P2 = Q'2 x (quadrupole), P3 = Q'3 xx (octupole), P4 = Q'4 xxx
+ *   (hexadecapole), a_n = P_n . x,
+ *   pot -= M/r + d3 a2 / 2 + d4 a3 / 3 + d5 a4 / 4,
+ *   acc += (d3 P2 + d4 P3 + d5 P4 - x G) / r,
+ *   G = M/r + 5/2 d3 a2 + 7/3 d4 a3 + 9/4 d5 a4,
+ * which is the reference's evaluation with its gammas g2 = 3 R^2/r^3,
+ * g3 = 5 g2 R/r, g4 = 7 g3 R/r folded into the moments. */
 __device__ __forceinline__ void hex_pair(const float4* __restrict__ w, f2 tx2, f2 ty2, f2 tz2,
                                          f2 tm2, f2& pot2, f2& ax2, f2& ay2, f2& az2,
                                          float& idt2) {
-  const f2 C3 = pk2(3.f, 3.f), C5 = pk2(5.f, 5.f), C7 = pk2(7.f, 7.f), C9 = pk2(9.f, 9.f);
   const f2 CH = pk2(0.5f, 0.5f), CMH = pk2(-0.5f, -0.5f), CQ = pk2(0.25f, 0.25f);
   const float third = 0.3333333432674408f;  // the reference's single-precision 1/3
   const f2 C13 = pk2(third, third);
-  const float4 w0 = w[0], w1 = w[1], w2 = w[2];
+  const f2 K2 = pk2(2.5f, 2.5f), K3 = pk2(7.f * third, 7.f * third), K4 = pk2(2.25f, 2.25f);
+  const float4 w0 = w[0], w1 = w[1];
   const f2 rx = sub2(tx2, lo2(w0)), ry = sub2(ty2, hi2(w0)), rz = sub2(tz2, lo2(w1));
   const f2 M = hi2(w1);
   const f2 rsq = fma2(rx, rx, fma2(ry, ry, mul2(rz, rz)));
@@ -2025,10 +2053,9 @@ __device__ __forceinline__ void hex_pair(const float4* __restrict__ w, f2 tx2, f
   /* rsq = 0 (a cell at the target) contributes nothing, as in
    * hex_interact; the far padding records give rsq = inf and dir = 0 */
   const f2 dir = pk2(q0 > 0.f ? rsqrt_ftz(q0) : 0.f, q1 > 0.f ? rsqrt_ftz(q1) : 0.f);
-  const f2 u = mul2(lo2(w2), dir);
-  f2 g2 = mul2(mul2(mul2(C3, dir), u), u);
-  f2 g3 = mul2(mul2(C5, g2), u);
-  f2 g4 = mul2(mul2(C7, g3), u);
+  const f2 d2 = mul2(dir, dir);
+  const f2 d3 = mul2(d2, dir), d4 = mul2(d2, d2);
+  const f2 d5 = mul2(d4, dir);
   const f2 x = mul2(rx, dir), y = mul2(ry, dir), z = mul2(rz, dir);
   f2 xx = mul2(mul2(CH, x), x), yy = mul2(mul2(CH, y), y);
   const f2 xy = mul2(x, y), xz = mul2(x, z), yz = mul2(y, z);
@@ -2038,74 +2065,79 @@ __device__ __forceinline__ void hex_pair(const float4* __restrict__ w, f2 tx2, f
   xx = add2(xx, nzz);
   yy = add2(yy, nzz);
   const f2 xxy = mul2(y, xx), xyy = mul2(x, yy), xyz = mul2(xy, z);
-  const float4 w3 = w[3], w4 = w[4], w5 = w[5], w6 = w[6], w7 = w[7], w8 = w[8], w9 = w[9],
-               w10 = w[10], w11 = w[11], w12 = w[12];
-  /* q[k] is field 5 + k */
-  const f2 Q0 = hi2(w2), Q1 = lo2(w3), Q2 = hi2(w3), Q3 = lo2(w4), Q4 = hi2(w4), Q5 = lo2(w5),
-           Q6 = hi2(w5), Q7 = lo2(w6), Q8 = hi2(w6), Q9 = lo2(w7), Q10 = hi2(w7), Q11 = lo2(w8),
-           Q12 = hi2(w8), Q13 = lo2(w9), Q14 = hi2(w9), Q15 = lo2(w10), Q16 = hi2(w10),
-           Q17 = lo2(w11), Q18 = hi2(w11), Q19 = lo2(w12), Q20 = hi2(w12);
+  const float4 w2 = w[2], w3 = w[3], w4 = w[4], w5 = w[5], w6 = w[6], w7 = w[7], w8 = w[8],
+               w9 = w[9], w10 = w[10], w11 = w[11], w12 = w[12], w13 = w[13], w14 = w[14];
+  /* scaled moment k is field 4 + k */
+  const f2 Q0 = lo2(w2), Q1 = hi2(w2), Q2 = lo2(w3), Q3 = hi2(w3), Q4 = lo2(w4), Q5 = hi2(w4),
+           Q6 = lo2(w5), Q7 = hi2(w5), Q8 = lo2(w6), Q9 = hi2(w6), Q10 = lo2(w7), Q11 = hi2(w7),
+           Q12 = lo2(w8), Q13 = hi2(w8), Q14 = lo2(w9), Q15 = hi2(w9), Q16 = lo2(w10),
+           Q17 = hi2(w10), Q18 = lo2(w11), Q19 = hi2(w11), Q20 = lo2(w12);
+  const f2 nQ03 = hi2(w12), Q56 = lo2(w13), Q78 = hi2(w13), Q1314 = lo2(w14);
+  /* hexadecapole */
   f2 t = mul2(Q12, xxx);
   t = fma2(Q13, yyy, t);
   t = fma2(Q14, xxy, t);
   t = fma2(Q16, xxz, t);
   t = fma2(Q18, xyy, t);
   t = fma2(Q19, xyz, t);
-  const f2 tx = mul2(g4, fma2(Q20, yyz, t));
+  const f2 p4x = fma2(Q20, yyz, t);
   t = mul2(Q13, xyy);
   t = fma2(Q14, xxx, t);
   t = fma2(Q15, yyy, t);
   t = fma2(Q17, yyz, t);
   t = fma2(Q18, xxy, t);
   t = fma2(Q19, xxz, t);
-  const f2 ty = mul2(g4, fma2(Q20, xyz, t));
+  const f2 p4y = fma2(Q20, xyz, t);
   t = mul2(Q16, xxx);
   t = fma2(Q17, yyy, t);
   t = fma2(Q19, xxy, t);
   t = fma2(Q20, xyy, t);
   f2 sm = mul2(Q12, xxz);
-  sm = fma2(add2(Q13, Q14), xyz, sm);
+  sm = fma2(Q1314, xyz, sm);
   sm = fma2(Q15, yyz, sm);
   sm = fma2(Q18, add2(xxz, yyz), sm);
-  const f2 tz = mul2(g4, sub2(t, sm));
-  g4 = mul2(CQ, fma2(tx, x, fma2(ty, y, mul2(tz, z))));
+  const f2 p4z = sub2(t, sm);
+  const f2 b4 = mul2(d5, fma2(p4x, x, fma2(p4y, y, mul2(p4z, z))));
+  /* octupole */
   t = mul2(Q5, xx);
   t = fma2(Q6, yy, t);
   t = fma2(Q7, xy, t);
   t = fma2(Q9, xz, t);
-  const f2 o3x = mul2(g3, fma2(Q11, yz, t));
+  const f2 p3x = fma2(Q11, yz, t);
   t = mul2(Q6, xy);
   t = fma2(Q7, xx, t);
   t = fma2(Q8, yy, t);
   t = fma2(Q10, yz, t);
-  const f2 o3y = mul2(g3, fma2(Q11, xz, t));
+  const f2 p3y = fma2(Q11, xz, t);
   t = mul2(Q9, xx);
   t = fma2(Q10, yy, t);
   t = fma2(Q11, xy, t);
-  sm = mul2(add2(Q5, Q6), xz);
-  sm = fma2(add2(Q7, Q8), yz, sm);
-  const f2 o3z = mul2(g3, sub2(t, sm));
-  g3 = mul2(C13, fma2(o3x, x, fma2(o3y, y, mul2(o3z, z))));
-  const f2 o2x = mul2(g2, fma2(Q0, x, fma2(Q1, y, mul2(Q2, z))));
-  const f2 o2y = mul2(g2, fma2(Q3, y, fma2(Q1, x, mul2(Q4, z))));
-  const f2 o2z = mul2(g2, sub2(fma2(Q2, x, mul2(Q4, y)), mul2(add2(Q0, Q3), z)));
-  g2 = mul2(CH, fma2(o2x, x, fma2(o2y, y, mul2(o2z, z))));
-  f2 g0 = mul2(dir, M);
-  /* pot -= g0 + g2 + g3 + g4: accumulated with the opposite sign */
-  pot2 = add2(pot2, add2(add2(g0, g2), add2(g3, g4)));
-  g0 = fma2(C5, g2, fma2(C7, g3, fma2(C9, g4, g0)));
-  ax2 = fma2(dir, sub2(add2(add2(o2x, o3x), tx), mul2(x, g0)), ax2);
-  ay2 = fma2(dir, sub2(add2(add2(o2y, o3y), ty), mul2(y, g0)), ay2);
-  az2 = fma2(dir, sub2(add2(add2(o2z, o3z), tz), mul2(z, g0)), az2);
-  float d0, d1;
-  up2(mul2(add2(tm2, M), mul2(dir, mul2(dir, dir))), d0, d1);
-  idt2 = fmax3(idt2, d0, d1);
+  const f2 p3z = sub2(t, fma2(Q56, xz, mul2(Q78, yz)));
+  const f2 b3 = mul2(d4, fma2(p3x, x, fma2(p3y, y, mul2(p3z, z))));
+  /* quadrupole */
+  const f2 p2x = fma2(Q0, x, fma2(Q1, y, mul2(Q2, z)));
+  const f2 p2y = fma2(Q3, y, fma2(Q1, x, mul2(Q4, z)));
+  const f2 p2z = fma2(Q2, x, fma2(Q4, y, mul2(nQ03, z)));
+  const f2 b2 = mul2(d3, fma2(p2x, x, fma2(p2y, y, mul2(p2z, z))));
+  const f2 g0 = mul2(dir, M);
+  /* pot -= g0 + b2/2 + b3/3 + b4/4: accumulated with the opposite sign */
+  pot2 = add2(pot2, fma2(CH, b2, fma2(C13, b3, fma2(CQ, b4, g0))));
+  const f2 ng = sub2(pk2(0.f, 0.f), fma2(K2, b2, fma2(K3, b3, fma2(K4, b4, g0))));
+  const f2 sx = fma2(d5, p4x, fma2(d4, p3x, mul2(d3, p2x)));
+  const f2 sy = fma2(d5, p4y, fma2(d4, p3y, mul2(d3, p2y)));
+  const f2 sz = fma2(d5, p4z, fma2(d4, p3z, mul2(d3, p2z)));
+  ax2 = fma2(dir, fma2(x, ng, sx), ax2);
+  ay2 = fma2(dir, fma2(y, ng, sy), ay2);
+  az2 = fma2(dir, fma2(z, ng, sz), az2);
+  float e0, e1;
+  up2(mul2(add2(tm2, M), d3), e0, e1);
+  idt2 = fmax3(idt2, e0, e1);
 }
 
 template <int FORM, int MINB>
 __global__ void __launch_bounds__(kThreads, MINB) list_kernel_hex2(const ListArgs a) {
   static_assert(FORM == kMix || FORM == kF32, "FP32 arithmetic forms only");
-  constexpr int PW = 13;  // float4 words per staged pair
+  constexpr int PW = kHexFields / 2;  // float4 words per staged pair
   __shared__ __align__(16) float4 stage[kWarps][16 * PW];
   __shared__ double red[kWarps][5][32];
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
