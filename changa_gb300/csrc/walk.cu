@@ -715,8 +715,13 @@ __global__ void __launch_bounds__(WARPS * 32, kFusedWarpsPerSM / WARPS)
     gdepth = __shfl_sync(kFull, gdepth, 0);
     const long long tbase = a.info[4 * (size_t)bn + 2];
     const int n = a.info[4 * (size_t)bn + 3];
-    if (depth < 0 || gdepth < 0 || n <= 0 || tbase < 0 || tbase + n > f.parts.n_src) {
+    if (depth < 0 || gdepth < 0) {
       if (lane == 0) atomicExch(a.error, 1);
+      continue;
+    }
+    if (n == 0) continue;  // no targets
+    if (n < 0 || tbase < 0 || tbase + n > f.parts.n_src) {  // memory safety
+      if (lane == 0) atomicExch(a.error, 3);
       continue;
     }
     /* the bucket's reference point: its first particle's split position */
@@ -1261,6 +1266,10 @@ static void walk_run(const WalkArgs& a, int mode, cudaStream_t s, int phase = 0)
 }
 
 static int walk_error(int h_err) {
+  if (h_err == 3)
+    return record_error(CHANGA_E_INVALID_ARG,
+                        "walk_forces: a bucket's particles lie outside the particle array",
+                        __FILE__, __LINE__);
   return record_error(CHANGA_E_TOO_LARGE, h_err == 1 ? "walk: tree deeper than 64 levels"
                                                      : "walk: traversal stack exhausted",
                       __FILE__, __LINE__);

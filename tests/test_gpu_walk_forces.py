@@ -103,3 +103,31 @@ def test_walk_forces_rejects_hexadecapole(cuda_ok):
     with pytest.raises(RuntimeError, match="1001"):  # CHANGA_E_INVALID_ARG
         walk_forces(L)
     assert lib.changa_gb300_last_error() == 1001  # read, and so cleared
+
+
+def test_walk_forces_rejects_short_particle_array(cuda_ok):
+    """A particle count below the tree's: the buckets past it are refused
+    by the kernel's range check (nothing is read past the array) and the
+    call returns CHANGA_E_INVALID_ARG."""
+    import ctypes as C
+
+    import torch
+    from changa_gb300 import _native as N
+    lib = N.cuda_lib()
+    p = ics.plummer(4096, ics.rng_for(4), soft=0.01)
+    L = tree.build_lists(p["pos"], p["mass"], p["soft"], n_bucket=16, theta=0.7)
+    t = lambda a: torch.from_numpy(np.ascontiguousarray(a)).cuda()
+    m = L.meta
+    geom, bbox, info = t(m["node_geom"]), t(m["node_bbox"]), t(m["node_info"])
+    parent, bnode = t(m["parent"]), t(m["bucket_node"])
+    moments, parts = t(L.moments), t(L.parts)
+    tv = N.ChangaTreeView(geom.data_ptr(), bbox.data_ptr(), info.data_ptr(), parent.data_ptr(),
+                          int(geom.shape[0]), bnode.data_ptr(), int(bnode.shape[0]))
+    wp = N.ChangaWalkParams(0.7, 2, 0.0, 0)
+    out = torch.zeros((L.n, 5), dtype=torch.float64, device="cuda")
+    lib.changa_gb300_last_error()  # clear
+    rc = lib.changa_walk_forces(C.byref(tv), C.byref(wp), moments.data_ptr(), parts.data_ptr(),
+                                L.n // 2, None, out.data_ptr(),
+                                torch.cuda.current_stream().cuda_stream)
+    assert rc == 1001
+    assert lib.changa_gb300_last_error() == 1001
