@@ -206,6 +206,31 @@ __global__ void __launch_bounds__(kThreads, 4) vjp_kernel(const VjpArgs a) {
         const int nh0 = (ntile + 1) >> 1;
         const int my0 = t16 + (half ? nh0 : 0);
         const int myn = half ? ntile - nh0 : nh0;
+        /* the tile's bounding box and largest softening: a step whose
+         * sources all lie beyond (source softening + that softening) of the
+         * box has no softened pair and no pair at r = 0 */
+        float blo[3], bhi[3], tsm;
+        {
+          const bool in = hl < ntile;
+          const float4 tp = tpos[warp][t16 + (in ? hl : 0)];
+          const float ts = in ? tsoft[warp][t16 + hl] : 0.f;
+          const float c3[3] = {tp.x, tp.y, tp.z};
+#pragma unroll
+          for (int k = 0; k < 3; ++k) {
+            float lo_ = in ? c3[k] : 3.4e38f, hi_ = in ? c3[k] : -3.4e38f;
+#pragma unroll
+            for (int o = 8; o > 0; o >>= 1) {
+              lo_ = fminf(lo_, __shfl_xor_sync(kFull, lo_, o));
+              hi_ = fmaxf(hi_, __shfl_xor_sync(kFull, hi_, o));
+            }
+            blo[k] = lo_;
+            bhi[k] = hi_;
+          }
+          float m = ts;
+#pragma unroll
+          for (int o = 8; o > 0; o >>= 1) m = fmaxf(m, __shfl_xor_sync(kFull, m, o));
+          tsm = m;
+        }
         float v[32];
 #pragma unroll
         for (int k = 0; k < 32; ++k) v[k] = 0.f;
@@ -217,10 +242,11 @@ __global__ void __launch_bounds__(kThreads, 4) vjp_kernel(const VjpArgs a) {
           const float ox = (float)((cur.code & 7) - 3) * a.fperiod,
                       oy = (float)(((cur.code >> 3) & 7) - 3) * a.fperiod,
                       oz = (float)(((cur.code >> 6) & 7) - 3) * a.fperiod;
-          const float sx = ((cur.h.x - chi.x) + ox) + (cur.l.x - clo.x);
-          const float sy = ((cur.h.y - chi.y) + oy) + (cur.l.y - clo.y);
-          const float sz = ((cur.h.z - chi.z) + oz) + (cur.l.z - clo.z);
-          const float sm = cur.h.w, ss = cur.l.w;
+          float sx = ((cur.h.x - chi.x) + ox) + (cur.l.x - clo.x);
+          float sy = ((cur.h.y - chi.y) + oy) + (cur.l.y - clo.y);
+          float sz = ((cur.h.z - chi.z) + oz) + (cur.l.z - clo.z);
+          float sm = cur.h.w;
+          const float ss = cur.l.w;
           float xx = 0.f, xy = 0.f, xz = 0.f, yy = 0.f, yz = 0.f, zz = 0.f, tr = 0.f;
           if constexpr (CELL) {
             xx = cur.q0.x;
@@ -231,10 +257,93 @@ __global__ void __launch_bounds__(kThreads, 4) vjp_kernel(const VjpArgs a) {
             zz = cur.q1.y;
             tr = cur.q1.z;
           }
+          if (!cur.valid) {
+            /* past the list end: a source without mass or moments far away
+             * (r^2 stays finite in FP32), whose every term is an exact zero */
+            sx = sy = sz = 1e15f;
+            sm = xx = xy = xz = yy = yz = zz = tr = 0.f;
+          }
           /* this source's gradient over this half's targets */
           float g0 = 0.f, g1 = 0.f, g2 = 0.f, g3 = 0.f;
           float q_xx = 0.f, q_xy = 0.f, q_xz = 0.f, q_yy = 0.f, q_yz = 0.f, q_zz = 0.f;
-          if (cur.valid) {
+          bool far_src;
+          {
+            const float bx = fmaxf(fmaxf(blo[0] - sx, sx - bhi[0]), 0.f);
+            const float by = fmaxf(fmaxf(blo[1] - sy, sy - bhi[1]), 0.f);
+            const float bz = fmaxf(fmaxf(blo[2] - sz, sz - bhi[2]), 0.f);
+            const float bound = ss + tsm;
+            far_src = !cur.valid ||
+                      fmaf(bx, bx, fmaf(by, by, bz * bz)) > bound * bound * 1.0001f;
+          }
+          if (__all_sync(kFull, far_src)) {
+            /* no softened pair and r > 0 for every pair of the step: the
+             * far-field coefficients without per-pair tests (invalid
+             * entries are discarded below) */
+#pragma unroll
+            for (int tt = 0; tt < 8; ++tt) {
+              if (tt < myn) {
+                const float4 tp = tpos[warp][my0 + tt];
+                const float4 la = tlam[warp][my0 + tt];
+                if constexpr (CELL) {
+                  const float rx = tp.x - sx, ry = tp.y - sy, rz = tp.z - sz;
+                  const float rsq = fmaf(rx, rx, fmaf(ry, ry, rz * rz));
+                  const float dir = rsqrtf(rsq);
+                  const float dir2 = dir * dir;
+                  const float bv = dir2 * dir, cv = bv * (3.f * dir2), dv = cv * (5.f * dir2),
+                              ev = dv * (7.f * dir2);
+                  const float Qrx = fmaf(xx, rx, fmaf(xy, ry, xz * rz));
+                  const float Qry = fmaf(xy, rx, fmaf(yy, ry, yz * rz));
+                  const float Qrz = fmaf(xz, rx, fmaf(yz, ry, zz * rz));
+                  const float Qlx = fmaf(xx, la.x, fmaf(xy, la.y, xz * la.z));
+                  const float Qly = fmaf(xy, la.x, fmaf(yy, la.y, yz * la.z));
+                  const float Qlz = fmaf(xz, la.x, fmaf(yz, la.y, zz * la.z));
+                  const float qir = 0.5f * fmaf(Qrx, rx, fmaf(Qry, ry, Qrz * rz));
+                  const float rl = fmaf(rx, la.x, fmaf(ry, la.y, rz * la.z));
+                  const float lQr = fmaf(la.x, Qrx, fmaf(la.y, Qry, la.z * Qrz));
+                  const float cl = tr * cv - sm * bv - qir * dv;
+                  const float cr = rl * (sm * cv + qir * ev - tr * dv) - dv * lQr;
+                  const float cq = -dv * rl;
+                  const float gx = cl * la.x + cr * rx + cq * Qrx + cv * Qlx;
+                  const float gy = cl * la.y + cr * ry + cq * Qry + cv * Qly;
+                  const float gz = cl * la.z + cr * rz + cq * Qrz + cv * Qlz;
+                  v[4 * tt + 0] += gx;
+                  v[4 * tt + 1] += gy;
+                  v[4 * tt + 2] += gz;
+                  g0 -= gx;
+                  g1 -= gy;
+                  g2 -= gz;
+                  g3 -= bv * rl;
+                  const float hr = -0.5f * dv * rl;
+                  const float ht = 0.5f * cv * rl;
+                  const float hrx = hr * rx, hry = hr * ry;
+                  q_xx += fmaf(hrx, rx, fmaf(cv * la.x, rx, ht));
+                  q_yy += fmaf(hry, ry, fmaf(cv * la.y, ry, ht));
+                  q_zz += fmaf(hr * rz, rz, fmaf(cv * la.z, rz, ht));
+                  q_xy += fmaf(2.f * hrx, ry, cv * fmaf(la.x, ry, la.y * rx));
+                  q_xz += fmaf(2.f * hrx, rz, cv * fmaf(la.x, rz, la.z * rx));
+                  q_yz += fmaf(2.f * hry, rz, cv * fmaf(la.y, rz, la.z * ry));
+                } else {
+                  const float rx = sx - tp.x, ry = sy - tp.y, rz = sz - tp.z;
+                  const float rsq = fmaf(rx, rx, fmaf(ry, ry, rz * rz));
+                  const float dir = rsqrtf(rsq);
+                  const float dir2 = dir * dir;
+                  const float bv = dir2 * dir, cv = bv * (3.f * dir2);
+                  const float rl = fmaf(rx, la.x, fmaf(ry, la.y, rz * la.z));
+                  const float crl = cv * rl;
+                  const float gx = sm * fmaf(bv, la.x, -crl * rx);
+                  const float gy = sm * fmaf(bv, la.y, -crl * ry);
+                  const float gz = sm * fmaf(bv, la.z, -crl * rz);
+                  v[4 * tt + 0] -= gx;
+                  v[4 * tt + 1] -= gy;
+                  v[4 * tt + 2] -= gz;
+                  g0 += gx;
+                  g1 += gy;
+                  g2 += gz;
+                  g3 += bv * rl;
+                }
+              }
+            }
+          } else if (cur.valid) {
 #pragma unroll
             for (int tt = 0; tt < 8; ++tt) {
               if (tt < myn) {
