@@ -1171,17 +1171,23 @@ __global__ void __launch_bounds__(kThreads, MINB) list_kernel_tp2(const ListArgs
           }
         }
         ssoft[warp][buf][lane] = ls;
-        const float ss = warp_max(ls) + tsmax;
-        const float near2 = ss * ss;
-        /* no source of the block within the softening bound of the targets'
-         * box (then no pair of the block is softened; the margin covers the
-         * rounding of the box distance) */
+        /* no source of the block within its own softening plus the
+         * targets' largest of the targets' box (then no pair of the block
+         * is softened; the margin covers the rounding of the box distance);
+         * the block-wide bound for the marked pairs only where some source
+         * is near */
         bool far_block;
         {
           const float bx = fmaxf(fmaxf(blo.x - rec[0].x, rec[0].x - bhi.x), 0.f);
           const float by = fmaxf(fmaxf(blo.y - rec[0].y, rec[0].y - bhi.y), 0.f);
           const float bz = fmaxf(fmaxf(blo.z - rec[0].z, rec[0].z - bhi.z), 0.f);
-          far_block = __all_sync(kFull, fmaf(bx, bx, fmaf(by, by, bz * bz)) > near2 * 1.0001f);
+          const float own = ls + tsmax;
+          far_block = __all_sync(kFull, fmaf(bx, bx, fmaf(by, by, bz * bz)) > own * own * 1.0001f);
+        }
+        float near2 = 0.f;
+        if (!far_block) {
+          const float ss = warp_max(ls) + tsmax;
+          near2 = ss * ss;
         }
         __syncwarp();
         if (e0 + 32 < e_end) {
@@ -1440,15 +1446,21 @@ __device__ __forceinline__ void rb_chunk(const ListArgs& a, const int lane, cons
       }
     }
     ssoft[buf][lane] = ls;
-    const float ss = warp_max(ls) + tsmax;
-    const float near2 = ss * ss;
-    /* no source of the block within the softening bound of the targets' box */
+    /* no source of the block within its own softening plus the targets'
+     * largest of the targets' box; the block-wide bound only where some
+     * source is near */
     bool far_block;
     {
       const float bx = fmaxf(fmaxf(blo.x - rec[0].x, rec[0].x - bhi.x), 0.f);
       const float by = fmaxf(fmaxf(blo.y - rec[0].y, rec[0].y - bhi.y), 0.f);
       const float bz = fmaxf(fmaxf(blo.z - rec[0].z, rec[0].z - bhi.z), 0.f);
-      far_block = __all_sync(kFull, fmaf(bx, bx, fmaf(by, by, bz * bz)) > near2 * 1.0001f);
+      const float own = ls + tsmax;
+      far_block = __all_sync(kFull, fmaf(bx, bx, fmaf(by, by, bz * bz)) > own * own * 1.0001f);
+    }
+    float near2 = 0.f;
+    if (!far_block) {
+      const float ss = warp_max(ls) + tsmax;
+      near2 = ss * ss;
     }
     __syncwarp();
     if (e0 + 32 < e_end) {
