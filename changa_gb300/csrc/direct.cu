@@ -1,6 +1,6 @@
 /*
  * Direct-sum accuracy yardstick: the force on sampled particles from every
- * particle, without a tree.  No reference counterpart (ChaNGa judges its
+ * particle, without a tree.  No reference counterpart (ChaNGa checks its
  * tree against nothing at run time); it gives the "error against the
  * direct sum" of every force form on workloads far too large for the CPU.
  *

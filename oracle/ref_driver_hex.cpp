@@ -6,7 +6,7 @@
  * moments.c by oracle/Makefile when the reference sources are present;
  * loaded only by tests).
  *
- * gravity.h is included unmodified.  In this build nodeBucketForce
+ * gravity.h is included unmodified.  With HEXADECAPOLE, nodeBucketForce
  * (gravity.h:398-421, 439-446) evaluates a cell with momEvalFmomrcm
  * (moments.c:1469-1525) unless the cell's softening sphere meets the bucket
  * (openSoftening, gravity.h:252-260), in which case the cell acts as a

@@ -31,7 +31,7 @@ FP64_TOL = 1e-6        # the plain FP64 form, relative per particle
 MIX_MEDIAN_TOL = 2e-6  # FP32-mixed against the FP64 oracle, relative
 MIX_P99_TOL = 1e-4
 # periodic lattice: forces are small residuals of O(1) replica terms, so the
-# FP32-mixed form is judged against the rms force (as for the smaller
+# FP32-mixed form is measured against the rms force (as for the smaller
 # lattice of test_gpu_forces); measured at 128^3: median 3.7e-5, max 1.4e-4,
 # set by the FP32 rounding of the O(1) Ewald hole terms
 MIX_RMS_MEDIAN = 1e-4

@@ -185,7 +185,7 @@ def test_fp64_form_matches_golden(cuda_ok, name):
 
 def test_ewald_forms(lattice):
     """Tree + Ewald on a perturbed periodic lattice.  The FP64 form matches
-    the oracle per particle; FP32 forms are judged against rms|a| and
+    the oracle per particle; FP32 forms are measured against rms|a| and
     rms(pot) because the net lattice force is a small residual of O(1)
     replica terms (the FP32 forms are still ~1e-5 relative per particle)."""
     L, ew, ref = lattice
@@ -199,7 +199,7 @@ def test_ewald_forms(lattice):
     assert np.median(e) < 5e-5 and e.max() < 2e-3
     assert np.median(force_rel_err(vmx, ref)) < 1e-4
     # the periodic potential of a near-uniform lattice (~3e-3) is the residual
-    # of O(10) replica terms of size G M / L = 1: judge it in those units
+    # of O(10) replica terms of size G M / L = 1: measure it in those units
     assert np.abs(vmx[:, 3] - ref[:, 3]).max() < 5e-5
 
 

@@ -156,7 +156,7 @@ def test_hex_forms_with_ewald(cuda_ok):
     """changa_gravity_step_hexa with its Ewald term (the root's complete
     moments to fourth order) on a clustered periodic box: the FP64 form
     against the oracle per particle, the FP32-mixed form as the quadrupole
-    mixed Ewald is judged (rms|a| and G M / L units)."""
+    mixed Ewald is measured (rms|a| and G M / L units)."""
     p = ics.nfw_halos(32768, ics.rng_for(2), soft=1e-3)
     L = tree.build_lists(p["pos"], p["mass"], p["soft"], n_bucket=16, theta=0.7, period=1.0,
                          order=4)

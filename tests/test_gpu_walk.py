@@ -38,7 +38,7 @@ def _check(L, ewald=None):
     vm = gravity.DeviceSystem(L, ewald=ewald, device_reqs=reqs).step("mixed").cpu().numpy()
     if ewald is None:
         assert np.median(force_rel_err(vm, host)) < 2e-6
-    else:  # near-uniform periodic lattice: judged against rms|a|, as the Ewald tests are
+    else:  # near-uniform periodic lattice: measured against rms|a|, as the Ewald tests are
         assert np.median(force_rms_err(vm, host)) < 5e-5
 
 
