@@ -533,3 +533,36 @@ def test_host_entry_particle_runs(plummer, lattice):
         finally:
             lib.changa_gb300_set_host_chunk_bytes(512 << 20)
         np.testing.assert_array_equal(small, gravity.gravity_step_host(L, "mixed", ewald=ew))
+
+
+def test_two_replica_layers_with_ewald(cuda_ok):
+    """Lists over 5^3 replica roots (two replica layers: offset codes with
+    components of magnitude 2) and the Ewald term with nReps = 2 (its hole
+    spans those 125 replicas), on a clustered periodic box: the FP64 form
+    against the oracle per particle, the FP32-mixed form against the FP64
+    oracle, and the FP32 drop-in against the oracle on its FP32 inputs."""
+    p = ics.nfw_halos(16384, ics.rng_for(10), soft=1e-3)
+    L = tree.build_lists(p["pos"], p["mass"], p["soft"], n_bucket=16, theta=0.7, period=1.0,
+                         n_replicas=2)
+    codes = np.concatenate([(L.cells.list[:, 1] >> 22) & 0x1ff, (L.plist.list[:, 1] >> 22) & 0x1ff])
+    assert ((codes & 7) == 5).any() and ((codes & 7) == 1).any()  # x offsets of +2 and -2
+    ew = gravity.EwaldConfig(1.0, 2, 2.6, 2.8)
+    ref = oracle_vars(L, 1.0, ew)
+    v64 = gravity.DeviceSystem(L, ewald=ew).step("fp64").cpu().numpy()
+    assert force_rel_err(v64, ref).max() < FP64_TOL
+    assert pot_rms_err(v64, ref).max() < FP64_TOL
+    vmx = gravity.DeviceSystem(L, ewald=ew).step("mixed").cpu().numpy()
+    e = force_rms_err(vmx, ref)
+    assert np.median(e) < 5e-5 and e.max() < 2e-3
+    assert np.median(force_rel_err(vmx, ref)) < 1e-4
+    ref32 = oracle_vars(L, 1.0, ew, f32_inputs=True)
+    inp = gravity.DropInInputs(L, ewald=ew)
+    try:
+        v = gravity.dropin_step(inp).astype(np.float64)
+    finally:
+        inp.free()
+    e32 = force_rms_err(v, ref32)
+    print("two replica layers: fp64 max rel %.2e; mixed rms median %.2e max %.2e; drop-in rms "
+          "median %.2e max %.2e" % (force_rel_err(v64, ref).max(), np.median(e), e.max(),
+                                    np.median(e32), e32.max()))
+    assert np.median(e32) < 5e-5 and e32.max() < 2e-3

@@ -131,3 +131,12 @@ def test_walk_forces_rejects_short_particle_array(cuda_ok):
                                 torch.cuda.current_stream().cuda_stream)
     assert rc == 1001
     assert lib.changa_gb300_last_error() == 1001
+
+
+def test_walk_forces_two_replica_layers(cuda_ok):
+    """Two replica layers (5^3 replica roots on the root check list) and the
+    Ewald term with nReps = 2, walked and evaluated in one pass."""
+    p = ics.nfw_halos(16384, ics.rng_for(10), soft=1e-3)
+    L = tree.build_lists(p["pos"], p["mass"], p["soft"], n_bucket=16, theta=0.7, period=1.0,
+                         n_replicas=2)
+    _compare(L, ewald=gravity.EwaldConfig(1.0, 2, 2.6, 2.8), periodic=True)
