@@ -566,3 +566,30 @@ def test_two_replica_layers_with_ewald(cuda_ok):
           "median %.2e max %.2e" % (force_rel_err(v64, ref).max(), np.median(e), e.max(),
                                     np.median(e32), e32.max()))
     assert np.median(e32) < 5e-5 and e32.max() < 2e-3
+
+
+def test_coincident_particles(cuda_ok):
+    """Every particle twice at the same position: the pairs at r = 0 are
+    skipped (partBucketForce's rsq = 0 test, gravity.h:276-301) in every
+    form, and the rest matches the oracle."""
+    p = ics.plummer(4096, ics.rng_for(12), soft=0.01)
+    pos = np.concatenate([p["pos"], p["pos"]])
+    mass = np.concatenate([p["mass"], p["mass"]]) / 2
+    soft = np.concatenate([p["soft"], p["soft"]])
+    L = tree.build_lists(pos, mass, soft, n_bucket=16, theta=0.7)
+    ref = oracle_vars(L)
+    assert np.isfinite(ref).all()
+    v64 = gravity.DeviceSystem(L).step("fp64").cpu().numpy()
+    assert force_rel_err(v64, ref).max() < FP64_TOL
+    vmx = gravity.DeviceSystem(L).step("mixed").cpu().numpy()
+    assert np.isfinite(vmx).all()
+    assert np.median(force_rel_err(vmx, ref)) < MIX_MEDIAN_TOL
+    assert np.percentile(force_rel_err(vmx, ref), 99) < MIX_P99_TOL
+    ref32 = oracle_vars(L, f32_inputs=True)
+    inp = gravity.DropInInputs(L)
+    try:
+        v32 = gravity.dropin_step(inp).astype(np.float64)
+    finally:
+        inp.free()
+    assert np.isfinite(v32).all()
+    assert np.median(force_rel_err(v32, ref32)) < F32_MEDIAN_TOL

@@ -182,3 +182,28 @@ def test_hex_forms_with_ewald(cuda_ok):
     assert np.median(e) < 5e-5 and e.max() < 2e-3
     assert np.median(force_rel_err(vmx, ref)) < 1e-4
     assert np.abs(vmx[:, 3] - ref[:, 3]).max() < 5e-5
+
+
+def test_hex_two_replica_layers_with_ewald(cuda_ok):
+    """The hexadecapole build over two replica layers (5^3 replica roots)
+    with its Ewald term at nReps = 2: the FP64 form against the oracle, the
+    FP32-mixed form against the FP64 oracle."""
+    p = ics.nfw_halos(16384, ics.rng_for(11), soft=1e-3)
+    L = tree.build_lists(p["pos"], p["mass"], p["soft"], n_bucket=16, theta=0.7, period=1.0,
+                         n_replicas=2, order=4)
+    ew = gravity.EwaldConfig(1.0, 2, 2.6, 2.8)
+    ref = np.zeros((L.n, 5))
+    for req in (L.cells, L.softcells):
+        if req.n_buckets:
+            ref = oracle.cell_forces_hex(L.moments, L.parts, req, oracle.bucket_geometry(L, req),
+                                         fperiod=1.0, vars=ref)
+    ref = oracle.part_forces(L.parts, L.parts, L.plist, fperiod=1.0, vars=ref)
+    ref = oracle.ewald_forces_hex(L.parts, L.moments[0], 1.0, 2, 2.6, 2.8, vars=ref)
+    ds = gravity.DeviceSystem(L, ewald=ew)
+    v64 = ds.step("fp64").cpu().numpy()
+    vmx = ds.step("mixed").cpu().numpy()
+    e64, e = force_rel_err(v64, ref), force_rms_err(vmx, ref)
+    print("hex two replica layers: fp64 max %.2e; mixed rms median %.2e max %.2e" % (
+        e64.max(), np.median(e), e.max()))
+    assert e64.max() < 1e-6
+    assert np.median(e) < 5e-5 and e.max() < 2e-3
