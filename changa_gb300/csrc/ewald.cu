@@ -29,6 +29,7 @@
  *                     turn from the integer h before the hardware sin/cos.
  */
 #include <cmath>
+#include <type_traits>
 #include <vector>
 
 #include "chg_internal.h"
@@ -490,36 +491,44 @@ __global__ void __launch_bounds__(kMixWarps * 32) ewald_mix_kernel(
   }
   const int nE = P.nEwReps, nR = P.nReps, side = 2 * nE + 1, nrep = side * side * side;
   const float L = P.L;
-  /* candidate replicas: inside the hole, or within the cut of some point of
-   * the warp's box */
-  int count = 0;
-  for (int base = 0; base < nrep; base += 32) {
-    const int r = base + lane;
-    bool keep = false;
-    if (r < nrep) {
-      const int ix = r / (side * side) - nE, iy = (r / side) % side - nE, iz = r % side - nE;
-      const bool hole = ix >= -nR && ix <= nR && iy >= -nR && iy <= nR && iz >= -nR && iz <= nR;
-      float d2 = 0.f;
-      const int ii[3] = {ix, iy, iz};
+  /* candidate replicas: the hole's first (all of them), then those within
+   * the cut of some point of the warp's box */
+  int count = 0, nhole = 0;
+  for (int pass = 0; pass < 2; ++pass) {
+    for (int base = 0; base < nrep; base += 32) {
+      const int r = base + lane;
+      bool keep = false;
+      int ix = 0, iy = 0, iz = 0;
+      bool hole = false;
+      if (r < nrep) {
+        ix = r / (side * side) - nE;
+        iy = (r / side) % side - nE;
+        iz = r % side - nE;
+        hole = ix >= -nR && ix <= nR && iy >= -nR && iy <= nR && iz >= -nR && iz <= nR;
+        if (pass == 0) {
+          keep = hole;
+        } else if (!hole) {
+          float d2 = 0.f;
+          const int ii[3] = {ix, iy, iz};
 #pragma unroll
-      for (int c = 0; c < 3; ++c) {
-        const float a = lo[c] + ii[c] * L, b = hi[c] + ii[c] * L;
-        const float m = a > 0.f ? a : (b < 0.f ? -b : 0.f);
-        d2 = fmaf(m, m, d2);
+          for (int c = 0; c < 3; ++c) {
+            const float a = lo[c] + ii[c] * L, b = hi[c] + ii[c] * L;
+            const float m = a > 0.f ? a : (b < 0.f ? -b : 0.f);
+            d2 = fmaf(m, m, d2);
+          }
+          keep = d2 <= P.cut2 * 1.0001f;
+        }
       }
-      keep = hole || d2 <= P.cut2 * 1.0001f;
-    }
-    const unsigned bal = __ballot_sync(0xffffffffu, keep);
-    if (keep) {
+      const unsigned bal = __ballot_sync(0xffffffffu, keep);
       /* the replica as packed offsets (each + 8 in four bits) and its hole
        * flag, so the term loop decodes it with shifts instead of integer
        * divisions */
-      const int ix = r / (side * side) - nE, iy = (r / side) % side - nE, iz = r % side - nE;
-      const bool hole = ix >= -nR && ix <= nR && iy >= -nR && iy <= nR && iz >= -nR && iz <= nR;
-      repl[warp][count + __popc(bal & ((1u << lane) - 1u))] =
-          (short)((ix + 8) | ((iy + 8) << 4) | ((iz + 8) << 8) | ((int)hole << 12));
+      if (keep)
+        repl[warp][count + __popc(bal & ((1u << lane) - 1u))] =
+            (short)((ix + 8) | ((iy + 8) << 4) | ((iz + 8) << 8) | ((int)hole << 12));
+      count += __popc(bal);
     }
-    count += __popc(bal);
+    if (pass == 0) nhole = count;
   }
   __syncwarp();
   if (!live) return;
@@ -594,10 +603,14 @@ __global__ void __launch_bounds__(kMixWarps * 32) ewald_mix_kernel(
              yy = pk2(P.yy, P.yy), yz = pk2(P.yz, P.yz), zz = pk2(P.zz, P.zz);
     f2 fp2 = 0ull, fx2 = 0ull, fy2 = 0ull, fz2 = 0ull;
     const f2 bias2 = pk2(8388616.0f, 8388616.0f);
-    for (int q = 0; q < count; q += 2) {
-      const bool two = q + 1 < count;
+    /* one step over culled replicas q and q + 1 of a region ending at
+     * qend: the hole's (H, every replica kept, the series near the root)
+     * or the rest (no hole terms, the cut per replica) */
+    auto step = [&](int q, int qend, auto holes) {
+      constexpr bool H = decltype(holes)::value;
+      const bool two = q + 1 < qend;
       const int pk0 = repl[warp][q], pk1 = two ? repl[warp][q + 1] : pk0;
-      const bool hole0 = (pk0 >> 12) & 1, hole1 = (pk1 >> 12) & 1;
+      const bool hole0 = H, hole1 = H;
       const f2 x = fma2(sub2(pk2(nibr(pk0, 0), nibr(pk1, 0)), bias2), L2, dx2);
       const f2 y = fma2(sub2(pk2(nibr(pk0, 4), nibr(pk1, 4)), bias2), L2, dy2);
       const f2 z = fma2(sub2(pk2(nibr(pk0, 8), nibr(pk1, 8)), bias2), L2, dz2);
@@ -605,7 +618,7 @@ __global__ void __launch_bounds__(kMixWarps * 32) ewald_mix_kernel(
       float r20, r21;
       up2(r2, r20, r21);
       const bool k0 = hole0 || r20 <= P.cut2, k1 = two && (hole1 || r21 <= P.cut2);
-      if (!(k0 || k1)) continue;
+      if (!(k0 || k1)) return;
       const f2 s2 = mul2(a2p, r2);
       float s0, s1;
       up2(s2, s0, s1);
@@ -631,13 +644,13 @@ __global__ void __launch_bounds__(kMixWarps * 32) ewald_mix_kernel(
       float p0, p1;
       up2(sub2(pp, s2), p0, p1);
       const f2 ec = mul2(t, pk2(__expf(p0), __expf(p1)));
-      f2 g0 = mul2(sub2(ec, pk2(hole0 ? 1.f : 0.f, hole1 ? 1.f : 0.f)), dir);
+      f2 g0 = mul2(H ? sub2(ec, pk2(1.f, 1.f)) : ec, dir);
       f2 g1 = fma2(g0, dir2, av);
       f2 g2 = fma2(mul2(pk2(3.f, 3.f), g1), dir2, mul2(twoa2p, av));
       f2 g3 = fma2(mul2(pk2(5.f, 5.f), g2), dir2, mul2(foura4p, av));
       /* hole terms with alpha^2 r^2 < 1: the convergent series instead */
-      const bool ser0 = hole0 && s0 < 1.0f, ser1 = hole1 && s1 < 1.0f;
-      if (ser0 || ser1) {
+      const bool ser0 = H && s0 < 1.0f, ser1 = H && two && s1 < 1.0f;
+      if (H && (ser0 || ser1)) {
         float a0_, a1_, b0_, b1_, c0_, c1_, d0_, d1_;
         up2(g0, a0_, a1_);
         up2(g1, b0_, b1_);
@@ -675,7 +688,9 @@ __global__ void __launch_bounds__(kMixWarps * 32) ewald_mix_kernel(
       fx2 = fma2(g2, Q2mirx, sub2(fx2, mul2(x, Qta)));
       fy2 = fma2(g2, Q2miry, sub2(fy2, mul2(y, Qta)));
       fz2 = fma2(g2, Q2mirz, sub2(fz2, mul2(z, Qta)));
-    }
+    };
+    for (int q = 0; q < nhole; q += 2) step(q, nhole, std::true_type{});
+    for (int q = nhole; q < count; q += 2) step(q, count, std::false_type{});
     float u0, u1;
     up2(fp2, u0, u1);
     fp += u0 + u1;
