@@ -240,3 +240,30 @@ def test_ewald_vjp_rejects_hexadecapole_tables():
         assert lib.changa_gb300_last_error() == 1001
     finally:
         lib.changa_gb300_set_error_mode(N.CHANGA_ERRORS_ABORT)
+
+
+def test_walk_forces_argument_checks():
+    """changa_walk_forces refuses a missing tree, the hexadecapole rules
+    (order 4) and missing arrays before anything runs on the device."""
+    import ctypes as C
+    lib = N.cuda_lib()
+    lib.changa_gb300_set_error_mode(N.CHANGA_ERRORS_RECORD)
+    try:
+        lib.changa_gb300_last_error()
+        dummy = C.c_void_p(8)  # never dereferenced
+        wp = N.ChangaWalkParams(0.7, 2, 0.0, 0)
+        assert lib.changa_walk_forces(None, C.byref(wp), dummy, dummy, 16, None, dummy, None) == 1001
+        assert lib.changa_gb300_last_error() == 1001
+        tv = N.ChangaTreeView(8, 8, 8, 8, 3, 8, 1)
+        wp4 = N.ChangaWalkParams(0.7, 4, 0.0, 0)
+        assert lib.changa_walk_forces(C.byref(tv), C.byref(wp4), dummy, dummy, 16, None, dummy,
+                                      None) == 1001
+        assert lib.changa_gb300_last_error() == 1001
+        assert lib.changa_walk_forces(C.byref(tv), C.byref(wp), None, dummy, 16, None, dummy,
+                                      None) == 1001
+        assert lib.changa_gb300_last_error() == 1001
+        assert lib.changa_walk_forces(C.byref(tv), C.byref(wp), dummy, dummy, 0, None, dummy,
+                                      None) == 1001
+        assert lib.changa_gb300_last_error() == 1001
+    finally:
+        lib.changa_gb300_set_error_mode(N.CHANGA_ERRORS_ABORT)
