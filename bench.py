@@ -816,7 +816,8 @@ def measure_e2e(lists, ew, stream, steps, world, runs=None):
     t_e2e = max_over_ranks(world, sorted(tt)[len(tt) // 2])  # median step
     I = lists.interactions
     api = ("changa_gravity_step_host (include/changa_gb300.h), pinned host buffers, "
-           "CHANGA_STEP_OVERWRITE; lists uploaded in 512 MiB chunks (halving toward the end) on a "
+           "CHANGA_STEP_OVERWRITE; particles uploaded first in 64 MiB slices, each packed and given "
+           "its Ewald term as it lands; lists in 256 MiB chunks (halving toward the end) on a "
            "copy stream overlapping the list kernels; each chunk's particles read back on a "
            "second copy stream once final")
     if runs is not None:

@@ -151,19 +151,22 @@ static void signal(cudaStream_t s, void* cb) {
 
 static size_t align256(size_t x) { return (x + 255) & ~(size_t)255; }
 
-static std::atomic<size_t> g_host_chunk_bytes{size_t(512) << 20};
+constexpr size_t kDefaultHostChunkBytes = size_t(256) << 20;
+static std::atomic<size_t> g_host_chunk_bytes{kDefaultHostChunkBytes};
 
-/* The copy streams of the host-array entries on each device (created
- * once): which 0 carries the uploads, which 1 the read-backs, so the two
- * directions of the host link run at once. */
+/* The library-owned streams of the host-array entries on each device
+ * (created once): which 0 carries the uploads, which 1 the read-backs, so
+ * the two directions of the host link run at once; which 2 is the second
+ * compute lane of changa_gravity_step_host. */
 static cudaStream_t copy_stream(int which = 0) {
-  static cudaStream_t st[64][2] = {{nullptr}};
+  static cudaStream_t st[64][3] = {{nullptr}};
   static std::mutex mu;
   int dev = 0;
   cudaGetDevice(&dev);
   if (dev < 0 || dev >= 64) dev = 0;
+  if (which < 0 || which > 2) which = 0;
   std::lock_guard<std::mutex> lk(mu);
-  cudaStream_t& x = st[dev][which & 1];
+  cudaStream_t& x = st[dev][which];
   if (!x && cudaStreamCreateWithFlags(&x, cudaStreamNonBlocking) != cudaSuccess) x = nullptr;
   return x;
 }
@@ -1142,7 +1145,7 @@ int changa_gravity_step_hexa(int form, const double* moments, long long n_moment
 }
 
 void changa_gb300_set_host_chunk_bytes(size_t bytes) {
-  g_host_chunk_bytes.store(bytes < 4096 ? 4096 : bytes);
+  g_host_chunk_bytes.store(bytes == 0 ? kDefaultHostChunkBytes : bytes < 4096 ? 4096 : bytes);
 }
 
 /* Page-locked (or registered) host memory: a read-back into it returns at
@@ -1171,11 +1174,13 @@ static std::pair<long long, long long> target_range(const ChangaListRequest* r, 
   return {lo, hi};
 }
 
-/* Host-array evaluation, pipelined: the small arrays go first, then each
- * interaction list in chunks of about kChunkBytes, on a copy stream; the
- * compute stream packs, runs Ewald, and launches the list kernel on each
- * chunk's bucket range as soon as its entries have landed, so the list
- * stream from host memory overlaps the force arithmetic.  The last list's
+/* Host-array evaluation, pipelined: the particles go first, in slices that
+ * the compute stream packs and gives their Ewald term as they land; then
+ * the moments and the small arrays, then each interaction list in chunks of
+ * about kChunkBytes, all on a copy stream.  The compute stream packs the
+ * moments and launches the list kernel on each chunk's bucket range as
+ * soon as its entries have landed, so the list stream from host memory
+ * overlaps the force arithmetic.  The last list's
  * chunks shrink toward its end, and when their particle ranges are
  * disjoint and vars is page-locked, each range's results go back on a
  * second copy stream as soon as its kernel is done (every other
@@ -1276,6 +1281,19 @@ static int step_host_impl(int form, const double* moments, long long n_moments,
   float4* pp = (float4*)(block + mb + 2 * pb + cpb);
   unsigned int* q = (unsigned int*)(block + qoff);
 
+  /* particle slices of about a quarter chunk, uploaded first: each is
+   * packed and given its Ewald term as soon as it lands, while the rest of
+   * the particles, the moments and the first list chunks are still on the
+   * link.  Slices start on multiples of 32 particles, so every warp of the
+   * Ewald kernel holds the particles (and culls the replicas) it holds in
+   * one launch over all of them: the results do not depend on the slicing. */
+  std::vector<std::pair<long long, long long>> slices;
+  {
+    const long long per =
+        std::max<long long>(32, (long long)(kChunkBytes / 4 / (5 * sizeof(double))) & ~31LL);
+    for (long long a = 0; a < n_parts; a += per) slices.push_back({a, std::min(n_parts, a + per)});
+  }
+
   std::vector<cudaEvent_t> evs;
   auto event = [&](cudaStream_t on) -> cudaEvent_t {
     cudaEvent_t e = nullptr;
@@ -1289,14 +1307,21 @@ static int step_host_impl(int form, const double* moments, long long n_moments,
   do {
     cudaEvent_t ready = event(s);  // the block is allocated on s
     if (!ready || (e = cudaStreamWaitEvent(c, ready, 0)) != cudaSuccess) break;
-    /* small arrays first */
+    /* the particles (and the vars they accumulate into) slice by slice */
+    std::vector<cudaEvent_t> sliced;
+    for (auto& sl : slices) {
+      const size_t o = (size_t)sl.first * 5, b = (size_t)(sl.second - sl.first) * 5 * sizeof(double);
+      if ((e = cudaMemcpyAsync(d_parts + o, parts + o, b, cudaMemcpyHostToDevice, c)) !=
+              cudaSuccess ||
+          (!overwrite &&
+           (e = cudaMemcpyAsync(d_vars + o, vars + o, b, cudaMemcpyHostToDevice, c)) != cudaSuccess))
+        break;
+      sliced.push_back(event(c));
+    }
+    if (e != cudaSuccess) break;
+    /* then the moments and the small arrays */
     if ((e = cudaMemcpyAsync(d_mom, moments, (size_t)n_moments * 12 * sizeof(double),
-                             cudaMemcpyHostToDevice, c)) != cudaSuccess ||
-        (e = cudaMemcpyAsync(d_parts, parts, (size_t)n_parts * 5 * sizeof(double),
                              cudaMemcpyHostToDevice, c)) != cudaSuccess)
-      break;
-    if (!overwrite && (e = cudaMemcpyAsync(d_vars, vars, (size_t)n_parts * 5 * sizeof(double),
-                                           cudaMemcpyHostToDevice, c)) != cudaSuccess)
       break;
     for (int k = 0; k < 2 && e == cudaSuccess; ++k) {
       const ChangaListRequest* r = reqs[k];
@@ -1357,47 +1382,88 @@ static int step_host_impl(int form, const double* moments, long long n_moments,
       }
       if (at < n_parts) gaps.push_back({at, n_parts});
     }
-    auto read_back = [&](long long lo, long long hi) -> cudaError_t {
+    /* Two compute lanes: consecutive chunks of a list alternate between s
+     * and a library-owned stream, so each chunk's kernel takes the SMs that
+     * the previous chunk's kernel frees while it drains.  Only for a list
+     * whose consecutive chunks write disjoint particle ranges (checked
+     * here); any other list runs on s alone.  The lanes join before each
+     * list and before the last read-back. */
+    cudaStream_t s2 = copy_stream(2);
+    bool dual[2] = {false, false};
+    for (int k = 0; k < 2 && s2; ++k) {
+      if (chunks[k].size() < 2) continue;
+      dual[k] = true;
+      std::pair<long long, long long> prev = {0, 0};
+      for (size_t i = 0; i < chunks[k].size() && dual[k]; ++i) {
+        const auto g = target_range(reqs[k], chunks[k][i].first, chunks[k][i].second, n_parts);
+        if (i > 0 && g.first < g.second && prev.first < prev.second)
+          dual[k] = g.second <= prev.first || prev.second <= g.first;
+        prev = g;
+      }
+    }
+    auto join = [&]() -> cudaError_t {
+      if (!s2) return cudaSuccess;
+      cudaEvent_t x2 = event(s2);
+      if (!x2) return cudaErrorUnknown;
+      cudaError_t x = cudaStreamWaitEvent(s, x2, 0);
+      if (x != cudaSuccess) return x;
+      cudaEvent_t x1 = event(s);
+      if (!x1) return cudaErrorUnknown;
+      return cudaStreamWaitEvent(s2, x1, 0);
+    };
+    auto read_back = [&](long long lo, long long hi, cudaStream_t on) -> cudaError_t {
       if (lo >= hi) return cudaSuccess;
-      cudaEvent_t done = event(s);
+      cudaEvent_t done = event(on);
       if (!done) return cudaErrorUnknown;
       cudaError_t x = cudaStreamWaitEvent(rb, done, 0);
       if (x != cudaSuccess) return x;
       return cudaMemcpyAsync(vars + 5 * lo, d_vars + 5 * lo, (size_t)(hi - lo) * 5 * sizeof(double),
                              cudaMemcpyDeviceToHost, rb);
     };
-    /* compute stream */
-    if ((e = cudaStreamWaitEvent(s, small, 0)) != cudaSuccess) break;
+    /* compute stream: each particle slice as it lands, then the moments */
     if (overwrite && (e = cudaMemsetAsync(d_vars, 0, (size_t)n_parts * 5 * sizeof(double), s)) !=
                          cudaSuccess)
       break;
+    for (size_t i = 0; i < slices.size() && e == cudaSuccess; ++i) {
+      const long long a = slices[i].first, n = slices[i].second - slices[i].first;
+      if (!sliced[i]) e = cudaErrorUnknown;
+      if (e != cudaSuccess || (e = cudaStreamWaitEvent(s, sliced[i], 0)) != cudaSuccess) break;
+      if (f == kMix && (e = launch_pack_parts(d_parts + 5 * a, n, pp + kPartPackF4 * a, s)) !=
+                           cudaSuccess)
+        break;
+      if (ewald && (e = launch_ewald_fp(f, d_parts + 5 * a, n, nullptr, n, *ewald, d_vars + 5 * a,
+                                        s)) != cudaSuccess)
+        break;
+    }
+    if (e != cudaSuccess || (e = cudaStreamWaitEvent(s, small, 0)) != cudaSuccess) break;
     const void* ksrc = d_mom;
     const void* kpart = d_parts;
     if (f == kMix) {
-      if ((e = launch_pack_cells(d_mom, n_moments, pc, s)) != cudaSuccess ||
-          (e = launch_pack_parts(d_parts, n_parts, pp, s)) != cudaSuccess)
-        break;
+      if ((e = launch_pack_cells(d_mom, n_moments, pc, s)) != cudaSuccess) break;
       ksrc = pc;
       kpart = pp;
     }
-    if (ewald && (e = launch_ewald_fp(f, d_parts, n_parts, nullptr, n_parts, *ewald, d_vars, s)) !=
-                     cudaSuccess)
-      break;
     for (int k = 0; k < 2 && !rc && e == cudaSuccess; ++k) {
       const ChangaListRequest* r = reqs[k];
+      /* both lanes past the packs, the Ewald term and the previous list */
+      if ((e = join()) != cudaSuccess) break;
       if (k == last && early) {
         for (size_t i = 0; i < gaps.size() && e == cudaSuccess; ++i)
-          e = read_back(gaps[i].first, gaps[i].second);
+          e = read_back(gaps[i].first, gaps[i].second, s);
         if (e != cudaSuccess) break;
       }
       for (size_t i = 0; i < chunks[k].size() && !rc && e == cudaSuccess; ++i) {
-        if (!landed[k][i] || (e = cudaStreamWaitEvent(s, landed[k][i], 0)) != cudaSuccess) break;
+        const bool second = dual[k] && (i & 1);
+        cudaStream_t on = second ? s2 : s;
+        if (!landed[k][i]) e = cudaErrorUnknown;
+        if (e != cudaSuccess || (e = cudaStreamWaitEvent(on, landed[k][i], 0)) != cudaSuccess)
+          break;
         const int b0 = chunks[k][i].first, b1 = chunks[k][i].second;
         if (k == 1 && pruns &&
             (e = launch_expand_runs((const ILPart*)(block + roff), pruns->n_runs,
                                     (const int*)(block + rmoff) + b0,
                                     (const int*)(block + off[k][1]) + b0, b1 - b0,
-                                    (ILCell*)(block + off[k][0]), plist->n_entries, s)) !=
+                                    (ILCell*)(block + off[k][0]), plist->n_entries, on)) !=
                 cudaSuccess)
           break;
         ChangaListRequest sub;
@@ -1407,20 +1473,27 @@ static int step_host_impl(int form, const double* moments, long long n_moments,
         sub.sizes = (const int*)(block + off[k][3]) + b0;
         sub.n_buckets = b1 - b0;
         sub.n_entries = r->markers[b1];
-        rc = k == 0 ? run_fp(f, true, ksrc, n_moments, kpart, n_parts, &sub, fperiod, d_vars, s, q)
-                    : run_fp(f, false, kpart, n_parts, kpart, n_parts, &sub, fperiod, d_vars, s,
-                             q + 32);
-        if (!rc && k == last && early) e = read_back(ranges[i].first, ranges[i].second);
+        /* a queue counter per list and lane (the block's last 256 bytes) */
+        unsigned int* qk = q + 32 * k + (second ? 16 : 0);
+        rc = k == 0
+                 ? run_fp(f, true, ksrc, n_moments, kpart, n_parts, &sub, fperiod, d_vars, on, qk)
+                 : run_fp(f, false, kpart, n_parts, kpart, n_parts, &sub, fperiod, d_vars, on, qk);
+        if (!rc && k == last && early) e = read_back(ranges[i].first, ranges[i].second, on);
       }
     }
-    if (rc || e != cudaSuccess) break;
+    if (rc || e != cudaSuccess || (e = join()) != cudaSuccess) break;
     if (!early)
       e = cudaMemcpyAsync(vars, d_vars, (size_t)n_parts * 5 * sizeof(double),
                           cudaMemcpyDeviceToHost, s);
   } while (0);
-  /* both copy streams must be idle before the block goes back to the pool */
+  /* the copy streams and the second lane must be idle before the block goes
+   * back to the pool */
   cudaEvent_t copies_done = event(c);
   if (copies_done) cudaStreamWaitEvent(s, copies_done, 0);
+  if (cudaStream_t s2 = copy_stream(2)) {
+    cudaEvent_t lane_done = event(s2);
+    if (lane_done) cudaStreamWaitEvent(s, lane_done, 0);
+  }
   cudaEvent_t reads_done = event(rb);
   if (reads_done) cudaStreamWaitEvent(s, reads_done, 0);
   cudaError_t ef = cudaFreeAsync(block, s);

@@ -236,7 +236,9 @@ int changa_gravity_step_host_runs(int form, const double *moments, long long n_m
                                   cudaStream_t stream);
 
 /* List bytes per upload chunk of changa_gravity_step_host and of the
- * drop-in list transfers (default 512 MiB, at least 4 KiB).  A drop-in
+ * drop-in list transfers (default 256 MiB, at least 4 KiB; 0 restores the
+ * default).  changa_gravity_step_host uploads the particles first, in
+ * slices of a quarter chunk.  A drop-in
  * request whose list exceeds two chunks uploads it chunk by chunk on the
  * library's copy stream, each chunk's buckets evaluated as it lands. */
 void changa_gb300_set_host_chunk_bytes(size_t bytes);

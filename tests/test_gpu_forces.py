@@ -113,7 +113,33 @@ def test_host_entry_pipelined_chunks(plummer, lattice):
                 acc = gravity.gravity_step_host(L, form, ewald=ew, vars=np.ones((L.n, 5)))
                 np.testing.assert_allclose(acc[:, :4], dev[:, :4] + 1.0, rtol=1e-12, atol=1e-12)
     finally:
-        lib.changa_gb300_set_host_chunk_bytes(512 << 20)
+        lib.changa_gb300_set_host_chunk_bytes(0)  # the default
+
+
+def test_host_entry_particle_slices(cuda_ok):
+    """The host entry uploads the particles in slices (a quarter chunk,
+    started on multiples of 32) and gives each its Ewald term as it lands.
+    Every warp of the Ewald kernel then holds the particles it holds in one
+    launch over all, so the slicing changes no bit: a clustered periodic set
+    of a particle count that is no multiple of 32, both forms, overwriting
+    and accumulating, in slices of 96 particles against one slice."""
+    lib = N.cuda_lib()
+    p = ics.nfw_halos(20001, ics.rng_for(11), soft=1e-3)
+    L = tree.build_lists(p["pos"], p["mass"], p["soft"], n_bucket=16, theta=0.7, period=1.0,
+                         n_replicas=1)
+    ew = gravity.EwaldConfig(1.0, 1, 2.6, 2.8)
+    start = np.random.Generator(np.random.PCG64(3)).standard_normal((L.n, 5))
+    for form in ("mixed", "fp64"):
+        one = gravity.gravity_step_host(L, form, ewald=ew, overwrite=True)
+        acc_one = gravity.gravity_step_host(L, form, ewald=ew, vars=start.copy())
+        lib.changa_gb300_set_host_chunk_bytes(16 * 1024)  # 96-particle slices
+        try:
+            many = gravity.gravity_step_host(L, form, ewald=ew, overwrite=True)
+            acc_many = gravity.gravity_step_host(L, form, ewald=ew, vars=start.copy())
+        finally:
+            lib.changa_gb300_set_host_chunk_bytes(0)  # the default
+        assert np.array_equal(many, one), form
+        assert np.array_equal(acc_many, acc_one), form
 
 
 def _reordered(req, order):
@@ -163,7 +189,7 @@ def test_host_entry_early_readback(plummer, lattice):
                     finally:
                         out.free()
     finally:
-        lib.changa_gb300_set_host_chunk_bytes(512 << 20)
+        lib.changa_gb300_set_host_chunk_bytes(0)  # the default
 
 
 @pytest.mark.parametrize("name", FIXTURES)
@@ -505,7 +531,7 @@ def test_dropin_chunked_upload(plummer, lattice):
             try:
                 chunked = gravity.dropin_step(inp).copy()
             finally:
-                lib.changa_gb300_set_host_chunk_bytes(512 << 20)
+                lib.changa_gb300_set_host_chunk_bytes(0)  # the default
         finally:
             inp.free()
         assert n_entries * 8 > 2 * chunk
@@ -531,7 +557,7 @@ def test_host_entry_particle_runs(plummer, lattice):
         try:
             small = gravity.gravity_step_host(L, "mixed", ewald=ew, runs=pr)
         finally:
-            lib.changa_gb300_set_host_chunk_bytes(512 << 20)
+            lib.changa_gb300_set_host_chunk_bytes(0)  # the default
         np.testing.assert_array_equal(small, gravity.gravity_step_host(L, "mixed", ewald=ew))
 
 
