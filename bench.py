@@ -58,7 +58,7 @@ def parse():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default="nfw8m")
     ap.add_argument("--fp64-steps", type=int, default=2)
-    ap.add_argument("--e2e-steps", type=int, default=5)
+    ap.add_argument("--e2e-steps", type=int, default=9)
     ap.add_argument("--cpu-sample", type=float, default=1.5e10,
                     help="interactions in the bounded CPU sample")
     ap.add_argument("--no-cpu", action="store_true")
