@@ -158,7 +158,7 @@ static std::atomic<size_t> g_host_chunk_bytes{kDefaultHostChunkBytes};
  * (created once): which 0 carries the uploads, which 1 the read-backs, so
  * the two directions of the host link run at once; which 2 is the second
  * compute lane of changa_gravity_step_host. */
-static cudaStream_t copy_stream(int which = 0) {
+static cudaStream_t library_stream(int which = 0) {
   static cudaStream_t st[64][3] = {{nullptr}};
   static std::mutex mu;
   int dev = 0;
@@ -343,7 +343,7 @@ static int run_request(CudaRequest* r, bool cell, const void* sources, long long
   /* a list of more than two chunks streams in chunk by chunk */
   const long long per = (long long)(g_host_chunk_bytes.load() / sizeof(ILCell));
   if (r->numInteractions > 2 * per) {
-    cudaStream_t c = copy_stream();
+    cudaStream_t c = library_stream();
     if (c) return run_request_chunked(r, cell, sources, n_src, n_tgt, nb, per, c);
   }
   ReqDev d;
@@ -1216,11 +1216,11 @@ static int step_host_impl(int form, const double* moments, long long n_moments,
   prepare_pool();
   const unsigned long long tma_before = tma_launches();
   const int f = form == CHANGA_FORM_FP64 ? kF64 : kMix;
-  cudaStream_t c = copy_stream();
+  cudaStream_t c = library_stream();
   if (!c) return record_error(cudaErrorUnknown, "gravity_step_host: copy stream", __FILE__, __LINE__);
   const size_t kChunkBytes = g_host_chunk_bytes.load();
 
-  cudaStream_t rb = copy_stream(1);
+  cudaStream_t rb = library_stream(1);
   if (!rb) return record_error(cudaErrorUnknown, "gravity_step_host: copy stream", __FILE__, __LINE__);
 
   /* chunks: [request][bucket range] by entry bytes */
@@ -1388,7 +1388,7 @@ static int step_host_impl(int form, const double* moments, long long n_moments,
      * whose consecutive chunks write disjoint particle ranges (checked
      * here); any other list runs on s alone.  The lanes join before each
      * list and before the last read-back. */
-    cudaStream_t s2 = copy_stream(2);
+    cudaStream_t s2 = library_stream(2);
     bool dual[2] = {false, false};
     for (int k = 0; k < 2 && s2; ++k) {
       if (chunks[k].size() < 2) continue;
@@ -1490,7 +1490,7 @@ static int step_host_impl(int form, const double* moments, long long n_moments,
    * back to the pool */
   cudaEvent_t copies_done = event(c);
   if (copies_done) cudaStreamWaitEvent(s, copies_done, 0);
-  if (cudaStream_t s2 = copy_stream(2)) {
+  if (cudaStream_t s2 = library_stream(2)) {
     cudaEvent_t lane_done = event(s2);
     if (lane_done) cudaStreamWaitEvent(s, lane_done, 0);
   }
