@@ -229,6 +229,27 @@ def test_ewald_forms(lattice):
     assert np.abs(vmx[:, 3] - ref[:, 3]).max() < 5e-5
 
 
+def test_perfect_lattice_forms(cuda_ok):
+    """A perfect periodic lattice (8^3, Ewald): every coordinate an exact
+    float, both halves of each split equal across rows, and the net force
+    only the residual of cancelling replica terms (zero by symmetry; about
+    0.4 of a neighbour's force from ChaNGa's algorithm at theta 0.7).  The
+    FP64 form equals the oracle to the 1e-6 bar of the rms force and the
+    rms potential; the FP32-mixed form stays within the rounding of the
+    O(1) terms, as on the perturbed lattice."""
+    p = ics.lattice_grf(8, ics.rng_for(1), rms_frac=0.0)
+    L = tree.build_lists(p["pos"], p["mass"], p["soft"], n_bucket=16, theta=0.7, period=1.0)
+    ew = gravity.EwaldConfig(1.0, 1, 2.6, 2.8)
+    ref = oracle_vars(L, 1.0, ew)
+    v64 = gravity.DeviceSystem(L, ewald=ew).step("fp64").cpu().numpy()
+    assert force_rms_err(v64, ref).max() < FP64_TOL
+    assert pot_rms_err(v64, ref).max() < FP64_TOL
+    vmx = gravity.DeviceSystem(L, ewald=ew).step("mixed").cpu().numpy()
+    e = force_rms_err(vmx, ref)
+    assert np.median(e) < 5e-5 and e.max() < 2e-3
+    assert np.abs(vmx[:, 3] - ref[:, 3]).max() < 5e-5
+
+
 def test_ewald_dropin(lattice):
     L, ew, _ = lattice
     ref32 = oracle_vars(L, 1.0, ew, f32_inputs=True)
