@@ -85,6 +85,26 @@ def test_mixed_form_matches_fp64(plummer):
     assert np.median(pot_rel_err(v, ref)) < MIX_MEDIAN_TOL
 
 
+def test_mixed_form_far_from_origin(cuda_ok):
+    """The FP32-mixed form keeps its accuracy for a system far from the
+    origin: coordinates split into hi + lo and differences formed relative
+    to the target bucket, so a Plummer sphere shifted by ~1e3 (where one
+    FP32 coordinate resolves 6e-5, against a softening of 0.01) matches
+    the FP64 oracle as closely as the same sphere at the origin."""
+    p = ics.plummer(16384, ics.rng_for(12), soft=0.01)
+    shift = np.array([1000.25, -3000.5, 777.125])
+    errs = []
+    for pos in (p["pos"], p["pos"] + shift):
+        L = tree.build_lists(pos, p["mass"], p["soft"], n_bucket=16, theta=0.7)
+        ref = oracle_vars(L)
+        v = gravity.DeviceSystem(L).step("mixed").cpu().numpy()
+        e = force_rel_err(v, ref)
+        assert np.median(e) < MIX_MEDIAN_TOL and np.percentile(e, 99) < MIX_P99_TOL
+        assert np.median(pot_rel_err(v, ref)) < MIX_MEDIAN_TOL
+        errs.append(np.median(e))
+    assert errs[1] < 3.0 * errs[0]
+
+
 def test_host_entry_matches_device_entry(plummer):
     L, ref, _ = plummer
     v = gravity.gravity_step_host(L, "fp64")
