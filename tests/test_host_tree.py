@@ -101,3 +101,31 @@ def test_part_runs_round_trip():
         per_bucket = np.add.reduceat(pr.runs[:, 2].astype(np.int64), rm[:-1]) * (np.diff(rm) > 0)
         np.testing.assert_array_equal(per_bucket, np.diff(L.plist.markers.astype(np.int64)))
         assert pr.n_runs * 4 < L.plist.n_entries
+
+
+@pytest.mark.parametrize("case", ["open", "periodic1", "periodic2", "hexadecapole"])
+def test_walk_accounts_every_source_once(built, case):
+    """Each bucket's lists (accepted cells and opened particles, over every
+    replica) account for every source particle exactly once: their masses
+    sum to the total mass times the number of replicas walked, (2 n + 1)^3.
+    A missed or repeated subtree of the walk (TreeWalk.cpp:297-434) shows
+    here; unequal random masses keep swapped entries from cancelling."""
+    rng = np.random.Generator(np.random.PCG64(21))
+    if case == "open" or case == "hexadecapole":
+        p = ics.plummer(8192, ics.rng_for(0), soft=0.01)
+        kw = dict(order=4) if case == "hexadecapole" else {}
+        reps = 1
+    else:
+        p = ics.nfw_halos(16384, ics.rng_for(3), soft=1e-3)
+        nr = 1 if case == "periodic1" else 2
+        kw = dict(period=1.0, n_replicas=nr)
+        reps = (2 * nr + 1) ** 3
+    mass = rng.uniform(0.5, 1.5, len(p["mass"])) / len(p["mass"])
+    L = tree.build_lists(p["pos"], mass, p["soft"], n_bucket=16, theta=0.7, **kw)
+    total = np.zeros(int(max(L.cells.bucket_ids.max(), L.plist.bucket_ids.max())) + 1)
+    for req, w in ((L.cells, L.moments[:, 2]), (L.plist, L.parts[:, 0])):
+        seg = w[req.list[:, 0]]
+        s = np.add.reduceat(seg, req.markers[:-1]) if len(seg) else np.zeros(req.n_buckets)
+        s[req.markers[1:] == req.markers[:-1]] = 0.0
+        np.add.at(total, req.bucket_ids, s)
+    np.testing.assert_allclose(total, reps * mass.sum(), rtol=1e-12)
