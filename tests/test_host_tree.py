@@ -129,3 +129,27 @@ def test_walk_accounts_every_source_once(built, case):
         s[req.markers[1:] == req.markers[:-1]] = 0.0
         np.add.at(total, req.bucket_ids, s)
     np.testing.assert_allclose(total, reps * mass.sum(), rtol=1e-12)
+
+
+@pytest.mark.parametrize("n_replicas", [1, 2])
+def test_walk_accounts_every_replica_once(built, n_replicas):
+    """Per replica: each entry's offsetID carries its replica in bits 22-30
+    (x + 3, y + 3, z + 3 in three bits each; TreePiece.cpp:3631-3652), and
+    each bucket's entries of every one of the (2 n + 1)^3 replicas account
+    for every source particle exactly once (masses summing to the total)."""
+    rng = np.random.Generator(np.random.PCG64(21))
+    p = ics.nfw_halos(16384, ics.rng_for(3), soft=1e-3)
+    mass = rng.uniform(0.5, 1.5, len(p["mass"])) / len(p["mass"])
+    L = tree.build_lists(p["pos"], mass, p["soft"], n_bucket=16, theta=0.7, period=1.0,
+                         n_replicas=n_replicas)
+    side = 2 * n_replicas + 1
+    nb = int(max(L.cells.bucket_ids.max(), L.plist.bucket_ids.max())) + 1
+    total = np.zeros((nb, side ** 3))
+    for req, w in ((L.cells, L.moments[:, 2]), (L.plist, L.parts[:, 0])):
+        code = (req.list[:, 1].astype(np.int64) >> 22) & 0x1FF
+        off = [((code >> (3 * k)) & 7) - 3 for k in range(3)]
+        assert max(np.abs(o).max() for o in off) <= n_replicas
+        rep = ((off[0] + n_replicas) * side + (off[1] + n_replicas)) * side + off[2] + n_replicas
+        b = np.repeat(req.bucket_ids, np.diff(req.markers))
+        np.add.at(total, (b, rep), w[req.list[:, 0]])
+    np.testing.assert_allclose(total, mass.sum(), rtol=1e-12)
