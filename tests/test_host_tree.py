@@ -153,3 +153,53 @@ def test_walk_accounts_every_replica_once(built, n_replicas):
         b = np.repeat(req.bucket_ids, np.diff(req.markers))
         np.add.at(total, (b, rep), w[req.list[:, 0]])
     np.testing.assert_allclose(total, mass.sum(), rtol=1e-12)
+
+
+@pytest.mark.parametrize("case", ["open", "open_theta04", "periodic1"])
+def test_walk_decisions_follow_opening_criterion(built, case):
+    """The walk's decisions against ChaNGa's opening criterion, restated here
+    apart from the host walk: a node opens when it holds 6 particles or
+    fewer, or when the sphere of radius max(2/sqrt(3) R / theta, R) about
+    its centre of mass plus the replica offset meets the box of the local
+    node tested (gravity.h:597-723).  Every accepted cell of a bucket holds
+    more than 6 particles and its sphere misses the bucket's box (accepted
+    at any local level above, it missed a larger box), and its parent was
+    opened for that bucket.  A source bucket that only partially meets a
+    local ancestor is opened into particles for every bucket below it
+    (Compute.cpp:717-760 with codes.h:21-22 and the local table of
+    Opt.h:85-123), so particle entries are checked one level up: the parent
+    of each source leaf was opened for the bucket."""
+    if case == "periodic1":
+        p = ics.nfw_halos(16384, ics.rng_for(3), soft=1e-3)
+        theta, kw, period = 0.7, dict(period=1.0, n_replicas=1), 1.0
+    else:
+        p = ics.plummer(8192, ics.rng_for(0), soft=0.01)
+        theta, kw, period = (0.4 if case == "open_theta04" else 0.7), {}, 0.0
+    L = tree.build_lists(p["pos"], p["mass"], p["soft"], n_bucket=16, theta=theta, **kw)
+    g, bb, cnt, par = L.meta["node_geom"], L.meta["node_bbox"], L.meta["count"], L.meta["parent"]
+    leaf, bnode = L.meta["leaf"], L.meta["bucket_node"]
+
+    def ratio(nodes, off, buckets):
+        """squared distance from the node's sphere centre to the bucket's box
+        over the squared opening radius"""
+        c = g[nodes, :3] + off
+        box = bb[bnode[buckets]]
+        d = np.maximum(np.maximum(box[:, :3] - c, c - box[:, 3:]), 0.0)
+        r = np.maximum(2.0 / np.sqrt(3.0) * g[nodes, 3] / theta, g[nodes, 3])
+        return (d * d).sum(1) / (r * r)
+
+    def entries(req):
+        code = (req.list[:, 1].astype(np.int64) >> 22) & 0x1FF
+        off = np.stack([((code >> (3 * k)) & 7) - 3 for k in range(3)], 1) * period
+        return req.list[:, 0], off, np.repeat(req.bucket_ids, np.diff(req.markers))
+
+    idx, off, b = entries(L.cells)
+    assert (cnt[idx] > 6).all()
+    assert (ratio(idx, off, b) > 1.0 - 1e-12).all()
+    up = par[idx]
+    has = up >= 0
+    assert ((ratio(up[has], off[has], b[has]) <= 1.0 + 1e-12) | (cnt[up[has]] <= 6)).all()
+    idx, off, b = entries(L.plist)
+    up = par[leaf[idx]]
+    has = up >= 0
+    assert ((ratio(up[has], off[has], b[has]) <= 1.0 + 1e-12) | (cnt[up[has]] <= 6)).all()
