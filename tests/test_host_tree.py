@@ -105,14 +105,17 @@ def test_part_runs_round_trip():
 
 @pytest.mark.parametrize("case", ["open", "periodic1", "periodic2", "hexadecapole"])
 def test_walk_accounts_every_source_once(built, case):
-    """Each bucket's lists (accepted cells and opened particles, over every
-    replica) account for every source particle exactly once: their masses
+    """Each bucket's lists (accepted cells, opened particles and, in the
+    hexadecapole build, softened cells, over every replica) account for
+    every source particle exactly once: their masses
     sum to the total mass times the number of replicas walked, (2 n + 1)^3.
     A missed or repeated subtree of the walk (TreeWalk.cpp:297-434) shows
     here; unequal random masses keep swapped entries from cancelling."""
     rng = np.random.Generator(np.random.PCG64(21))
     if case == "open" or case == "hexadecapole":
-        p = ics.plummer(8192, ics.rng_for(0), soft=0.01)
+        # softening 0.3: the hexadecapole walk sends cells whose softening
+        # overlaps the bucket to its third list, as softened point masses
+        p = ics.plummer(8192, ics.rng_for(0), soft=0.3 if case == "hexadecapole" else 0.01)
         kw = dict(order=4) if case == "hexadecapole" else {}
         reps = 1
     else:
@@ -122,8 +125,12 @@ def test_walk_accounts_every_source_once(built, case):
         reps = (2 * nr + 1) ** 3
     mass = rng.uniform(0.5, 1.5, len(p["mass"])) / len(p["mass"])
     L = tree.build_lists(p["pos"], mass, p["soft"], n_bucket=16, theta=0.7, **kw)
-    total = np.zeros(int(max(L.cells.bucket_ids.max(), L.plist.bucket_ids.max())) + 1)
-    for req, w in ((L.cells, L.moments[:, 2]), (L.plist, L.parts[:, 0])):
+    reqs = [(L.cells, L.moments[:, 2]), (L.plist, L.parts[:, 0])]
+    if case == "hexadecapole":
+        assert L.softcells.n_entries > 0
+        reqs.append((L.softcells, L.moments[:, 2]))
+    total = np.zeros(int(max(r.bucket_ids.max() for r, _ in reqs)) + 1)
+    for req, w in reqs:
         seg = w[req.list[:, 0]]
         s = np.add.reduceat(seg, req.markers[:-1]) if len(seg) else np.zeros(req.n_buckets)
         s[req.markers[1:] == req.markers[:-1]] = 0.0
