@@ -210,3 +210,37 @@ def test_walk_decisions_follow_opening_criterion(built, case):
     up = par[leaf[idx]]
     has = up >= 0
     assert ((ratio(up[has], off[has], b[has]) <= 1.0 + 1e-12) | (cnt[up[has]] <= 6)).all()
+
+
+def test_hexadecapole_walk_decisions(built):
+    """The hexadecapole walk's accepted cells against its rules, restated
+    apart from the walk: every cell and softened cell of a bucket holds
+    more than 6 particles and its theta sphere misses the bucket's box
+    (gravity.h:597-640), and the two lists split on openSoftening
+    (gravity.h:245-260: the cell's and the bucket's spheres of twice their
+    softening meet, or the cell's meets the bucket's box): true for every
+    softened cell, false for every cell.  (Parents are not checked: there a
+    local node is opened for every bucket below it when the monopole sphere
+    meets its box, gravity.h:690-702.)"""
+    p = ics.plummer(8192, ics.rng_for(0), soft=0.3)
+    theta = 0.7
+    L = tree.build_lists(p["pos"], p["mass"], p["soft"], n_bucket=16, theta=theta, order=4)
+    g, bb, cnt = L.meta["node_geom"], L.meta["node_bbox"], L.meta["count"]
+    bnode = L.meta["bucket_node"]
+
+    def box_d2(c, buckets):
+        box = bb[bnode[buckets]]
+        d = np.maximum(np.maximum(box[:, :3] - c, c - box[:, 3:]), 0.0)
+        return (d * d).sum(1)
+
+    for req, soft_expected in ((L.cells, False), (L.softcells, True)):
+        assert req.n_entries > 0
+        idx = req.list[:, 0]
+        b = np.repeat(req.bucket_ids, np.diff(req.markers))
+        c = g[idx, :3]
+        r = np.maximum(2.0 / np.sqrt(3.0) * g[idx, 3] / theta, g[idx, 3])
+        assert (cnt[idx] > 6).all()
+        assert (box_d2(c, b) > r * r * (1.0 - 1e-12)).all()
+        rs, rb = 2.0 * g[idx, 4], 2.0 * g[bnode[b], 4]
+        soft = (((c - g[bnode[b], :3]) ** 2).sum(1) <= (rs + rb) ** 2) | (box_d2(c, b) <= rs * rs)
+        assert (soft == soft_expected).all()
