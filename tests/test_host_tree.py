@@ -216,12 +216,12 @@ def test_hexadecapole_walk_decisions(built):
     """The hexadecapole walk's accepted cells against its rules, restated
     apart from the walk: every cell and softened cell of a bucket holds
     more than 6 particles and its theta sphere misses the bucket's box
-    (gravity.h:597-640), and the two lists split on openSoftening
-    (gravity.h:245-260: the cell's and the bucket's spheres of twice their
+    (gravity.h:597-633), and the two lists split on openSoftening
+    (gravity.h:251-260: the cell's and the bucket's spheres of twice their
     softening meet, or the cell's meets the bucket's box): true for every
     softened cell, false for every cell.  (Parents are not checked: there a
     local node is opened for every bucket below it when the monopole sphere
-    meets its box, gravity.h:690-702.)"""
+    meets its box, gravity.h:705-717.)"""
     p = ics.plummer(8192, ics.rng_for(0), soft=0.3)
     theta = 0.7
     L = tree.build_lists(p["pos"], p["mass"], p["soft"], n_bucket=16, theta=theta, order=4)
