@@ -244,3 +244,44 @@ def test_hexadecapole_walk_decisions(built):
         rs, rb = 2.0 * g[idx, 4], 2.0 * g[bnode[b], 4]
         soft = (((c - g[bnode[b], :3]) ** 2).sum(1) <= (rs + rb) ** 2) | (box_d2(c, b) <= rs * rs)
         assert (soft == soft_expected).all()
+
+
+@pytest.mark.parametrize("case", ["open", "periodic"])
+def test_tree_nodes_follow_reference_rules(built, case):
+    """The host build's nodes against ChaNGa's rules, restated apart from
+    the build: a node is a bucket when it holds nBucket particles or fewer
+    (Compute.cpp:2476-2482, no node reaching the depth limit here), its box
+    is the tight box of its particles, its centre of mass the mass-weighted
+    mean; a bucket of several distinct particles takes the distance from
+    its centre of mass to its farthest particle as its radius
+    (GenericTreeNode.h:219-256, MultipoleMoments.h:487-504), an internal
+    node the distance to its box's farthest corner (Compute.cpp:2576,
+    MultipoleMoments.h:460-471).  (A one-particle bucket keeps half the
+    diagonal of its spatial cell, which is not exported.)"""
+    if case == "open":
+        p, kw, nb = ics.plummer(8192, ics.rng_for(0), soft=0.01), {}, 16
+    else:
+        p, kw, nb = ics.nfw_halos(16384, ics.rng_for(3), soft=1e-3), dict(period=1.0), 8
+    L = tree.build_lists(p["pos"], p["mass"], p["soft"], n_bucket=nb, theta=0.7, **kw)
+    g, bb, info = L.meta["node_geom"], L.meta["node_bbox"], L.meta["node_info"]
+    first, count = L.meta["first"], L.meta["count"]
+    pos, m = L.parts[:, 2:5], L.parts[:, 0]
+    leaf = (info[:, 0] < 0) & (info[:, 1] < 0)  # an empty child is -1 as well
+    live = count > 0
+    assert set(np.where(leaf & live)[0]) == set(L.meta["bucket_node"])
+    assert count[leaf & live].max() <= nb and count[~leaf & live].min() > nb
+    for i in np.where(live)[0]:
+        x, w = pos[first[i]:first[i] + count[i]], m[first[i]:first[i] + count[i]]
+        assert np.array_equal(x.min(0), bb[i, :3]) and np.array_equal(x.max(0), bb[i, 3:])
+        np.testing.assert_allclose(g[i, :3], (w[:, None] * x).sum(0) / w.sum(), rtol=1e-12,
+                                   atol=1e-14)
+        np.testing.assert_allclose(g[i, 5], w.sum(), rtol=1e-13)
+        if leaf[i]:
+            far = np.sqrt(((x - g[i, :3]) ** 2).sum(1).max())
+            if count[i] > 1 and far > 0:
+                np.testing.assert_allclose(g[i, 3], far, rtol=1e-13)
+            else:
+                assert g[i, 3] > 0
+        else:
+            d = np.maximum(g[i, :3] - bb[i, :3], bb[i, 3:] - g[i, :3])
+            np.testing.assert_allclose(g[i, 3], np.sqrt((d * d).sum()), rtol=1e-13)
