@@ -257,12 +257,19 @@ def test_tree_nodes_follow_reference_rules(built, case):
     (GenericTreeNode.h:219-256, MultipoleMoments.h:487-504), an internal
     node the distance to its box's farthest corner (Compute.cpp:2576,
     MultipoleMoments.h:460-471).  (A one-particle bucket keeps half the
-    diagonal of its spatial cell, which is not exported.)"""
+    diagonal of its spatial cell, which is not exported.)  The softening is
+    the mass-weighted mean and the second moments are raw, sum m dx dx about
+    the centre of mass, not trace-free (MultipoleMoments.h:207-225,
+    330-348); unequal masses and softenings keep each rule distinct."""
     if case == "open":
         p, kw, nb = ics.plummer(8192, ics.rng_for(0), soft=0.01), {}, 16
     else:
         p, kw, nb = ics.nfw_halos(16384, ics.rng_for(3), soft=1e-3), dict(period=1.0), 8
-    L = tree.build_lists(p["pos"], p["mass"], p["soft"], n_bucket=nb, theta=0.7, **kw)
+    rng = np.random.Generator(np.random.PCG64(4))
+    n = len(p["mass"])
+    mass = rng.uniform(0.5, 1.5, n) / n
+    soft = p["soft"] * rng.uniform(0.5, 5.0, n)
+    L = tree.build_lists(p["pos"], mass, soft, n_bucket=nb, theta=0.7, **kw)
     g, bb, info = L.meta["node_geom"], L.meta["node_bbox"], L.meta["node_info"]
     first, count = L.meta["first"], L.meta["count"]
     pos, m = L.parts[:, 2:5], L.parts[:, 0]
@@ -276,6 +283,18 @@ def test_tree_nodes_follow_reference_rules(built, case):
         np.testing.assert_allclose(g[i, :3], (w[:, None] * x).sum(0) / w.sum(), rtol=1e-12,
                                    atol=1e-14)
         np.testing.assert_allclose(g[i, 5], w.sum(), rtol=1e-13)
+        sf = L.parts[first[i]:first[i] + count[i], 1]
+        np.testing.assert_allclose(g[i, 4], (w * sf).sum() / w.sum(), rtol=1e-13)
+        dx = x - L.moments[i, 3:6]
+        q = [(w * dx[:, a] * dx[:, b]).sum() for a, b in ((0, 0), (0, 1), (0, 2), (1, 1), (1, 2),
+                                                          (2, 2))]
+        # the build accumulates child by child with parallel-axis shifts, so
+        # its rounding scales with m |x|^2 about the origin, not with the
+        # node's own trace (which a trace-free Q would miss by a third)
+        tr = (w * (dx * dx).sum(1)).sum()
+        tol = 1e-12 * (w * (x * x).sum(1)).sum()
+        assert tol < 0.01 * tr or count[i] == 1 or tr == 0
+        np.testing.assert_allclose(L.moments[i, 6:12], q, rtol=0, atol=tol + 1e-300)
         if leaf[i]:
             far = np.sqrt(((x - g[i, :3]) ** 2).sum(1).max())
             if count[i] > 1 and far > 0:
