@@ -50,6 +50,8 @@ def load(kind="port"):
             f.restype = i
         if kind == "port":
             _bind_hex(lib)
+            lib.oracle_direct_energy.argtypes = [vp, l, i]
+            lib.oracle_direct_energy.restype = d
         _libs[kind] = lib
     return _libs[kind]
 
@@ -241,6 +243,14 @@ def spline_ab(r2, twoh):
         a[near] = an
         b[near] = bn
     return a, b
+
+
+def direct_energy(parts, nthreads=0):
+    """Potential energy 0.5 sum_i m_i phi_i of an open system, by FP64
+    direct summation over every pair with the P-P spline softening (the C
+    port, all host cores)."""
+    parts = np.ascontiguousarray(parts, dtype=np.float64)
+    return float(load("port").oracle_direct_energy(_p(parts), parts.shape[0], nthreads))
 
 
 def direct_sum(parts, targets_idx, chunk=4096):

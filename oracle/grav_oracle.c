@@ -145,6 +145,33 @@ static void part_bucket_force(const double* src, const double* off, const double
   }
 }
 
+/* Potential energy of an open system by direct summation,
+ * 0.5 sum_i m_i phi_i with phi_i = -sum_{j != i} m_j a(r_ij): a is the
+ * SPLINE potential of partBucketForce (gravity.h:147-182, 290) at
+ * twoh = soft_i + soft_j, coincident pairs skipped as there.  Every pair
+ * once, OpenMP over i with a reduction. */
+double oracle_direct_energy(const double* parts, long n, int nthreads) {
+  if (nthreads > 0) omp_set_num_threads(nthreads);
+  double u = 0.0;
+#pragma omp parallel for schedule(dynamic, 64) reduction(+ : u)
+  for (long i = 0; i < n; ++i) {
+    const double* p = parts + 5 * (size_t)i;
+    double s = 0.0;
+    for (long j = i + 1; j < n; ++j) {
+      const double* q = parts + 5 * (size_t)j;
+      const double rx = q[2] - p[2], ry = q[3] - p[3], rz = q[4] - p[4];
+      const double rsq = rx * rx + ry * ry + rz * rz;
+      if (rsq != 0) {
+        double a, b;
+        spline(rsq, p[1] + q[1], &a, &b);
+        s += q[0] * a;
+      }
+    }
+    u -= p[0] * s;
+  }
+  return u;
+}
+
 int oracle_cell_list_forces(const double* moments, long n_moments,
                             const double* parts, long n_parts,
                             const int* list, const int* markers,

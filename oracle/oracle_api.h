@@ -32,6 +32,10 @@
 extern "C" {
 #endif
 
+/* Potential energy 0.5 sum_i m_i phi_i of an open system by FP64 direct
+ * summation with partBucketForce's spline softening (port only). */
+double oracle_direct_energy(const double* parts, long n, int nthreads);
+
 /* Cell (quadrupole multipole) interaction lists: nodeBucketForce per entry.
  * bucket_ids (may be NULL) restricts the work to those buckets. */
 int oracle_cell_list_forces(const double* moments, long n_moments,

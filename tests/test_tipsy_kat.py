@@ -84,3 +84,25 @@ def test_king_model_integration_energy(built):
         if (k + 1) % sub == 0:
             assert abs(energy(pot) - e0) < 2e-3, (k, energy(pot), e0)
     assert abs(energy(pot) + 32.19) < 0.005, energy(pot)
+
+
+@pytest.mark.skipif(not KING or not os.path.exists(KING),
+                    reason="reference test data not present (set CHANGA_REFERENCE)")
+def test_king_model_direct_energy(built):
+    """pkdtest.log's U = -64.84776 at t = 0 (PKDGRAV) against the exact
+    potential energy of the model as the reader returns it: an FP64 direct
+    sum over all 36000 x 35999 / 2 pairs with the P-P spline softening and
+    the per-particle softenings of the file.  They agree to 6.7e-6 (the
+    last digits of the log and PKDGRAV's own expansion error); the
+    quadrupole tree (nBucket 8, theta 0.7) sits 3.3e-5 from the exact
+    value."""
+    import oracle
+    from changa_gb300 import tree
+    d = tipsy.read(KING)
+    L = tree.build_lists(d["pos"], d["mass"], d["soft"], n_bucket=8, theta=0.7)
+    U = oracle.direct_energy(L.parts)
+    assert abs(U / -64.84776 - 1) < 2e-5, U
+    v = oracle.cell_forces(L.moments, L.parts, L.cells)
+    v = oracle.part_forces(L.parts, L.parts, L.plist, vars=v)
+    U_tree = 0.5 * (L.parts[:, 0] * v[:, 3]).sum()
+    assert abs(U_tree / U - 1) < 1e-4, (U_tree, U)
